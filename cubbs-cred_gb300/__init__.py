@@ -1,0 +1,527 @@
+"""Python binding of libcubbs_bbs_cuda.so (the GB300 BBS drop-in) over ctypes.
+
+The shared library exports the reference's C ABI v2 (include/cubbs_bbs_gpu_abi.h);
+this module mirrors the ABI structs and offers batch helpers shaped like the
+Rust loader's wrappers (crates/cubbs-bbs/src/gpu_runtime.rs:548-2196):
+sign_batch / verify_batch / proof_gen_batch / proof_verify_batch and the
+primitive MSM, hashing and pairing entry points.
+
+There is no CPU path: loading fails loudly when the library is missing.
+"""
+import ctypes
+import os
+import pathlib
+
+_HERE = pathlib.Path(__file__).resolve().parent
+LIB_PATH = _HERE / "lib" / "libcubbs_bbs_cuda.so"
+ABI_VERSION = 2
+
+SUCCESS, ERR_INVALID_INPUT, ERR_INSUFFICIENT_OUTPUT, ERR_INTERNAL = 0, 1, 2, 3
+BACKEND_KIND_CUDA = 1
+API_ID = b"BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_H2G_HM2S_"
+MAP_DST = API_ID + b"MAP_MSG_TO_SCALAR_AS_HASH_"
+H2S_DST = API_ID + b"H2S_"
+
+
+class ByteSlice(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("len", ctypes.c_size_t)]
+
+
+class ByteBuffer(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("capacity", ctypes.c_size_t), ("len", ctypes.c_size_t)]
+
+
+class IndexSlice(ctypes.Structure):
+    _fields_ = [("data", ctypes.c_void_p), ("len", ctypes.c_size_t)]
+
+
+class Result(ctypes.Structure):
+    _fields_ = [("code", ctypes.c_int32), ("value", ctypes.c_uint8), ("bytes_written", ctypes.c_size_t)]
+
+
+class BackendInfo(ctypes.Structure):
+    _fields_ = [("backend_kind", ctypes.c_uint32), ("hardware_acceleration", ctypes.c_uint8)]
+
+
+class SignItem(ctypes.Structure):
+    _fields_ = [("secret_key", ByteSlice), ("public_key", ByteSlice), ("header", ByteSlice),
+                ("messages", ctypes.c_void_p), ("message_count", ctypes.c_size_t), ("signature_out", ByteBuffer)]
+
+
+class VerifyItem(ctypes.Structure):
+    _fields_ = [("public_key", ByteSlice), ("signature", ByteSlice), ("header", ByteSlice),
+                ("messages", ctypes.c_void_p), ("message_count", ctypes.c_size_t)]
+
+
+class ProofGenItem(ctypes.Structure):
+    _fields_ = [("public_key", ByteSlice), ("signature", ByteSlice), ("header", ByteSlice),
+                ("presentation_header", ByteSlice), ("messages", ctypes.c_void_p),
+                ("message_count", ctypes.c_size_t), ("disclosed_indexes", IndexSlice), ("proof_out", ByteBuffer)]
+
+
+class ProofVerifyItem(ctypes.Structure):
+    _fields_ = [("public_key", ByteSlice), ("proof", ByteSlice), ("header", ByteSlice),
+                ("presentation_header", ByteSlice), ("disclosed_messages", ctypes.c_void_p),
+                ("disclosed_count", ctypes.c_size_t), ("disclosed_indexes", IndexSlice),
+                ("total_message_count", ctypes.c_size_t)]
+
+
+class MessagesToScalarItem(ctypes.Structure):
+    _fields_ = [("message", ByteSlice), ("dst", ByteSlice), ("scalar_out", ByteBuffer)]
+
+
+class SignEFromResidentScalarsItem(ctypes.Structure):
+    _fields_ = [("secret_key", ByteSlice), ("domain", ByteSlice), ("messages", ctypes.c_void_p),
+                ("message_scalar_offset", ctypes.c_size_t), ("message_count", ctypes.c_size_t),
+                ("message_scalars_out", ByteBuffer), ("scalar_out", ByteBuffer)]
+
+
+class PrepareBItem(ctypes.Structure):
+    _fields_ = [("public_key", ByteSlice), ("header", ByteSlice), ("message_scalars", ctypes.c_void_p),
+                ("message_count", ctypes.c_size_t), ("b_out", ByteBuffer)]
+
+
+class G1MsmItem(ctypes.Structure):
+    _fields_ = [("points", ctypes.c_void_p), ("scalars", ctypes.c_void_p), ("term_count", ctypes.c_size_t),
+                ("point_out", ByteBuffer)]
+
+
+class G1MsmCommonPointsBatchItem(ctypes.Structure):
+    _fields_ = [("points", ctypes.c_void_p), ("term_count", ctypes.c_size_t), ("scalar_rows", ctypes.c_void_p),
+                ("scalar_rows_be", ctypes.c_void_p), ("scalar_row_stride", ctypes.c_size_t),
+                ("output_count", ctypes.c_size_t), ("point_outs", ctypes.c_void_p)]
+
+
+class G1MsmCommonPointsPlusVariableItem(ctypes.Structure):
+    _fields_ = [("points", ctypes.c_void_p), ("term_count", ctypes.c_size_t), ("scalar_rows", ctypes.c_void_p),
+                ("variable_points", ctypes.c_void_p), ("variable_scalars", ctypes.c_void_p),
+                ("output_count", ctypes.c_size_t), ("point_outs", ctypes.c_void_p)]
+
+
+class ProofVerifyMsmPairItem(ctypes.Structure):
+    _fields_ = [("common_points", ctypes.c_void_p), ("common_term_count", ctypes.c_size_t),
+                ("common_scalar_rows", ctypes.c_void_p), ("proof_points", ctypes.c_void_p),
+                ("proof_scalars", ctypes.c_void_p), ("output_count", ctypes.c_size_t),
+                ("t1_outs", ctypes.c_void_p), ("t2_outs", ctypes.c_void_p)]
+
+
+class G1DualMsmSamePointsItem(ctypes.Structure):
+    _fields_ = [("points", ctypes.c_void_p), ("lhs_scalars", ctypes.c_void_p), ("rhs_scalars", ctypes.c_void_p),
+                ("term_count", ctypes.c_size_t), ("lhs_out", ByteBuffer), ("rhs_out", ByteBuffer)]
+
+
+class G1DualMsmSamePointsLanesItem(ctypes.Structure):
+    _fields_ = [("points", ctypes.c_void_p), ("lhs_scalars", ctypes.c_void_p), ("rhs_scalars", ctypes.c_void_p),
+                ("term_count", ctypes.c_size_t), ("lane_count", ctypes.c_size_t), ("lhs_outs", ByteBuffer),
+                ("rhs_outs", ByteBuffer)]
+
+
+class G1AddItem(ctypes.Structure):
+    _fields_ = [("lhs", ByteSlice), ("rhs", ByteSlice), ("point_out", ByteBuffer)]
+
+
+class PairingEqItem(ctypes.Structure):
+    _fields_ = [("lhs_g1", ByteSlice), ("lhs_g2", ByteSlice), ("rhs_g1", ByteSlice), ("rhs_g2", ByteSlice)]
+
+
+class PairingEqScaledItem(ctypes.Structure):
+    _fields_ = [("lhs_g1", ByteSlice), ("lhs_g2", ByteSlice), ("rhs_g1", ByteSlice), ("rhs_g2", ByteSlice),
+                ("coefficient", ByteSlice)]
+
+
+class ProofGenT2PrepareItem(ctypes.Structure):
+    _fields_ = [("compressed_b", ByteSlice), ("signature_a", ByteSlice), ("scalars_be", ByteSlice * 7),
+                ("seed", ByteSlice), ("d_out", ByteBuffer), ("abar_out", ByteBuffer), ("bbar_out", ByteBuffer),
+                ("t1_out", ByteBuffer)]
+
+
+_LIB = None
+
+
+def build():
+    """Compile the CUDA library in-tree (sm_103a)."""
+    from importlib import util
+    spec = util.spec_from_file_location("_cubbs_build", _HERE / "build.py")
+    mod = util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.build()
+
+
+def lib():
+    """Load libcubbs_bbs_cuda.so; raises if it has not been built."""
+    global _LIB
+    if _LIB is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"{LIB_PATH} is missing: run build() (no CPU fallback exists)")
+        _LIB = ctypes.CDLL(str(LIB_PATH))
+        U32, P, S = ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t
+        special = {
+            "cubbs_bbs_gpu_backend_info_v2": [U32, P],
+            "cubbs_bbs_gpu_proof_gen_seeded_batch_v2": [U32, P, S, P, P],
+            "cubbs_bbs_gpu_sign_e_from_resident_scalars_batch_v2": [U32, P, S, ByteSlice, ByteSlice, P],
+            "cubbs_bbs_gpu_sha256_batch_for_test_v2": [U32, P, P, P, S, P],
+            "cubbs_bbs_gpu_expand_xmd_sha256_48_batch_for_test_v2": [U32, P, P, P, S, P, S, P],
+            "cubbs_bbs_gpu_hash_to_scalar_sha256_batch_for_test_v2": [U32, P, P, P, S, P, S, P],
+        }
+        for name in _SYMBOLS:
+            fn = getattr(_LIB, name)
+            fn.restype = ctypes.c_int32
+            fn.argtypes = special.get(name, [U32, P, S, P])
+    return _LIB
+
+
+_SYMBOLS = [
+    "cubbs_bbs_gpu_backend_info_v2", "cubbs_bbs_gpu_sign_batch_v2", "cubbs_bbs_gpu_verify_batch_v2",
+    "cubbs_bbs_gpu_proof_gen_batch_v2", "cubbs_bbs_gpu_proof_verify_batch_v2",
+    "cubbs_bbs_gpu_proof_gen_seeded_batch_v2", "cubbs_bbs_gpu_messages_to_scalar_batch_v2",
+    "cubbs_bbs_gpu_sign_e_from_resident_scalars_batch_v2", "cubbs_bbs_gpu_prepare_b_batch_v2",
+    "cubbs_bbs_gpu_g1_msm_batch_v2", "cubbs_bbs_gpu_g1_msm_common_points_batch_v2",
+    "cubbs_bbs_gpu_g1_msm_fused_common_points_batch_v2",
+    "cubbs_bbs_gpu_g1_msm_common_points_plus_variable_batch_v2",
+    "cubbs_bbs_gpu_proof_verify_msm_pair_batch_v2", "cubbs_bbs_gpu_g1_dual_msm_same_points_batch_v2",
+    "cubbs_bbs_gpu_g1_dual_msm_same_points_lanes_batch_v2", "cubbs_bbs_gpu_g1_add_batch_v2",
+    "cubbs_bbs_gpu_pairing_eq_batch_v2", "cubbs_bbs_gpu_pairing_eq_aggregate_v2",
+    "cubbs_bbs_gpu_proof_gen_t2_prepare_batch_v2", "cubbs_bbs_gpu_sha256_batch_for_test_v2",
+    "cubbs_bbs_gpu_expand_xmd_sha256_48_batch_for_test_v2",
+    "cubbs_bbs_gpu_hash_to_scalar_sha256_batch_for_test_v2",
+]
+
+
+class _Keep:
+    """Holds ctypes buffers alive for the duration of one call."""
+
+    def __init__(self):
+        self.refs = []
+
+    def bytes(self, b: bytes):
+        if not b:
+            return ByteSlice(None, 0)
+        buf = ctypes.create_string_buffer(bytes(b), len(b))
+        self.refs.append(buf)
+        return ByteSlice(ctypes.cast(buf, ctypes.c_void_p), len(b))
+
+    def slices(self, items):
+        arr = (ByteSlice * max(1, len(items)))(*[self.bytes(x) for x in items])
+        self.refs.append(arr)
+        return ctypes.cast(arr, ctypes.c_void_p)
+
+    def out(self, cap: int):
+        buf = ctypes.create_string_buffer(max(1, cap))
+        self.refs.append(buf)
+        return ByteBuffer(ctypes.cast(buf, ctypes.c_void_p), cap, 0), buf
+
+    def index(self, idx):
+        arr = (ctypes.c_size_t * max(1, len(idx)))(*idx)
+        self.refs.append(arr)
+        return IndexSlice(ctypes.cast(arr, ctypes.c_void_p), len(idx))
+
+
+def _call(name, *args):
+    conv = []
+    for a in args:
+        if isinstance(a, ctypes.Array):
+            a = ctypes.cast(a, ctypes.c_void_p)
+        elif isinstance(a, ctypes.Structure) and not isinstance(a, ByteSlice):
+            a = ctypes.cast(ctypes.pointer(a), ctypes.c_void_p)
+        conv.append(a)
+    args = conv
+    rc = getattr(lib(), name)(*args)
+    if rc != SUCCESS:
+        raise RuntimeError(f"{name} returned {rc}")
+
+
+def backend_info():
+    info = BackendInfo()
+    _call("cubbs_bbs_gpu_backend_info_v2", ABI_VERSION, (info))
+    return info.backend_kind, info.hardware_acceleration
+
+
+def proof_capacity(message_count: int, disclosed_count: int) -> int:
+    """Output capacity the Rust engine allocates (crates/cubbs-bbs/src/execution.rs:3726-3728)."""
+    return 512 + message_count * 48 + disclosed_count * 48
+
+
+def sign_batch(reqs):
+    """reqs: list of (sk, pk, header, [messages]) -> list of (code, signature bytes)."""
+    k = _Keep()
+    items = (SignItem * len(reqs))()
+    outs = []
+    for i, (sk, pk, hdr, msgs) in enumerate(reqs):
+        ob, buf = k.out(80)
+        outs.append(buf)
+        items[i] = SignItem(k.bytes(sk), k.bytes(pk), k.bytes(hdr), k.slices(msgs), len(msgs), ob)
+    res = (Result * len(reqs))()
+    _call("cubbs_bbs_gpu_sign_batch_v2", ABI_VERSION, items, len(reqs), res)
+    return [(res[i].code, outs[i].raw[:items[i].signature_out.len]) for i in range(len(reqs))]
+
+
+def verify_batch(reqs):
+    """reqs: list of (pk, signature, header, [messages]) -> list of (code, valid)."""
+    k = _Keep()
+    items = (VerifyItem * len(reqs))()
+    for i, (pk, sig, hdr, msgs) in enumerate(reqs):
+        items[i] = VerifyItem(k.bytes(pk), k.bytes(sig), k.bytes(hdr), k.slices(msgs), len(msgs))
+    res = (Result * len(reqs))()
+    _call("cubbs_bbs_gpu_verify_batch_v2", ABI_VERSION, items, len(reqs), res)
+    return [(res[i].code, bool(res[i].value)) for i in range(len(reqs))]
+
+
+def _proof_gen_items(k, reqs):
+    items = (ProofGenItem * len(reqs))()
+    outs = []
+    for i, (pk, sig, hdr, ph, msgs, disclosed) in enumerate(reqs):
+        ob, buf = k.out(proof_capacity(len(msgs), len(disclosed)))
+        outs.append(buf)
+        items[i] = ProofGenItem(k.bytes(pk), k.bytes(sig), k.bytes(hdr), k.bytes(ph), k.slices(msgs), len(msgs),
+                                k.index(disclosed), ob)
+    return items, outs
+
+
+def proof_gen_batch(reqs, seeds=None):
+    """reqs: list of (pk, signature, header, ph, [messages], [disclosed]).  With seeds
+    (one 32-byte seed per item) the blinding is deterministic; otherwise OS randomness."""
+    k = _Keep()
+    items, outs = _proof_gen_items(k, reqs)
+    res = (Result * len(reqs))()
+    if seeds is None:
+        _call("cubbs_bbs_gpu_proof_gen_batch_v2", ABI_VERSION, items, len(reqs), res)
+    else:
+        sb = ctypes.create_string_buffer(b"".join(seeds), 32 * len(seeds))
+        _call("cubbs_bbs_gpu_proof_gen_seeded_batch_v2", ABI_VERSION, items, len(reqs), sb, res)
+    return [(res[i].code, outs[i].raw[:items[i].proof_out.len]) for i in range(len(reqs))]
+
+
+def proof_verify_batch(reqs):
+    """reqs: list of (pk, proof, header, ph, [disclosed messages], [disclosed indexes], L)."""
+    k = _Keep()
+    items = (ProofVerifyItem * len(reqs))()
+    for i, (pk, proof, hdr, ph, dmsgs, didx, L) in enumerate(reqs):
+        items[i] = ProofVerifyItem(k.bytes(pk), k.bytes(proof), k.bytes(hdr), k.bytes(ph), k.slices(dmsgs),
+                                   len(dmsgs), k.index(didx), L)
+    res = (Result * len(reqs))()
+    _call("cubbs_bbs_gpu_proof_verify_batch_v2", ABI_VERSION, items, len(reqs), res)
+    return [(res[i].code, bool(res[i].value)) for i in range(len(reqs))]
+
+
+def messages_to_scalar(msgs, dst=MAP_DST):
+    k = _Keep()
+    items = (MessagesToScalarItem * len(msgs))()
+    outs = []
+    for i, m in enumerate(msgs):
+        ob, buf = k.out(32)
+        outs.append(buf)
+        items[i] = MessagesToScalarItem(k.bytes(m), k.bytes(dst), ob)
+    res = (Result * len(msgs))()
+    _call("cubbs_bbs_gpu_messages_to_scalar_batch_v2", ABI_VERSION, items, len(msgs), res)
+    return [outs[i].raw[:32] for i in range(len(msgs))]
+
+
+def _flat(msgs):
+    data = b"".join(msgs)
+    offs, cur = [], 0
+    for m in msgs:
+        offs.append(cur)
+        cur += len(m)
+    n = len(msgs)
+    return (ctypes.create_string_buffer(data, max(1, len(data))), (ctypes.c_size_t * max(1, n))(*offs),
+            (ctypes.c_size_t * max(1, n))(*[len(m) for m in msgs]))
+
+
+def sha256_batch(msgs):
+    d, o, l = _flat(msgs)
+    out = ctypes.create_string_buffer(32 * max(1, len(msgs)))
+    _call("cubbs_bbs_gpu_sha256_batch_for_test_v2", ABI_VERSION, d, o, l, ctypes.c_size_t(len(msgs)), out)
+    return [out.raw[32 * i:32 * i + 32] for i in range(len(msgs))]
+
+
+def expand_xmd48_batch(msgs, dst):
+    d, o, l = _flat(msgs)
+    out = ctypes.create_string_buffer(48 * max(1, len(msgs)))
+    _call("cubbs_bbs_gpu_expand_xmd_sha256_48_batch_for_test_v2", ABI_VERSION, d, o, l,
+          ctypes.c_size_t(len(msgs)), dst, ctypes.c_size_t(len(dst)), out)
+    return [out.raw[48 * i:48 * i + 48] for i in range(len(msgs))]
+
+
+def hash_to_scalar_batch(msgs, dst):
+    d, o, l = _flat(msgs)
+    out = ctypes.create_string_buffer(32 * max(1, len(msgs)))
+    _call("cubbs_bbs_gpu_hash_to_scalar_sha256_batch_for_test_v2", ABI_VERSION, d, o, l,
+          ctypes.c_size_t(len(msgs)), dst, ctypes.c_size_t(len(dst)), out)
+    return [out.raw[32 * i:32 * i + 32] for i in range(len(msgs))]
+
+
+def g1_msm_batch(msms):
+    """msms: list of ([points48], [scalars32]) -> list of (code, point48)."""
+    k = _Keep()
+    items = (G1MsmItem * len(msms))()
+    outs = []
+    for i, (pts, scs) in enumerate(msms):
+        ob, buf = k.out(48)
+        outs.append(buf)
+        items[i] = G1MsmItem(k.slices(pts), k.slices(scs), len(pts), ob)
+    res = (Result * len(msms))()
+    _call("cubbs_bbs_gpu_g1_msm_batch_v2", ABI_VERSION, items, len(msms), res)
+    return [(res[i].code, outs[i].raw[:48]) for i in range(len(msms))]
+
+
+def g1_msm_common_points(points, rows, fused=False, packed_scale=None):
+    """One group: common points, rows of scalars.  packed_scale: optional per-row
+    scale factors, sent through the packed (K+1)*32 stride form."""
+    k = _Keep()
+    R = len(rows)
+    outs = (ByteBuffer * max(1, R))()
+    bufs = []
+    for r in range(R):
+        ob, buf = k.out(48)
+        bufs.append(buf)
+        outs[r] = ob
+    item = G1MsmCommonPointsBatchItem()
+    item.points = k.slices(points)
+    item.term_count = len(points)
+    if packed_scale is None:
+        item.scalar_rows = k.slices([s for row in rows for s in row])
+        item.scalar_rows_be = None
+        item.scalar_row_stride = 0
+    else:
+        blob = b"".join(packed_scale[r] + b"".join(rows[r]) for r in range(R))
+        b = ctypes.create_string_buffer(blob, max(1, len(blob)))
+        k.refs.append(b)
+        item.scalar_rows = None
+        item.scalar_rows_be = ctypes.cast(b, ctypes.c_void_p)
+        item.scalar_row_stride = (len(points) + 1) * 32
+    item.output_count = R
+    item.point_outs = ctypes.cast(outs, ctypes.c_void_p)
+    res = (Result * max(1, R))()
+    name = "cubbs_bbs_gpu_g1_msm_fused_common_points_batch_v2" if fused else "cubbs_bbs_gpu_g1_msm_common_points_batch_v2"
+    _call(name, ABI_VERSION, (item), 1, res)
+    return [(res[r].code, res[r].value, bufs[r].raw[:48]) for r in range(R)]
+
+
+def g1_msm_common_points_plus_variable(points, rows, var_points, var_scalars):
+    k = _Keep()
+    R = len(rows)
+    outs = (ByteBuffer * max(1, R))()
+    bufs = []
+    for r in range(R):
+        ob, buf = k.out(48)
+        bufs.append(buf)
+        outs[r] = ob
+    item = G1MsmCommonPointsPlusVariableItem(k.slices(points), len(points), k.slices([s for row in rows for s in row]),
+                                             k.slices(var_points), k.slices(var_scalars), R,
+                                             ctypes.cast(outs, ctypes.c_void_p))
+    res = (Result * max(1, R))()
+    _call("cubbs_bbs_gpu_g1_msm_common_points_plus_variable_batch_v2", ABI_VERSION, (item), 1, res)
+    return [(res[r].code, bufs[r].raw[:48]) for r in range(R)]
+
+
+def proof_verify_msm_pair(points, rows, proof_points, proof_scalars):
+    """proof_points rows [Bbar, Abar, D]; proof_scalars rows [c, e^, r1^, r3^]."""
+    k = _Keep()
+    R = len(rows)
+    t1 = (ByteBuffer * max(1, R))()
+    t2 = (ByteBuffer * max(1, R))()
+    b1, b2 = [], []
+    for r in range(R):
+        o1, x1 = k.out(48)
+        o2, x2 = k.out(48)
+        t1[r], t2[r] = o1, o2
+        b1.append(x1)
+        b2.append(x2)
+    item = ProofVerifyMsmPairItem(k.slices(points), len(points), k.slices([s for row in rows for s in row]),
+                                  k.slices([p for row in proof_points for p in row]),
+                                  k.slices([s for row in proof_scalars for s in row]), R,
+                                  ctypes.cast(t1, ctypes.c_void_p), ctypes.cast(t2, ctypes.c_void_p))
+    res = (Result * max(1, R))()
+    _call("cubbs_bbs_gpu_proof_verify_msm_pair_batch_v2", ABI_VERSION, (item), 1, res)
+    return [(res[r].code, b1[r].raw[:48], b2[r].raw[:48]) for r in range(R)]
+
+
+def g1_dual_msm_same_points(points, lhs, rhs, lanes=None):
+    k = _Keep()
+    if lanes is None:
+        o1, x1 = k.out(48)
+        o2, x2 = k.out(48)
+        item = G1DualMsmSamePointsItem(k.slices(points), k.slices(lhs), k.slices(rhs), len(points), o1, o2)
+        res = Result()
+        _call("cubbs_bbs_gpu_g1_dual_msm_same_points_batch_v2", ABI_VERSION, (item), 1, (res))
+        return res.code, x1.raw[:48], x2.raw[:48]
+    o1, x1 = k.out(48 * lanes)
+    o2, x2 = k.out(48 * lanes)
+    item = G1DualMsmSamePointsLanesItem(k.slices(points), k.slices(lhs), k.slices(rhs), len(points), lanes, o1, o2)
+    res = Result()
+    _call("cubbs_bbs_gpu_g1_dual_msm_same_points_lanes_batch_v2", ABI_VERSION, (item), 1,
+          (res))
+    return res.code, [x1.raw[48 * j:48 * j + 48] for j in range(lanes)], [x2.raw[48 * j:48 * j + 48] for j in range(lanes)]
+
+
+def g1_add_batch(pairs):
+    k = _Keep()
+    items = (G1AddItem * len(pairs))()
+    bufs = []
+    for i, (a, b) in enumerate(pairs):
+        ob, buf = k.out(48)
+        bufs.append(buf)
+        items[i] = G1AddItem(k.bytes(a), k.bytes(b), ob)
+    res = (Result * len(pairs))()
+    _call("cubbs_bbs_gpu_g1_add_batch_v2", ABI_VERSION, items, len(pairs), res)
+    return [(res[i].code, bufs[i].raw[:48]) for i in range(len(pairs))]
+
+
+def prepare_b_batch(reqs):
+    """reqs: list of (pk, header64, [message scalars])."""
+    k = _Keep()
+    items = (PrepareBItem * len(reqs))()
+    bufs = []
+    for i, (pk, hdr, scs) in enumerate(reqs):
+        ob, buf = k.out(48)
+        bufs.append(buf)
+        items[i] = PrepareBItem(k.bytes(pk), k.bytes(hdr), k.slices(scs), len(scs), ob)
+    res = (Result * len(reqs))()
+    _call("cubbs_bbs_gpu_prepare_b_batch_v2", ABI_VERSION, items, len(reqs), res)
+    return [(res[i].code, bufs[i].raw[:48]) for i in range(len(reqs))]
+
+
+def proof_gen_t2_prepare(reqs):
+    """reqs: list of (B48, A48, [7 scalars]) -> list of (code, d, abar, bbar, t1)."""
+    k = _Keep()
+    items = (ProofGenT2PrepareItem * len(reqs))()
+    bufs = []
+    for i, (b, a, scs) in enumerate(reqs):
+        it = ProofGenT2PrepareItem()
+        it.compressed_b = k.bytes(b)
+        it.signature_a = k.bytes(a)
+        for s in range(7):
+            it.scalars_be[s] = k.bytes(scs[s])
+        it.seed = k.bytes(bytes(32))
+        outs = []
+        for f in ("d_out", "abar_out", "bbar_out", "t1_out"):
+            ob, buf = k.out(48)
+            setattr(it, f, ob)
+            outs.append(buf)
+        bufs.append(outs)
+        items[i] = it
+    res = (Result * len(reqs))()
+    _call("cubbs_bbs_gpu_proof_gen_t2_prepare_batch_v2", ABI_VERSION, items, len(reqs), res)
+    return [(res[i].code, *[b.raw[:48] for b in bufs[i]]) for i in range(len(reqs))]
+
+
+def pairing_eq_batch(reqs):
+    """reqs: list of (a48, b96, c48, d96): value = e(a, b) == e(c, d)."""
+    k = _Keep()
+    items = (PairingEqItem * len(reqs))()
+    for i, (a, b, c, d) in enumerate(reqs):
+        items[i] = PairingEqItem(k.bytes(a), k.bytes(b), k.bytes(c), k.bytes(d))
+    res = (Result * len(reqs))()
+    _call("cubbs_bbs_gpu_pairing_eq_batch_v2", ABI_VERSION, items, len(reqs), res)
+    return [(res[i].code, bool(res[i].value)) for i in range(len(reqs))]
+
+
+def pairing_eq_aggregate(reqs):
+    """reqs: list of (a48, b96, c48, d96, coef32) -> (code, value)."""
+    k = _Keep()
+    items = (PairingEqScaledItem * max(1, len(reqs)))()
+    for i, (a, b, c, d, co) in enumerate(reqs):
+        items[i] = PairingEqScaledItem(k.bytes(a), k.bytes(b), k.bytes(c), k.bytes(d), k.bytes(co))
+    res = Result()
+    _call("cubbs_bbs_gpu_pairing_eq_aggregate_v2", ABI_VERSION, items, len(reqs), (res))
+    return res.code, bool(res.value)

@@ -1,0 +1,351 @@
+// G1 / G2 group law, encodings and scalar multiplication on sm_103a.
+//
+// G1 accumulators use XYZZ coordinates (x = X/ZZ, y = Y/ZZZ; EFD formulas
+// madd-2008-s, add-2008-s, dbl-2008-s-1, mdbl-2008-s-1).  G2 uses Jacobian
+// coordinates over Fp2.  Encodings follow the zkcrypto/bls12_381_plus
+// compressed format used by the reference (G1 48 B, G2 96 B with x.c1 first;
+// flag bits: 0x80 compressed, 0x40 infinity, 0x20 y lexicographically largest;
+// reference decode/encode: native/cuda/src/g1_msm_blst.cpp:614-732).
+#pragma once
+#include "field.cuh"
+
+struct g1a { fp x, y; };               // affine, no infinity
+struct g1 { fp X, Y, ZZ, ZZZ; };       // XYZZ, ZZ == 0 is infinity
+
+DEV g1 g1_inf() { g1 r; r.X = fp_one(); r.Y = fp_one(); r.ZZ = fp_zero(); r.ZZZ = fp_zero(); return r; }
+DEV bool g1_is_inf(const g1 &p) { return fp_is_zero(p.ZZ); }
+DEV g1 g1_from_aff(const g1a &a) { g1 r; r.X = a.x; r.Y = a.y; r.ZZ = fp_one(); r.ZZZ = fp_one(); return r; }
+DEV g1 g1_neg(const g1 &p) { g1 r = p; r.Y = fp_neg(p.Y); return r; }
+DEV g1a g1a_neg(const g1a &p) { g1a r = p; r.y = fp_neg(p.y); return r; }
+
+DEVNI g1 g1_dbl(g1 p) {
+  if (g1_is_inf(p)) return p;
+  fp U = fp_dbl(p.Y);
+  fp V = fp_sqr(U);
+  fp W = fp_mul(U, V);
+  fp S = fp_mul(p.X, V);
+  fp X2 = fp_sqr(p.X);
+  fp M = fp_add(fp_dbl(X2), X2);
+  g1 r;
+  r.X = fp_sub(fp_sub(fp_sqr(M), S), S);
+  r.Y = fp_sub(fp_mul(M, fp_sub(S, r.X)), fp_mul(W, p.Y));
+  r.ZZ = fp_mul(V, p.ZZ);
+  r.ZZZ = fp_mul(W, p.ZZZ);
+  return r;
+}
+DEVNI g1 g1_dbl_aff(g1a p) {
+  fp U = fp_dbl(p.y);
+  fp V = fp_sqr(U);
+  fp W = fp_mul(U, V);
+  fp S = fp_mul(p.x, V);
+  fp X2 = fp_sqr(p.x);
+  fp M = fp_add(fp_dbl(X2), X2);
+  g1 r;
+  r.X = fp_sub(fp_sub(fp_sqr(M), S), S);
+  r.Y = fp_sub(fp_mul(M, fp_sub(S, r.X)), fp_mul(W, p.y));
+  r.ZZ = V;
+  r.ZZZ = W;
+  return r;
+}
+// p + q with q affine
+DEVNI g1 g1_add_aff(g1 p, g1a q) {
+  if (g1_is_inf(p)) return g1_from_aff(q);
+  fp U2 = fp_mul(q.x, p.ZZ);
+  fp S2 = fp_mul(q.y, p.ZZZ);
+  fp P = fp_sub(U2, p.X);
+  fp R = fp_sub(S2, p.Y);
+  if (fp_is_zero(P)) {
+    if (fp_is_zero(R)) return g1_dbl_aff(q);
+    return g1_inf();
+  }
+  fp PP = fp_sqr(P);
+  fp PPP = fp_mul(P, PP);
+  fp Q = fp_mul(p.X, PP);
+  g1 r;
+  r.X = fp_sub(fp_sub(fp_sqr(R), PPP), fp_dbl(Q));
+  r.Y = fp_sub(fp_mul(R, fp_sub(Q, r.X)), fp_mul(p.Y, PPP));
+  r.ZZ = fp_mul(p.ZZ, PP);
+  r.ZZZ = fp_mul(p.ZZZ, PPP);
+  return r;
+}
+DEVNI g1 g1_add(g1 p, g1 q) {
+  if (g1_is_inf(p)) return q;
+  if (g1_is_inf(q)) return p;
+  fp U1 = fp_mul(p.X, q.ZZ);
+  fp U2 = fp_mul(q.X, p.ZZ);
+  fp S1 = fp_mul(p.Y, q.ZZZ);
+  fp S2 = fp_mul(q.Y, p.ZZZ);
+  fp P = fp_sub(U2, U1);
+  fp R = fp_sub(S2, S1);
+  if (fp_is_zero(P)) {
+    if (fp_is_zero(R)) return g1_dbl(p);
+    return g1_inf();
+  }
+  fp PP = fp_sqr(P);
+  fp PPP = fp_mul(P, PP);
+  fp Q = fp_mul(U1, PP);
+  g1 r;
+  r.X = fp_sub(fp_sub(fp_sqr(R), PPP), fp_dbl(Q));
+  r.Y = fp_sub(fp_mul(R, fp_sub(Q, r.X)), fp_mul(S1, PPP));
+  r.ZZ = fp_mul(fp_mul(p.ZZ, q.ZZ), PP);
+  r.ZZZ = fp_mul(fp_mul(p.ZZZ, q.ZZZ), PPP);
+  return r;
+}
+// affine conversion with a single inversion; returns false for infinity
+DEVNI bool g1_to_aff(g1 p, g1a &out) {
+  if (g1_is_inf(p)) return false;
+  fp t = fp_inv(fp_mul(p.ZZ, p.ZZZ));
+  out.x = fp_mul(p.X, fp_mul(t, p.ZZZ));  // X / ZZ
+  out.y = fp_mul(p.Y, fp_mul(t, p.ZZ));   // Y / ZZZ
+  return true;
+}
+DEV bool g1_eq(const g1 &p, const g1 &q) {
+  bool pi = g1_is_inf(p), qi = g1_is_inf(q);
+  if (pi || qi) return pi && qi;
+  return fp_eq(fp_mul(p.X, q.ZZ), fp_mul(q.X, p.ZZ)) && fp_eq(fp_mul(p.Y, q.ZZZ), fp_mul(q.Y, p.ZZZ));
+}
+// GLV endomorphism image of an XYZZ point: [z^2]P = (beta x, -y)
+DEV g1 g1_endo(const g1 &p) {
+  const fp beta = C_GLV_BETA;
+  g1 r = p;
+  r.X = fp_mul(p.X, beta);
+  r.Y = fp_neg(p.Y);
+  return r;
+}
+
+// ---- encodings
+DEV void g1_compress_aff(const g1a &a, uint8_t out[48]) {
+  fp_to_be48(a.x, out);
+  out[0] |= 0x80;
+  if (fp_lex_largest(a.y)) out[0] |= 0x20;
+}
+DEVNI void g1_compress(g1 p, uint8_t out[48]) {
+  g1a a;
+  if (!g1_to_aff(p, a)) {
+    out[0] = 0xc0;
+    #pragma unroll 1
+    for (int i = 1; i < 48; i++) out[i] = 0;
+    return;
+  }
+  g1_compress_aff(a, out);
+}
+
+// [|z|]P for |z| = 0xd201000000010000 (bits 63,62,60,57,48,16)
+DEVNI g1 g1_mul_zabs(g1 p) {
+  g1 acc = p;
+  const uint64_t z = 0xd201000000010000ull;
+  #pragma unroll 1
+  for (int i = 62; i >= 0; i--) {
+    acc = g1_dbl(acc);
+    if ((z >> i) & 1) acc = g1_add(acc, p);
+  }
+  return acc;
+}
+// G1 membership for a curve point: phi(P) == -[z^2]P  <=>  [z^2]P == (beta x, -y)
+DEVNI bool g1_in_subgroup(g1a a) {
+  g1 t = g1_mul_zabs(g1_mul_zabs(g1_from_aff(a)));
+  if (g1_is_inf(t)) return false;
+  const fp beta = C_GLV_BETA;
+  fp bx = fp_mul(a.x, beta);
+  fp ny = fp_neg(a.y);
+  return fp_eq(t.X, fp_mul(bx, t.ZZ)) && fp_eq(t.Y, fp_mul(ny, t.ZZZ));
+}
+
+// Decode status values
+#define DEC_OK 0
+#define DEC_INF 1
+#define DEC_BAD 2
+// G1Affine::from_compressed (unchecked decode + torsion check).  Returns DEC_OK
+// with the affine point, DEC_INF for the canonical identity encoding, DEC_BAD otherwise.
+DEVNI int g1_decompress(const uint8_t in[48], g1a &out, bool check_subgroup = true) {
+  uint8_t f = in[0];
+  bool comp = f & 0x80, inf = f & 0x40, sort = f & 0x20;
+  uint8_t t[48];
+  t[0] = f & 0x1f;
+  #pragma unroll 1
+  for (int i = 1; i < 48; i++) t[i] = in[i];
+  fp x;
+  if (!fp_from_be48(t, x)) return DEC_BAD;
+  if (inf) return (comp && !sort && fp_is_zero(x)) ? DEC_INF : DEC_BAD;
+  if (!comp) return DEC_BAD;
+  const fp four = C_FP_FOUR;
+  fp y;
+  if (!fp_sqrt(fp_add(fp_mul(fp_sqr(x), x), four), y)) return DEC_BAD;
+  if (fp_lex_largest(y) != sort) y = fp_neg(y);
+  out.x = x;
+  out.y = y;
+  if (check_subgroup && !g1_in_subgroup(out)) return DEC_BAD;
+  return DEC_OK;
+}
+
+// ---- scalar multiplication (variable base, GLV + signed 4-bit windows)
+// Split k (canonical, < r) as k = q * lambda + s with lambda = z^2 (128-bit),
+// so k P = s P + q [lambda]P with [lambda]P = g1_endo(P).  Both halves are
+// below 2^128 (q < r / lambda < 2^128).
+DEVNI void glv_split(fr k, uint32_t s[4], uint32_t q[4]) {
+  // schoolbook shift-subtract long division of a 256-bit k by the 128-bit lambda
+  const uint64_t lam_lo = C_GLV_LAMBDA_LO, lam_hi = C_GLV_LAMBDA_HI;
+  uint64_t rem_lo = 0, rem_hi = 0;  // remainder < lambda < 2^128
+  uint64_t q_lo = 0, q_hi = 0;
+  #pragma unroll 1
+  for (int i = 255; i >= 0; i--) {
+    uint32_t bit = (k.w[i >> 5] >> (i & 31)) & 1;
+    // rem = rem*2 + bit (rem < 2^128 so rem*2 < 2^129: track the carry)
+    uint64_t carry = rem_hi >> 63;
+    rem_hi = (rem_hi << 1) | (rem_lo >> 63);
+    rem_lo = (rem_lo << 1) | bit;
+    bool ge = carry || rem_hi > lam_hi || (rem_hi == lam_hi && rem_lo >= lam_lo);
+    if (ge) {
+      uint64_t nlo = rem_lo - lam_lo;
+      uint64_t borrow = rem_lo < lam_lo ? 1 : 0;
+      rem_hi = rem_hi - lam_hi - borrow;
+      rem_lo = nlo;
+    }
+    // q = q*2 + ge  (q < 2^128)
+    q_hi = (q_hi << 1) | (q_lo >> 63);
+    q_lo = (q_lo << 1) | (ge ? 1 : 0);
+  }
+  s[0] = (uint32_t)rem_lo; s[1] = (uint32_t)(rem_lo >> 32); s[2] = (uint32_t)rem_hi; s[3] = (uint32_t)(rem_hi >> 32);
+  q[0] = (uint32_t)q_lo; q[1] = (uint32_t)(q_lo >> 32); q[2] = (uint32_t)q_hi; q[3] = (uint32_t)(q_hi >> 32);
+}
+// signed 4-bit digits of a 128-bit value: 33 digits in [-7, 8]
+DEV void recode_w4(const uint32_t v[4], int8_t d[33]) {
+  int carry = 0;
+  for (int i = 0; i < 32; i++) {
+    int x = (int)((v[i >> 3] >> ((i & 7) * 4)) & 15) + carry;
+    if (x > 8) { x -= 16; carry = 1; } else { carry = 0; }
+    d[i] = (int8_t)x;
+  }
+  d[32] = (int8_t)carry;
+}
+// k * P (P affine, k canonical raw Fr).  Returns XYZZ.
+DEVNI g1 g1_mul_glv(g1a p, fr k) {
+  uint32_t s[4], q[4];
+  glv_split(k, s, q);
+  int8_t ds[33], dq[33];
+  recode_w4(s, ds);
+  recode_w4(q, dq);
+  g1 tab[8];
+  tab[0] = g1_from_aff(p);
+  tab[1] = g1_dbl_aff(p);
+  #pragma unroll 1
+  for (int i = 2; i < 8; i++) tab[i] = g1_add_aff(tab[i - 1], p);
+  g1 acc = g1_inf();
+  #pragma unroll 1
+  for (int i = 32; i >= 0; i--) {
+    if (i != 32) {
+      acc = g1_dbl(acc); acc = g1_dbl(acc); acc = g1_dbl(acc); acc = g1_dbl(acc);
+    }
+    int a = ds[i];
+    if (a) {
+      g1 t = tab[(a > 0 ? a : -a) - 1];
+      acc = g1_add(acc, a > 0 ? t : g1_neg(t));
+    }
+    int b = dq[i];
+    if (b) {
+      g1 t = g1_endo(tab[(b > 0 ? b : -b) - 1]);
+      acc = g1_add(acc, b > 0 ? t : g1_neg(t));
+    }
+  }
+  return acc;
+}
+
+// ------------------------------------------------------------------ G2 (Jacobian over Fp2)
+struct g2a { fp2 x, y; };
+struct g2j { fp2 X, Y, Z; };
+
+DEV fp2 g2_b() { const fp four = C_FP_FOUR; return {four, four}; }
+DEV bool g2j_is_inf(const g2j &p) { return fp2_is_zero(p.Z); }
+DEV g2j g2j_inf() { return {fp2_one(), fp2_one(), fp2_zero()}; }
+DEV g2j g2j_from_aff(const g2a &a) { return {a.x, a.y, fp2_one()}; }
+DEVNI g2j g2j_dbl(g2j p) {
+  if (g2j_is_inf(p)) return p;
+  fp2 A = fp2_sqr(p.X), B = fp2_sqr(p.Y), C = fp2_sqr(B);
+  fp2 D = fp2_dbl(fp2_sub(fp2_sub(fp2_sqr(fp2_add(p.X, B)), A), C));
+  fp2 E = fp2_add(fp2_dbl(A), A), F = fp2_sqr(E);
+  g2j r;
+  r.X = fp2_sub(F, fp2_dbl(D));
+  fp2 C8 = fp2_dbl(fp2_dbl(fp2_dbl(C)));
+  r.Y = fp2_sub(fp2_mul(E, fp2_sub(D, r.X)), C8);
+  r.Z = fp2_dbl(fp2_mul(p.Y, p.Z));
+  return r;
+}
+DEVNI g2j g2j_add(g2j p, g2j q) {
+  if (g2j_is_inf(p)) return q;
+  if (g2j_is_inf(q)) return p;
+  fp2 Z1Z1 = fp2_sqr(p.Z), Z2Z2 = fp2_sqr(q.Z);
+  fp2 U1 = fp2_mul(p.X, Z2Z2), U2 = fp2_mul(q.X, Z1Z1);
+  fp2 S1 = fp2_mul(fp2_mul(p.Y, q.Z), Z2Z2), S2 = fp2_mul(fp2_mul(q.Y, p.Z), Z1Z1);
+  if (fp2_eq(U1, U2)) {
+    if (fp2_eq(S1, S2)) return g2j_dbl(p);
+    return g2j_inf();
+  }
+  fp2 H = fp2_sub(U2, U1), I = fp2_sqr(fp2_dbl(H)), J = fp2_mul(H, I);
+  fp2 rr = fp2_dbl(fp2_sub(S2, S1));
+  fp2 V = fp2_mul(U1, I);
+  g2j r;
+  r.X = fp2_sub(fp2_sub(fp2_sqr(rr), J), fp2_dbl(V));
+  r.Y = fp2_sub(fp2_mul(rr, fp2_sub(V, r.X)), fp2_dbl(fp2_mul(S1, J)));
+  r.Z = fp2_mul(fp2_sub(fp2_sub(fp2_sqr(fp2_add(p.Z, q.Z)), Z1Z1), Z2Z2), H);
+  return r;
+}
+DEV g2j g2j_neg(const g2j &p) { return {p.X, fp2_neg(p.Y), p.Z}; }
+DEVNI bool g2j_to_aff(g2j p, g2a &out) {
+  if (g2j_is_inf(p)) return false;
+  fp2 zi = fp2_inv(p.Z), zi2 = fp2_sqr(zi);
+  out.x = fp2_mul(p.X, zi2);
+  out.y = fp2_mul(fp2_mul(p.Y, zi2), zi);
+  return true;
+}
+// [r]P == O (naive membership test, used once per public key)
+DEVNI bool g2_in_subgroup(g2a a) {
+  const fr rm = FR_MOD_INIT;
+  g2j p = g2j_from_aff(a), acc = g2j_inf();
+  #pragma unroll 1
+  for (int i = 254; i >= 0; i--) {
+    acc = g2j_dbl(acc);
+    if ((rm.w[i >> 5] >> (i & 31)) & 1) acc = g2j_add(acc, p);
+  }
+  return g2j_is_inf(acc);
+}
+DEVNI g2j g2j_mul_raw(g2a a, fr k) {
+  g2j p = g2j_from_aff(a), acc = g2j_inf();
+  #pragma unroll 1
+  for (int i = 255; i >= 0; i--) {
+    acc = g2j_dbl(acc);
+    if ((k.w[i >> 5] >> (i & 31)) & 1) acc = g2j_add(acc, p);
+  }
+  return acc;
+}
+DEVNI int g2_decompress(const uint8_t in[96], g2a &out) {
+  uint8_t f = in[0];
+  bool comp = f & 0x80, inf = f & 0x40, sort = f & 0x20;
+  uint8_t t[48];
+  t[0] = f & 0x1f;
+  #pragma unroll 1
+  for (int i = 1; i < 48; i++) t[i] = in[i];
+  fp2 x;
+  if (!fp_from_be48(t, x.c1) || !fp_from_be48(in + 48, x.c0)) return DEC_BAD;
+  if (inf) return (comp && !sort && fp2_is_zero(x)) ? DEC_INF : DEC_BAD;
+  if (!comp) return DEC_BAD;
+  fp2 y;
+  if (!fp2_sqrt(fp2_add(fp2_mul(fp2_sqr(x), x), g2_b()), y)) return DEC_BAD;
+  if (fp2_lex_largest(y) != sort) y = fp2_neg(y);
+  out.x = x;
+  out.y = y;
+  if (!g2_in_subgroup(out)) return DEC_BAD;
+  return DEC_OK;
+}
+DEV void g2_compress_aff(const g2a &a, uint8_t out[96]) {
+  fp_to_be48(a.x.c1, out);
+  fp_to_be48(a.x.c0, out + 48);
+  out[0] |= 0x80;
+  if (fp2_lex_largest(a.y)) out[0] |= 0x20;
+}
+DEV g2a g2_generator() {
+  g2a g;
+  const fp x0 = C_G2_GEN_X0, x1 = C_G2_GEN_X1, y0 = C_G2_GEN_Y0, y1 = C_G2_GEN_Y1;
+  g.x = {x0, x1};
+  g.y = {y0, y1};
+  return g;
+}

@@ -1,0 +1,374 @@
+// BLS12-381 field tower on sm_103a: Fp (12 x 32-bit limbs, Montgomery,
+// R = 2^384), Fr (8 x 32-bit limbs, R = 2^256), Fp2 = Fp[u]/(u^2+1),
+// Fp6 = Fp2[v]/(v^3 - (1+u)), Fp12 = Fp6[w]/(w^2 - v).
+//
+// The tower and encodings follow the curve arithmetic the reference protocol
+// delegates to (bls12_381_plus 0.8.18; reference device types are SPPARK
+// fp_t/fr_t/fp2_t, prepare_b_msm.cu:40-49, pairing.cuh:3-321).  Multiplication
+// is CIOS over inline-PTX carry chains generated by gen_field_ptx.py.
+#pragma once
+#include <stdint.h>
+
+#include "curve_constants.cuh"
+#include "field_ptx.cuh"
+
+#define DEV __device__ __forceinline__
+#define DEVNI static __device__ __noinline__
+
+struct fp { uint32_t w[12]; };
+struct fr { uint32_t w[8]; };
+struct fp2 { fp c0, c1; };
+struct fp6 { fp2 c0, c1, c2; };
+struct fp12 { fp6 c0, c1; };
+
+// ------------------------------------------------------------------ Fp
+DEV fp fp_zero() { fp r; _Pragma("unroll") for (int i = 0; i < 12; i++) r.w[i] = 0; return r; }
+DEV fp fp_one() { const fp r = C_FP_ONE; return r; }
+DEV bool fp_is_zero(const fp &a) {
+  uint32_t x = 0;
+  _Pragma("unroll") for (int i = 0; i < 12; i++) x |= a.w[i];
+  return x == 0;
+}
+DEV bool fp_eq(const fp &a, const fp &b) {
+  uint32_t x = 0;
+  _Pragma("unroll") for (int i = 0; i < 12; i++) x |= a.w[i] ^ b.w[i];
+  return x == 0;
+}
+DEV fp fp_add(const fp &a, const fp &b) { fp r; fp_add_raw(r.w, a.w, b.w); return r; }
+DEV fp fp_sub(const fp &a, const fp &b) { fp r; fp_sub_raw(r.w, a.w, b.w); return r; }
+DEV fp fp_dbl(const fp &a) { return fp_add(a, a); }
+DEV fp fp_neg(const fp &a) { return fp_sub(fp_zero(), a); }
+DEV fp fp_mul(const fp &a, const fp &b) {
+  uint32_t t[25];
+  _Pragma("unroll") for (int i = 0; i < 13; i++) t[i] = 0;
+  _Pragma("unroll") for (int i = 0; i < 12; i++) {
+    t[i + 12] = 0;
+    fp_cios_row(&t[i], a.w, b.w[i]);
+  }
+  fp r;
+  fp_reduce_once(r.w, &t[12]);
+  return r;
+}
+DEV fp fp_sqr(const fp &a) { return fp_mul(a, a); }
+// raw canonical limbs (little-endian words) -> Montgomery
+DEV fp fp_to_mont(const fp &a) { const fp r2 = FP_R2_INIT; return fp_mul(a, r2); }
+DEV fp fp_from_mont(const fp &a) { fp one = fp_zero(); one.w[0] = 1; return fp_mul(a, one); }
+DEV bool fp_lt_mod(const fp &a) {  // canonical a < p ?
+  const fp m = FP_MOD_INIT;
+  _Pragma("unroll") for (int i = 11; i >= 0; i--) {
+    if (a.w[i] != m.w[i]) return a.w[i] < m.w[i];
+  }
+  return false;
+}
+// square-and-multiply by a 12-word exponent (most significant word first scan)
+DEV fp fp_pow(const fp &a, const uint32_t *e, int nwords) {
+  fp r = fp_one();
+  #pragma unroll 1
+  for (int i = nwords * 32 - 1; i >= 0; i--) {
+    r = fp_sqr(r);
+    if ((e[i >> 5] >> (i & 31)) & 1) r = fp_mul(r, a);
+  }
+  return r;
+}
+// a^(p-2) via 4-bit fixed windows
+DEVNI fp fp_pow_window(fp a, const uint32_t *e) {
+  fp tab[16];
+  tab[0] = fp_one();
+  tab[1] = a;
+  #pragma unroll 1
+  for (int i = 2; i < 16; i++) tab[i] = fp_mul(tab[i - 1], a);
+  fp r = fp_one();
+  #pragma unroll 1
+  for (int i = 95; i >= 0; i--) {
+    r = fp_sqr(r); r = fp_sqr(r); r = fp_sqr(r); r = fp_sqr(r);
+    uint32_t nib = (e[i >> 3] >> ((i & 7) * 4)) & 15;
+    if (nib) r = fp_mul(r, tab[nib]);
+  }
+  return r;
+}
+DEVNI fp fp_inv(fp a) {
+  // p - 2
+  const uint32_t e[12] = {0xffffaaa9u, 0xb9feffffu, 0xb153ffffu, 0x1eabfffeu, 0xf6b0f624u, 0x6730d2a0u,
+                          0xf38512bfu, 0x64774b84u, 0x434bacd7u, 0x4b1ba7b6u, 0x397fe69au, 0x1a0111eau};
+  return fp_pow_window(a, e);
+}
+// sqrt for p = 3 mod 4: s = a^((p+1)/4); returns false if a is not a square.
+DEVNI bool fp_sqrt(fp a, fp &out) {
+  const uint32_t e[12] = {0xffffeaabu, 0xee7fbfffu, 0xac54ffffu, 0x07aaffffu, 0x3dac3d89u, 0xd9cc34a8u,
+                          0x3ce144afu, 0xd91dd2e1u, 0x90d2eb35u, 0x92c6e9edu, 0x8e5ff9a6u, 0x0680447au};
+  fp s = fp_pow_window(a, e);
+  out = s;
+  return fp_eq(fp_sqr(s), a);
+}
+// canonical value > (p-1)/2 ?
+DEVNI bool fp_lex_largest(fp a) {
+  fp c = fp_from_mont(a);
+  // (p-1)/2
+  const uint32_t h[12] = {0xffffd555u, 0xdcff7fffu, 0x58a9ffffu, 0x0f55ffffu, 0x7b587b12u, 0xb3986950u,
+                          0x79c2895fu, 0xb23ba5c2u, 0x21a5d66bu, 0x258dd3dbu, 0x1cbff34du, 0x0d0088f5u};
+  _Pragma("unroll") for (int i = 11; i >= 0; i--) {
+    if (c.w[i] != h[i]) return c.w[i] > h[i];
+  }
+  return false;
+}
+DEV bool fp_parity(const fp &a) { return fp_from_mont(a).w[0] & 1; }
+// 48-byte big-endian canonical encoding (flag bits must be cleared by the caller)
+DEVNI bool fp_from_be48(const uint8_t *b, fp &out) {
+  fp c;
+  _Pragma("unroll") for (int i = 0; i < 12; i++) {
+    const uint8_t *q = b + (11 - i) * 4;
+    c.w[i] = ((uint32_t)q[0] << 24) | ((uint32_t)q[1] << 16) | ((uint32_t)q[2] << 8) | q[3];
+  }
+  if (!fp_lt_mod(c)) return false;
+  out = fp_to_mont(c);
+  return true;
+}
+DEVNI void fp_to_be48(fp a, uint8_t *b) {
+  fp c = fp_from_mont(a);
+  _Pragma("unroll") for (int i = 0; i < 12; i++) {
+    uint8_t *q = b + (11 - i) * 4;
+    q[0] = (uint8_t)(c.w[i] >> 24); q[1] = (uint8_t)(c.w[i] >> 16);
+    q[2] = (uint8_t)(c.w[i] >> 8); q[3] = (uint8_t)c.w[i];
+  }
+}
+// OS2IP(64 bytes) mod p: value = hi*2^384 + lo, hi < 2^128
+DEVNI fp fp_from_be64_mod(const uint8_t *b) {
+  fp lo, hi = fp_zero();
+  _Pragma("unroll") for (int i = 0; i < 12; i++) {
+    const uint8_t *q = b + 16 + (11 - i) * 4;
+    lo.w[i] = ((uint32_t)q[0] << 24) | ((uint32_t)q[1] << 16) | ((uint32_t)q[2] << 8) | q[3];
+  }
+  _Pragma("unroll") for (int i = 0; i < 4; i++) {
+    const uint8_t *q = b + (3 - i) * 4;
+    hi.w[i] = ((uint32_t)q[0] << 24) | ((uint32_t)q[1] << 16) | ((uint32_t)q[2] << 8) | q[3];
+  }
+  // lo < 2^384 < 10p: subtract p while lo >= p
+  const fp m = FP_MOD_INIT;
+  #pragma unroll 1
+  for (int k = 0; k < 10 && !fp_lt_mod(lo); k++) {
+    uint32_t borrow = 0;
+    _Pragma("unroll") for (int i = 0; i < 12; i++) {
+      uint64_t d = (uint64_t)lo.w[i] - m.w[i] - borrow;
+      lo.w[i] = (uint32_t)d;
+      borrow = (uint32_t)(d >> 63);
+    }
+  }
+  // hi*2^384 mod p = mont(hi * R^2) (a canonical value); both terms canonical -> add in canonical domain
+  const fp r2 = FP_R2_INIT;
+  fp h = fp_mul(hi, r2);
+  fp s = fp_add(h, lo);
+  return fp_to_mont(s);
+}
+DEV fp fp_select(bool c, const fp &a, const fp &b) {
+  fp r;
+  _Pragma("unroll") for (int i = 0; i < 12; i++) r.w[i] = c ? a.w[i] : b.w[i];
+  return r;
+}
+
+// ------------------------------------------------------------------ Fr
+DEV fr fr_zero() { fr r; _Pragma("unroll") for (int i = 0; i < 8; i++) r.w[i] = 0; return r; }
+DEV fr fr_one() { const fr r = FR_ONE_INIT; return r; }
+DEV bool fr_is_zero(const fr &a) {
+  uint32_t x = 0;
+  _Pragma("unroll") for (int i = 0; i < 8; i++) x |= a.w[i];
+  return x == 0;
+}
+DEV bool fr_eq(const fr &a, const fr &b) {
+  uint32_t x = 0;
+  _Pragma("unroll") for (int i = 0; i < 8; i++) x |= a.w[i] ^ b.w[i];
+  return x == 0;
+}
+DEV fr fr_add(const fr &a, const fr &b) { fr r; fr_add_raw(r.w, a.w, b.w); return r; }
+DEV fr fr_sub(const fr &a, const fr &b) { fr r; fr_sub_raw(r.w, a.w, b.w); return r; }
+DEV fr fr_mul(const fr &a, const fr &b) {
+  uint32_t t[17];
+  _Pragma("unroll") for (int i = 0; i < 9; i++) t[i] = 0;
+  _Pragma("unroll") for (int i = 0; i < 8; i++) {
+    t[i + 8] = 0;
+    fr_cios_row(&t[i], a.w, b.w[i]);
+  }
+  fr r;
+  fr_reduce_once(r.w, &t[8]);
+  return r;
+}
+DEV fr fr_to_mont(const fr &a) { const fr r2 = FR_R2_INIT; return fr_mul(a, r2); }
+DEV fr fr_from_mont(const fr &a) { fr one = fr_zero(); one.w[0] = 1; return fr_mul(a, one); }
+DEV bool fr_lt_mod(const fr &a) {
+  const fr m = FR_MOD_INIT;
+  _Pragma("unroll") for (int i = 7; i >= 0; i--) {
+    if (a.w[i] != m.w[i]) return a.w[i] < m.w[i];
+  }
+  return false;
+}
+DEVNI fr fr_inv(fr a) {
+  // r - 2
+  const uint32_t e[8] = {0xffffffffu, 0xfffffffeu, 0xfffe5bfeu, 0x53bda402u,
+                         0x09a1d805u, 0x3339d808u, 0x299d7d48u, 0x73eda753u};
+  fr tab[16];
+  tab[0] = fr_one();
+  tab[1] = a;
+  #pragma unroll 1
+  for (int i = 2; i < 16; i++) tab[i] = fr_mul(tab[i - 1], a);
+  fr r = fr_one();
+  #pragma unroll 1
+  for (int i = 63; i >= 0; i--) {
+    r = fr_mul(r, r); r = fr_mul(r, r); r = fr_mul(r, r); r = fr_mul(r, r);
+    uint32_t nib = (e[i >> 3] >> ((i & 7) * 4)) & 15;
+    if (nib) r = fr_mul(r, tab[nib]);
+  }
+  return r;
+}
+// canonical 32-byte big-endian -> raw canonical words; false if >= r
+DEV bool fr_raw_from_be32(const uint8_t *b, fr &out) {
+  _Pragma("unroll") for (int i = 0; i < 8; i++) {
+    const uint8_t *q = b + (7 - i) * 4;
+    out.w[i] = ((uint32_t)q[0] << 24) | ((uint32_t)q[1] << 16) | ((uint32_t)q[2] << 8) | q[3];
+  }
+  return fr_lt_mod(out);
+}
+DEV void fr_raw_to_be32(const fr &c, uint8_t *b) {
+  _Pragma("unroll") for (int i = 0; i < 8; i++) {
+    uint8_t *q = b + (7 - i) * 4;
+    q[0] = (uint8_t)(c.w[i] >> 24); q[1] = (uint8_t)(c.w[i] >> 16);
+    q[2] = (uint8_t)(c.w[i] >> 8); q[3] = (uint8_t)c.w[i];
+  }
+}
+// OS2IP(48 bytes) mod r (Scalar::from_okm): value = hi*2^256 + lo, hi < 2^128.  Returns
+// the CANONICAL (non-Montgomery) residue.
+DEVNI fr fr_raw_from_okm(const uint8_t *b) {
+  fr lo, hi = fr_zero();
+  _Pragma("unroll") for (int i = 0; i < 8; i++) {
+    const uint8_t *q = b + 16 + (7 - i) * 4;
+    lo.w[i] = ((uint32_t)q[0] << 24) | ((uint32_t)q[1] << 16) | ((uint32_t)q[2] << 8) | q[3];
+  }
+  _Pragma("unroll") for (int i = 0; i < 4; i++) {
+    const uint8_t *q = b + (3 - i) * 4;
+    hi.w[i] = ((uint32_t)q[0] << 24) | ((uint32_t)q[1] << 16) | ((uint32_t)q[2] << 8) | q[3];
+  }
+  const fr m = FR_MOD_INIT;
+  #pragma unroll 1
+  for (int k = 0; k < 3 && !fr_lt_mod(lo); k++) {
+    uint32_t borrow = 0;
+    _Pragma("unroll") for (int i = 0; i < 8; i++) {
+      uint64_t d = (uint64_t)lo.w[i] - m.w[i] - borrow;
+      lo.w[i] = (uint32_t)d;
+      borrow = (uint32_t)(d >> 63);
+    }
+  }
+  const fr r2 = FR_R2_INIT;
+  fr h = fr_mul(hi, r2);  // hi * 2^256 mod r, canonical
+  return fr_add(h, lo);
+}
+
+// ------------------------------------------------------------------ Fp2
+DEV fp2 fp2_zero() { return {fp_zero(), fp_zero()}; }
+DEV fp2 fp2_one() { return {fp_one(), fp_zero()}; }
+DEV bool fp2_is_zero(const fp2 &a) { return fp_is_zero(a.c0) && fp_is_zero(a.c1); }
+DEV bool fp2_eq(const fp2 &a, const fp2 &b) { return fp_eq(a.c0, b.c0) && fp_eq(a.c1, b.c1); }
+DEV fp2 fp2_add(const fp2 &a, const fp2 &b) { return {fp_add(a.c0, b.c0), fp_add(a.c1, b.c1)}; }
+DEV fp2 fp2_sub(const fp2 &a, const fp2 &b) { return {fp_sub(a.c0, b.c0), fp_sub(a.c1, b.c1)}; }
+DEV fp2 fp2_dbl(const fp2 &a) { return fp2_add(a, a); }
+DEV fp2 fp2_neg(const fp2 &a) { return {fp_neg(a.c0), fp_neg(a.c1)}; }
+DEV fp2 fp2_conj(const fp2 &a) { return {a.c0, fp_neg(a.c1)}; }
+DEVNI fp2 fp2_mul(fp2 a, fp2 b) {
+  fp t0 = fp_mul(a.c0, b.c0), t1 = fp_mul(a.c1, b.c1);
+  fp t2 = fp_mul(fp_add(a.c0, a.c1), fp_add(b.c0, b.c1));
+  return {fp_sub(t0, t1), fp_sub(fp_sub(t2, t0), t1)};
+}
+DEVNI fp2 fp2_sqr(fp2 a) {
+  // (a0 + a1)(a0 - a1) + 2 a0 a1 u
+  fp t = fp_mul(a.c0, a.c1);
+  return {fp_mul(fp_add(a.c0, a.c1), fp_sub(a.c0, a.c1)), fp_dbl(t)};
+}
+DEV fp2 fp2_mul_fp(const fp2 &a, const fp &s) { return {fp_mul(a.c0, s), fp_mul(a.c1, s)}; }
+DEV fp2 fp2_mul_xi(const fp2 &a) { return {fp_sub(a.c0, a.c1), fp_add(a.c0, a.c1)}; }  // *(1+u)
+DEVNI fp2 fp2_inv(fp2 a) {
+  fp n = fp_inv(fp_add(fp_sqr(a.c0), fp_sqr(a.c1)));
+  return {fp_mul(a.c0, n), fp_neg(fp_mul(a.c1, n))};
+}
+DEV bool fp2_lex_largest(const fp2 &a) {
+  if (!fp_is_zero(a.c1)) return fp_lex_largest(a.c1);
+  return fp_lex_largest(a.c0);
+}
+// square root in Fp2 via the norm: for a = a0 + a1 u, sqrt(a) = x0 + x1 u with
+// x0^2 = (a0 +- sqrt(a0^2+a1^2))/2, x1 = a1/(2 x0).
+DEVNI bool fp2_sqrt(fp2 a, fp2 &out) {
+  if (fp_is_zero(a.c1)) {
+    fp s;
+    if (fp_sqrt(a.c0, s)) { out = {s, fp_zero()}; return true; }
+    if (fp_sqrt(fp_neg(a.c0), s)) { out = {fp_zero(), s}; return true; }
+    return false;
+  }
+  fp n = fp_add(fp_sqr(a.c0), fp_sqr(a.c1)), s;
+  if (!fp_sqrt(n, s)) return false;
+  const fp inv2 = C_FP_INV2;
+  fp t = fp_mul(fp_add(a.c0, s), inv2), x0;
+  if (!fp_sqrt(t, x0)) {
+    t = fp_mul(fp_sub(a.c0, s), inv2);
+    if (!fp_sqrt(t, x0)) return false;
+  }
+  fp x1 = fp_mul(a.c1, fp_inv(fp_dbl(x0)));
+  fp2 r = {x0, x1};
+  if (!fp2_eq(fp2_sqr(r), a)) return false;
+  out = r;
+  return true;
+}
+
+// ------------------------------------------------------------------ Fp6
+DEV fp6 fp6_zero() { return {fp2_zero(), fp2_zero(), fp2_zero()}; }
+DEV fp6 fp6_one() { return {fp2_one(), fp2_zero(), fp2_zero()}; }
+DEV fp6 fp6_add(const fp6 &a, const fp6 &b) { return {fp2_add(a.c0, b.c0), fp2_add(a.c1, b.c1), fp2_add(a.c2, b.c2)}; }
+DEV fp6 fp6_sub(const fp6 &a, const fp6 &b) { return {fp2_sub(a.c0, b.c0), fp2_sub(a.c1, b.c1), fp2_sub(a.c2, b.c2)}; }
+DEV fp6 fp6_neg(const fp6 &a) { return {fp2_neg(a.c0), fp2_neg(a.c1), fp2_neg(a.c2)}; }
+DEV bool fp6_eq(const fp6 &a, const fp6 &b) { return fp2_eq(a.c0, b.c0) && fp2_eq(a.c1, b.c1) && fp2_eq(a.c2, b.c2); }
+DEVNI fp6 fp6_mul(fp6 a, fp6 b) {
+  fp2 a0 = fp2_mul(a.c0, b.c0), a1 = fp2_mul(a.c1, b.c1), a2 = fp2_mul(a.c2, b.c2);
+  fp2 t0 = fp2_add(fp2_mul_xi(fp2_sub(fp2_sub(fp2_mul(fp2_add(a.c1, a.c2), fp2_add(b.c1, b.c2)), a1), a2)), a0);
+  fp2 t1 = fp2_add(fp2_sub(fp2_sub(fp2_mul(fp2_add(a.c0, a.c1), fp2_add(b.c0, b.c1)), a0), a1), fp2_mul_xi(a2));
+  fp2 t2 = fp2_add(fp2_sub(fp2_sub(fp2_mul(fp2_add(a.c0, a.c2), fp2_add(b.c0, b.c2)), a0), a2), a1);
+  return {t0, t1, t2};
+}
+DEV fp6 fp6_mul_v(const fp6 &a) { return {fp2_mul_xi(a.c2), a.c0, a.c1}; }
+DEVNI fp6 fp6_inv(fp6 a) {
+  fp2 t0 = fp2_sub(fp2_sqr(a.c0), fp2_mul_xi(fp2_mul(a.c1, a.c2)));
+  fp2 t1 = fp2_sub(fp2_mul_xi(fp2_sqr(a.c2)), fp2_mul(a.c0, a.c1));
+  fp2 t2 = fp2_sub(fp2_sqr(a.c1), fp2_mul(a.c0, a.c2));
+  fp2 d = fp2_add(fp2_mul(a.c0, t0), fp2_mul_xi(fp2_add(fp2_mul(a.c2, t1), fp2_mul(a.c1, t2))));
+  d = fp2_inv(d);
+  return {fp2_mul(t0, d), fp2_mul(t1, d), fp2_mul(t2, d)};
+}
+
+// ------------------------------------------------------------------ Fp12
+DEV fp12 fp12_one() { return {fp6_one(), fp6_zero()}; }
+DEV bool fp12_eq(const fp12 &a, const fp12 &b) { return fp6_eq(a.c0, b.c0) && fp6_eq(a.c1, b.c1); }
+DEV bool fp12_is_one(const fp12 &a) { return fp12_eq(a, fp12_one()); }
+DEVNI fp12 fp12_mul(fp12 a, fp12 b) {
+  fp6 t0 = fp6_mul(a.c0, b.c0), t1 = fp6_mul(a.c1, b.c1);
+  fp6 t2 = fp6_sub(fp6_sub(fp6_mul(fp6_add(a.c0, a.c1), fp6_add(b.c0, b.c1)), t0), t1);
+  return {fp6_add(t0, fp6_mul_v(t1)), t2};
+}
+DEVNI fp12 fp12_sqr(fp12 a) {
+  // (a0 + a1 w)^2 = (a0^2 + v a1^2) + 2 a0 a1 w ; via (a0+a1)(a0+v a1) - a0a1 - v a0a1
+  fp6 ab = fp6_mul(a.c0, a.c1);
+  fp6 t = fp6_mul(fp6_add(a.c0, a.c1), fp6_add(a.c0, fp6_mul_v(a.c1)));
+  fp6 c0 = fp6_sub(fp6_sub(t, ab), fp6_mul_v(ab));
+  return {c0, fp6_add(ab, ab)};
+}
+DEV fp12 fp12_conj(const fp12 &a) { return {a.c0, fp6_neg(a.c1)}; }
+DEVNI fp12 fp12_inv(fp12 a) {
+  fp6 t = fp6_inv(fp6_sub(fp6_mul(a.c0, a.c0), fp6_mul_v(fp6_mul(a.c1, a.c1))));
+  return {fp6_mul(a.c0, t), fp6_neg(fp6_mul(a.c1, t))};
+}
+// Frobenius x -> x^p: conjugate each Fp2 coefficient and scale the basis
+// element w^k by gamma_k = xi^(k(p-1)/6).
+DEVNI fp12 fp12_frobenius(fp12 a) {
+  const fp2 g[6] = C_FROB_GAMMA;
+  fp12 r;
+  r.c0.c0 = fp2_conj(a.c0.c0);
+  r.c0.c1 = fp2_mul(fp2_conj(a.c0.c1), g[2]);
+  r.c0.c2 = fp2_mul(fp2_conj(a.c0.c2), g[4]);
+  r.c1.c0 = fp2_mul(fp2_conj(a.c1.c0), g[1]);
+  r.c1.c1 = fp2_mul(fp2_conj(a.c1.c1), g[3]);
+  r.c1.c2 = fp2_mul(fp2_conj(a.c1.c2), g[5]);
+  return r;
+}

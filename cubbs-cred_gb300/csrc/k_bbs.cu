@@ -1,0 +1,1067 @@
+// The four BBS operations, fully on the device, behind the required ABI
+// symbols (reference stubs: native/cuda/src/cubbs_bbs_cuda.cu:826-835,1169-1200).
+//
+// Protocol steps follow crates/cubbs-bbs-protocol/src/bbsplus/signature.rs:
+// 544-728 (Sign, Verify) and proof.rs:1568-1867, 2155-2426, 3015-3078
+// (ProofGen, ProofVerify); Verify uses the fixed-G2 rewrite
+// e(A, PK) * e(B - e A, -P2) == 1 (crates/cubbs-bbs/src/execution.rs:390-430)
+// so both G2 arguments have resident Miller lines.
+//
+// Pipeline per batch (one stream): hash messages -> decode points -> domain ->
+// per-item scalar prep (Fr) -> fixed-base MSM against the generator tables +
+// GLV variable-base terms -> per-item finish (compress, challenge hash) ->
+// 2-pair pairing check.  The host only validates argument shapes, sorts
+// disclosed indexes, packs bytes and copies results back.
+#include <sys/random.h>
+
+#include <algorithm>
+#include <cstring>
+
+#include "runtime.cuh"
+#include "sha256.cuh"
+
+namespace cubbs {
+
+// ----------------------------------------------------------------------------- raw Fr helpers
+DEVNI fr frr_mul(fr a, fr b) { return fr_mul(a, fr_to_mont(b)); }
+DEVNI fr frr_inv(fr a) { return fr_from_mont(fr_inv(fr_to_mont(a))); }
+DEV fr frr_neg(const fr &a) { return fr_sub(fr_zero(), a); }
+DEV fr frr_one() { fr r = fr_zero(); r.w[0] = 1; return r; }
+
+__device__ __constant__ static const uint8_t API_ID_K[44] = {
+    'B', 'B', 'S', '_', 'B', 'L', 'S', '1', '2', '3', '8', '1', 'G', '1', '_', 'X', 'M', 'D', ':', 'S', 'H', 'A',
+    '-', '2', '5', '6', '_', 'S', 'S', 'W', 'U', '_', 'R', 'O', '_', 'H', '2', 'G', '_', 'H', 'M', '2', 'S', '_'};
+
+DEV void h2s_dst(uint8_t dst[48]) {
+  for (int k = 0; k < 44; k++) dst[k] = API_ID_K[k];
+  dst[44] = 'H'; dst[45] = '2'; dst[46] = 'S'; dst[47] = '_';
+}
+DEV void sha_fr_be(sha_ctx &c, const fr &raw) {
+  uint8_t b[32];
+  fr_raw_to_be32(raw, b);
+  sha_bytes(c, b, 32);
+}
+
+// Item status codes kept on the device
+#define ST_OK 0
+#define ST_INVALID 1      // verification input does not decode: value 0
+#define ST_ERROR 2        // per-item error (code INVALID_INPUT)
+
+// ============================================================================ ProofVerify
+struct PvItem {
+  uint32_t proof_off, U, hdr_off, hdr_len, ph_off, ph_len, idx_off, R, msg_base, L;
+  int32_t pk_slot, pk_status;
+  int32_t status;  // host-side status
+};
+
+// Parse the scalars of the proof, build the T2 fixed-base row and the four
+// variable-base jobs (Bbar*c, Abar*e^, D*r1^, D*r3^).
+__global__ void __launch_bounds__(128) k_pv_prep(PvItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
+                                                 const fr *domain, const int32_t *dec_status, fr *rows,
+                                                 uint32_t stride, uint32_t *nterms, VarJob *jobs, fr *jscal) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  PvItem it = items[i];
+  bool ok = it.status == ST_OK && it.pk_status != DEC_BAD;
+  #pragma unroll 1
+  for (int k = 0; k < 3 && ok; k++) ok = dec_status[3 * i + k] != DEC_BAD;
+  const uint8_t *pr = blob + it.proof_off;
+  fr ecap, r1cap, r3cap, c;
+  if (ok) ok = fr_raw_from_be32(pr + 144, ecap) && fr_raw_from_be32(pr + 176, r1cap) &&
+               fr_raw_from_be32(pr + 208, r3cap) && fr_raw_from_be32(pr + 240 + 32 * it.U, c);
+  #pragma unroll 1
+  for (uint32_t j = 0; j < it.U && ok; j++) {
+    fr t;
+    ok = fr_raw_from_be32(pr + 240 + 32 * j, t);
+  }
+  fr *row = rows + (size_t)i * stride;
+  if (!ok) {
+    items[i].status = ST_INVALID;
+    nterms[i] = 0;
+    for (int k = 0; k < 4; k++) jobs[4 * i + k] = {0, 1};
+    return;
+  }
+  nterms[i] = it.L + 2;
+  row[0] = c;
+  row[1] = frr_mul(domain[i], c);
+  const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
+  uint32_t k = 0, u = 0;
+  #pragma unroll 1
+  for (uint32_t m = 0; m < it.L; m++) {
+    if (k < it.R && idx[k] == m) {
+      row[2 + m] = frr_mul(msc[it.msg_base + k], c);
+      k++;
+    } else {
+      fr t;
+      fr_raw_from_be32(pr + 240 + 32 * u, t);
+      row[2 + m] = t;
+      u++;
+    }
+  }
+  // points: 3i+0 Abar, 3i+1 Bbar, 3i+2 D
+  uint32_t fa = dec_status[3 * i] == DEC_INF, fb = dec_status[3 * i + 1] == DEC_INF, fd = dec_status[3 * i + 2] == DEC_INF;
+  jobs[4 * i + 0] = {3 * i + 1, fb};
+  jscal[4 * i + 0] = c;
+  jobs[4 * i + 1] = {3 * i + 0, fa};
+  jscal[4 * i + 1] = ecap;
+  jobs[4 * i + 2] = {3 * i + 2, fd};
+  jscal[4 * i + 2] = r1cap;
+  jobs[4 * i + 3] = {3 * i + 2, fd};
+  jscal[4 * i + 3] = r3cap;
+}
+
+// T1, T2 -> compressed; recompute the challenge; set up the pairing job.
+__global__ void __launch_bounds__(64) k_pv_finish(PvItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
+                                                  const fr *domain, const g1 *t2fix, const g1 *v,
+                                                  const g1a *pts, const int32_t *dec_status, PairJob *pj) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  PvItem it = items[i];
+  PairJob job;
+  job.active = 0;
+  job.flags = 0;
+  job.slot_a = it.pk_slot < 0 ? 0 : it.pk_slot;
+  job.slot_b = 0;
+  job.pa = pts[3 * i];
+  job.pb = pts[3 * i + 1];
+  if (it.status != ST_OK) {
+    pj[i] = job;
+    return;
+  }
+  g1 T1 = g1_add(g1_add(v[4 * i], v[4 * i + 1]), v[4 * i + 2]);
+  g1 T2 = g1_add(t2fix[i], v[4 * i + 3]);
+  uint8_t t1c[48], t2c[48];
+  g1_compress(T1, t1c);
+  g1_compress(T2, t2c);
+  const uint8_t *pr = blob + it.proof_off;
+  const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
+  sha_ctx c;
+  xmd_begin(c);
+  sha_u64be(c, it.R, 8);
+  #pragma unroll 1
+  for (uint32_t k = 0; k < it.R; k++) {
+    sha_u64be(c, idx[k], 8);
+    sha_fr_be(c, msc[it.msg_base + k]);
+  }
+  sha_bytes(c, pr, 144);
+  sha_bytes(c, t1c, 48);
+  sha_bytes(c, t2c, 48);
+  sha_fr_be(c, domain[i]);
+  sha_u64be(c, it.ph_len, 8);
+  sha_bytes(c, blob + it.ph_off, it.ph_len);
+  uint8_t dst[48];
+  h2s_dst(dst);
+  fr ch = h2s_finish(c, dst, 48);
+  fr cp;
+  fr_raw_from_be32(pr + 240 + 32 * it.U, cp);
+  if (!fr_eq(ch, cp)) {
+    items[i].status = ST_INVALID;
+    pj[i] = job;
+    return;
+  }
+  job.active = 1;
+  if (dec_status[3 * i] == DEC_INF || it.pk_status == DEC_INF) job.flags |= 1;
+  if (dec_status[3 * i + 1] == DEC_INF) job.flags |= 2;
+  pj[i] = job;
+}
+
+// ============================================================================ Sign
+struct SignItem {
+  uint32_t sk_off, pk_off, hdr_off, hdr_len, msg_base, L;
+  int32_t pk_status;
+  int32_t status;
+};
+
+__global__ void __launch_bounds__(64) k_sign_prep(SignItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
+                                                  const fr *domain, fr *rows, uint32_t stride, uint32_t *nterms,
+                                                  fr *e_out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  SignItem it = items[i];
+  fr sk;
+  bool ok = it.status == ST_OK && it.pk_status != DEC_BAD && fr_raw_from_be32(blob + it.sk_off, sk);
+  if (!ok) {
+    items[i].status = ST_ERROR;
+    nterms[i] = 0;
+    return;
+  }
+  // e = hash_to_scalar(sk || m_1..m_L || domain, api_id || "H2S_")  (signature.rs:564-577)
+  sha_ctx c;
+  xmd_begin(c);
+  sha_fr_be(c, sk);
+  #pragma unroll 1
+  for (uint32_t k = 0; k < it.L; k++) sha_fr_be(c, msc[it.msg_base + k]);
+  sha_fr_be(c, domain[i]);
+  uint8_t dst[48];
+  h2s_dst(dst);
+  fr e = h2s_finish(c, dst, 48);
+  e_out[i] = e;
+  fr ske = fr_add(sk, e);
+  if (fr_is_zero(ske)) {
+    items[i].status = ST_ERROR;
+    nterms[i] = 0;
+    return;
+  }
+  // A = B / (sk + e) = sum_g (s_g / (sk + e)) G_g: scale the B row (execution.rs:3400-3447)
+  fr inv = frr_inv(ske);
+  fr *row = rows + (size_t)i * stride;
+  nterms[i] = it.L + 2;
+  row[0] = inv;
+  row[1] = frr_mul(domain[i], inv);
+  #pragma unroll 1
+  for (uint32_t k = 0; k < it.L; k++) row[2 + k] = frr_mul(msc[it.msg_base + k], inv);
+}
+
+__global__ void __launch_bounds__(64) k_sign_finish(SignItem *items, uint32_t n, const g1 *A, const fr *e,
+                                                    uint8_t *sig) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (items[i].status != ST_OK) return;
+  if (g1_is_inf(A[i])) {  // "A == Identity_G1" (signature.rs:653-657)
+    items[i].status = ST_ERROR;
+    return;
+  }
+  g1_compress(A[i], sig + 80 * (size_t)i);
+  fr_raw_to_be32(e[i], sig + 80 * (size_t)i + 48);
+}
+
+// ============================================================================ Verify
+struct VerifyItem {
+  uint32_t sig_off, hdr_off, hdr_len, msg_base, L;
+  int32_t pk_slot, pk_status;
+  int32_t status;
+};
+
+__global__ void __launch_bounds__(128) k_verify_prep(VerifyItem *items, uint32_t n, const uint8_t *blob,
+                                                     const fr *msc, const fr *domain, const int32_t *dec_status,
+                                                     fr *rows, uint32_t stride, uint32_t *nterms, VarJob *jobs,
+                                                     fr *jscal) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  VerifyItem it = items[i];
+  fr e;
+  bool ok = it.status == ST_OK && it.pk_status != DEC_BAD && dec_status[i] != DEC_BAD &&
+            fr_raw_from_be32(blob + it.sig_off + 48, e);
+  if (!ok) {
+    if (items[i].status == ST_OK) items[i].status = ST_INVALID;
+    nterms[i] = 0;
+    jobs[i] = {i, 1};
+    return;
+  }
+  fr *row = rows + (size_t)i * stride;
+  nterms[i] = it.L + 2;
+  row[0] = frr_one();
+  row[1] = domain[i];
+  #pragma unroll 1
+  for (uint32_t k = 0; k < it.L; k++) row[2 + k] = msc[it.msg_base + k];
+  jobs[i] = {i, dec_status[i] == DEC_INF ? 1u : 0u};
+  jscal[i] = frr_neg(e);
+}
+
+__global__ void __launch_bounds__(64) k_verify_finish(const VerifyItem *items, uint32_t n, const g1 *B,
+                                                      const g1 *v, const g1a *A, const int32_t *dec_status,
+                                                      PairJob *pj) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  VerifyItem it = items[i];
+  PairJob job;
+  job.active = 0;
+  job.flags = 0;
+  job.slot_a = it.pk_slot < 0 ? 0 : it.pk_slot;
+  job.slot_b = 0;
+  job.pa = A[i];
+  if (it.status != ST_OK) {
+    job.pb = A[i];
+    pj[i] = job;
+    return;
+  }
+  g1 C = g1_add(B[i], v[i]);  // B - e A
+  g1a ca;
+  if (!g1_to_aff(C, ca)) {
+    ca = A[i];
+    job.flags |= 2;
+  }
+  job.pb = ca;
+  if (dec_status[i] == DEC_INF || it.pk_status == DEC_INF) job.flags |= 1;
+  job.active = 1;
+  pj[i] = job;
+}
+
+// ============================================================================ ProofGen
+struct PgItem {
+  uint32_t sig_off, hdr_off, hdr_len, ph_off, ph_len, idx_off, R, U, msg_base, L, seed_off, out_off;
+  int32_t pk_status;
+  int32_t status;
+};
+
+// seeded_random_scalars(5+U, seed, api_id || "MOCK_RANDOM_SCALARS_DST_") (util.rs:329-358);
+// more than 170 scalars are drawn in chunks keyed by seed || I2OSP(chunk, 2).
+__global__ void __launch_bounds__(64) k_pg_random(const PgItem *items, uint32_t n, const uint8_t *blob,
+                                                  fr *rs, uint32_t rs_stride) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  PgItem it = items[i];
+  if (it.status != ST_OK) return;
+  uint8_t dst[68];
+  for (int k = 0; k < 44; k++) dst[k] = API_ID_K[k];
+  const char *sfx = "MOCK_RANDOM_SCALARS_DST_";
+  for (int k = 0; k < 24; k++) dst[44 + k] = (uint8_t)sfx[k];
+  uint32_t count = 5 + it.U;
+  const uint32_t CH = 170;
+  fr *out = rs + (size_t)i * rs_stride;
+  #pragma unroll 1
+  for (uint32_t c0 = 0; c0 < count; c0 += CH) {
+    uint32_t m = min(CH, count - c0);
+    sha_ctx c;
+    xmd_begin(c);
+    sha_bytes(c, blob + it.seed_off, 32);
+    if (count > CH) {
+      uint32_t chunk = c0 / CH;
+      sha_byte(c, (uint8_t)(chunk >> 8));
+      sha_byte(c, (uint8_t)chunk);
+    }
+    // expand 48*m bytes, one 32-byte block at a time, reducing every 48 bytes
+    // (xmd_finish into a per-thread buffer of at most 8160 bytes would not fit in
+    // registers; stream the b_i blocks instead)
+    uint32_t nbytes = 48 * m;
+    sha_byte(c, (uint8_t)(nbytes >> 8));
+    sha_byte(c, (uint8_t)nbytes);
+    sha_byte(c, 0);
+    sha_bytes(c, dst, 68);
+    sha_byte(c, 68);
+    uint8_t b0[32], bi[32];
+    sha_final(c, b0);
+    uint8_t okm[48];
+    uint32_t fill = 0, produced = 0;
+    uint32_t ell = (nbytes + 31) / 32;
+    #pragma unroll 1
+    for (uint32_t b = 1; b <= ell; b++) {
+      sha_ctx s;
+      sha_init(s);
+      for (int j = 0; j < 32; j++) sha_byte(s, b == 1 ? b0[j] : (uint8_t)(b0[j] ^ bi[j]));
+      sha_byte(s, (uint8_t)b);
+      sha_bytes(s, dst, 68);
+      sha_byte(s, 68);
+      sha_final(s, bi);
+      for (int j = 0; j < 32; j++) {
+        okm[fill++] = bi[j];
+        if (fill == 48) {
+          out[c0 + produced] = fr_raw_from_okm(okm);
+          produced++;
+          fill = 0;
+        }
+      }
+    }
+  }
+}
+
+// rows 0..n-1: B = P1 + Q1 domain + sum H_i m_i ; rows n..2n-1: T2 fixed part sum_{j in U} H_j m~_j
+__global__ void __launch_bounds__(128) k_pg_prep(PgItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
+                                                 const fr *domain, const fr *rs, uint32_t rs_stride,
+                                                 const int32_t *dec_status, fr *rows, uint32_t stride,
+                                                 uint32_t *nterms) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  PgItem it = items[i];
+  fr e;
+  bool ok = it.status == ST_OK && it.pk_status != DEC_BAD && dec_status[i] != DEC_BAD &&
+            fr_raw_from_be32(blob + it.sig_off + 48, e);
+  if (!ok) {
+    items[i].status = ST_ERROR;
+    nterms[i] = 0;
+    nterms[n + i] = 0;
+    return;
+  }
+  fr *rb = rows + (size_t)i * stride;
+  fr *rt = rows + (size_t)(n + i) * stride;
+  nterms[i] = it.L + 2;
+  nterms[n + i] = it.L + 2;
+  rb[0] = frr_one();
+  rb[1] = domain[i];
+  rt[0] = fr_zero();
+  rt[1] = fr_zero();
+  const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
+  const fr *r = rs + (size_t)i * rs_stride;
+  uint32_t k = 0, u = 0;
+  #pragma unroll 1
+  for (uint32_t m = 0; m < it.L; m++) {
+    rb[2 + m] = msc[it.msg_base + m];
+    if (k < it.R && idx[k] == m) {
+      rt[2 + m] = fr_zero();
+      k++;
+    } else {
+      rt[2 + m] = r[5 + u];
+      u++;
+    }
+  }
+}
+
+// Variable-base jobs on B (affine) and A: D = r2 B, Abar = r1r2 A,
+// Bbar = r1r2 B - e r1r2 A, T1 = r1~ r2 B + e~ r1r2 A, T2 += r3~ r2 B.
+__global__ void __launch_bounds__(64) k_pg_vars(const PgItem *items, uint32_t n, const uint8_t *blob, const g1 *Bx,
+                                                const g1a *A, const int32_t *dec_status, const fr *rs,
+                                                uint32_t rs_stride, g1a *pts, VarJob *jobs, fr *jscal) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  PgItem it = items[i];
+  for (int k = 0; k < 7; k++) jobs[7 * i + k] = {2 * i, 1};
+  if (it.status != ST_OK) return;
+  g1a b;
+  bool binf = !g1_to_aff(Bx[i], b);
+  pts[2 * i] = A[i];
+  pts[2 * i + 1] = binf ? A[i] : b;
+  uint32_t fa = dec_status[i] == DEC_INF ? 1 : 0, fb = binf ? 1 : 0;
+  fr e;
+  fr_raw_from_be32(blob + it.sig_off + 48, e);
+  const fr *r = rs + (size_t)i * rs_stride;
+  fr r1 = r[0], r2 = r[1], et = r[2], r1t = r[3], r3t = r[4];
+  fr r1r2 = frr_mul(r1, r2);
+  jobs[7 * i + 0] = {2 * i + 1, fb}; jscal[7 * i + 0] = r2;
+  jobs[7 * i + 1] = {2 * i, fa};     jscal[7 * i + 1] = r1r2;
+  jobs[7 * i + 2] = {2 * i + 1, fb}; jscal[7 * i + 2] = r1r2;
+  jobs[7 * i + 3] = {2 * i, fa};     jscal[7 * i + 3] = frr_neg(frr_mul(e, r1r2));
+  jobs[7 * i + 4] = {2 * i + 1, fb}; jscal[7 * i + 4] = frr_mul(r1t, r2);
+  jobs[7 * i + 5] = {2 * i, fa};     jscal[7 * i + 5] = frr_mul(et, r1r2);
+  jobs[7 * i + 6] = {2 * i + 1, fb}; jscal[7 * i + 6] = frr_mul(r3t, r2);
+}
+
+__global__ void __launch_bounds__(64) k_pg_finish(PgItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
+                                                  const fr *domain, const fr *rs, uint32_t rs_stride,
+                                                  const g1 *t2fix, const g1 *v, uint8_t *out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  PgItem it = items[i];
+  if (it.status != ST_OK) return;
+  const g1 *vi = v + 7 * (size_t)i;
+  uint8_t *o = out + it.out_off;
+  g1 D = vi[0], Abar = vi[1];
+  g1 Bbar = g1_add(vi[2], vi[3]);
+  g1 T1 = g1_add(vi[4], vi[5]);
+  g1 T2 = g1_add(t2fix[i], vi[6]);
+  g1_compress(Abar, o);
+  g1_compress(Bbar, o + 48);
+  g1_compress(D, o + 96);
+  uint8_t t1c[48], t2c[48];
+  g1_compress(T1, t1c);
+  g1_compress(T2, t2c);
+  const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
+  sha_ctx c;
+  xmd_begin(c);
+  sha_u64be(c, it.R, 8);
+  #pragma unroll 1
+  for (uint32_t k = 0; k < it.R; k++) {
+    sha_u64be(c, idx[k], 8);
+    sha_fr_be(c, msc[it.msg_base + idx[k]]);
+  }
+  sha_bytes(c, o, 144);
+  sha_bytes(c, t1c, 48);
+  sha_bytes(c, t2c, 48);
+  sha_fr_be(c, domain[i]);
+  sha_u64be(c, it.ph_len, 8);
+  sha_bytes(c, blob + it.ph_off, it.ph_len);
+  uint8_t dst[48];
+  h2s_dst(dst);
+  fr ch = h2s_finish(c, dst, 48);
+  const fr *r = rs + (size_t)i * rs_stride;
+  fr r1 = r[0], r2 = r[1], et = r[2], r1t = r[3], r3t = r[4];
+  if (fr_is_zero(r2)) {  // "Invert scalar failed" (proof.rs:2340-2341)
+    items[i].status = ST_ERROR;
+    return;
+  }
+  fr e;
+  fr_raw_from_be32(blob + it.sig_off + 48, e);
+  fr r3 = frr_inv(r2);
+  fr_raw_to_be32(fr_add(et, frr_mul(e, ch)), o + 144);
+  fr_raw_to_be32(fr_sub(r1t, frr_mul(r1, ch)), o + 176);
+  fr_raw_to_be32(fr_sub(r3t, frr_mul(r3, ch)), o + 208);
+  uint32_t k = 0, u = 0;
+  #pragma unroll 1
+  for (uint32_t m = 0; m < it.L; m++) {
+    if (k < it.R && idx[k] == m) {
+      k++;
+      continue;
+    }
+    fr_raw_to_be32(fr_add(r[5 + u], frr_mul(msc[it.msg_base + m], ch)), o + 240 + 32 * u);
+    u++;
+  }
+  fr_raw_to_be32(ch, o + 240 + 32 * it.U);
+}
+
+// ============================================================================ host side
+namespace {
+
+bool abi_ok(uint32_t v) { return v == CUBBS_BBS_GPU_ABI_VERSION; }
+const size_t MAX_MESSAGES = 16384;  // generators kept resident: L + 2 <= 16386
+
+// Growable host byte blob (packed inputs for one batch).
+struct Blob {
+  std::vector<uint8_t> b;
+  uint32_t put(const uint8_t *p, size_t n) {
+    uint32_t off = (uint32_t)b.size();
+    if (n) b.insert(b.end(), p, p + n);
+    return off;
+  }
+  uint32_t put_u32s(const std::vector<uint32_t> &v) {
+    while (b.size() & 3) b.push_back(0);
+    uint32_t off = (uint32_t)b.size();
+    const uint8_t *p = reinterpret_cast<const uint8_t *>(v.data());
+    b.insert(b.end(), p, p + 4 * v.size());
+    return off;
+  }
+};
+
+struct MsgList {
+  std::vector<const uint8_t *> ptrs;
+  std::vector<size_t> lens;
+  size_t bytes = 0;
+  uint32_t add(const uint8_t *p, size_t n) {
+    ptrs.push_back(p);
+    lens.push_back(n);
+    bytes += n;
+    return (uint32_t)(ptrs.size() - 1);
+  }
+};
+
+template <typename T> T *upload(Runtime &rt, const T *h, size_t n) {
+  T *d = rt.arena.alloc<T>(n ? n : 1);
+  if (n) {
+    uint8_t *st = rt.staging.alloc(n * sizeof(T));
+    std::memcpy(st, h, n * sizeof(T));
+    CUBBS_CHECK(cudaMemcpyAsync(d, st, n * sizeof(T), cudaMemcpyHostToDevice, rt.stream));
+  }
+  return d;
+}
+
+// Upload the message list and hash it to scalars with api_id || MAP_MSG_TO_SCALAR_AS_HASH_.
+fr *hash_messages(Runtime &rt, const MsgList &ml) {
+  size_t n = ml.ptrs.size();
+  fr *out = rt.arena.alloc<fr>(n ? n : 1);
+  if (!n) return out;
+  uint8_t *h = rt.staging.alloc(ml.bytes + 8 * n);
+  uint32_t *ho = reinterpret_cast<uint32_t *>(h), *hl = ho + n;
+  uint8_t *hb = h + 8 * n;
+  size_t cur = 0;
+  #pragma unroll 1
+  for (size_t i = 0; i < n; i++) {
+    ho[i] = (uint32_t)cur;
+    hl[i] = (uint32_t)ml.lens[i];
+    if (ml.lens[i]) std::memcpy(hb + cur, ml.ptrs[i], ml.lens[i]);
+    cur += ml.lens[i];
+  }
+  uint8_t *d = rt.arena.alloc<uint8_t>(ml.bytes + 8 * n);
+  CUBBS_CHECK(cudaMemcpyAsync(d, h, ml.bytes + 8 * n, cudaMemcpyHostToDevice, rt.stream));
+  static const char MAP_DST[] = "BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_H2G_HM2S_MAP_MSG_TO_SCALAR_AS_HASH_";
+  uint8_t *ddst = upload(rt, reinterpret_cast<const uint8_t *>(MAP_DST), sizeof(MAP_DST) - 1);
+  launch_h2s_flat(rt.stream, d + 8 * n, reinterpret_cast<uint32_t *>(d), reinterpret_cast<uint32_t *>(d) + n,
+                  (uint32_t)n, ddst, sizeof(MAP_DST) - 1, out);
+  return out;
+}
+
+void sort_dedup(const size_t *p, size_t n, std::vector<size_t> &out) {
+  out.assign(p, p + n);
+  std::sort(out.begin(), out.end());
+  out.erase(std::unique(out.begin(), out.end()), out.end());
+}
+
+size_t reserve_for(size_t items, size_t maxL, size_t blob_bytes, size_t msgs) {
+  size_t stride = maxL + 2;
+  return 4096 + blob_bytes * 2 + msgs * 64 + items * (stride * 2 * sizeof(fr) + 16 * sizeof(g1) + 8 * sizeof(fr) +
+                                                      4 * sizeof(g1a) + sizeof(PairJob) + 512);
+}
+
+}  // namespace
+
+}  // namespace cubbs
+
+using namespace cubbs;
+
+// ----------------------------------------------------------------------------- ProofVerify
+extern "C" int32_t cubbs_bbs_gpu_proof_verify_batch_v2(uint32_t abi, const CuBbsBbsGpuProofVerifyItem *items,
+                                                       size_t n, CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
+  #pragma unroll 1
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    if (it.public_key.data == nullptr || it.public_key.len != 96 || (it.proof.len && !it.proof.data) ||
+        (it.header.len && !it.header.data) || (it.presentation_header.len && !it.presentation_header.data) ||
+        (it.disclosed_count && !it.disclosed_messages) ||
+        (it.disclosed_indexes.len && !it.disclosed_indexes.data))
+      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+    #pragma unroll 1
+    for (size_t k = 0; k < it.disclosed_count; k++)
+      if (it.disclosed_messages[k].len && !it.disclosed_messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  }
+  try {
+    Runtime &rt = Runtime::get();
+    CallScope scope(rt);
+    Blob blob;
+    MsgList ml;
+    std::vector<PvItem> hi(n);
+    std::vector<const uint8_t *> pks(n);
+    size_t maxL = 0;
+    std::vector<size_t> di;
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) {
+      const auto &it = items[i];
+      PvItem &p = hi[i];
+      std::memset(&p, 0, sizeof p);
+      pks[i] = it.public_key.data;
+      p.status = ST_OK;
+      size_t plen = it.proof.len;
+      sort_dedup(it.disclosed_indexes.data, it.disclosed_indexes.len, di);
+      size_t U = plen >= 272 ? (plen - 240) / 32 - 1 : 0;
+      size_t R = di.size(), L = U + R;
+      bool ok = plen >= 272 && it.disclosed_count == R && L <= MAX_MESSAGES;
+      #pragma unroll 1
+      for (size_t k = 0; k < R && ok; k++) ok = di[k] < L;
+      p.msg_base = (uint32_t)ml.ptrs.size();
+      if (!ok) {
+        p.status = ST_INVALID;
+        p.proof_off = blob.put(nullptr, 0);
+        continue;
+      }
+      #pragma unroll 1
+      for (size_t k = 0; k < it.disclosed_count; k++) ml.add(it.disclosed_messages[k].data, it.disclosed_messages[k].len);
+      p.U = (uint32_t)U;
+      p.R = (uint32_t)R;
+      p.L = (uint32_t)L;
+      p.proof_off = blob.put(it.proof.data, 240 + 32 * (U + 1));
+      p.hdr_off = blob.put(it.header.data, it.header.len);
+      p.hdr_len = (uint32_t)it.header.len;
+      p.ph_off = blob.put(it.presentation_header.data, it.presentation_header.len);
+      p.ph_len = (uint32_t)it.presentation_header.len;
+      std::vector<uint32_t> d32(di.begin(), di.end());
+      p.idx_off = blob.put_u32s(d32);
+      maxL = std::max(maxL, L);
+    }
+    std::vector<uint32_t> pk_off(n);
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) pk_off[i] = blob.put(pks[i], 96);
+    std::vector<int> slots, pst;
+    rt.resolve_pks(pks, slots, pst);
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) {
+      hi[i].pk_slot = slots[i];
+      hi[i].pk_status = pst[i];
+      if (pst[i] == DEC_BAD) hi[i].status = ST_ERROR;
+    }
+    rt.ensure_table((int)maxL + 2);
+    size_t stride = maxL + 2;
+    rt.arena.reserve(reserve_for(n, maxL, blob.b.size(), ml.ptrs.size()));
+    rt.staging.reserve(blob.b.size() * 2 + ml.bytes + 16 * ml.ptrs.size() + n * 256 + 65536);
+    cudaStream_t s = rt.stream;
+    uint8_t *dblob = upload(rt, blob.b.data(), blob.b.size());
+    fr *msc = hash_messages(rt, ml);
+    // decode Abar, Bbar, D (items that failed host checks decode a zero buffer -> DEC_BAD)
+    std::vector<uint8_t> pbytes(144 * n, 0);
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++)
+      if (hi[i].status == ST_OK) std::memcpy(&pbytes[144 * i], items[i].proof.data, 144);
+    uint8_t *dp = upload(rt, pbytes.data(), pbytes.size());
+    g1a *pts = rt.arena.alloc<g1a>(3 * n);
+    int32_t *dst = rt.arena.alloc<int32_t>(3 * n);
+    launch_g1_decode(s, dp, 48, (uint32_t)(3 * n), pts, dst, true);
+    std::vector<DomainJob> dj(n);
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) dj[i] = {pk_off[i], hi[i].hdr_off, hi[i].hdr_len, hi[i].L};
+    DomainJob *ddj = upload(rt, dj.data(), n);
+    fr *domain = rt.arena.alloc<fr>(n);
+    launch_domain(s, ddj, (uint32_t)n, dblob, rt.d_gens_c, domain);
+    PvItem *ditems = upload(rt, hi.data(), n);
+    fr *rows = rt.arena.alloc<fr>(n * stride);
+    uint32_t *nterms = rt.arena.alloc<uint32_t>(n);
+    VarJob *jobs = rt.arena.alloc<VarJob>(4 * n);
+    fr *jscal = rt.arena.alloc<fr>(4 * n);
+    k_pv_prep<<<blocks_for(n, 128), 128, 0, s>>>(ditems, (uint32_t)n, dblob, msc, domain, dst, rows,
+                                                 (uint32_t)stride, nterms, jobs, jscal);
+    g1 *t2fix = rt.arena.alloc<g1>(n);
+    launch_fixed_msm(s, rt.table, rows, (uint32_t)stride, nterms, (uint32_t)n, t2fix);
+    g1 *v = rt.arena.alloc<g1>(4 * n);
+    launch_var_mul(s, pts, jobs, jscal, (uint32_t)(4 * n), v);
+    PairJob *pj = rt.arena.alloc<PairJob>(n);
+    k_pv_finish<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, dblob, msc, domain, t2fix, v, pts, dst, pj);
+    uint8_t *ok = rt.arena.alloc<uint8_t>(n);
+    launch_pairing_check(s, pj, (uint32_t)n, rt.d_lines, ok);
+    CUBBS_CHECK(cudaGetLastError());
+    std::vector<uint8_t> hok(n);
+    std::vector<PvItem> hout(n);
+    CUBBS_CHECK(cudaMemcpyAsync(hok.data(), ok, n, cudaMemcpyDeviceToHost, s));
+    CUBBS_CHECK(cudaMemcpyAsync(hout.data(), ditems, n * sizeof(PvItem), cudaMemcpyDeviceToHost, s));
+    CUBBS_CHECK(cudaStreamSynchronize(s));
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) {
+      if (hout[i].status == ST_ERROR) results[i] = {CUBBS_BBS_GPU_ERR_INVALID_INPUT, 0, 0};
+      else results[i] = {CUBBS_BBS_GPU_SUCCESS, (uint8_t)(hout[i].status == ST_OK && hok[i] ? 1 : 0), 0};
+    }
+    return CUBBS_BBS_GPU_SUCCESS;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}
+
+// ----------------------------------------------------------------------------- Sign
+extern "C" int32_t cubbs_bbs_gpu_sign_batch_v2(uint32_t abi, CuBbsBbsGpuSignItem *items, size_t n,
+                                               CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
+  #pragma unroll 1
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    if (it.secret_key.data == nullptr || it.public_key.data == nullptr || (it.header.len && !it.header.data) ||
+        (it.message_count && !it.messages) || it.signature_out.data == nullptr)
+      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+    #pragma unroll 1
+    for (size_t k = 0; k < it.message_count; k++)
+      if (it.messages[k].len && !it.messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  }
+  try {
+    Runtime &rt = Runtime::get();
+    CallScope scope(rt);
+    Blob blob;
+    MsgList ml;
+    std::vector<SignItem> hi(n);
+    std::vector<const uint8_t *> pks(n);
+    std::vector<uint8_t> zero96(96, 0);
+    size_t maxL = 0;
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) {
+      const auto &it = items[i];
+      SignItem &p = hi[i];
+      std::memset(&p, 0, sizeof p);
+      bool ok = it.secret_key.len == 32 && it.public_key.len == 96 && it.signature_out.capacity >= 80 &&
+                it.message_count <= MAX_MESSAGES;
+      p.status = ok ? ST_OK : ST_ERROR;
+      pks[i] = it.public_key.len == 96 ? it.public_key.data : zero96.data();
+      p.sk_off = blob.put(ok ? it.secret_key.data : zero96.data(), 32);
+      p.pk_off = blob.put(pks[i], 96);
+      p.hdr_off = blob.put(it.header.data, it.header.len);
+      p.hdr_len = (uint32_t)it.header.len;
+      p.msg_base = (uint32_t)ml.ptrs.size();
+      p.L = ok ? (uint32_t)it.message_count : 0;
+      if (ok)
+        #pragma unroll 1
+        for (size_t k = 0; k < it.message_count; k++) ml.add(it.messages[k].data, it.messages[k].len);
+      maxL = std::max(maxL, (size_t)p.L);
+    }
+    std::vector<int> slots, pst;
+    rt.resolve_pks(pks, slots, pst);
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) hi[i].pk_status = pst[i];
+    rt.ensure_table((int)maxL + 2);
+    size_t stride = maxL + 2;
+    rt.arena.reserve(reserve_for(n, maxL, blob.b.size(), ml.ptrs.size()));
+    rt.staging.reserve(blob.b.size() * 2 + ml.bytes + 16 * ml.ptrs.size() + n * 256 + 65536);
+    cudaStream_t s = rt.stream;
+    uint8_t *dblob = upload(rt, blob.b.data(), blob.b.size());
+    fr *msc = hash_messages(rt, ml);
+    std::vector<DomainJob> dj(n);
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) dj[i] = {hi[i].pk_off, hi[i].hdr_off, hi[i].hdr_len, hi[i].L};
+    DomainJob *ddj = upload(rt, dj.data(), n);
+    fr *domain = rt.arena.alloc<fr>(n);
+    launch_domain(s, ddj, (uint32_t)n, dblob, rt.d_gens_c, domain);
+    SignItem *ditems = upload(rt, hi.data(), n);
+    fr *rows = rt.arena.alloc<fr>(n * stride);
+    uint32_t *nterms = rt.arena.alloc<uint32_t>(n);
+    fr *e = rt.arena.alloc<fr>(n);
+    k_sign_prep<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, dblob, msc, domain, rows, (uint32_t)stride,
+                                                 nterms, e);
+    g1 *A = rt.arena.alloc<g1>(n);
+    launch_fixed_msm(s, rt.table, rows, (uint32_t)stride, nterms, (uint32_t)n, A);
+    uint8_t *sig = rt.arena.alloc<uint8_t>(80 * n);
+    k_sign_finish<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, A, e, sig);
+    CUBBS_CHECK(cudaGetLastError());
+    std::vector<uint8_t> hsig(80 * n);
+    std::vector<SignItem> hout(n);
+    CUBBS_CHECK(cudaMemcpyAsync(hsig.data(), sig, 80 * n, cudaMemcpyDeviceToHost, s));
+    CUBBS_CHECK(cudaMemcpyAsync(hout.data(), ditems, n * sizeof(SignItem), cudaMemcpyDeviceToHost, s));
+    CUBBS_CHECK(cudaStreamSynchronize(s));
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) {
+      if (items[i].signature_out.capacity < 80 && items[i].secret_key.len == 32 && items[i].public_key.len == 96) {
+        results[i] = {CUBBS_BBS_GPU_ERR_INSUFFICIENT_OUTPUT, 0, 0};
+      } else if (hout[i].status != ST_OK) {
+        results[i] = {CUBBS_BBS_GPU_ERR_INVALID_INPUT, 0, 0};
+      } else {
+        std::memcpy(items[i].signature_out.data, &hsig[80 * i], 80);
+        items[i].signature_out.len = 80;
+        results[i] = {CUBBS_BBS_GPU_SUCCESS, 0, 80};
+      }
+    }
+    return CUBBS_BBS_GPU_SUCCESS;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}
+
+// ----------------------------------------------------------------------------- Verify
+extern "C" int32_t cubbs_bbs_gpu_verify_batch_v2(uint32_t abi, const CuBbsBbsGpuVerifyItem *items, size_t n,
+                                                 CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
+  #pragma unroll 1
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    if (it.public_key.data == nullptr || it.public_key.len != 96 || (it.signature.len && !it.signature.data) ||
+        (it.header.len && !it.header.data) || (it.message_count && !it.messages))
+      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+    #pragma unroll 1
+    for (size_t k = 0; k < it.message_count; k++)
+      if (it.messages[k].len && !it.messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  }
+  try {
+    Runtime &rt = Runtime::get();
+    CallScope scope(rt);
+    Blob blob;
+    MsgList ml;
+    std::vector<VerifyItem> hi(n);
+    std::vector<const uint8_t *> pks(n);
+    std::vector<uint8_t> sigA(48 * n, 0);
+    size_t maxL = 0;
+    std::vector<uint32_t> pk_off(n);
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) {
+      const auto &it = items[i];
+      VerifyItem &p = hi[i];
+      std::memset(&p, 0, sizeof p);
+      pks[i] = it.public_key.data;
+      bool ok = it.signature.len == 80 && it.message_count <= MAX_MESSAGES;
+      p.status = ok ? ST_OK : ST_INVALID;
+      static const uint8_t zeros[80] = {0};
+      p.sig_off = blob.put(ok ? it.signature.data : zeros, 80);
+      if (ok) std::memcpy(&sigA[48 * i], it.signature.data, 48);
+      pk_off[i] = blob.put(it.public_key.data, 96);
+      p.hdr_off = blob.put(it.header.data, it.header.len);
+      p.hdr_len = (uint32_t)it.header.len;
+      p.msg_base = (uint32_t)ml.ptrs.size();
+      p.L = ok ? (uint32_t)it.message_count : 0;
+      if (ok)
+        #pragma unroll 1
+        for (size_t k = 0; k < it.message_count; k++) ml.add(it.messages[k].data, it.messages[k].len);
+      maxL = std::max(maxL, (size_t)p.L);
+    }
+    std::vector<int> slots, pst;
+    rt.resolve_pks(pks, slots, pst);
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) {
+      hi[i].pk_slot = slots[i];
+      hi[i].pk_status = pst[i];
+      if (pst[i] == DEC_BAD) hi[i].status = ST_ERROR;
+    }
+    rt.ensure_table((int)maxL + 2);
+    size_t stride = maxL + 2;
+    rt.arena.reserve(reserve_for(n, maxL, blob.b.size(), ml.ptrs.size()));
+    rt.staging.reserve(blob.b.size() * 2 + ml.bytes + 16 * ml.ptrs.size() + n * 256 + 65536);
+    cudaStream_t s = rt.stream;
+    uint8_t *dblob = upload(rt, blob.b.data(), blob.b.size());
+    fr *msc = hash_messages(rt, ml);
+    uint8_t *dsa = upload(rt, sigA.data(), sigA.size());
+    g1a *A = rt.arena.alloc<g1a>(n);
+    int32_t *dst = rt.arena.alloc<int32_t>(n);
+    launch_g1_decode(s, dsa, 48, (uint32_t)n, A, dst, true);
+    std::vector<DomainJob> dj(n);
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) dj[i] = {pk_off[i], hi[i].hdr_off, hi[i].hdr_len, hi[i].L};
+    DomainJob *ddj = upload(rt, dj.data(), n);
+    fr *domain = rt.arena.alloc<fr>(n);
+    launch_domain(s, ddj, (uint32_t)n, dblob, rt.d_gens_c, domain);
+    VerifyItem *ditems = upload(rt, hi.data(), n);
+    fr *rows = rt.arena.alloc<fr>(n * stride);
+    uint32_t *nterms = rt.arena.alloc<uint32_t>(n);
+    VarJob *jobs = rt.arena.alloc<VarJob>(n);
+    fr *jscal = rt.arena.alloc<fr>(n);
+    k_verify_prep<<<blocks_for(n, 128), 128, 0, s>>>(ditems, (uint32_t)n, dblob, msc, domain, dst, rows,
+                                                     (uint32_t)stride, nterms, jobs, jscal);
+    g1 *B = rt.arena.alloc<g1>(n);
+    launch_fixed_msm(s, rt.table, rows, (uint32_t)stride, nterms, (uint32_t)n, B);
+    g1 *v = rt.arena.alloc<g1>(n);
+    launch_var_mul(s, A, jobs, jscal, (uint32_t)n, v);
+    PairJob *pj = rt.arena.alloc<PairJob>(n);
+    k_verify_finish<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, B, v, A, dst, pj);
+    uint8_t *ok = rt.arena.alloc<uint8_t>(n);
+    launch_pairing_check(s, pj, (uint32_t)n, rt.d_lines, ok);
+    CUBBS_CHECK(cudaGetLastError());
+    std::vector<uint8_t> hok(n);
+    std::vector<VerifyItem> hout(n);
+    CUBBS_CHECK(cudaMemcpyAsync(hok.data(), ok, n, cudaMemcpyDeviceToHost, s));
+    CUBBS_CHECK(cudaMemcpyAsync(hout.data(), ditems, n * sizeof(VerifyItem), cudaMemcpyDeviceToHost, s));
+    CUBBS_CHECK(cudaStreamSynchronize(s));
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) {
+      if (hout[i].status == ST_ERROR) results[i] = {CUBBS_BBS_GPU_ERR_INVALID_INPUT, 0, 0};
+      else results[i] = {CUBBS_BBS_GPU_SUCCESS, (uint8_t)(hout[i].status == ST_OK && hok[i] ? 1 : 0), 0};
+    }
+    return CUBBS_BBS_GPU_SUCCESS;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}
+
+// ----------------------------------------------------------------------------- ProofGen
+static int32_t proof_gen_impl(CuBbsBbsGpuProofGenItem *items, size_t n, const uint8_t (*seeds)[32],
+                              CuBbsBbsGpuResult *results) {
+  #pragma unroll 1
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    if (it.public_key.data == nullptr || it.public_key.len != 96 || (it.signature.len && !it.signature.data) ||
+        (it.header.len && !it.header.data) || (it.presentation_header.len && !it.presentation_header.data) ||
+        (it.message_count && !it.messages) || (it.disclosed_indexes.len && !it.disclosed_indexes.data) ||
+        it.proof_out.data == nullptr)
+      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+    #pragma unroll 1
+    for (size_t k = 0; k < it.message_count; k++)
+      if (it.messages[k].len && !it.messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  }
+  std::vector<uint8_t> os_seeds;
+  if (seeds == nullptr) {  // production blinding: 32 bytes of OS randomness per item
+    os_seeds.resize(32 * n);
+    size_t got = 0;
+    while (got < os_seeds.size()) {
+      ssize_t r = getrandom(os_seeds.data() + got, os_seeds.size() - got, 0);
+      if (r <= 0) return CUBBS_BBS_GPU_ERR_INTERNAL;
+      got += (size_t)r;
+    }
+  }
+  try {
+    Runtime &rt = Runtime::get();
+    CallScope scope(rt);
+    Blob blob;
+    MsgList ml;
+    std::vector<PgItem> hi(n);
+    std::vector<const uint8_t *> pks(n);
+    std::vector<uint8_t> sigA(48 * n, 0);
+    std::vector<uint32_t> pk_off(n);
+    std::vector<int32_t> code(n, CUBBS_BBS_GPU_SUCCESS);
+    size_t maxL = 0, maxU = 0, out_total = 0;
+    std::vector<size_t> di;
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) {
+      const auto &it = items[i];
+      PgItem &p = hi[i];
+      std::memset(&p, 0, sizeof p);
+      pks[i] = it.public_key.data;
+      sort_dedup(it.disclosed_indexes.data, it.disclosed_indexes.len, di);
+      size_t L = it.message_count, R = di.size();
+      bool ok = it.signature.len == 80 && L <= MAX_MESSAGES && R <= L;
+      #pragma unroll 1
+      for (size_t k = 0; k < R && ok; k++) ok = di[k] < L;
+      size_t U = ok ? L - R : 0;
+      size_t need = 272 + 32 * U;
+      if (ok && it.proof_out.capacity < need) {
+        code[i] = CUBBS_BBS_GPU_ERR_INSUFFICIENT_OUTPUT;
+        ok = false;
+      } else if (!ok) {
+        code[i] = CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+      }
+      p.status = ok ? ST_OK : ST_ERROR;
+      static const uint8_t zeros[80] = {0};
+      p.sig_off = blob.put(ok ? it.signature.data : zeros, 80);
+      if (ok) std::memcpy(&sigA[48 * i], it.signature.data, 48);
+      pk_off[i] = blob.put(it.public_key.data, 96);
+      p.hdr_off = blob.put(it.header.data, it.header.len);
+      p.hdr_len = (uint32_t)it.header.len;
+      p.ph_off = blob.put(it.presentation_header.data, it.presentation_header.len);
+      p.ph_len = (uint32_t)it.presentation_header.len;
+      std::vector<uint32_t> d32(di.begin(), di.end());
+      p.idx_off = blob.put_u32s(d32);
+      p.seed_off = blob.put(seeds ? seeds[i] : &os_seeds[32 * i], 32);
+      p.msg_base = (uint32_t)ml.ptrs.size();
+      p.L = ok ? (uint32_t)L : 0;
+      p.R = ok ? (uint32_t)R : 0;
+      p.U = (uint32_t)U;
+      p.out_off = (uint32_t)out_total;
+      if (ok) {
+        out_total += need;
+        #pragma unroll 1
+        for (size_t k = 0; k < L; k++) ml.add(it.messages[k].data, it.messages[k].len);
+      }
+      maxL = std::max(maxL, (size_t)p.L);
+      maxU = std::max(maxU, U);
+    }
+    std::vector<int> slots, pst;
+    rt.resolve_pks(pks, slots, pst);
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) {
+      hi[i].pk_status = pst[i];
+      if (pst[i] == DEC_BAD && hi[i].status == ST_OK) {
+        hi[i].status = ST_ERROR;
+        code[i] = CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+      }
+    }
+    rt.ensure_table((int)maxL + 2);
+    size_t stride = maxL + 2, rs_stride = maxU + 5;
+    rt.arena.reserve(reserve_for(2 * n, maxL, blob.b.size(), ml.ptrs.size()) + n * rs_stride * sizeof(fr) +
+                     out_total + 14 * n * sizeof(g1));
+    rt.staging.reserve(blob.b.size() * 2 + ml.bytes + 16 * ml.ptrs.size() + n * 256 + out_total + 65536);
+    cudaStream_t s = rt.stream;
+    uint8_t *dblob = upload(rt, blob.b.data(), blob.b.size());
+    fr *msc = hash_messages(rt, ml);
+    uint8_t *dsa = upload(rt, sigA.data(), sigA.size());
+    g1a *A = rt.arena.alloc<g1a>(n);
+    int32_t *dst = rt.arena.alloc<int32_t>(n);
+    launch_g1_decode(s, dsa, 48, (uint32_t)n, A, dst, true);
+    std::vector<DomainJob> dj(n);
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) dj[i] = {pk_off[i], hi[i].hdr_off, hi[i].hdr_len, hi[i].L};
+    DomainJob *ddj = upload(rt, dj.data(), n);
+    fr *domain = rt.arena.alloc<fr>(n);
+    launch_domain(s, ddj, (uint32_t)n, dblob, rt.d_gens_c, domain);
+    PgItem *ditems = upload(rt, hi.data(), n);
+    fr *rs = rt.arena.alloc<fr>(n * rs_stride);
+    k_pg_random<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, dblob, rs, (uint32_t)rs_stride);
+    fr *rows = rt.arena.alloc<fr>(2 * n * stride);
+    uint32_t *nterms = rt.arena.alloc<uint32_t>(2 * n);
+    k_pg_prep<<<blocks_for(n, 128), 128, 0, s>>>(ditems, (uint32_t)n, dblob, msc, domain, rs, (uint32_t)rs_stride,
+                                                 dst, rows, (uint32_t)stride, nterms);
+    g1 *fixed = rt.arena.alloc<g1>(2 * n);
+    launch_fixed_msm(s, rt.table, rows, (uint32_t)stride, nterms, (uint32_t)(2 * n), fixed);
+    g1a *pts = rt.arena.alloc<g1a>(2 * n);
+    VarJob *jobs = rt.arena.alloc<VarJob>(7 * n);
+    fr *jscal = rt.arena.alloc<fr>(7 * n);
+    k_pg_vars<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, dblob, fixed, A, dst, rs, (uint32_t)rs_stride,
+                                               pts, jobs, jscal);
+    g1 *v = rt.arena.alloc<g1>(7 * n);
+    launch_var_mul(s, pts, jobs, jscal, (uint32_t)(7 * n), v);
+    uint8_t *out = rt.arena.alloc<uint8_t>(out_total + 1);
+    k_pg_finish<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, dblob, msc, domain, rs, (uint32_t)rs_stride,
+                                                 fixed + n, v, out);
+    CUBBS_CHECK(cudaGetLastError());
+    std::vector<uint8_t> hout_b(out_total + 1);
+    std::vector<PgItem> hout(n);
+    CUBBS_CHECK(cudaMemcpyAsync(hout_b.data(), out, out_total + 1, cudaMemcpyDeviceToHost, s));
+    CUBBS_CHECK(cudaMemcpyAsync(hout.data(), ditems, n * sizeof(PgItem), cudaMemcpyDeviceToHost, s));
+    CUBBS_CHECK(cudaStreamSynchronize(s));
+    #pragma unroll 1
+    for (size_t i = 0; i < n; i++) {
+      if (code[i] != CUBBS_BBS_GPU_SUCCESS) {
+        results[i] = {code[i], 0, 0};
+      } else if (hout[i].status != ST_OK) {
+        results[i] = {CUBBS_BBS_GPU_ERR_INVALID_INPUT, 0, 0};
+      } else {
+        size_t need = 272 + 32 * (size_t)hi[i].U;
+        std::memcpy(items[i].proof_out.data, &hout_b[hi[i].out_off], need);
+        items[i].proof_out.len = need;
+        results[i] = {CUBBS_BBS_GPU_SUCCESS, 0, need};
+      }
+    }
+    return CUBBS_BBS_GPU_SUCCESS;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}
+
+extern "C" int32_t cubbs_bbs_gpu_proof_gen_batch_v2(uint32_t abi, CuBbsBbsGpuProofGenItem *items, size_t n,
+                                                    CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
+  return proof_gen_impl(items, n, nullptr, results);
+}
+
+extern "C" int32_t cubbs_bbs_gpu_proof_gen_seeded_batch_v2(uint32_t abi, CuBbsBbsGpuProofGenItem *items, size_t n,
+                                                           const uint8_t (*seeds)[32], CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr || seeds == nullptr)))
+    return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
+  return proof_gen_impl(items, n, seeds, results);
+}

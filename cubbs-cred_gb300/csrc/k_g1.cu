@@ -1,0 +1,177 @@
+// G1 kernels: point decoding (decompress + subgroup check), fixed-base window
+// tables over the resident generators, the fixed-base MSM (one warp per MSM
+// row, signed w-bit windows, affine table entries, mixed XYZZ additions),
+// GLV variable-base multiplication and point compression.
+//
+// Reference counterparts: comb tables and comb MSMs
+// (native/cuda/src/kernels/comb_precompute.cuh:8-268, comb_msm.cuh:3-363),
+// GLV variable base (kernels/variable_base_universal.cuh:25-331), BLST decode
+// and compress on the host (native/cuda/src/g1_msm_blst.cpp:614-732).  Here
+// decode and compress run on the device.
+#include "runtime.cuh"
+
+namespace cubbs {
+
+__global__ void __launch_bounds__(128) k_g1_decode(const uint8_t *pts, uint32_t stride, uint32_t n, g1a *out,
+                                                   int32_t *status, bool check_subgroup) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint8_t b[48];
+  for (int k = 0; k < 48; k++) b[k] = pts[(size_t)i * stride + k];
+  g1a a;
+  int st = g1_decompress(b, a, check_subgroup);
+  if (st != DEC_OK) {
+    a.x = fp_zero();
+    a.y = fp_zero();
+  }
+  out[i] = a;
+  status[i] = st;
+}
+
+// One thread per (generator, window): entries d * 2^(w k) G_g for d = 1..half,
+// normalised to affine with one batched inversion.
+__global__ void __launch_bounds__(64) k_table_build(const g1a *gens, int g0, int g1n, FixedTable t, g1 *scratch,
+                                                    fp *prod) {
+  int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  int total = (g1n - g0) * t.nwin;
+  if (tid >= total) return;
+  int g = g0 + tid / t.nwin, k = tid % t.nwin;
+  g1 B = g1_from_aff(gens[g]);
+  #pragma unroll 1
+  for (int i = 0; i < t.w * k; i++) B = g1_dbl(B);
+  g1a Ba;
+  g1_to_aff(B, Ba);
+  g1 *E = scratch + (size_t)tid * t.half;
+  fp *Pp = prod + (size_t)tid * t.half;
+  g1 e = g1_from_aff(Ba);
+  fp acc = fp_one();
+  #pragma unroll 1
+  for (int j = 0; j < t.half; j++) {
+    if (j > 0) e = g1_add_aff(e, Ba);
+    E[j] = e;
+    acc = fp_mul(acc, fp_mul(e.ZZ, e.ZZZ));
+    Pp[j] = acc;
+  }
+  fp inv = fp_inv(acc);  // inverse of prod_j ZZ_j ZZZ_j
+  g1a *dst = t.entries + ((size_t)g * t.nwin + k) * t.half;
+  #pragma unroll 1
+  for (int j = t.half - 1; j >= 0; j--) {
+    fp zinv = j > 0 ? fp_mul(inv, Pp[j - 1]) : inv;  // 1 / (ZZ_j ZZZ_j)
+    g1 ej = E[j];
+    inv = fp_mul(inv, fp_mul(ej.ZZ, ej.ZZZ));
+    g1a a;
+    a.x = fp_mul(ej.X, fp_mul(zinv, ej.ZZZ));
+    a.y = fp_mul(ej.Y, fp_mul(zinv, ej.ZZ));
+    dst[j] = a;
+  }
+}
+
+// w-bit field of a raw 256-bit scalar starting at bit pos
+DEV uint32_t scalar_bits(const fr &s, int pos, int w) {
+  if (pos >= 256) return 0;
+  int wi = pos >> 5, sh = pos & 31;
+  uint64_t lo = s.w[wi];
+  uint64_t hi = wi + 1 < 8 ? s.w[wi + 1] : 0;
+  uint64_t v = (lo | (hi << 32)) >> sh;
+  return (uint32_t)(v & ((1u << w) - 1));
+}
+
+DEV g1 shfl_down_g1(const g1 &p, int delta) {
+  g1 r;
+#pragma unroll
+  for (int i = 0; i < 12; i++) {
+    r.X.w[i] = __shfl_down_sync(0xffffffffu, p.X.w[i], delta);
+    r.Y.w[i] = __shfl_down_sync(0xffffffffu, p.Y.w[i], delta);
+    r.ZZ.w[i] = __shfl_down_sync(0xffffffffu, p.ZZ.w[i], delta);
+    r.ZZZ.w[i] = __shfl_down_sync(0xffffffffu, p.ZZZ.w[i], delta);
+  }
+  return r;
+}
+DEV g1 warp_sum_g1(g1 acc) {
+  #pragma unroll 1
+  for (int d = 16; d > 0; d >>= 1) {
+    g1 o = shfl_down_g1(acc, d);
+    acc = g1_add(acc, o);
+  }
+  return acc;
+}
+
+// Fixed-base MSM: row r = sum_g scalars[r*stride + g] * G_g, g < nterms[r].
+// One warp per row; lane l takes generators l, l+32, ...; per generator the
+// scalar is recoded into signed w-bit digits on the fly and each nonzero digit
+// costs one table lookup and one mixed addition.
+__global__ void __launch_bounds__(128) k_fixed_msm(FixedTable t, const fr *scalars, uint32_t stride,
+                                                   const uint32_t *nterms, uint32_t rows, g1 *out) {
+  uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  int lane = threadIdx.x & 31;
+  if (row >= rows) return;  // whole warp exits together
+  uint32_t n = nterms[row];
+  g1 acc = g1_inf();
+  const uint32_t full = 1u << t.w;
+  #pragma unroll 1
+  for (uint32_t g = lane; g < n; g += 32) {
+    fr s = scalars[(size_t)row * stride + g];
+    uint32_t carry = 0;
+    const g1a *base = t.entries + (size_t)g * t.nwin * t.half;
+    #pragma unroll 1
+    for (int k = 0; k < t.nwin; k++) {
+      uint32_t d = scalar_bits(s, k * t.w, t.w) + carry;
+      bool neg = false;
+      if (d > (uint32_t)t.half) {
+        d = full - d;
+        neg = true;
+        carry = 1;
+      } else {
+        carry = 0;
+      }
+      if (d) {
+        g1a e = base[(size_t)k * t.half + d - 1];
+        if (neg) e.y = fp_neg(e.y);
+        acc = g1_add_aff(acc, e);
+      }
+    }
+  }
+  acc = warp_sum_g1(acc);
+  if (lane == 0) out[row] = acc;
+}
+
+__global__ void __launch_bounds__(128) k_var_mul(const g1a *points, const VarJob *jobs, const fr *scalars,
+                                                 uint32_t n, g1 *out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  VarJob j = jobs[i];
+  if (j.flags & 1) {
+    out[i] = g1_inf();
+    return;
+  }
+  out[i] = g1_mul_glv(points[j.point], scalars[i]);
+}
+
+__global__ void __launch_bounds__(128) k_g1_compress(const g1 *pts, uint32_t n, uint8_t *out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint8_t b[48];
+  g1_compress(pts[i], b);
+  for (int k = 0; k < 48; k++) out[48 * (size_t)i + k] = b[k];
+}
+
+void launch_g1_decode(cudaStream_t s, const uint8_t *pts48, uint32_t stride, uint32_t n, g1a *out, int32_t *status,
+                      bool check_subgroup) {
+  if (n) k_g1_decode<<<blocks_for(n, 128), 128, 0, s>>>(pts48, stride, n, out, status, check_subgroup);
+}
+void launch_build_table(cudaStream_t s, const g1a *gens, int g0, int g1n, FixedTable t, g1 *scratch, fp *prod) {
+  int total = (g1n - g0) * t.nwin;
+  if (total > 0) k_table_build<<<blocks_for(total, 64), 64, 0, s>>>(gens, g0, g1n, t, scratch, prod);
+}
+void launch_fixed_msm(cudaStream_t s, const FixedTable &t, const fr *scalars, uint32_t stride,
+                      const uint32_t *nterms, uint32_t rows, g1 *out) {
+  if (rows) k_fixed_msm<<<blocks_for((size_t)rows * 32, 128), 128, 0, s>>>(t, scalars, stride, nterms, rows, out);
+}
+void launch_var_mul(cudaStream_t s, const g1a *points, const VarJob *jobs, const fr *scalars, uint32_t n, g1 *out) {
+  if (n) k_var_mul<<<blocks_for(n, 128), 128, 0, s>>>(points, jobs, scalars, n, out);
+}
+void launch_g1_compress(cudaStream_t s, const g1 *pts, uint32_t n, uint8_t *out48) {
+  if (n) k_g1_compress<<<blocks_for(n, 128), 128, 0, s>>>(pts, n, out48);
+}
+
+}  // namespace cubbs

@@ -1,0 +1,60 @@
+// Pairing kernels: G2 public-key preparation (decompress, subgroup check,
+// 68 Miller lines kept resident per key), the lines of +-P2, and the 2-pair
+// pairing check  e(P_a, Q_a) * e(P_b, Q_b) == 1  with a shared Miller loop
+// and one final exponentiation per check.
+//
+// Reference: G2 line precompute by BLST on the host (g1_msm_blst.cpp:441-486),
+// Miller loop over precomputed lines and final-verify kernels
+// (native/cuda/src/kernels/pairing.cuh:376-478, host :579-737).
+#include "runtime.cuh"
+
+namespace cubbs {
+
+__global__ void k_p2_lines(line2 *lines) {
+  if (blockIdx.x != 0 || threadIdx.x > 1) return;
+  g2a g = g2_generator();
+  if (threadIdx.x == 0) g.y = fp2_neg(g.y);  // slot 0: -P2
+  g2_precompute_lines(g, lines + (size_t)threadIdx.x * MILLER_LINES);
+}
+
+__global__ void k_pk_prepare(const uint8_t *pks, uint32_t n, int slot0, g2a *pk_aff, line2 *lines,
+                             int32_t *status) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  uint8_t b[96];
+  for (int k = 0; k < 96; k++) b[k] = pks[96 * (size_t)i + k];
+  g2a a;
+  int st = g2_decompress(b, a);
+  status[i] = st;
+  if (st != DEC_OK) return;
+  pk_aff[slot0 + i] = a;
+  g2_precompute_lines(a, lines + (size_t)(slot0 + i) * MILLER_LINES);
+}
+
+void launch_p2_lines(cudaStream_t s, line2 *lines) { k_p2_lines<<<1, 32, 0, s>>>(lines); }
+void launch_pk_prepare(cudaStream_t s, const uint8_t *pks96, uint32_t n, int slot0, g2a *pk_aff, line2 *lines,
+                       int32_t *status) {
+  if (n) k_pk_prepare<<<blocks_for(n, 32), 32, 0, s>>>(pks96, n, slot0, pk_aff, lines, status);
+}
+
+__global__ void __launch_bounds__(64) k_pairing_check(const PairJob *jobs, uint32_t n, const line2 *lines,
+                                                      uint8_t *ok) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PairJob &j = jobs[i];
+  if (!j.active) {
+    ok[i] = 0;
+    return;
+  }
+  g1a P[2] = {j.pa, j.pb};
+  const line2 *L[2] = {lines + (size_t)j.slot_a * MILLER_LINES, lines + (size_t)j.slot_b * MILLER_LINES};
+  bool skip[2] = {(j.flags & 1) != 0, (j.flags & 2) != 0};
+  fp12 f = miller_loop_lines<2>(P, L, skip);
+  ok[i] = fp12_is_one(final_exponentiation(f)) ? 1 : 0;
+}
+
+void launch_pairing_check(cudaStream_t s, const PairJob *jobs, uint32_t n, const line2 *lines, uint8_t *ok) {
+  if (n) k_pairing_check<<<blocks_for(n, 64), 64, 0, s>>>(jobs, n, lines, ok);
+}
+
+}  // namespace cubbs

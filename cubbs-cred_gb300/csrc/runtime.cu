@@ -1,0 +1,237 @@
+// Runtime singleton: device selection, streams, arena, the resident prepared
+// state (generators built on the device by hash_to_curve, fixed-base window
+// tables, Miller lines of +-P2 and of every public key seen) and
+// backend_info.  Reference: host pools/caches in prepare_b_msm.cu:165-301,
+// kernels/common_cache.cuh:112-486 and the canary probe cubbs_bbs_cuda.cu:719-824.
+#include <cstdlib>
+#include <cstring>
+
+#include "runtime.cuh"
+
+namespace cubbs {
+
+void DeviceArena::reserve(size_t bytes) {
+  if (bytes <= cap) return;
+  size_t ncap = cap ? cap : ((size_t)64 << 20);
+  while (ncap < bytes) ncap *= 2;
+  if (base) CUBBS_CHECK(cudaFree(base));
+  base = nullptr;
+  cap = 0;
+  CUBBS_CHECK(cudaMalloc(&base, ncap));
+  cap = ncap;
+  used = 0;
+}
+
+void HostStaging::reserve(size_t bytes) {
+  if (bytes <= cap) return;
+  size_t ncap = cap ? cap : ((size_t)16 << 20);
+  while (ncap < bytes) ncap *= 2;
+  if (base) CUBBS_CHECK(cudaFreeHost(base));
+  base = nullptr;
+  cap = 0;
+  CUBBS_CHECK(cudaMallocHost(&base, ncap));
+  cap = ncap;
+  used = 0;
+}
+
+Runtime &Runtime::get() {
+  static Runtime rt;
+  return rt;
+}
+
+static int env_int(const char *name, int dflt) {
+  const char *v = std::getenv(name);
+  if (!v || !*v) return dflt;
+  return std::atoi(v);
+}
+
+void Runtime::init() {
+  if (initialised) return;
+  int ndev = 0;
+  CUBBS_CHECK(cudaGetDeviceCount(&ndev));
+  if (ndev <= 0) throw CudaError(cudaErrorNoDevice, "no CUDA device");
+  device = env_int("CUBBS_BBS_DEVICE", 0);
+  CUBBS_CHECK(cudaSetDevice(device));
+  CUBBS_CHECK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
+  CUBBS_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  CUBBS_CHECK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+  // The kernels are register heavy; give them room for local-memory spills.
+  CUBBS_CHECK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
+  table_w = env_int("CUBBS_BBS_TABLE_WINDOW", 8);
+  if (table_w < 4 || table_w > 16) table_w = 8;
+  line_capacity = 2 + 1024;
+  CUBBS_CHECK(cudaMalloc(&d_lines, (size_t)line_capacity * MILLER_LINES * sizeof(line2)));
+  CUBBS_CHECK(cudaMalloc(&d_pk_aff, (size_t)line_capacity * sizeof(g2a)));
+  launch_p2_lines(stream, d_lines);
+  CUBBS_CHECK(cudaGetLastError());
+  CUBBS_CHECK(cudaStreamSynchronize(stream));
+  line_used = 2;
+  slot_info.assign(2, PkSlot{DEC_OK});
+  arena.reserve((size_t)256 << 20);
+  staging.reserve((size_t)64 << 20);
+  initialised = true;
+}
+
+// Build generators up to d_gens[count) on the device: P1 is decoded from its
+// published encoding; Q1, H1, ... come from the seed chain + hash_to_curve.
+void Runtime::ensure_generators(int count) {
+  if (count <= gen_count) return;
+  int ncap = gen_capacity ? gen_capacity : 256;
+  while (ncap < count) ncap *= 2;
+  if (ncap != gen_capacity) {
+    g1a *ng = nullptr;
+    uint8_t *nc = nullptr;
+    CUBBS_CHECK(cudaMalloc(&ng, (size_t)ncap * sizeof(g1a)));
+    CUBBS_CHECK(cudaMalloc(&nc, (size_t)ncap * 48 + 48));
+    if (gen_count) {
+      CUBBS_CHECK(cudaMemcpyAsync(ng, d_gens, (size_t)gen_count * sizeof(g1a), cudaMemcpyDeviceToDevice, stream));
+      CUBBS_CHECK(cudaMemcpyAsync(nc, d_gens_c, (size_t)gen_count * 48 + 48, cudaMemcpyDeviceToDevice, stream));
+      CUBBS_CHECK(cudaStreamSynchronize(stream));
+      cudaFree(d_gens);
+      cudaFree(d_gens_c);
+    }
+    d_gens = ng;
+    d_gens_c = nc;
+    gen_capacity = ncap;
+  }
+  static uint8_t *d_seed_state = nullptr;
+  if (!d_seed_state) CUBBS_CHECK(cudaMalloc(&d_seed_state, 64));
+  if (gen_count == 0) {
+    launch_decode_p1(stream, d_gens, d_gens_c);
+    gen_count = 1;
+  }
+  int first = gen_count;  // 1-based generator number == d_gens index
+  int n = count - gen_count;
+  uint8_t *seeds = nullptr;
+  CUBBS_CHECK(cudaMalloc(&seeds, (size_t)n * 48));
+  launch_make_generator_seeds(stream, first, n, d_seed_state, seeds);
+  launch_hash_generators(stream, first, n, seeds, d_gens, d_gens_c);
+  CUBBS_CHECK(cudaGetLastError());
+  CUBBS_CHECK(cudaStreamSynchronize(stream));
+  cudaFree(seeds);
+  gen_count = count;
+}
+
+// Fixed-base window table over d_gens[0..gens).  Rebuilt (all generators)
+// when it must grow; built in generator chunks to bound the scratch.
+void Runtime::ensure_table(int gens) {
+  if (table.entries && table.gens >= gens && table.w == table_w) return;
+  int want = 1;
+  while (want < gens) want *= 2;
+  if (want < 64) want = 64;
+  ensure_generators(want);
+  FixedTable t;
+  t.w = table_w;
+  t.nwin = 255 / t.w + 1;
+  t.half = 1 << (t.w - 1);
+  t.gens = want;
+  size_t per_gen = (size_t)t.nwin * t.half;
+  g1a *entries = nullptr;
+  CUBBS_CHECK(cudaMalloc(&entries, (size_t)want * per_gen * sizeof(g1a)));
+  t.entries = entries;
+  // chunk so that the XYZZ + prefix scratch stays below ~1 GiB
+  size_t per_gen_scratch = per_gen * (sizeof(g1) + sizeof(fp));
+  int chunk = (int)std::max<size_t>(1, ((size_t)1 << 30) / per_gen_scratch);
+  if (chunk > want) chunk = want;
+  g1 *scratch = nullptr;
+  fp *prod = nullptr;
+  CUBBS_CHECK(cudaMalloc(&scratch, (size_t)chunk * per_gen * sizeof(g1)));
+  CUBBS_CHECK(cudaMalloc(&prod, (size_t)chunk * per_gen * sizeof(fp)));
+  for (int g0 = 0; g0 < want; g0 += chunk) {
+    int g1n = std::min(want, g0 + chunk);
+    // the kernel indexes scratch by (g - g0) * nwin + k
+    launch_build_table(stream, d_gens, g0, g1n, t, scratch, prod);
+    CUBBS_CHECK(cudaGetLastError());
+    CUBBS_CHECK(cudaStreamSynchronize(stream));
+  }
+  cudaFree(scratch);
+  cudaFree(prod);
+  if (table.entries) cudaFree(table.entries);
+  table = t;
+}
+
+void Runtime::resolve_pks(const std::vector<const uint8_t *> &pk_ptrs, std::vector<int> &slots,
+                          std::vector<int> &status) {
+  slots.assign(pk_ptrs.size(), -1);
+  status.assign(pk_ptrs.size(), DEC_BAD);
+  std::vector<std::string> fresh;
+  std::unordered_map<std::string, int> fresh_idx;
+  for (size_t i = 0; i < pk_ptrs.size(); i++) {
+    std::string key(reinterpret_cast<const char *>(pk_ptrs[i]), 96);
+    if (pk_slots.count(key) || fresh_idx.count(key)) continue;
+    fresh_idx[key] = (int)fresh.size();
+    fresh.push_back(key);
+  }
+  if (!fresh.empty()) {
+    if (line_used + (int)fresh.size() > line_capacity) {
+      int ncap = line_capacity;
+      while (ncap < line_used + (int)fresh.size()) ncap *= 2;
+      line2 *nl = nullptr;
+      g2a *na = nullptr;
+      CUBBS_CHECK(cudaMalloc(&nl, (size_t)ncap * MILLER_LINES * sizeof(line2)));
+      CUBBS_CHECK(cudaMalloc(&na, (size_t)ncap * sizeof(g2a)));
+      CUBBS_CHECK(cudaMemcpy(nl, d_lines, (size_t)line_used * MILLER_LINES * sizeof(line2), cudaMemcpyDeviceToDevice));
+      CUBBS_CHECK(cudaMemcpy(na, d_pk_aff, (size_t)line_used * sizeof(g2a), cudaMemcpyDeviceToDevice));
+      cudaFree(d_lines);
+      cudaFree(d_pk_aff);
+      d_lines = nl;
+      d_pk_aff = na;
+      line_capacity = ncap;
+    }
+    std::vector<uint8_t> h(96 * fresh.size());
+    for (size_t i = 0; i < fresh.size(); i++) std::memcpy(h.data() + 96 * i, fresh[i].data(), 96);
+    uint8_t *d = nullptr;
+    int32_t *dst = nullptr;
+    CUBBS_CHECK(cudaMalloc(&d, h.size()));
+    CUBBS_CHECK(cudaMalloc(&dst, 4 * fresh.size()));
+    CUBBS_CHECK(cudaMemcpyAsync(d, h.data(), h.size(), cudaMemcpyHostToDevice, stream));
+    launch_pk_prepare(stream, d, (uint32_t)fresh.size(), line_used, d_pk_aff, d_lines, dst);
+    CUBBS_CHECK(cudaGetLastError());
+    std::vector<int32_t> st(fresh.size());
+    CUBBS_CHECK(cudaMemcpyAsync(st.data(), dst, 4 * fresh.size(), cudaMemcpyDeviceToHost, stream));
+    CUBBS_CHECK(cudaStreamSynchronize(stream));
+    cudaFree(d);
+    cudaFree(dst);
+    for (size_t i = 0; i < fresh.size(); i++) {
+      pk_slots[fresh[i]] = line_used + (int)i;
+      slot_info.push_back(PkSlot{st[i]});
+    }
+    line_used += (int)fresh.size();
+  }
+  for (size_t i = 0; i < pk_ptrs.size(); i++) {
+    std::string key(reinterpret_cast<const char *>(pk_ptrs[i]), 96);
+    int s = pk_slots[key];
+    slots[i] = s;
+    status[i] = slot_info[s].status;
+  }
+}
+
+}  // namespace cubbs
+
+using namespace cubbs;
+
+__global__ void k_canary(uint32_t *out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *out = 0x0BB52023u;
+}
+
+extern "C" int32_t cubbs_bbs_gpu_backend_info_v2(uint32_t abi, CuBbsBbsGpuBackendInfo *info) {
+  if (abi != CUBBS_BBS_GPU_ABI_VERSION || info == nullptr) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  info->backend_kind = CUBBS_BBS_GPU_BACKEND_KIND_UNKNOWN;
+  info->hardware_acceleration = 0;
+  try {
+    Runtime &rt = Runtime::get();
+    CallScope scope(rt);
+    uint32_t *d = rt.arena.alloc<uint32_t>(1);
+    k_canary<<<1, 1, 0, rt.stream>>>(d);
+    CUBBS_CHECK(cudaGetLastError());
+    uint32_t h = 0;
+    CUBBS_CHECK(cudaMemcpyAsync(&h, d, 4, cudaMemcpyDeviceToHost, rt.stream));
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    if (h == 0x0BB52023u) {
+      info->backend_kind = CUBBS_BBS_GPU_BACKEND_KIND_CUDA;
+      info->hardware_acceleration = 1;
+    }
+  } catch (const CudaError &) {
+  }
+  return CUBBS_BBS_GPU_SUCCESS;
+}

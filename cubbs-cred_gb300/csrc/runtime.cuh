@@ -1,0 +1,164 @@
+// Host runtime shared by the translation units of libcubbs_bbs_cuda.so:
+// device arena, pinned staging, the resident prepared state (generators,
+// fixed-base window tables, public-key Miller lines) and launch helpers.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <mutex>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "../../include/cubbs_bbs_gpu_abi.h"
+#include "pairing.cuh"
+
+namespace cubbs {
+
+#define CUBBS_CHECK(expr)                                 \
+  do {                                                    \
+    cudaError_t _e = (expr);                              \
+    if (_e != cudaSuccess) throw CudaError(_e, #expr);    \
+  } while (0)
+
+struct CudaError {
+  cudaError_t code;
+  const char *what;
+  CudaError(cudaError_t c, const char *w) : code(c), what(w) {}
+};
+
+// Bump allocator over one growable device allocation.  Reset at the start of
+// every ABI call (calls are serialised by Runtime::mu).
+struct DeviceArena {
+  uint8_t *base = nullptr;
+  size_t cap = 0, used = 0;
+  void reset() { used = 0; }
+  void reserve(size_t bytes);
+  template <typename T> T *alloc(size_t n) {
+    size_t bytes = (n * sizeof(T) + 255) & ~(size_t)255;
+    if (used + bytes > cap) throw CudaError(cudaErrorMemoryAllocation, "arena exhausted");
+    T *p = reinterpret_cast<T *>(base + used);
+    used += bytes;
+    return p;
+  }
+};
+
+// Pinned host staging buffer (one per runtime).
+struct HostStaging {
+  uint8_t *base = nullptr;
+  size_t cap = 0, used = 0;
+  void reset() { used = 0; }
+  void reserve(size_t bytes);
+  uint8_t *alloc(size_t bytes) {
+    bytes = (bytes + 15) & ~(size_t)15;
+    if (used + bytes > cap) throw CudaError(cudaErrorMemoryAllocation, "staging exhausted");
+    uint8_t *p = base + used;
+    used += bytes;
+    return p;
+  }
+};
+
+// Fixed-base window table over the generator list [P1, Q1, H1, ...]:
+// entry (g, k, d-1) = d * 2^(w k) * G_g (affine), d = 1..2^(w-1).
+struct FixedTable {
+  int w = 0, nwin = 0, half = 0, gens = 0;
+  g1a *entries = nullptr;
+};
+
+struct PkSlot {
+  int status = DEC_BAD;  // DEC_OK / DEC_INF / DEC_BAD
+};
+
+struct Runtime {
+  std::mutex mu;
+  int device = 0;
+  cudaStream_t stream = nullptr, stream2 = nullptr;
+  DeviceArena arena;
+  HostStaging staging;
+  // generators: d_gens[0] = P1, d_gens[1] = Q1, d_gens[1 + i] = H_i
+  int gen_count = 0;      // entries of d_gens built (P1 included)
+  int gen_capacity = 0;
+  g1a *d_gens = nullptr;
+  uint8_t *d_gens_c = nullptr;  // compressed, same indexing as d_gens
+  FixedTable table;
+  int table_w = 8;
+  // Miller lines: slot 0 = -P2, slot 1 = P2, slots >= 2 = public keys
+  line2 *d_lines = nullptr;
+  g2a *d_pk_aff = nullptr;
+  int line_capacity = 0, line_used = 0;
+  std::unordered_map<std::string, int> pk_slots;
+  std::vector<PkSlot> slot_info;
+  bool initialised = false;
+  int sm_count = 0;
+
+  static Runtime &get();
+  void init();                             // device, streams, -P2/P2 lines
+  void ensure_generators(int count);       // d_gens[0..count) (P1 + count-1 generators)
+  void ensure_table(int gens);             // fixed-base table covering d_gens[0..gens)
+  // Resolve public keys to line slots (decoding + subgroup check + lines on the
+  // device for new keys).  pk_ptrs[i] -> slot index; status per key.
+  void resolve_pks(const std::vector<const uint8_t *> &pk_ptrs, std::vector<int> &slots,
+                   std::vector<int> &status);
+};
+
+// Lock + reset helper for ABI calls.
+struct CallScope {
+  Runtime &rt;
+  std::lock_guard<std::mutex> lock;
+  explicit CallScope(Runtime &r) : rt(r), lock(r.mu) {
+    rt.init();
+    rt.arena.reset();
+    rt.staging.reset();
+  }
+};
+
+inline unsigned blocks_for(size_t n, unsigned tpb) { return (unsigned)((n + tpb - 1) / tpb); }
+
+// Launchers implemented in the kernel translation units.
+void launch_h2s_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens,
+                     uint32_t n, const uint8_t *dst, uint32_t dlen, fr *out_raw);
+void launch_sha256_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens,
+                        uint32_t n, uint8_t *digests);
+void launch_xmd48_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens,
+                       uint32_t n, const uint8_t *dst, uint32_t dlen, uint8_t *out);
+// domain = H2S(PK || I2OSP(L,8) || Q1..H_L || api_id || I2OSP(hlen,8) || header)
+struct DomainJob {
+  uint32_t pk_off, hdr_off, hdr_len, L;
+};
+void launch_domain(cudaStream_t s, const DomainJob *jobs, uint32_t n, const uint8_t *blob,
+                   const uint8_t *gens_c, fr *out_raw);
+void launch_make_generator_seeds(cudaStream_t s, int first, int count, uint8_t *seeds_state,
+                                 uint8_t *seeds_out);
+void launch_hash_generators(cudaStream_t s, int first, int count, const uint8_t *seeds, g1a *gens,
+                            uint8_t *gens_c);
+void launch_decode_p1(cudaStream_t s, g1a *gens, uint8_t *gens_c);
+void launch_build_table(cudaStream_t s, const g1a *gens, int g0, int g1n, FixedTable t, g1 *scratch_xyzz,
+                        fp *scratch_prod);
+// decode N compressed G1 points: status DEC_*; affine out
+void launch_g1_decode(cudaStream_t s, const uint8_t *pts48, uint32_t stride, uint32_t n, g1a *out,
+                      int32_t *status, bool check_subgroup);
+// fixed-base MSM rows: scalars raw Fr [row * stride + g] for g < nterms[row]
+void launch_fixed_msm(cudaStream_t s, const FixedTable &t, const fr *scalars, uint32_t stride,
+                      const uint32_t *nterms, uint32_t rows, g1 *out);
+// variable-base jobs: out[i] = k[i] * P[i]; P given as affine points
+struct VarJob {
+  uint32_t point;  // index into the point array
+  uint32_t flags;  // bit0: point is infinity (result infinity)
+};
+void launch_var_mul(cudaStream_t s, const g1a *points, const VarJob *jobs, const fr *scalars, uint32_t n,
+                    g1 *out);
+void launch_g1_compress(cudaStream_t s, const g1 *pts, uint32_t n, uint8_t *out48);
+void launch_pk_prepare(cudaStream_t s, const uint8_t *pks96, uint32_t n, int slot0, g2a *pk_aff,
+                       line2 *lines, int32_t *status);
+void launch_p2_lines(cudaStream_t s, line2 *lines);
+// Pairing check job: e(pa, Q_slot_a) * e(pb, Q_slot_b) == 1.  flags bit0/bit1:
+// pair a / pair b is skipped (its G1 or G2 side is the identity).
+struct PairJob {
+  g1a pa, pb;
+  int32_t slot_a, slot_b;
+  uint32_t flags;
+  uint32_t active;  // 0: not evaluated (result 0)
+};
+void launch_pairing_check(cudaStream_t s, const PairJob *jobs, uint32_t n, const line2 *lines, uint8_t *ok);
+
+}  // namespace cubbs

@@ -1,0 +1,356 @@
+/*
+ * cubbs_bbs_gpu_abi.h -- C ABI v2 of the GB300 BBS (BLS12-381-SHA-256) library
+ * libcubbs_bbs_cuda.so.
+ *
+ * The structs and entry points keep the exact layout and calling convention
+ * of the reference ABI (native/cuda/include/cubbs_bbs_gpu_abi.h:1-314) so the
+ * library drops in under the Rust loader (crates/cubbs-bbs/src/gpu_runtime.rs:
+ * 269-497), which resolves the four required symbols and probes the optional
+ * ones.  Each declaration cites the reference declaration it replaces.
+ *
+ * Conventions (reference cubbs_bbs_gpu_abi.h:25-59; docs/gpu-bbs-backend-design.md:
+ * 145-169):
+ *   - every call returns 0 (success), 1 (invalid input), 2 (insufficient
+ *     output) or 3 (internal); a call-level error means malformed arguments;
+ *   - per-item results[i] = {code, value, bytes_written}; value is the
+ *     verification boolean (1/0) or an MSM route id;
+ *   - an invalid signature or proof is code 0 with value 0, not an error;
+ *   - buffers are caller-owned and must stay valid until the call returns;
+ *     every call is synchronous and thread-safe.
+ * Encodings: Fr scalars 32-byte big-endian canonical (< r); G1 48-byte and G2
+ * 96-byte compressed (zkcrypto / ZCash flag bits); signature A || e (80 B);
+ * proof Abar || Bbar || D || e^ || r1^ || r3^ || m^_j... || c.
+ *
+ * All BBS work runs on the GPU; there is no CPU fallback.
+ */
+#ifndef CUBBS_BBS_GPU_ABI_H
+#define CUBBS_BBS_GPU_ABI_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CUBBS_BBS_GPU_ABI_VERSION 2u
+
+/* MSM route ids reported in CuBbsBbsGpuResult.value (reference :13-23).
+ * This library uses route 2 for fixed-base (common point) MSMs against the
+ * resident generator tables and route 4 for general variable-base MSMs. */
+#define CUBBS_BBS_MSM_ROUTE_CUBBS_ITEM 1u
+#define CUBBS_BBS_MSM_ROUTE_CUBBS_COMMON_POINTS 2u
+#define CUBBS_BBS_MSM_ROUTE_CUBBS_LARGE 3u
+#define CUBBS_BBS_MSM_ROUTE_CUBBS_UNIVERSAL 4u
+#define CUBBS_BBS_MSM_ROUTE_BLST_ITEM 5u
+#define CUBBS_BBS_MSM_ROUTE_BLST_COMMON_POINTS 6u
+#define CUBBS_BBS_MSM_ROUTE_SPPARK_ITEM_REFERENCE 7u
+#define CUBBS_BBS_MSM_ROUTE_SPPARK_COMMON_POINTS_REFERENCE 8u
+
+#define CUBBS_BBS_GPU_SUCCESS 0
+#define CUBBS_BBS_GPU_ERR_INVALID_INPUT 1
+#define CUBBS_BBS_GPU_ERR_INSUFFICIENT_OUTPUT 2
+#define CUBBS_BBS_GPU_ERR_INTERNAL 3
+
+#define CUBBS_BBS_GPU_BACKEND_KIND_UNKNOWN 0u
+#define CUBBS_BBS_GPU_BACKEND_KIND_CUDA 1u
+#define CUBBS_BBS_GPU_BACKEND_KIND_CPU_ABI_TEST 2u
+
+#define CUBBS_BBS_SECRET_KEY_LEN 32u
+#define CUBBS_BBS_PUBLIC_KEY_LEN 96u
+#define CUBBS_BBS_SIGNATURE_LEN 80u
+#define CUBBS_BBS_2023_HEADER_LEN 64u
+
+/* Byte and index views (reference :34-53). */
+typedef struct CuBbsBbsGpuByteSlice {
+  const uint8_t *data;
+  size_t len;
+} CuBbsBbsGpuByteSlice;
+
+typedef struct CuBbsBbsGpuByteBuffer {
+  uint8_t *data;
+  size_t capacity;
+  size_t len;
+} CuBbsBbsGpuByteBuffer;
+
+typedef struct CuBbsBbsGpuIndexSlice {
+  const size_t *data;
+  size_t len;
+} CuBbsBbsGpuIndexSlice;
+
+typedef struct CuBbsBbsGpuResult {
+  int32_t code;
+  uint8_t value;
+  size_t bytes_written;
+} CuBbsBbsGpuResult;
+
+typedef struct CuBbsBbsGpuBackendInfo {
+  uint32_t backend_kind;
+  uint8_t hardware_acceleration;
+} CuBbsBbsGpuBackendInfo;
+
+/* Four-operation items (reference :66-103). */
+typedef struct CuBbsBbsGpuSignItem {
+  CuBbsBbsGpuByteSlice secret_key;
+  CuBbsBbsGpuByteSlice public_key;
+  CuBbsBbsGpuByteSlice header;
+  const CuBbsBbsGpuByteSlice *messages;
+  size_t message_count;
+  CuBbsBbsGpuByteBuffer signature_out;
+} CuBbsBbsGpuSignItem;
+
+typedef struct CuBbsBbsGpuVerifyItem {
+  CuBbsBbsGpuByteSlice public_key;
+  CuBbsBbsGpuByteSlice signature;
+  CuBbsBbsGpuByteSlice header;
+  const CuBbsBbsGpuByteSlice *messages;
+  size_t message_count;
+} CuBbsBbsGpuVerifyItem;
+
+typedef struct CuBbsBbsGpuProofGenItem {
+  CuBbsBbsGpuByteSlice public_key;
+  CuBbsBbsGpuByteSlice signature;
+  CuBbsBbsGpuByteSlice header;
+  CuBbsBbsGpuByteSlice presentation_header;
+  const CuBbsBbsGpuByteSlice *messages;
+  size_t message_count;
+  CuBbsBbsGpuIndexSlice disclosed_indexes;
+  CuBbsBbsGpuByteBuffer proof_out;
+} CuBbsBbsGpuProofGenItem;
+
+typedef struct CuBbsBbsGpuProofVerifyItem {
+  CuBbsBbsGpuByteSlice public_key;
+  CuBbsBbsGpuByteSlice proof;
+  CuBbsBbsGpuByteSlice header;
+  CuBbsBbsGpuByteSlice presentation_header;
+  const CuBbsBbsGpuByteSlice *disclosed_messages;
+  size_t disclosed_count;
+  CuBbsBbsGpuIndexSlice disclosed_indexes;
+  size_t total_message_count;
+} CuBbsBbsGpuProofVerifyItem;
+
+/* Primitive items (reference :105-225). */
+typedef struct CuBbsBbsGpuMessagesToScalarItem {
+  CuBbsBbsGpuByteSlice message;
+  CuBbsBbsGpuByteSlice dst;
+  CuBbsBbsGpuByteBuffer scalar_out;
+} CuBbsBbsGpuMessagesToScalarItem;
+
+typedef struct CuBbsBbsGpuSignEFromResidentScalarsItem {
+  CuBbsBbsGpuByteSlice secret_key;
+  CuBbsBbsGpuByteSlice domain;
+  const CuBbsBbsGpuByteSlice *messages;
+  size_t message_scalar_offset;
+  size_t message_count;
+  CuBbsBbsGpuByteBuffer message_scalars_out;
+  CuBbsBbsGpuByteBuffer scalar_out;
+} CuBbsBbsGpuSignEFromResidentScalarsItem;
+
+typedef struct CuBbsBbsGpuPrepareBItem {
+  CuBbsBbsGpuByteSlice public_key;
+  CuBbsBbsGpuByteSlice header;
+  const CuBbsBbsGpuByteSlice *message_scalars;
+  size_t message_count;
+  CuBbsBbsGpuByteBuffer b_out;
+} CuBbsBbsGpuPrepareBItem;
+
+typedef struct CuBbsBbsGpuG1MsmItem {
+  const CuBbsBbsGpuByteSlice *points;
+  const CuBbsBbsGpuByteSlice *scalars;
+  size_t term_count;
+  CuBbsBbsGpuByteBuffer point_out;
+} CuBbsBbsGpuG1MsmItem;
+
+typedef struct CuBbsBbsGpuG1MsmCommonPointsBatchItem {
+  const CuBbsBbsGpuByteSlice *points;
+  size_t term_count;
+  const CuBbsBbsGpuByteSlice *scalar_rows;
+  const uint8_t *scalar_rows_be;
+  size_t scalar_row_stride;
+  size_t output_count;
+  CuBbsBbsGpuByteBuffer *point_outs;
+} CuBbsBbsGpuG1MsmCommonPointsBatchItem;
+
+typedef struct CuBbsBbsGpuG1MsmCommonPointsPlusVariableItem {
+  const CuBbsBbsGpuByteSlice *points;
+  size_t term_count;
+  const CuBbsBbsGpuByteSlice *scalar_rows;
+  const CuBbsBbsGpuByteSlice *variable_points;
+  const CuBbsBbsGpuByteSlice *variable_scalars;
+  size_t output_count;
+  CuBbsBbsGpuByteBuffer *point_outs;
+} CuBbsBbsGpuG1MsmCommonPointsPlusVariableItem;
+
+/* T1 = challenge*Bbar + e_cap*Abar + r1_cap*D ;
+ * T2 = MSM(common_points, common_scalars) + r3_cap*D ;
+ * proof_points rows [Bbar, Abar, D], proof_scalars rows [challenge, e_cap, r1_cap, r3_cap]. */
+typedef struct CuBbsBbsGpuProofVerifyMsmPairItem {
+  const CuBbsBbsGpuByteSlice *common_points;
+  size_t common_term_count;
+  const CuBbsBbsGpuByteSlice *common_scalar_rows;
+  const CuBbsBbsGpuByteSlice *proof_points;
+  const CuBbsBbsGpuByteSlice *proof_scalars;
+  size_t output_count;
+  CuBbsBbsGpuByteBuffer *t1_outs;
+  CuBbsBbsGpuByteBuffer *t2_outs;
+} CuBbsBbsGpuProofVerifyMsmPairItem;
+
+typedef struct CuBbsBbsGpuG1DualMsmSamePointsItem {
+  const CuBbsBbsGpuByteSlice *points;
+  const CuBbsBbsGpuByteSlice *lhs_scalars;
+  const CuBbsBbsGpuByteSlice *rhs_scalars;
+  size_t term_count;
+  CuBbsBbsGpuByteBuffer lhs_out;
+  CuBbsBbsGpuByteBuffer rhs_out;
+} CuBbsBbsGpuG1DualMsmSamePointsItem;
+
+typedef struct CuBbsBbsGpuG1DualMsmSamePointsLanesItem {
+  const CuBbsBbsGpuByteSlice *points;
+  const CuBbsBbsGpuByteSlice *lhs_scalars;
+  const CuBbsBbsGpuByteSlice *rhs_scalars;
+  size_t term_count;
+  size_t lane_count;
+  CuBbsBbsGpuByteBuffer lhs_outs;
+  CuBbsBbsGpuByteBuffer rhs_outs;
+} CuBbsBbsGpuG1DualMsmSamePointsLanesItem;
+
+typedef struct CuBbsBbsGpuG1AddItem {
+  CuBbsBbsGpuByteSlice lhs;
+  CuBbsBbsGpuByteSlice rhs;
+  CuBbsBbsGpuByteBuffer point_out;
+} CuBbsBbsGpuG1AddItem;
+
+typedef struct CuBbsBbsGpuPairingEqItem {
+  CuBbsBbsGpuByteSlice lhs_g1;
+  CuBbsBbsGpuByteSlice lhs_g2;
+  CuBbsBbsGpuByteSlice rhs_g1;
+  CuBbsBbsGpuByteSlice rhs_g2;
+} CuBbsBbsGpuPairingEqItem;
+
+typedef struct CuBbsBbsGpuPairingEqScaledItem {
+  CuBbsBbsGpuByteSlice lhs_g1;
+  CuBbsBbsGpuByteSlice lhs_g2;
+  CuBbsBbsGpuByteSlice rhs_g1;
+  CuBbsBbsGpuByteSlice rhs_g2;
+  CuBbsBbsGpuByteSlice coefficient;
+} CuBbsBbsGpuPairingEqScaledItem;
+
+/* d = B*r2, abar = A*(r1 r2), bbar = d*r1 - abar*e, t1 = abar*e~ + d*r1~
+ * from 7 host-supplied multipliers r2, r1r2, r1r2, r1r2e, r1r2e~, r2r1~, r3~. */
+typedef struct CuBbsBbsGpuProofGenT2PrepareItem {
+  CuBbsBbsGpuByteSlice compressed_b;
+  CuBbsBbsGpuByteSlice signature_a;
+  CuBbsBbsGpuByteSlice scalars_be[7];
+  CuBbsBbsGpuByteSlice seed;
+  CuBbsBbsGpuByteBuffer d_out;
+  CuBbsBbsGpuByteBuffer abar_out;
+  CuBbsBbsGpuByteBuffer bbar_out;
+  CuBbsBbsGpuByteBuffer t1_out;
+} CuBbsBbsGpuProofGenT2PrepareItem;
+
+/* reference :227-228 (the reference always reports hardware_acceleration=0,
+ * cubbs_bbs_cuda.cu:822; this library reports 1: the four operations run on
+ * the GPU). */
+int32_t cubbs_bbs_gpu_backend_info_v2(uint32_t abi_version, CuBbsBbsGpuBackendInfo *info_out);
+
+/* reference :230-247 -- required symbols; stubs in the reference
+ * (cubbs_bbs_cuda.cu:826-835,1169-1200), implemented here fully on device. */
+int32_t cubbs_bbs_gpu_sign_batch_v2(uint32_t abi_version, CuBbsBbsGpuSignItem *items,
+                                    size_t item_count, CuBbsBbsGpuResult *results);
+int32_t cubbs_bbs_gpu_verify_batch_v2(uint32_t abi_version, const CuBbsBbsGpuVerifyItem *items,
+                                      size_t item_count, CuBbsBbsGpuResult *results);
+/* Blinding scalars come from a per-item 32-byte seed drawn from the OS
+ * (getrandom) and expanded on the device. */
+int32_t cubbs_bbs_gpu_proof_gen_batch_v2(uint32_t abi_version, CuBbsBbsGpuProofGenItem *items,
+                                         size_t item_count, CuBbsBbsGpuResult *results);
+int32_t cubbs_bbs_gpu_proof_verify_batch_v2(uint32_t abi_version,
+                                            const CuBbsBbsGpuProofVerifyItem *items,
+                                            size_t item_count, CuBbsBbsGpuResult *results);
+
+/* ABI-compatible addition: ProofGen with caller-chosen blinding.  Item i draws
+ * its 5+U scalars with seeded_random_scalars(seed_i, api_id ||
+ * "MOCK_RANDOM_SCALARS_DST_") (crates/cubbs-bbs-protocol/src/utils/util.rs:
+ * 329-358); with seed "3.141592653589793238462643383279" this reproduces the
+ * CFRG proof fixtures.  Past 170 scalars the expansion runs in chunks of 170
+ * keyed by seed || I2OSP(chunk, 2). */
+int32_t cubbs_bbs_gpu_proof_gen_seeded_batch_v2(uint32_t abi_version,
+                                                CuBbsBbsGpuProofGenItem *items, size_t item_count,
+                                                const uint8_t (*seeds)[32],
+                                                CuBbsBbsGpuResult *results);
+
+/* reference :249-251 */
+int32_t cubbs_bbs_gpu_messages_to_scalar_batch_v2(uint32_t abi_version,
+                                                  CuBbsBbsGpuMessagesToScalarItem *items,
+                                                  size_t item_count, CuBbsBbsGpuResult *results);
+/* reference :253-256 ("resident" reuses the previous call's device scalars,
+ * cubbs_bbs_cuda.cu:523-534) */
+int32_t cubbs_bbs_gpu_sign_e_from_resident_scalars_batch_v2(
+    uint32_t abi_version, CuBbsBbsGpuSignEFromResidentScalarsItem *items, size_t item_count,
+    CuBbsBbsGpuByteSlice message_dst, CuBbsBbsGpuByteSlice e_dst, CuBbsBbsGpuResult *results);
+/* reference :258-261 (B = P1 + Q1*domain + sum H_i*m_i, header 64 bytes) */
+int32_t cubbs_bbs_gpu_prepare_b_batch_v2(uint32_t abi_version, CuBbsBbsGpuPrepareBItem *items,
+                                         size_t item_count, CuBbsBbsGpuResult *results);
+/* reference :263-266 */
+int32_t cubbs_bbs_gpu_g1_msm_batch_v2(uint32_t abi_version, CuBbsBbsGpuG1MsmItem *items,
+                                      size_t item_count, CuBbsBbsGpuResult *results);
+/* reference :268-271 */
+int32_t cubbs_bbs_gpu_g1_msm_common_points_batch_v2(uint32_t abi_version,
+                                                    CuBbsBbsGpuG1MsmCommonPointsBatchItem *items,
+                                                    size_t group_count,
+                                                    CuBbsBbsGpuResult *results);
+/* reference :273-275 */
+int32_t cubbs_bbs_gpu_g1_msm_fused_common_points_batch_v2(
+    uint32_t abi_version, CuBbsBbsGpuG1MsmCommonPointsBatchItem *items, size_t group_count,
+    CuBbsBbsGpuResult *results);
+/* reference :277-280 */
+int32_t cubbs_bbs_gpu_g1_msm_common_points_plus_variable_batch_v2(
+    uint32_t abi_version, CuBbsBbsGpuG1MsmCommonPointsPlusVariableItem *items, size_t group_count,
+    CuBbsBbsGpuResult *results);
+/* reference :282-284 */
+int32_t cubbs_bbs_gpu_proof_verify_msm_pair_batch_v2(uint32_t abi_version,
+                                                     CuBbsBbsGpuProofVerifyMsmPairItem *items,
+                                                     size_t group_count,
+                                                     CuBbsBbsGpuResult *results);
+/* reference :286-288 */
+int32_t cubbs_bbs_gpu_g1_dual_msm_same_points_batch_v2(uint32_t abi_version,
+                                                       CuBbsBbsGpuG1DualMsmSamePointsItem *items,
+                                                       size_t item_count,
+                                                       CuBbsBbsGpuResult *results);
+/* reference :290-292 */
+int32_t cubbs_bbs_gpu_g1_dual_msm_same_points_lanes_batch_v2(
+    uint32_t abi_version, CuBbsBbsGpuG1DualMsmSamePointsLanesItem *items, size_t item_count,
+    CuBbsBbsGpuResult *results);
+/* reference :294-297 */
+int32_t cubbs_bbs_gpu_g1_add_batch_v2(uint32_t abi_version, CuBbsBbsGpuG1AddItem *items,
+                                      size_t item_count, CuBbsBbsGpuResult *results);
+/* reference :299-301: value = e(lhs_g1, lhs_g2) == e(rhs_g1, rhs_g2) */
+int32_t cubbs_bbs_gpu_pairing_eq_batch_v2(uint32_t abi_version,
+                                          const CuBbsBbsGpuPairingEqItem *items,
+                                          size_t item_count, CuBbsBbsGpuResult *results);
+/* reference :303-305: one result for the whole batch,
+ * value = prod_i (e(lhs_i, lhs2_i) / e(rhs_i, rhs2_i))^{coef_i} == 1 */
+int32_t cubbs_bbs_gpu_pairing_eq_aggregate_v2(uint32_t abi_version,
+                                              const CuBbsBbsGpuPairingEqScaledItem *items,
+                                              size_t item_count, CuBbsBbsGpuResult *result);
+/* reference :307-309 */
+int32_t cubbs_bbs_gpu_proof_gen_t2_prepare_batch_v2(uint32_t abi_version,
+                                                    CuBbsBbsGpuProofGenT2PrepareItem *items,
+                                                    size_t item_count,
+                                                    CuBbsBbsGpuResult *results);
+
+/* Test exports outside the reference header (reference cubbs_bbs_cuda.cu:53,117,230). */
+int32_t cubbs_bbs_gpu_sha256_batch_for_test_v2(uint32_t abi_version, const uint8_t *messages,
+                                               const size_t *offsets, const size_t *lengths,
+                                               size_t item_count, uint8_t *digests);
+int32_t cubbs_bbs_gpu_expand_xmd_sha256_48_batch_for_test_v2(
+    uint32_t abi_version, const uint8_t *messages, const size_t *offsets, const size_t *lengths,
+    size_t item_count, const uint8_t *dst, size_t dst_len, uint8_t *outputs);
+int32_t cubbs_bbs_gpu_hash_to_scalar_sha256_batch_for_test_v2(
+    uint32_t abi_version, const uint8_t *messages, const size_t *offsets, const size_t *lengths,
+    size_t item_count, const uint8_t *dst, size_t dst_len, uint8_t *scalars);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif

@@ -1318,6 +1318,18 @@ int oracle_proof_verify(const uint8_t pk[96], const uint8_t *proof, size_t proof
   return pairing_product_is_one(pairs) ? 0 : 2;
 }
 
+int oracle_calculate_domain(const uint8_t pk[96], const uint8_t *header, size_t hlen, size_t L,
+                            uint8_t out32[32]) {
+  ensure_init();
+  std::vector<G1P> gens;
+  std::vector<Bytes> gc;
+  generators(L + 1, gens, &gc);
+  Fr d;
+  if (!calculate_domain(pk, gc, L, header, hlen, d)) return 1;
+  d.to_be32(out32);
+  return 0;
+}
+
 int oracle_g1_msm(const uint8_t *points48, const uint8_t *scalars32_be, size_t n, uint8_t out48[48]) {
   ensure_init();
   G1P acc = G1::infinity();

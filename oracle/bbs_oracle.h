@@ -57,6 +57,9 @@ int oracle_proof_verify(const uint8_t pk[96], const uint8_t *proof, size_t proof
                         const uint8_t *dmsgs, const size_t *dlens, size_t R,
                         const size_t *disclosed);
 
+/* calculate_domain (util.rs:147-189) for L messages */
+int oracle_calculate_domain(const uint8_t pk[96], const uint8_t *header, size_t hlen, size_t L,
+                            uint8_t out32[32]);
 /* Primitive checkers used by kernel-level parity tests. */
 int oracle_g1_msm(const uint8_t *points48, const uint8_t *scalars32_be, size_t n, uint8_t out48[48]);
 int oracle_g1_add(const uint8_t a48[48], const uint8_t b48[48], uint8_t out48[48]);

@@ -57,6 +57,7 @@ def _declare(L):
         "oracle_proof_gen": [P, P, S, P, S, P, S, P, P, S, P, S, P, S, P, S, P, S, P],
         "oracle_proof_verify": [P, P, S, P, S, P, S, P, P, S, P],
         "oracle_g1_msm": [P, P, S, P],
+        "oracle_calculate_domain": [P, P, S, S, P],
         "oracle_g1_add": [P, P, P],
         "oracle_g1_decompress": [P, P],
         "oracle_g1_mul": [P, P, P],
@@ -182,6 +183,13 @@ def proof_verify(pk, proof, header, ph, disclosed_msgs, disclosed) -> int:
     return lib().oracle_proof_verify(_buf(pk), _buf(proof), len(proof), _buf(header),
                                      len(header), _buf(ph), len(ph), _buf(data), lens,
                                      len(disclosed_msgs), idx)
+
+
+def calculate_domain(pk: bytes, header: bytes, L: int) -> bytes:
+    out = ctypes.create_string_buffer(32)
+    if lib().oracle_calculate_domain(_buf(pk), _buf(header), len(header), L, out):
+        raise ValueError("bad input")
+    return out.raw
 
 
 def g1_msm(points, scalars) -> bytes:

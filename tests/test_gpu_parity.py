@@ -1,0 +1,177 @@
+"""GPU parity: the sm_103a library through its C ABI against the CPU oracle and
+the golden vectors.  Integer/byte work, so every comparison is bit-exact."""
+import pytest
+
+from helpers import disclosed_subset, drbg, keypair, messages, scalar
+
+h = bytes.fromhex
+pytestmark = pytest.mark.gpu
+
+
+# ----------------------------------------------------------------------------- hashing
+def test_sha256_kats(gpu, golden):
+    kat = golden["sha256_kat"]
+    got = gpu.sha256_batch([m.encode() for m in kat["messages"]])
+    assert [g.hex() for g in got] == kat["digests"]
+
+
+def test_sha256_lengths(gpu, oracle):
+    msgs = [drbg(b"sha", b"len", n, n) for n in (0, 1, 55, 56, 63, 64, 65, 119, 120, 1000)]
+    assert gpu.sha256_batch(msgs) == [oracle.sha256(m) for m in msgs]
+
+
+def test_expand_xmd48(gpu, oracle):
+    dst = b"QUUX-V01-CS02-with-expander-SHA256-128"
+    msgs = [drbg(b"xmd", b"m", n, n) for n in (0, 3, 64, 200)]
+    assert gpu.expand_xmd48_batch(msgs, dst) == [oracle.expand_message_xmd(m, dst, 48) for m in msgs]
+
+
+def test_hash_to_scalar_fixture(gpu, golden):
+    g = golden["h2s"]
+    assert gpu.hash_to_scalar_batch([h(g["message"])], h(g["dst"]))[0].hex() == g["scalar"]
+
+
+def test_messages_to_scalar_fixture(gpu, golden):
+    g = golden["MapMessageToScalarAsHash"]
+    got = gpu.messages_to_scalar([h(c["message"]) for c in g["cases"]], h(g["dst"]))
+    assert [x.hex() for x in got] == [c["scalar"] for c in g["cases"]]
+
+
+# ----------------------------------------------------------------------------- Sign / Verify
+def test_sign_fixtures(gpu, golden):
+    reqs, want = [], []
+    for c in golden["signature"]:
+        if c["result"]["valid"]:
+            reqs.append((h(c["signerKeyPair"]["secretKey"]), h(c["signerKeyPair"]["publicKey"]), h(c["header"]),
+                         [h(m) for m in c["messages"]]))
+            want.append(c["signature"])
+    got = gpu.sign_batch(reqs)
+    assert [(code, sig.hex()) for code, sig in got] == [(0, w) for w in want]
+
+
+def test_verify_fixtures(gpu, golden):
+    cases = golden["signature"]
+    reqs = [(h(c["signerKeyPair"]["publicKey"]), h(c["signature"]), h(c["header"]), [h(m) for m in c["messages"]])
+            for c in cases]
+    got = gpu.verify_batch(reqs)
+    assert [v for _, v in got] == [c["result"]["valid"] for c in cases]
+    assert all(code == 0 for code, _ in got)
+
+
+@pytest.mark.parametrize("L", [1, 10, 100])
+def test_sign_verify_random(gpu, oracle, L):
+    seed = b"sign-verify-%d" % L
+    reqs, vreqs = [], []
+    for i in range(8):
+        sk, pk = keypair(oracle, seed, i % 3)
+        msgs = messages(seed, i, L, 32)
+        hdr = drbg(seed, b"hdr", i, 64)
+        reqs.append((sk, pk, hdr, msgs))
+    got = gpu.sign_batch(reqs)
+    for (sk, pk, hdr, msgs), (code, sig) in zip(reqs, got):
+        assert code == 0
+        assert sig == oracle.sign(sk, pk, hdr, msgs)[0]
+        vreqs.append((pk, sig, hdr, msgs))
+        vreqs.append((pk, sig, hdr, msgs[::-1] if L > 1 else [b"x"]))
+    ver = gpu.verify_batch(vreqs)
+    assert [v for _, v in ver] == [True, False] * len(reqs)
+
+
+def test_verify_rejects_malformed(gpu, oracle):
+    seed = b"verify-bad"
+    sk, pk = keypair(oracle, seed)
+    msgs = messages(seed, 0, 5, 32)
+    sig = oracle.sign(sk, pk, b"", msgs)[0]
+    bad_e = sig[:48] + (0x73EDA753299D7D483339D80809A1D80553BDA402FFFE5BFEFFFFFFFF00000001).to_bytes(32, "big")
+    not_on_curve = bytes([sig[0] ^ 0x01]) + sig[1:]
+    ident = bytes([0xC0]) + bytes(47) + sig[48:]
+    got = gpu.verify_batch([(pk, bad_e, b"", msgs), (pk, sig[:79], b"", msgs), (pk, ident, b"", msgs),
+                            (pk, sig, b"", msgs)])
+    assert [v for _, v in got] == [False, False, False, True]
+    # an off-curve / non-subgroup A never verifies
+    assert gpu.verify_batch([(pk, not_on_curve, b"", msgs)])[0][1] is False
+    # an undecodable public key is an item error
+    bad_pk = bytes([pk[0] ^ 0x01]) + pk[1:]
+    code, _ = gpu.verify_batch([(bad_pk, sig, b"", msgs)])[0]
+    assert code == gpu.ERR_INVALID_INPUT
+
+
+# ----------------------------------------------------------------------------- ProofGen / ProofVerify
+def test_proof_gen_fixtures(gpu, golden, oracle):
+    reqs, want = [], []
+    for c in golden["proof"]:
+        if c["result"]["valid"]:
+            reqs.append((h(c["signerPublicKey"]), h(c["signature"]), h(c["header"]), h(c["presentationHeader"]),
+                         [h(m) for m in c["messages"]], c["disclosedIndexes"]))
+            want.append(c["proof"])
+    got = gpu.proof_gen_batch(reqs, seeds=[oracle.SEED_MOCKED_SCALAR] * len(reqs))
+    assert [(code, p.hex()) for code, p in got] == [(0, w) for w in want]
+
+
+def test_proof_verify_fixtures(gpu, golden):
+    reqs, want = [], []
+    for c in golden["proof"]:
+        msgs = [h(m) for m in c["messages"]]
+        di = c["disclosedIndexes"]
+        reqs.append((h(c["signerPublicKey"]), h(c["proof"]), h(c["header"]), h(c["presentationHeader"]),
+                     [msgs[i] for i in di if i < len(msgs)], di, len(msgs)))
+        want.append(c["result"]["valid"])
+    got = gpu.proof_verify_batch(reqs)
+    assert [v for _, v in got] == want
+
+
+@pytest.mark.parametrize("L,R", [(10, 5), (100, 50), (100, 0), (100, 100), (30, 29)])
+def test_proof_roundtrip_random(gpu, oracle, L, R):
+    seed = b"proof-%d-%d" % (L, R)
+    sk, pk = keypair(oracle, seed)
+    reqs, seeds = [], []
+    for i in range(6):
+        msgs = messages(seed, i, L, 64)
+        hdr = drbg(seed, b"hdr", i, 64)
+        sig = oracle.sign(sk, pk, hdr, msgs)[0]
+        di = disclosed_subset(seed, i, L, R)
+        ph = drbg(seed, b"ph", i, 64)
+        reqs.append((pk, sig, hdr, ph, msgs, di))
+        seeds.append(drbg(seed, b"seed", i, 32))
+    got = gpu.proof_gen_batch(reqs, seeds=seeds)
+    vreqs = []
+    for (pk_, sig, hdr, ph, msgs, di), sd, (code, proof) in zip(reqs, seeds, got):
+        assert code == 0
+        assert proof == oracle.proof_gen(pk_, sig, hdr, ph, msgs, di, seed=sd)
+        dm = [msgs[j] for j in di]
+        vreqs.append((pk_, proof, hdr, ph, dm, di, L))
+        vreqs.append((pk_, proof, hdr, ph + b"!", dm, di, L))
+    ver = gpu.proof_verify_batch(vreqs)
+    assert [v for _, v in ver] == [True, False] * len(reqs)
+
+
+def test_proof_gen_os_randomness_verifies(gpu, oracle):
+    seed = b"proof-os"
+    sk, pk = keypair(oracle, seed)
+    msgs = messages(seed, 0, 12, 32)
+    sig = oracle.sign(sk, pk, b"h", msgs)[0]
+    di = [0, 3, 7]
+    (c1, p1), (c2, p2) = gpu.proof_gen_batch([(pk, sig, b"h", b"p", msgs, di)] * 2)
+    assert c1 == 0 and c2 == 0 and p1 != p2
+    for p in (p1, p2):
+        assert oracle.proof_verify(pk, p, b"h", b"p", [msgs[j] for j in di], di) == 0
+
+
+def test_proof_verify_tampered(gpu, oracle):
+    seed = b"proof-tamper"
+    sk, pk = keypair(oracle, seed)
+    msgs = messages(seed, 0, 20, 32)
+    sig = oracle.sign(sk, pk, b"h", msgs)[0]
+    di = [1, 2, 5, 19]
+    proof = oracle.proof_gen(pk, sig, b"h", b"p", msgs, di, seed=b"t" * 32)
+    dm = [msgs[j] for j in di]
+    flips = [proof[:200] + bytes([proof[200] ^ 1]) + proof[201:],  # r1^ changed
+             proof[:-1] + bytes([proof[-1] ^ 1]),                    # challenge changed
+             bytes([proof[0] ^ 0x20]) + proof[1:],                   # Abar negated
+             proof[:-32],                                            # truncated
+             proof + b"\x00" * 5]                                    # trailing bytes ignored as the reference does
+    reqs = [(pk, f, b"h", b"p", dm, di, 20) for f in flips] + [(pk, proof, b"h", b"p", dm[::-1], di, 20)]
+    got = [v for _, v in gpu.proof_verify_batch(reqs)]
+    want = [oracle.proof_verify(pk, f, b"h", b"p", dm, di) == 0 for f in flips] + [False]
+    assert got == want
+    assert want[-2] is True and not any(want[:4])
