@@ -525,3 +525,41 @@ def pairing_eq_aggregate(reqs):
     res = Result()
     _call("cubbs_bbs_gpu_pairing_eq_aggregate_v2", ABI_VERSION, items, len(reqs), (res))
     return res.code, bool(res.value)
+
+
+def fp_op_for_test(op, a_list, b_list):
+    """Device Fp op (0 mul, 1 inverse, 2 sqrt) on 48-byte BE canonical inputs."""
+    n = len(a_list)
+    a = ctypes.create_string_buffer(b"".join(a_list), max(1, 48 * n))
+    b = ctypes.create_string_buffer(b"".join(b_list), max(1, 48 * n))
+    out = ctypes.create_string_buffer(max(1, 48 * n))
+    st = (ctypes.c_int32 * max(1, n))()
+    fn = lib().cubbs_bbs_gpu_fp_op_for_test_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_uint32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                   ctypes.c_void_p, ctypes.c_void_p]
+    rc = fn(ABI_VERSION, op, ctypes.cast(a, ctypes.c_void_p), ctypes.cast(b, ctypes.c_void_p), n,
+            ctypes.cast(out, ctypes.c_void_p), ctypes.cast(st, ctypes.c_void_p))
+    if rc:
+        raise RuntimeError(f"fp_op_for_test returned {rc}")
+    return [(st[i], out.raw[48 * i:48 * i + 48]) for i in range(n)]
+
+
+def g1_op_for_test(points, scalars):
+    """Device decode (status 0 ok, 1 identity, 2 rejected) -> (status, x||y, k*P compressed)."""
+    n = len(points)
+    p = ctypes.create_string_buffer(b"".join(points), max(1, 48 * n))
+    k = ctypes.create_string_buffer(b"".join(scalars), max(1, 32 * n))
+    xy = ctypes.create_string_buffer(max(1, 96 * n))
+    kp = ctypes.create_string_buffer(max(1, 48 * 77 * n))
+    st = (ctypes.c_int32 * max(1, n))()
+    fn = lib().cubbs_bbs_gpu_g1_op_for_test_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_uint32] + [ctypes.c_void_p] * 2 + [ctypes.c_size_t] + [ctypes.c_void_p] * 3
+    rc = fn(ABI_VERSION, ctypes.cast(p, ctypes.c_void_p), ctypes.cast(k, ctypes.c_void_p), n,
+            ctypes.cast(xy, ctypes.c_void_p), ctypes.cast(kp, ctypes.c_void_p), ctypes.cast(st, ctypes.c_void_p))
+    if rc:
+        raise RuntimeError(f"g1_op_for_test returned {rc}")
+    diag = [[kp.raw[48 * (n + 12 * i + j):48 * (n + 12 * i + j + 1)] for j in range(12)] for i in range(n)]
+    chain = [[kp.raw[48 * (13 * n + 64 * i + j):48 * (13 * n + 64 * i + j + 1)] for j in range(64)] for i in range(n)]
+    return [(st[i], xy.raw[96 * i:96 * i + 96], kp.raw[48 * i:48 * i + 48], diag[i], chain[i]) for i in range(n)]

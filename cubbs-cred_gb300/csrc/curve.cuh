@@ -92,7 +92,7 @@ DEVNI g1 g1_add(g1 p, g1 q) {
   return r;
 }
 // affine conversion with a single inversion; returns false for infinity
-DEVNI bool g1_to_aff(g1 p, g1a &out) {
+DEV bool g1_to_aff(g1 p, g1a &out) {
   if (g1_is_inf(p)) return false;
   fp t = fp_inv(fp_mul(p.ZZ, p.ZZZ));
   out.x = fp_mul(p.X, fp_mul(t, p.ZZZ));  // X / ZZ
@@ -119,7 +119,7 @@ DEV void g1_compress_aff(const g1a &a, uint8_t out[48]) {
   out[0] |= 0x80;
   if (fp_lex_largest(a.y)) out[0] |= 0x20;
 }
-DEVNI void g1_compress(g1 p, uint8_t out[48]) {
+DEV void g1_compress(g1 p, uint8_t out[48]) {
   g1a a;
   if (!g1_to_aff(p, a)) {
     out[0] = 0xc0;
@@ -131,18 +131,17 @@ DEVNI void g1_compress(g1 p, uint8_t out[48]) {
 }
 
 // [|z|]P for |z| = 0xd201000000010000 (bits 63,62,60,57,48,16)
-DEVNI g1 g1_mul_zabs(g1 p) {
+DEV g1 g1_mul_zabs(g1 p) {
   g1 acc = p;
-  const uint64_t z = 0xd201000000010000ull;
   #pragma unroll 1
   for (int i = 62; i >= 0; i--) {
     acc = g1_dbl(acc);
-    if ((z >> i) & 1) acc = g1_add(acc, p);
+    if (zabs_bit(i)) acc = g1_add(acc, p);
   }
   return acc;
 }
 // G1 membership for a curve point: phi(P) == -[z^2]P  <=>  [z^2]P == (beta x, -y)
-DEVNI bool g1_in_subgroup(g1a a) {
+DEV bool g1_in_subgroup(g1a a) {
   g1 t = g1_mul_zabs(g1_mul_zabs(g1_from_aff(a)));
   if (g1_is_inf(t)) return false;
   const fp beta = C_GLV_BETA;
@@ -157,7 +156,7 @@ DEVNI bool g1_in_subgroup(g1a a) {
 #define DEC_BAD 2
 // G1Affine::from_compressed (unchecked decode + torsion check).  Returns DEC_OK
 // with the affine point, DEC_INF for the canonical identity encoding, DEC_BAD otherwise.
-DEVNI int g1_decompress(const uint8_t in[48], g1a &out, bool check_subgroup = true) {
+DEV int g1_decompress(const uint8_t in[48], g1a &out, bool check_subgroup = true) {
   uint8_t f = in[0];
   bool comp = f & 0x80, inf = f & 0x40, sort = f & 0x20;
   uint8_t t[48];
@@ -219,7 +218,7 @@ DEV void recode_w4(const uint32_t v[4], int8_t d[33]) {
   d[32] = (int8_t)carry;
 }
 // k * P (P affine, k canonical raw Fr).  Returns XYZZ.
-DEVNI g1 g1_mul_glv(g1a p, fr k) {
+DEV g1 g1_mul_glv(g1a p, fr k) {
   uint32_t s[4], q[4];
   glv_split(k, s, q);
   int8_t ds[33], dq[33];
@@ -258,7 +257,7 @@ DEV fp2 g2_b() { const fp four = C_FP_FOUR; return {four, four}; }
 DEV bool g2j_is_inf(const g2j &p) { return fp2_is_zero(p.Z); }
 DEV g2j g2j_inf() { return {fp2_one(), fp2_one(), fp2_zero()}; }
 DEV g2j g2j_from_aff(const g2a &a) { return {a.x, a.y, fp2_one()}; }
-DEVNI g2j g2j_dbl(g2j p) {
+DEV g2j g2j_dbl(g2j p) {
   if (g2j_is_inf(p)) return p;
   fp2 A = fp2_sqr(p.X), B = fp2_sqr(p.Y), C = fp2_sqr(B);
   fp2 D = fp2_dbl(fp2_sub(fp2_sub(fp2_sqr(fp2_add(p.X, B)), A), C));
@@ -270,7 +269,7 @@ DEVNI g2j g2j_dbl(g2j p) {
   r.Z = fp2_dbl(fp2_mul(p.Y, p.Z));
   return r;
 }
-DEVNI g2j g2j_add(g2j p, g2j q) {
+DEV g2j g2j_add(g2j p, g2j q) {
   if (g2j_is_inf(p)) return q;
   if (g2j_is_inf(q)) return p;
   fp2 Z1Z1 = fp2_sqr(p.Z), Z2Z2 = fp2_sqr(q.Z);
@@ -290,7 +289,7 @@ DEVNI g2j g2j_add(g2j p, g2j q) {
   return r;
 }
 DEV g2j g2j_neg(const g2j &p) { return {p.X, fp2_neg(p.Y), p.Z}; }
-DEVNI bool g2j_to_aff(g2j p, g2a &out) {
+DEV bool g2j_to_aff(g2j p, g2a &out) {
   if (g2j_is_inf(p)) return false;
   fp2 zi = fp2_inv(p.Z), zi2 = fp2_sqr(zi);
   out.x = fp2_mul(p.X, zi2);
@@ -298,7 +297,7 @@ DEVNI bool g2j_to_aff(g2j p, g2a &out) {
   return true;
 }
 // [r]P == O (naive membership test, used once per public key)
-DEVNI bool g2_in_subgroup(g2a a) {
+DEV bool g2_in_subgroup(g2a a) {
   const fr rm = FR_MOD_INIT;
   g2j p = g2j_from_aff(a), acc = g2j_inf();
   #pragma unroll 1
@@ -308,7 +307,7 @@ DEVNI bool g2_in_subgroup(g2a a) {
   }
   return g2j_is_inf(acc);
 }
-DEVNI g2j g2j_mul_raw(g2a a, fr k) {
+DEV g2j g2j_mul_raw(g2a a, fr k) {
   g2j p = g2j_from_aff(a), acc = g2j_inf();
   #pragma unroll 1
   for (int i = 255; i >= 0; i--) {
@@ -317,7 +316,7 @@ DEVNI g2j g2j_mul_raw(g2a a, fr k) {
   }
   return acc;
 }
-DEVNI int g2_decompress(const uint8_t in[96], g2a &out) {
+DEV int g2_decompress(const uint8_t in[96], g2a &out) {
   uint8_t f = in[0];
   bool comp = f & 0x80, inf = f & 0x40, sort = f & 0x20;
   uint8_t t[48];

@@ -21,6 +21,9 @@ struct fp2 { fp c0, c1; };
 struct fp6 { fp2 c0, c1, c2; };
 struct fp12 { fp6 c0, c1; };
 
+// Bit i of |z| = 0xd201000000010000 (the BLS parameter), from two 32-bit halves.
+DEV uint32_t zabs_bit(int i) { return i >= 32 ? (0xd2010000u >> (i - 32)) & 1u : (0x00010000u >> i) & 1u; }
+
 // ------------------------------------------------------------------ Fp
 DEV fp fp_zero() { fp r; _Pragma("unroll") for (int i = 0; i < 12; i++) r.w[i] = 0; return r; }
 DEV fp fp_one() { const fp r = C_FP_ONE; return r; }
@@ -86,14 +89,14 @@ DEVNI fp fp_pow_window(fp a, const uint32_t *e) {
   }
   return r;
 }
-DEVNI fp fp_inv(fp a) {
+DEV fp fp_inv(fp a) {
   // p - 2
   const uint32_t e[12] = {0xffffaaa9u, 0xb9feffffu, 0xb153ffffu, 0x1eabfffeu, 0xf6b0f624u, 0x6730d2a0u,
                           0xf38512bfu, 0x64774b84u, 0x434bacd7u, 0x4b1ba7b6u, 0x397fe69au, 0x1a0111eau};
   return fp_pow_window(a, e);
 }
 // sqrt for p = 3 mod 4: s = a^((p+1)/4); returns false if a is not a square.
-DEVNI bool fp_sqrt(fp a, fp &out) {
+DEV bool fp_sqrt(fp a, fp &out) {
   const uint32_t e[12] = {0xffffeaabu, 0xee7fbfffu, 0xac54ffffu, 0x07aaffffu, 0x3dac3d89u, 0xd9cc34a8u,
                           0x3ce144afu, 0xd91dd2e1u, 0x90d2eb35u, 0x92c6e9edu, 0x8e5ff9a6u, 0x0680447au};
   fp s = fp_pow_window(a, e);
@@ -282,7 +285,7 @@ DEVNI fp2 fp2_sqr(fp2 a) {
 }
 DEV fp2 fp2_mul_fp(const fp2 &a, const fp &s) { return {fp_mul(a.c0, s), fp_mul(a.c1, s)}; }
 DEV fp2 fp2_mul_xi(const fp2 &a) { return {fp_sub(a.c0, a.c1), fp_add(a.c0, a.c1)}; }  // *(1+u)
-DEVNI fp2 fp2_inv(fp2 a) {
+DEV fp2 fp2_inv(fp2 a) {
   fp n = fp_inv(fp_add(fp_sqr(a.c0), fp_sqr(a.c1)));
   return {fp_mul(a.c0, n), fp_neg(fp_mul(a.c1, n))};
 }
@@ -292,7 +295,7 @@ DEV bool fp2_lex_largest(const fp2 &a) {
 }
 // square root in Fp2 via the norm: for a = a0 + a1 u, sqrt(a) = x0 + x1 u with
 // x0^2 = (a0 +- sqrt(a0^2+a1^2))/2, x1 = a1/(2 x0).
-DEVNI bool fp2_sqrt(fp2 a, fp2 &out) {
+DEV bool fp2_sqrt(fp2 a, fp2 &out) {
   if (fp_is_zero(a.c1)) {
     fp s;
     if (fp_sqrt(a.c0, s)) { out = {s, fp_zero()}; return true; }
@@ -321,7 +324,7 @@ DEV fp6 fp6_add(const fp6 &a, const fp6 &b) { return {fp2_add(a.c0, b.c0), fp2_a
 DEV fp6 fp6_sub(const fp6 &a, const fp6 &b) { return {fp2_sub(a.c0, b.c0), fp2_sub(a.c1, b.c1), fp2_sub(a.c2, b.c2)}; }
 DEV fp6 fp6_neg(const fp6 &a) { return {fp2_neg(a.c0), fp2_neg(a.c1), fp2_neg(a.c2)}; }
 DEV bool fp6_eq(const fp6 &a, const fp6 &b) { return fp2_eq(a.c0, b.c0) && fp2_eq(a.c1, b.c1) && fp2_eq(a.c2, b.c2); }
-DEVNI fp6 fp6_mul(fp6 a, fp6 b) {
+DEV fp6 fp6_mul(fp6 a, fp6 b) {
   fp2 a0 = fp2_mul(a.c0, b.c0), a1 = fp2_mul(a.c1, b.c1), a2 = fp2_mul(a.c2, b.c2);
   fp2 t0 = fp2_add(fp2_mul_xi(fp2_sub(fp2_sub(fp2_mul(fp2_add(a.c1, a.c2), fp2_add(b.c1, b.c2)), a1), a2)), a0);
   fp2 t1 = fp2_add(fp2_sub(fp2_sub(fp2_mul(fp2_add(a.c0, a.c1), fp2_add(b.c0, b.c1)), a0), a1), fp2_mul_xi(a2));
@@ -329,7 +332,7 @@ DEVNI fp6 fp6_mul(fp6 a, fp6 b) {
   return {t0, t1, t2};
 }
 DEV fp6 fp6_mul_v(const fp6 &a) { return {fp2_mul_xi(a.c2), a.c0, a.c1}; }
-DEVNI fp6 fp6_inv(fp6 a) {
+DEV fp6 fp6_inv(fp6 a) {
   fp2 t0 = fp2_sub(fp2_sqr(a.c0), fp2_mul_xi(fp2_mul(a.c1, a.c2)));
   fp2 t1 = fp2_sub(fp2_mul_xi(fp2_sqr(a.c2)), fp2_mul(a.c0, a.c1));
   fp2 t2 = fp2_sub(fp2_sqr(a.c1), fp2_mul(a.c0, a.c2));
@@ -342,12 +345,12 @@ DEVNI fp6 fp6_inv(fp6 a) {
 DEV fp12 fp12_one() { return {fp6_one(), fp6_zero()}; }
 DEV bool fp12_eq(const fp12 &a, const fp12 &b) { return fp6_eq(a.c0, b.c0) && fp6_eq(a.c1, b.c1); }
 DEV bool fp12_is_one(const fp12 &a) { return fp12_eq(a, fp12_one()); }
-DEVNI fp12 fp12_mul(fp12 a, fp12 b) {
+DEV fp12 fp12_mul(fp12 a, fp12 b) {
   fp6 t0 = fp6_mul(a.c0, b.c0), t1 = fp6_mul(a.c1, b.c1);
   fp6 t2 = fp6_sub(fp6_sub(fp6_mul(fp6_add(a.c0, a.c1), fp6_add(b.c0, b.c1)), t0), t1);
   return {fp6_add(t0, fp6_mul_v(t1)), t2};
 }
-DEVNI fp12 fp12_sqr(fp12 a) {
+DEV fp12 fp12_sqr(fp12 a) {
   // (a0 + a1 w)^2 = (a0^2 + v a1^2) + 2 a0 a1 w ; via (a0+a1)(a0+v a1) - a0a1 - v a0a1
   fp6 ab = fp6_mul(a.c0, a.c1);
   fp6 t = fp6_mul(fp6_add(a.c0, a.c1), fp6_add(a.c0, fp6_mul_v(a.c1)));
@@ -355,13 +358,13 @@ DEVNI fp12 fp12_sqr(fp12 a) {
   return {c0, fp6_add(ab, ab)};
 }
 DEV fp12 fp12_conj(const fp12 &a) { return {a.c0, fp6_neg(a.c1)}; }
-DEVNI fp12 fp12_inv(fp12 a) {
+DEV fp12 fp12_inv(fp12 a) {
   fp6 t = fp6_inv(fp6_sub(fp6_mul(a.c0, a.c0), fp6_mul_v(fp6_mul(a.c1, a.c1))));
   return {fp6_mul(a.c0, t), fp6_neg(fp6_mul(a.c1, t))};
 }
 // Frobenius x -> x^p: conjugate each Fp2 coefficient and scale the basis
 // element w^k by gamma_k = xi^(k(p-1)/6).
-DEVNI fp12 fp12_frobenius(fp12 a) {
+DEV fp12 fp12_frobenius(fp12 a) {
   const fp2 g[6] = C_FROB_GAMMA;
   fp12 r;
   r.c0.c0 = fp2_conj(a.c0.c0);

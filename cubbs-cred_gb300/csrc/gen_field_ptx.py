@@ -71,7 +71,7 @@ def gen_field(name, mod, n):
     asm_text = "\\n\\t".join(body)
     w(f"// t[0..{n}] += a*b + m*mod with m = t0*pinv; afterwards t0 == 0 and the value is t[1..{n}].")
     w(f"__device__ __forceinline__ void {name}_cios_row(uint32_t *t, const uint32_t *a, uint32_t b) {{")
-    outs = ", ".join(f'"+r"(t[{i}])' for i in range(n + 1))
+    outs = ", ".join(f'"+&r"(t[{i}])' for i in range(n + 1))
     ins = ", ".join(f'"r"(a[{i}])' for i in range(n)) + ', "r"(b)'
     w(f'  asm volatile("{asm_text}" : {outs} : {ins});')
     w("}")
@@ -89,7 +89,7 @@ def gen_field(name, mod, n):
     body.append("}")
     asm_text = "\\n\\t".join(body)
     w(f"__device__ __forceinline__ void {name}_reduce_once(uint32_t *r, const uint32_t *t) {{")
-    outs = ", ".join(f'"=r"(r[{i}])' for i in range(n))
+    outs = ", ".join(f'"=&r"(r[{i}])' for i in range(n))
     ins = ", ".join(f'"r"(t[{i}])' for i in range(n))
     w(f'  asm("{asm_text}" : {outs} : {ins});')
     w("}")
@@ -110,7 +110,7 @@ def gen_field(name, mod, n):
     body.append("}")
     asm_text = "\\n\\t".join(body)
     w(f"__device__ __forceinline__ void {name}_add_raw(uint32_t *r, const uint32_t *a, const uint32_t *b) {{")
-    outs = ", ".join(f'"=r"(r[{i}])' for i in range(n))
+    outs = ", ".join(f'"=&r"(r[{i}])' for i in range(n))
     ins = ", ".join(f'"r"(a[{i}])' for i in range(n)) + ", " + ", ".join(f'"r"(b[{i}])' for i in range(n))
     w(f'  asm("{asm_text}" : {outs} : {ins});')
     w("}")

@@ -15,7 +15,7 @@ DEV fp poly_eval(const fp *c, int n, const fp &x) {
 }
 
 // simplified SWU onto E': y^2 = x^3 + A'x + B' (RFC 9380 6.6.2), then the isogeny onto E.
-DEVNI g1a map_to_curve_g1(fp u) {
+DEV g1a map_to_curve_g1(fp u) {
   const fp A = C_SSWU_A, B = C_SSWU_B, Z = C_SSWU_Z;
   const fp mBA = C_SSWU_MINUS_B_OVER_A, BZA = C_SSWU_B_OVER_ZA;
   fp u2 = fp_sqr(u);
@@ -47,7 +47,7 @@ DEVNI g1a map_to_curve_g1(fp u) {
 }
 
 // hash_to_curve(msg, dst): returns an XYZZ point (cofactor cleared with h_eff = |z| + 1).
-DEVNI g1 hash_to_curve_g1(const uint8_t *msg, uint32_t len, const uint8_t *dst, uint32_t dlen) {
+DEV g1 hash_to_curve_g1(const uint8_t *msg, uint32_t len, const uint8_t *dst, uint32_t dlen) {
   sha_ctx c;
   xmd_begin(c);
   sha_bytes(c, msg, len);

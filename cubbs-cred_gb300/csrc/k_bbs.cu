@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cstring>
 
+#include "bbs_dst.cuh"
 #include "runtime.cuh"
 #include "sha256.cuh"
 
@@ -24,22 +25,31 @@ namespace cubbs {
 
 // ----------------------------------------------------------------------------- raw Fr helpers
 DEVNI fr frr_mul(fr a, fr b) { return fr_mul(a, fr_to_mont(b)); }
-DEVNI fr frr_inv(fr a) { return fr_from_mont(fr_inv(fr_to_mont(a))); }
+DEV fr frr_inv(fr a) { return fr_from_mont(fr_inv(fr_to_mont(a))); }
 DEV fr frr_neg(const fr &a) { return fr_sub(fr_zero(), a); }
 DEV fr frr_one() { fr r = fr_zero(); r.w[0] = 1; return r; }
 
-__device__ __constant__ static const uint8_t API_ID_K[44] = {
-    'B', 'B', 'S', '_', 'B', 'L', 'S', '1', '2', '3', '8', '1', 'G', '1', '_', 'X', 'M', 'D', ':', 'S', 'H', 'A',
-    '-', '2', '5', '6', '_', 'S', 'S', 'W', 'U', '_', 'R', 'O', '_', 'H', '2', 'G', '_', 'H', 'M', '2', 'S', '_'};
-
-DEV void h2s_dst(uint8_t dst[48]) {
-  for (int k = 0; k < 44; k++) dst[k] = API_ID_K[k];
-  dst[44] = 'H'; dst[45] = '2'; dst[46] = 'S'; dst[47] = '_';
-}
 DEV void sha_fr_be(sha_ctx &c, const fr &raw) {
   uint8_t b[32];
   fr_raw_to_be32(raw, b);
   sha_bytes(c, b, 32);
+}
+
+// Debug record of item 0 of the last ProofGen / ProofVerify finish kernel:
+// [0,48) T1, [48,96) T2, [96,128) domain BE, [128,160) challenge BE,
+// [160,164) R, [164,180) first four disclosed indexes, [180,212) first disclosed scalar BE.
+__device__ uint8_t g_debug_record[256];
+DEV void debug_record(const uint8_t *t1c, const uint8_t *t2c, const fr &dom, const fr &ch, uint32_t R,
+                      const uint32_t *idx, const fr *m0) {
+  for (int k = 0; k < 48; k++) { g_debug_record[k] = t1c[k]; g_debug_record[48 + k] = t2c[k]; }
+  fr_raw_to_be32(dom, g_debug_record + 96);
+  fr_raw_to_be32(ch, g_debug_record + 128);
+  for (int k = 0; k < 4; k++) g_debug_record[160 + k] = (uint8_t)(R >> (8 * k));
+  for (uint32_t j = 0; j < 4; j++) {
+    uint32_t v = j < R ? idx[j] : 0xffffffffu;
+    for (int k = 0; k < 4; k++) g_debug_record[164 + 4 * j + k] = (uint8_t)(v >> (8 * k));
+  }
+  if (R && m0) fr_raw_to_be32(*m0, g_debug_record + 180);
 }
 
 // Item status codes kept on the device
@@ -149,9 +159,8 @@ __global__ void __launch_bounds__(64) k_pv_finish(PvItem *items, uint32_t n, con
   sha_fr_be(c, domain[i]);
   sha_u64be(c, it.ph_len, 8);
   sha_bytes(c, blob + it.ph_off, it.ph_len);
-  uint8_t dst[48];
-  h2s_dst(dst);
-  fr ch = h2s_finish(c, dst, 48);
+  fr ch = h2s_finish(c, DST_H2S, DST_H2S_LEN);
+  if (i == 0) debug_record(t1c, t2c, domain[i], ch, it.R, idx, it.R ? &msc[it.msg_base] : nullptr);
   fr cp;
   fr_raw_from_be32(pr + 240 + 32 * it.U, cp);
   if (!fr_eq(ch, cp)) {
@@ -192,9 +201,7 @@ __global__ void __launch_bounds__(64) k_sign_prep(SignItem *items, uint32_t n, c
   #pragma unroll 1
   for (uint32_t k = 0; k < it.L; k++) sha_fr_be(c, msc[it.msg_base + k]);
   sha_fr_be(c, domain[i]);
-  uint8_t dst[48];
-  h2s_dst(dst);
-  fr e = h2s_finish(c, dst, 48);
+  fr e = h2s_finish(c, DST_H2S, DST_H2S_LEN);
   e_out[i] = e;
   fr ske = fr_add(sk, e);
   if (fr_is_zero(ske)) {
@@ -302,10 +309,7 @@ __global__ void __launch_bounds__(64) k_pg_random(const PgItem *items, uint32_t 
   if (i >= n) return;
   PgItem it = items[i];
   if (it.status != ST_OK) return;
-  uint8_t dst[68];
-  for (int k = 0; k < 44; k++) dst[k] = API_ID_K[k];
-  const char *sfx = "MOCK_RANDOM_SCALARS_DST_";
-  for (int k = 0; k < 24; k++) dst[44 + k] = (uint8_t)sfx[k];
+  const uint8_t *dst = DST_MOCK;
   uint32_t count = 5 + it.U;
   const uint32_t CH = 170;
   fr *out = rs + (size_t)i * rs_stride;
@@ -327,8 +331,8 @@ __global__ void __launch_bounds__(64) k_pg_random(const PgItem *items, uint32_t 
     sha_byte(c, (uint8_t)(nbytes >> 8));
     sha_byte(c, (uint8_t)nbytes);
     sha_byte(c, 0);
-    sha_bytes(c, dst, 68);
-    sha_byte(c, 68);
+    sha_bytes(c, dst, DST_MOCK_LEN);
+    sha_byte(c, DST_MOCK_LEN);
     uint8_t b0[32], bi[32];
     sha_final(c, b0);
     uint8_t okm[48];
@@ -340,8 +344,8 @@ __global__ void __launch_bounds__(64) k_pg_random(const PgItem *items, uint32_t 
       sha_init(s);
       for (int j = 0; j < 32; j++) sha_byte(s, b == 1 ? b0[j] : (uint8_t)(b0[j] ^ bi[j]));
       sha_byte(s, (uint8_t)b);
-      sha_bytes(s, dst, 68);
-      sha_byte(s, 68);
+      sha_bytes(s, dst, DST_MOCK_LEN);
+      sha_byte(s, DST_MOCK_LEN);
       sha_final(s, bi);
       for (int j = 0; j < 32; j++) {
         okm[fill++] = bi[j];
@@ -459,9 +463,8 @@ __global__ void __launch_bounds__(64) k_pg_finish(PgItem *items, uint32_t n, con
   sha_fr_be(c, domain[i]);
   sha_u64be(c, it.ph_len, 8);
   sha_bytes(c, blob + it.ph_off, it.ph_len);
-  uint8_t dst[48];
-  h2s_dst(dst);
-  fr ch = h2s_finish(c, dst, 48);
+  fr ch = h2s_finish(c, DST_H2S, DST_H2S_LEN);
+  if (i == 0) debug_record(t1c, t2c, domain[i], ch, it.R, idx, it.R ? &msc[it.msg_base + idx[0]] : nullptr);
   const fr *r = rs + (size_t)i * rs_stride;
   fr r1 = r[0], r2 = r[1], et = r[2], r1t = r[3], r3t = r[4];
   if (fr_is_zero(r2)) {  // "Invert scalar failed" (proof.rs:2340-2341)
@@ -1064,4 +1067,90 @@ extern "C" int32_t cubbs_bbs_gpu_proof_gen_seeded_batch_v2(uint32_t abi, CuBbsBb
     return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   return proof_gen_impl(items, n, seeds, results);
+}
+
+// Test export: H2S(s_0 || ... || s_{n-1}, api_id || "H2S_") over canonical scalars,
+// absorbed exactly as the Sign e-hash and the challenge hash do (parse -> raw -> BE).
+__global__ void k_h2s_scalars_test(const uint8_t *be, uint32_t n, fr *out) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  sha_ctx c;
+  xmd_begin(c);
+  for (uint32_t k = 0; k < n; k++) {
+    fr s;
+    fr_raw_from_be32(be + 32 * k, s);
+    sha_fr_be(c, s);
+  }
+  out[0] = h2s_finish(c, DST_H2S, DST_H2S_LEN);
+}
+
+extern "C" int32_t cubbs_bbs_gpu_h2s_scalars_for_test_v2(uint32_t abi, const uint8_t *be, size_t n, uint8_t *out32) {
+  if (abi != CUBBS_BBS_GPU_ABI_VERSION || !be || !out32 || n == 0) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  try {
+    Runtime &rt = Runtime::get();
+    CallScope scope(rt);
+    uint8_t *d = rt.arena.alloc<uint8_t>(32 * n);
+    fr *o = rt.arena.alloc<fr>(1);
+    CUBBS_CHECK(cudaMemcpy(d, be, 32 * n, cudaMemcpyHostToDevice));
+    k_h2s_scalars_test<<<1, 32, 0, rt.stream>>>(d, (uint32_t)n, o);
+    CUBBS_CHECK(cudaGetLastError());
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    uint32_t raw[8];
+    CUBBS_CHECK(cudaMemcpy(raw, o, 32, cudaMemcpyDeviceToHost));
+    for (int w = 0; w < 8; w++)
+      for (int b = 0; b < 4; b++) out32[(7 - w) * 4 + (3 - b)] = (uint8_t)(raw[w] >> (8 * b));
+    return 0;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}
+
+// Test export: the disclosed-pair part of the challenge, H2S(I2OSP(R,8) || (I2OSP(i_k,8) || m_k)...),
+// with the indexes read as uint32 from a byte blob at offset idx_off (as the proof kernels do).
+__global__ void k_pairs_test(const uint8_t *blob, uint32_t idx_off, uint32_t R, const uint8_t *mbe, fr *out,
+                             uint32_t *echo) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + idx_off);
+  sha_ctx c;
+  xmd_begin(c);
+  sha_u64be(c, R, 8);
+  for (uint32_t k = 0; k < R; k++) {
+    echo[k] = idx[k];
+    sha_u64be(c, idx[k], 8);
+    fr m;
+    fr_raw_from_be32(mbe + 32 * k, m);
+    sha_fr_be(c, m);
+  }
+  out[0] = h2s_finish(c, DST_H2S, DST_H2S_LEN);
+}
+
+extern "C" int32_t cubbs_bbs_gpu_pairs_h2s_for_test_v2(uint32_t abi, const uint8_t *blob, size_t blob_len,
+                                                       uint32_t idx_off, uint32_t R, const uint8_t *mbe,
+                                                       uint8_t *out32, uint32_t *echo) {
+  if (abi != CUBBS_BBS_GPU_ABI_VERSION) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  try {
+    Runtime &rt = Runtime::get();
+    CallScope scope(rt);
+    uint8_t *d = rt.arena.alloc<uint8_t>(blob_len + 1);
+    uint8_t *dm = rt.arena.alloc<uint8_t>(32 * R + 1);
+    uint32_t *de = rt.arena.alloc<uint32_t>(R + 1);
+    fr *o = rt.arena.alloc<fr>(1);
+    CUBBS_CHECK(cudaMemcpy(d, blob, blob_len, cudaMemcpyHostToDevice));
+    if (R) CUBBS_CHECK(cudaMemcpy(dm, mbe, 32 * R, cudaMemcpyHostToDevice));
+    k_pairs_test<<<1, 32, 0, rt.stream>>>(d, idx_off, R, dm, o, de);
+    CUBBS_CHECK(cudaGetLastError());
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    uint32_t raw[8];
+    CUBBS_CHECK(cudaMemcpy(raw, o, 32, cudaMemcpyDeviceToHost));
+    if (R) CUBBS_CHECK(cudaMemcpy(echo, de, 4 * R, cudaMemcpyDeviceToHost));
+    for (int w = 0; w < 8; w++)
+      for (int b = 0; b < 4; b++) out32[(7 - w) * 4 + (3 - b)] = (uint8_t)(raw[w] >> (8 * b));
+    return 0;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}
+
+extern "C" int32_t cubbs_bbs_gpu_last_debug_record_for_test_v2(uint8_t *out256) {
+  if (!out256) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  return cudaMemcpyFromSymbol(out256, g_debug_record, 256) == cudaSuccess ? 0 : CUBBS_BBS_GPU_ERR_INTERNAL;
 }

@@ -5,13 +5,11 @@
 #include <cstring>
 
 #include "h2c.cuh"
+#include "bbs_dst.cuh"
 #include "runtime.cuh"
 
 namespace cubbs {
 
-__device__ __constant__ static const uint8_t API_ID_DEV[44] = {
-    'B', 'B', 'S', '_', 'B', 'L', 'S', '1', '2', '3', '8', '1', 'G', '1', '_', 'X', 'M', 'D', ':', 'S', 'H', 'A',
-    '-', '2', '5', '6', '_', 'S', 'S', 'W', 'U', '_', 'R', 'O', '_', 'H', '2', 'G', '_', 'H', 'M', '2', 'S', '_'};
 
 __global__ void k_sha256_flat(const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens, uint32_t n,
                               uint8_t *digests) {
@@ -55,13 +53,10 @@ __global__ void k_domain(const DomainJob *jobs, uint32_t n, const uint8_t *blob,
   sha_u64be(c, j.L, 8);
   // Q1, H1..H_L are d_gens_c[1 .. L+1]
   sha_bytes(c, gens_c + 48, 48 * (j.L + 1));
-  sha_bytes(c, API_ID_DEV, 44);
+  sha_bytes(c, API_ID, API_ID_LEN);
   sha_u64be(c, j.hdr_len, 8);
   sha_bytes(c, blob + j.hdr_off, j.hdr_len);
-  uint8_t dst[48];
-  for (int k = 0; k < 44; k++) dst[k] = API_ID_DEV[k];
-  dst[44] = 'H'; dst[45] = '2'; dst[46] = 'S'; dst[47] = '_';
-  out[i] = h2s_finish(c, dst, 48);
+  out[i] = h2s_finish(c, DST_H2S, DST_H2S_LEN);
 }
 
 // Generator seed chain (generators.rs:131-144): v_0 = expand(seed, seed_dst),
@@ -69,20 +64,13 @@ __global__ void k_domain(const DomainJob *jobs, uint32_t n, const uint8_t *blob,
 // state holds v_{first-1} (48 bytes) on entry and v_{first+count-1} on exit.
 __global__ void k_generator_seeds(int first, int count, uint8_t *state, uint8_t *seeds) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  uint8_t dst[63];
-  for (int k = 0; k < 44; k++) dst[k] = API_ID_DEV[k];
-  const char *sfx = "SIG_GENERATOR_SEED_";
-  for (int k = 0; k < 19; k++) dst[44 + k] = (uint8_t)sfx[k];
+  const uint8_t *dst = DST_GEN_SEED;
   uint8_t v[48];
   if (first == 1) {
-    const char *gs = "MESSAGE_GENERATOR_SEED";
-    uint8_t seed[66];
-    for (int k = 0; k < 44; k++) seed[k] = API_ID_DEV[k];
-    for (int k = 0; k < 22; k++) seed[44 + k] = (uint8_t)gs[k];
     sha_ctx c;
     xmd_begin(c);
-    sha_bytes(c, seed, 66);
-    xmd_finish(c, dst, 63, 48, v);
+    sha_bytes(c, GEN_SEED, GEN_SEED_LEN);
+    xmd_finish(c, dst, DST_GEN_SEED_LEN, 48, v);
   } else {
     for (int k = 0; k < 48; k++) v[k] = state[k];
   }
@@ -92,7 +80,7 @@ __global__ void k_generator_seeds(int first, int count, uint8_t *state, uint8_t 
     xmd_begin(c);
     sha_bytes(c, v, 48);
     sha_u64be(c, (uint64_t)i, 8);
-    xmd_finish(c, dst, 63, 48, v);
+    xmd_finish(c, dst, DST_GEN_SEED_LEN, 48, v);
     for (int k = 0; k < 48; k++) seeds[48 * (size_t)(i - first) + k] = v[k];
   }
   for (int k = 0; k < 48; k++) state[k] = v[k];
@@ -102,11 +90,7 @@ __global__ void k_generator_seeds(int first, int count, uint8_t *state, uint8_t 
 __global__ void k_hash_generators(int first, int count, const uint8_t *seeds, g1a *gens, uint8_t *gens_c) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= count) return;
-  uint8_t dst[62];
-  for (int k = 0; k < 44; k++) dst[k] = API_ID_DEV[k];
-  const char *sfx = "SIG_GENERATOR_DST_";
-  for (int k = 0; k < 18; k++) dst[44 + k] = (uint8_t)sfx[k];
-  g1 p = hash_to_curve_g1(seeds + 48 * (size_t)t, 48, dst, 62);
+  g1 p = hash_to_curve_g1(seeds + 48 * (size_t)t, 48, DST_GEN, DST_GEN_LEN);
   g1a a;
   g1_to_aff(p, a);
   int idx = first + t;  // d_gens index: P1 at 0, Q1 at 1

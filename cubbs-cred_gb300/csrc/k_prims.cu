@@ -73,13 +73,12 @@ __global__ void k_multi_pairing(const g1a *P, const int32_t *slots, const uint8_
                                 const line2 *lines, uint8_t *ok) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   fp12 f = fp12_one();
-  const uint64_t z = 0xd201000000010000ull;
   int idx = 0;
 #pragma unroll 1
   for (int i = 62; i >= 0; i--) {
     f = fp12_sqr(f);
 #pragma unroll 1
-    for (int step = 0; step < (((z >> i) & 1) ? 2 : 1); step++) {
+    for (int step = 0; step < (zabs_bit(i) ? 2 : 1); step++) {
 #pragma unroll 1
       for (uint32_t k = 0; k < K; k++) {
         if (skip[k]) continue;

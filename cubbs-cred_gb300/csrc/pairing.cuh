@@ -18,9 +18,8 @@
 struct line2 { fp2 a, b; };
 
 // Lines of the Miller loop for Q (affine, not infinity), written to out[0..67].
-DEVNI void g2_precompute_lines(g2a q, line2 *out) {
+DEV void g2_precompute_lines(g2a q, line2 *out) {
   g2j T = g2j_from_aff(q);
-  const uint64_t z = 0xd201000000010000ull;
   int idx = 0;
   #pragma unroll 1
   for (int i = 62; i >= 0; i--) {
@@ -36,7 +35,7 @@ DEVNI void g2_precompute_lines(g2a q, line2 *out) {
       idx++;
       T = g2j_dbl(T);
     }
-    if ((z >> i) & 1) {  // chord through T and Q
+    if (zabs_bit(i)) {  // chord through T and Q
       fp2 Z2 = fp2_sqr(T.Z);
       fp2 N = fp2_sub(fp2_mul(fp2_mul(q.y, Z2), T.Z), T.Y);
       fp2 D = fp2_mul(T.Z, fp2_sub(fp2_mul(q.x, Z2), T.X));
@@ -52,7 +51,7 @@ DEVNI void g2_precompute_lines(g2a q, line2 *out) {
 }
 
 // f *= (A + (B xP) v + yP v w)
-DEVNI fp12 fp12_mul_line(fp12 f, fp2 A, fp2 Bx, fp yP) {
+DEV fp12 fp12_mul_line(fp12 f, fp2 A, fp2 Bx, fp yP) {
   // l0 = (A, Bx, 0) in Fp6, l1 = (0, yP, 0) in Fp6 (coefficient of w)
   // f0*l0 (sparse)
   const fp6 &f0 = f.c0, &f1 = f.c1;
@@ -90,7 +89,6 @@ DEVNI fp12 fp12_mul_line(fp12 f, fp2 A, fp2 Bx, fp yP) {
 template <int NP>
 DEV fp12 miller_loop_lines(const g1a *P, const line2 *const *lines, const bool *skip) {
   fp12 f = fp12_one();
-  const uint64_t z = 0xd201000000010000ull;
   int idx = 0;
   #pragma unroll 1
   for (int i = 62; i >= 0; i--) {
@@ -102,7 +100,7 @@ DEV fp12 miller_loop_lines(const g1a *P, const line2 *const *lines, const bool *
       f = fp12_mul_line(f, l.a, fp2_mul_fp(l.b, P[k].x), P[k].y);
     }
     idx++;
-    if ((z >> i) & 1) {
+    if (zabs_bit(i)) {
       #pragma unroll 1
       for (int k = 0; k < NP; k++) {
         if (skip[k]) continue;
@@ -115,20 +113,19 @@ DEV fp12 miller_loop_lines(const g1a *P, const line2 *const *lines, const bool *
   return fp12_conj(f);  // z < 0
 }
 
-DEVNI fp12 fp12_exp_by_zabs(fp12 f) {
+DEV fp12 fp12_exp_by_zabs(fp12 f) {
   fp12 r = f;
-  const uint64_t z = 0xd201000000010000ull;
   #pragma unroll 1
   for (int i = 62; i >= 0; i--) {
     r = fp12_sqr(r);
-    if ((z >> i) & 1) r = fp12_mul(r, f);
+    if (zabs_bit(i)) r = fp12_mul(r, f);
   }
   return r;
 }
 // f^z for unitary f (z < 0)
 DEV fp12 fp12_exp_by_z(const fp12 &f) { return fp12_conj(fp12_exp_by_zabs(f)); }
 
-DEVNI fp12 final_exponentiation(fp12 f) {
+DEV fp12 final_exponentiation(fp12 f) {
   fp12 t = fp12_mul(fp12_conj(f), fp12_inv(f));
   t = fp12_mul(fp12_frobenius(fp12_frobenius(t)), t);
   fp12 a = fp12_mul(fp12_exp_by_z(t), fp12_conj(t));

@@ -68,13 +68,14 @@ DEV void sha_byte(sha_ctx &c, uint8_t b) {
     c.fill = 0;
   }
 }
-DEVNI void sha_bytes(sha_ctx &c, const uint8_t *p, uint32_t n) {
-  // word-at-a-time fast path when both the input and the block are 4-aligned
+DEV void sha_bytes(sha_ctx &c, const uint8_t *p, uint32_t n) {
+  // word-at-a-time when the block position is 4-aligned (bytes are assembled
+  // individually: the source may be a byte array just written by this thread)
   uint32_t i = 0;
-  if (((uintptr_t)p & 3) == 0 && (c.fill & 3) == 0) {
+  if ((c.fill & 3) == 0) {
+#pragma unroll 1
     while (i + 4 <= n) {
-      uint32_t v = *(const uint32_t *)(p + i);
-      c.w[c.fill >> 2] = __byte_perm(v, 0, 0x0123);
+      c.w[c.fill >> 2] = ((uint32_t)p[i] << 24) | ((uint32_t)p[i + 1] << 16) | ((uint32_t)p[i + 2] << 8) | p[i + 3];
       c.fill += 4;
       c.total += 4;
       i += 4;
@@ -85,14 +86,14 @@ DEVNI void sha_bytes(sha_ctx &c, const uint8_t *p, uint32_t n) {
       }
     }
   }
-  #pragma unroll 1
+#pragma unroll 1
   for (; i < n; i++) sha_byte(c, p[i]);
 }
-DEVNI void sha_u64be(sha_ctx &c, uint64_t x, int nbytes) {
+DEV void sha_u64be(sha_ctx &c, uint64_t x, int nbytes) {
   #pragma unroll 1
   for (int i = nbytes - 1; i >= 0; i--) sha_byte(c, (uint8_t)(x >> (8 * i)));
 }
-DEVNI void sha_final(sha_ctx &c, uint8_t out[32]) {
+DEV void sha_final(sha_ctx &c, uint8_t out[32]) {
   uint64_t bits = (uint64_t)c.total * 8;
   sha_byte(c, 0x80);
   while (c.fill != 56) sha_byte(c, 0);
@@ -108,12 +109,14 @@ DEVNI void sha_final(sha_ctx &c, uint8_t out[32]) {
 // expand_message_xmd: the caller absorbs msg into ctx after xmd_begin().
 DEV void xmd_begin(sha_ctx &c) {
   sha_init(c);
-  // Z_pad: one all-zero 64-byte block
+  // Z_pad: one all-zero 64-byte block (the compression overwrites w with the
+  // message schedule, so clear it again)
   sha256_compress(c.h, c.w);
+  for (int i = 0; i < 16; i++) c.w[i] = 0;
   c.total = 64;
 }
 // Finishes b_0 and writes n output bytes (n <= 255*32).
-DEVNI void xmd_finish(sha_ctx &c, const uint8_t *dst, uint32_t dlen, uint32_t n, uint8_t *out) {
+DEV void xmd_finish(sha_ctx &c, const uint8_t *dst, uint32_t dlen, uint32_t n, uint8_t *out) {
   sha_byte(c, (uint8_t)(n >> 8));
   sha_byte(c, (uint8_t)n);
   sha_byte(c, 0);
@@ -138,7 +141,7 @@ DEVNI void xmd_finish(sha_ctx &c, const uint8_t *dst, uint32_t dlen, uint32_t n,
 }
 // hash_to_scalar (util.rs:104-129): OS2IP(expand_message_xmd(msg, dst, 48)) mod r,
 // returned as the canonical raw residue.
-DEVNI fr h2s_finish(sha_ctx &c, const uint8_t *dst, uint32_t dlen) {
+DEV fr h2s_finish(sha_ctx &c, const uint8_t *dst, uint32_t dlen) {
   uint8_t okm[48];
   xmd_finish(c, dst, dlen, 48, okm);
   return fr_raw_from_okm(okm);

@@ -175,3 +175,40 @@ def test_proof_verify_tampered(gpu, oracle):
     want = [oracle.proof_verify(pk, f, b"h", b"p", dm, di) == 0 for f in flips] + [False]
     assert got == want
     assert want[-2] is True and not any(want[:4])
+
+
+def test_sign_e_resident(gpu, oracle):
+    import ctypes
+    seed = b"sign-e"
+    sk, pk = keypair(oracle, seed)
+    msgs = messages(seed, 0, 6, 32)
+    dom = scalar(seed, b"dom", 0)
+    k = gpu._Keep()
+    item = gpu.SignEFromResidentScalarsItem()
+    item.secret_key = k.bytes(sk)
+    item.domain = k.bytes(dom)
+    item.messages = k.slices(msgs)
+    item.message_scalar_offset = 0
+    item.message_count = len(msgs)
+    mo, mbuf = k.out(32 * len(msgs))
+    eo, ebuf = k.out(32)
+    item.message_scalars_out = mo
+    item.scalar_out = eo
+    res = (gpu.Result * 1)()
+    rc = gpu.lib().cubbs_bbs_gpu_sign_e_from_resident_scalars_batch_v2(
+        2, ctypes.cast(ctypes.pointer(item), ctypes.c_void_p), 1, k.bytes(gpu.MAP_DST), k.bytes(gpu.H2S_DST),
+        ctypes.cast(res, ctypes.c_void_p))
+    assert rc == 0 and res[0].code == 0
+    scal = [oracle.hash_to_scalar(m, gpu.MAP_DST) for m in msgs]
+    assert mbuf.raw[:32 * len(msgs)] == b"".join(scal)
+    assert ebuf.raw[:32] == oracle.hash_to_scalar(sk + b"".join(scal) + dom, gpu.H2S_DST)
+
+
+def test_sign_parts(gpu, oracle, golden):
+    c = golden["signature"][0]
+    sk, pk = h(c["signerKeyPair"]["secretKey"]), h(c["signerKeyPair"]["publicKey"])
+    msgs, hdr = [h(m) for m in c["messages"]], h(c["header"])
+    (code, sig), = gpu.sign_batch([(sk, pk, hdr, msgs)])
+    want = h(c["signature"])
+    assert (code, sig[48:].hex()) == (0, want[48:].hex()), "e differs"
+    assert sig[:48].hex() == want[:48].hex(), "A differs"
