@@ -1,0 +1,348 @@
+#!/usr/bin/env python3
+"""BBS ProofVerify / ProofGen throughput at L=100 on GB300 (one JSON line).
+
+Workload: BBS ProofGen + ProofVerify, BLS12-381-SHA-256, L = 100 messages of
+64 random bytes, a seeded 50-message disclosed subset per proof, 1024 proofs
+per batch (one step = one pass of the device pipeline over that batch).
+Inputs are synthetic and seeded (SHA-256 counter DRBG); signatures and proofs
+are produced by this library before timing.  Headline metric: ProofVerify
+ops/s; ProofGen, Sign and Verify ops/s are reported beside it.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+value       : device-resident pipeline throughput (inputs in HBM, CUDA events on
+              the library stream, L2 flushed between steps)
+e2e         : the same metric through the C ABI with host buffers (packing,
+              H2D and D2H inside the timed region)
+roofline    : the dominant stage vs the measured integer multiply-add peak
+cpu_baseline: the CPU oracle (a port of the reference's Rust CPU path) on all
+              host cores, on a bounded sample of the same workload
+--impl reference: the same metric for the reference's CPU implementation of
+              the path (the C++ oracle port; the Rust crates cannot be built
+              here), run on rank 0 only.
+"""
+import argparse
+import concurrent.futures as cf
+import hashlib
+import importlib.util
+import json
+import os
+import pathlib
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = pathlib.Path(__file__).resolve().parent
+R_MOD = 0x73EDA753299D7D483339D80809A1D80553BDA402FFFE5BFEFFFFFFFF00000001
+
+# CFRG draft keypair fixture (keypair.json): one signer for the whole batch.
+SK = bytes.fromhex("60e55110f76883a13d030b2f6bd11883422d5abde717569fc0731f51237169fc")
+PK = bytes.fromhex("a820f230f6ae38503b86c70dc50b61c58a77e45c39ab25c0652bbaa8fa136f2851bd4781c9dcde39fc9d1d52c9e60268"
+                   "061e7d7632171d91aa8d460acee0e96f1e7c4cfb12d3ff9ab5d5dc91c277db75c845d649ef3c4f63aebc364cd55ded0c")
+
+# Frozen per-op work model in 381-bit Montgomery products (M); 1 M = 600 IMAD.
+IMAD_PER_M = 600
+MODEL_M = {
+    "proof_verify": {"g1_decode": 3 * 1750, "fixed_msm": 102 * 260, "var_mul": 6700 + 2224, "challenge": 12,
+                     "pairing": 16470, "total": 57180},
+    "proof_gen": {"g1_decode": 1750, "fixed_msm": 102 * 260 + 50 * 260, "var_mul": 12896 + 2224, "finish": 30,
+                  "total": 56450},
+}
+
+
+def drbg(seed: bytes, label: bytes, i: int, n: int) -> bytes:
+    out, ctr = b"", 0
+    while len(out) < n:
+        out += hashlib.sha256(seed + label + i.to_bytes(8, "big") + ctr.to_bytes(4, "big")).digest()
+        ctr += 1
+    return out[:n]
+
+
+def load_package():
+    pkg = ROOT / "cubbs-cred_gb300"
+    spec = importlib.util.spec_from_file_location("cubbs_gb300", pkg / "__init__.py",
+                                                  submodule_search_locations=[str(pkg)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["cubbs_gb300"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def make_requests(n, L, R, msg_len, seed):
+    """Per proof: messages, header, presentation header, sorted disclosed subset."""
+    reqs = []
+    for i in range(n):
+        msgs = [drbg(seed, b"msg%d" % i, j, msg_len) for j in range(L)]
+        order = sorted(range(L), key=lambda j: drbg(seed, b"disc%d" % i, j, 8))
+        reqs.append({"msgs": msgs, "hdr": drbg(seed, b"hdr", i, 64), "ph": drbg(seed, b"ph", i, 64),
+                     "di": sorted(order[:R]), "seed": drbg(seed, b"blind", i, 32)})
+    return reqs
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in getattr(self, "lines", []):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() in ("active", "1", "yes"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_oracle_proof_verify(items, seconds_budget, threads):
+    """Times the oracle's ProofVerify over a bounded sample on `threads` host threads."""
+    sys.path.insert(0, str(ROOT))
+    from oracle import oracle_ctypes as O
+    O.lib()
+    # probe the single-op cost to size the sample to ~seconds_budget of CPU work
+    t0 = time.perf_counter()
+    it = items[0]
+    rc = O.proof_verify(it[0], it[1], it[2], it[3], it[4], it[5])
+    assert rc == 0, "oracle rejected a GPU-generated proof"
+    one = time.perf_counter() - t0
+    sample = max(threads, int(seconds_budget * threads / max(one, 1e-4)))
+    sample = min(sample, 20000)
+    sample = (sample // threads) * threads or threads
+    work = [items[i % len(items)] for i in range(sample)]
+    t0 = time.perf_counter()
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        rcs = list(ex.map(lambda x: O.proof_verify(x[0], x[1], x[2], x[3], x[4], x[5]), work))
+    dt = time.perf_counter() - t0
+    assert all(r == 0 for r in rcs)
+    return sample / dt, sample, dt
+
+
+def reference_arm(args):
+    """The reference's CPU implementation of the path (oracle port), rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    sys.path.insert(0, str(ROOT))
+    from oracle import oracle_ctypes as O
+    O.lib()
+    threads = os.cpu_count() or 1
+    reqs = make_requests(threads * 2, args.L, args.R, 64, b"cubbs-bench-ref")
+    # build the sample with the oracle itself: sign, then prove (untimed)
+    def prep(r):
+        sig, _, _ = O.sign(SK, PK, r["hdr"], r["msgs"])
+        proof = O.proof_gen(PK, sig, r["hdr"], r["ph"], r["msgs"], r["di"], seed=r["seed"])
+        return (PK, proof, r["hdr"], r["ph"], [r["msgs"][j] for j in r["di"]], r["di"])
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        items = list(ex.map(prep, reqs))
+    per_step = []
+    for k in range(args.warmup + args.steps):
+        t0 = time.perf_counter()
+        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+            rcs = list(ex.map(lambda x: O.proof_verify(*x), items))
+        dt = time.perf_counter() - t0
+        assert all(r == 0 for r in rcs)
+        if k >= args.warmup:
+            per_step.append(dt)
+    ms = 1e3 * statistics.mean(per_step)
+    value = len(items) / (ms / 1e3)
+    line = {"impl": "reference", "metric": "BBS ProofVerify ops/sec at L=100 (1 GB300)", "value": round(value, 2),
+            "unit": "ops/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "u32 (exact mod p / mod r)", "data": "synthetic (seeded DRBG)",
+            "config": {"workload": "BBS ProofVerify, L=100 x 64 B, 50 disclosed, CPU sample of %d proofs" % len(items),
+                       "L": args.L, "disclosed": args.R, "sample_proofs": len(items)},
+            "cpu_baseline": {"value": round(value, 2), "unit": "ops/s", "cores": threads, "kind": "port",
+                             "sample": "%d ProofVerify ops per step on %d threads (C++ oracle restating the "
+                                       "reference Rust CPU path)" % (len(items), threads)},
+            "e2e": {"value": round(value, 2), "unit": "ops/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="cubbs")
+    ap.add_argument("--batch", type=int, default=1024)
+    ap.add_argument("--L", type=int, default=100)
+    ap.add_argument("--R", type=int, default=50)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    if args.impl == "reference":
+        reference_arm(args)
+        return
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    os.environ["CUBBS_BBS_DEVICE"] = str(local)
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+
+    pkg = load_package()
+    pkg.build()
+    kind, hw = pkg.backend_info()
+    assert kind == pkg.BACKEND_KIND_CUDA and hw == 1
+
+    # ---------------- workload (untimed): signatures and proofs from this library
+    n, L, R = args.batch, args.L, args.R
+    seed = b"cubbs-bench-%d" % rank
+    reqs = make_requests(n, L, R, 64, seed)
+    sigs = pkg.sign_batch([(SK, PK, r["hdr"], r["msgs"]) for r in reqs])
+    assert all(c == 0 for c, _ in sigs)
+    pg_reqs = [(PK, s, r["hdr"], r["ph"], r["msgs"], r["di"]) for r, (_, s) in zip(reqs, sigs)]
+    proofs = pkg.proof_gen_batch(pg_reqs, seeds=[r["seed"] for r in reqs])
+    assert all(c == 0 for c, _ in proofs)
+    pv_reqs = [(PK, p, r["hdr"], r["ph"], [r["msgs"][j] for j in r["di"]], r["di"], L)
+               for r, (_, p) in zip(reqs, proofs)]
+
+    tera_imad, giga_fpmul = pkg.int_peaks()
+
+    # ---------------- timed: device-resident ProofVerify (headline) + ProofGen
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    barrier()
+    with ClockSampler(local) as clk:
+        pv_ms, pv_launch, pv_res, pv_stages = pkg.bench_device_steps(pkg.OP_PROOF_VERIFY, pv_reqs, args.warmup,
+                                                                     args.steps)
+    barrier()
+    assert all(c == 0 and v == 1 for c, v in pv_res), "ProofVerify rejected a valid proof"
+    pg_ms, pg_launch, pg_res, pg_stages = pkg.bench_device_steps(pkg.OP_PROOF_GEN, pg_reqs, args.warmup,
+                                                                 args.steps, seeds=[r["seed"] for r in reqs])
+    assert all(c == 0 for c, _ in pg_res)
+    sv_reqs = [(SK, PK, r["hdr"], r["msgs"][:10]) for r in reqs[:64]]
+    sg_ms, _, _, _ = pkg.bench_device_steps(pkg.OP_SIGN, sv_reqs, args.warmup, args.steps)
+    vsigs = pkg.sign_batch(sv_reqs)
+    vf_ms, _, vf_res, _ = pkg.bench_device_steps(pkg.OP_VERIFY, [(PK, s, r[2], r[3]) for r, (_, s) in
+                                                                 zip(sv_reqs, vsigs)], args.warmup, args.steps)
+    assert all(c == 0 and v == 1 for c, v in vf_res)
+
+    # ---------------- e2e: the C ABI with host buffers, transfers inside the timed region.
+    # The caller's item structs (its own data) are built once; each timed step is one
+    # synchronous cubbs_bbs_gpu_proof_verify_batch_v2 call: packing, H2D, the device
+    # pipeline, D2H and result mapping.
+    call = pkg.prepared_call(pkg.OP_PROOF_VERIFY, pv_reqs)
+    for _ in range(args.warmup):
+        call()
+    barrier()
+    e2e = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        out = call()
+        e2e.append(time.perf_counter() - t0)
+    barrier()
+    assert all(c == 0 and v for c, v in out)
+    h2d, d2h = pkg.last_transfer_bytes()
+
+    pv_step = statistics.mean(pv_ms)
+    e2e_step = statistics.mean(e2e) * 1e3
+    if dist is not None:
+        import torch
+        t = torch.tensor([pv_step, e2e_step], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        pv_step, e2e_step = float(t[0]), float(t[1])
+    value = world * n / (pv_step / 1e3)
+    e2e_value = world * n / (e2e_step / 1e3)
+
+    # ---------------- roofline: dominant stage of the ProofVerify pipeline vs the IMAD peak
+    stage = max(pv_stages, key=lambda s: s[1])
+    model = MODEL_M["proof_verify"].get(stage[0])
+    roof = None
+    if model:
+        achieved = n * model * IMAD_PER_M / (stage[1] / 1e3) / 1e12
+        roof = {"bound": "imad", "kernel": stage[0], "achieved": round(achieved, 3), "peak": round(tera_imad, 3),
+                "unit": "T IMAD/s (32-bit integer multiply-add)", "frac": round(achieved / tera_imad, 4),
+                "traffic": None, "peak_source": "measured in this run (k_imad_peak, 16 independent mad.lo chains)",
+                "model_m_per_op": model, "stage_ms": round(stage[1], 3)}
+    whole = n * MODEL_M["proof_verify"]["total"] * IMAD_PER_M / (pv_step / 1e3) / 1e12
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        items = [(PK, p[1], p[2], p[3], p[4], p[5]) for p in pv_reqs[:64]]
+        v, sample, dt = cpu_oracle_proof_verify(items, args.cpu_seconds, threads)
+        cpu = {"value": round(v, 2), "unit": "ops/s", "cores": threads, "kind": "port",
+               "sample": "%d ProofVerify ops (L=100, 50 disclosed) in %.1f s on %d threads; C++ oracle "
+                         "restating the reference Rust CPU path" % (sample, dt, threads)}
+
+    if rank == 0:
+        clocks = clk.summary()
+        line = {
+            "metric": "BBS ProofVerify ops/sec at L=100 (1 GB300)",
+            "value": round(value, 2), "unit": "ops/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(pv_step, 3), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "u32 (exact mod p / mod r)",
+            "data": "synthetic (seeded DRBG; signatures/proofs generated by this library)",
+            "config": {"workload": "BBS ProofGen+ProofVerify, L=100 x 64 B, 50 disclosed, 1024 proofs per batch",
+                       "batch": n, "L": L, "disclosed": R, "l2": "flushed (256 MiB write) between timed steps",
+                       "fixed_base_window": int(os.environ.get("CUBBS_BBS_TABLE_WINDOW", "8")),
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "per_op_ops_per_s": {
+                "proof_verify_L100": round(value / world, 2),
+                "proof_gen_L100": round(n / (statistics.mean(pg_ms) / 1e3), 2),
+                "sign_L10_batch64": round(len(sv_reqs) / (statistics.mean(sg_ms) / 1e3), 2),
+                "verify_L10_batch64": round(len(sv_reqs) / (statistics.mean(vf_ms) / 1e3), 2)},
+            "stages_ms": {"proof_verify": {k: round(v, 3) for k, v in pv_stages},
+                          "proof_gen": {k: round(v, 3) for k, v in pg_stages}},
+            "roofline": roof,
+            "roofline_whole_op": {"achieved_t_imad": round(whole, 3), "frac": round(whole / tera_imad, 4),
+                                  "model_m_per_op": MODEL_M["proof_verify"]["total"]},
+            "int_peaks": {"t_imad_per_s": round(tera_imad, 3), "g_fp_mul_per_s": round(giga_fpmul, 2)},
+            "cpu_baseline": cpu,
+            "e2e": {"value": round(e2e_value, 2), "unit": "ops/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": pv_launch * args.steps,
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -563,3 +563,101 @@ def g1_op_for_test(points, scalars):
     diag = [[kp.raw[48 * (n + 12 * i + j):48 * (n + 12 * i + j + 1)] for j in range(12)] for i in range(n)]
     chain = [[kp.raw[48 * (13 * n + 64 * i + j):48 * (13 * n + 64 * i + j + 1)] for j in range(64)] for i in range(n)]
     return [(st[i], xy.raw[96 * i:96 * i + 96], kp.raw[48 * i:48 * i + 48], diag[i], chain[i]) for i in range(n)]
+
+
+# --------------------------------------------------------------------------- benchmark helpers
+OP_SIGN, OP_VERIFY, OP_PROOF_GEN, OP_PROOF_VERIFY = 0, 1, 2, 3
+
+
+def _op_items(op, reqs, k):
+    if op == OP_SIGN:
+        items = (SignItem * len(reqs))()
+        for i, (sk, pk, hdr, msgs) in enumerate(reqs):
+            ob, _ = k.out(80)
+            items[i] = SignItem(k.bytes(sk), k.bytes(pk), k.bytes(hdr), k.slices(msgs), len(msgs), ob)
+        return items
+    if op == OP_VERIFY:
+        items = (VerifyItem * len(reqs))()
+        for i, (pk, sig, hdr, msgs) in enumerate(reqs):
+            items[i] = VerifyItem(k.bytes(pk), k.bytes(sig), k.bytes(hdr), k.slices(msgs), len(msgs))
+        return items
+    if op == OP_PROOF_GEN:
+        items, _ = _proof_gen_items(k, reqs)
+        return items
+    items = (ProofVerifyItem * len(reqs))()
+    for i, (pk, proof, hdr, ph, dmsgs, didx, L) in enumerate(reqs):
+        items[i] = ProofVerifyItem(k.bytes(pk), k.bytes(proof), k.bytes(hdr), k.bytes(ph), k.slices(dmsgs),
+                                   len(dmsgs), k.index(didx), L)
+    return items
+
+
+def bench_device_steps(op, reqs, warmup, steps, seeds=None):
+    """Replays the device pipeline of one packed batch (inputs resident in HBM).
+    Returns (per-step ms list, kernel launches per step, per-item (code, value), stage breakdown)."""
+    k = _Keep()
+    items = _op_items(op, reqs, k)
+    n = len(reqs)
+    ms = (ctypes.c_float * steps)()
+    launches = ctypes.c_int32(0)
+    res = (Result * n)()
+    fn = lib().cubbs_bbs_gpu_bench_device_steps_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_uint32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                   ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    sb = ctypes.create_string_buffer(b"".join(seeds), 32 * n) if seeds is not None else None
+    rc = fn(ABI_VERSION, op, ctypes.cast(items, ctypes.c_void_p), n,
+            ctypes.cast(sb, ctypes.c_void_p) if sb is not None else None, warmup, steps,
+            ctypes.cast(ms, ctypes.c_void_p), ctypes.cast(ctypes.pointer(launches), ctypes.c_void_p),
+            ctypes.cast(res, ctypes.c_void_p))
+    if rc:
+        raise RuntimeError(f"bench_device_steps returned {rc}")
+    names = ctypes.create_string_buffer(32 * 16)
+    sms = (ctypes.c_float * 16)()
+    fs = lib().cubbs_bbs_gpu_bench_stages_v2
+    fs.restype = ctypes.c_int32
+    fs.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32]
+    cnt = fs(ctypes.cast(names, ctypes.c_void_p), ctypes.cast(sms, ctypes.c_void_p), 16)
+    stages = [(names.raw[32 * j:32 * j + 32].split(b"\0")[0].decode(), sms[j]) for j in range(cnt)]
+    return list(ms), launches.value, [(res[i].code, res[i].value) for i in range(n)], stages
+
+
+def last_transfer_bytes():
+    h2d, d2h = ctypes.c_uint64(0), ctypes.c_uint64(0)
+    fn = lib().cubbs_bbs_gpu_last_transfer_bytes_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    fn(ctypes.cast(ctypes.pointer(h2d), ctypes.c_void_p), ctypes.cast(ctypes.pointer(d2h), ctypes.c_void_p))
+    return h2d.value, d2h.value
+
+
+def int_peaks():
+    """Measured (1e12 IMAD/s, 1e9 Fp products/s) on the current device."""
+    a, b = ctypes.c_double(0), ctypes.c_double(0)
+    fn = lib().cubbs_bbs_gpu_int_peaks_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    if fn(ctypes.cast(ctypes.pointer(a), ctypes.c_void_p), ctypes.cast(ctypes.pointer(b), ctypes.c_void_p)):
+        raise RuntimeError("int_peaks failed")
+    return a.value, b.value
+
+
+def prepared_call(op, reqs):
+    """Builds the ABI item array once and returns a function that performs one
+    synchronous batch call on it (the caller's data stays as built)."""
+    k = _Keep()
+    items = _op_items(op, reqs, k)
+    n = len(reqs)
+    res = (Result * n)()
+    name = {OP_SIGN: "cubbs_bbs_gpu_sign_batch_v2", OP_VERIFY: "cubbs_bbs_gpu_verify_batch_v2",
+            OP_PROOF_GEN: "cubbs_bbs_gpu_proof_gen_batch_v2",
+            OP_PROOF_VERIFY: "cubbs_bbs_gpu_proof_verify_batch_v2"}[op]
+    fn = getattr(lib(), name)
+    ip, rp = ctypes.cast(items, ctypes.c_void_p), ctypes.cast(res, ctypes.c_void_p)
+
+    def call():
+        rc = fn(ABI_VERSION, ip, n, rp)
+        if rc:
+            raise RuntimeError(f"{name} returned {rc}")
+        _ = k  # keep the buffers alive with the closure
+        return [(res[i].code, res[i].value) for i in range(n)]
+    return call

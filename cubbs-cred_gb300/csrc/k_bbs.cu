@@ -15,6 +15,7 @@
 #include <sys/random.h>
 
 #include <algorithm>
+#include <cstdio>
 #include <cstring>
 
 #include "bbs_dst.cuh"
@@ -513,52 +514,18 @@ struct Blob {
   }
 };
 
+// Flat message list: [offsets u32 * n][lengths u32 * n][bytes].
 struct MsgList {
-  std::vector<const uint8_t *> ptrs;
-  std::vector<size_t> lens;
-  size_t bytes = 0;
+  std::vector<uint32_t> offs, lens;
+  std::vector<uint8_t> bytes;
   uint32_t add(const uint8_t *p, size_t n) {
-    ptrs.push_back(p);
-    lens.push_back(n);
-    bytes += n;
-    return (uint32_t)(ptrs.size() - 1);
+    offs.push_back((uint32_t)bytes.size());
+    lens.push_back((uint32_t)n);
+    if (n) bytes.insert(bytes.end(), p, p + n);
+    return (uint32_t)(offs.size() - 1);
   }
+  size_t count() const { return offs.size(); }
 };
-
-template <typename T> T *upload(Runtime &rt, const T *h, size_t n) {
-  T *d = rt.arena.alloc<T>(n ? n : 1);
-  if (n) {
-    uint8_t *st = rt.staging.alloc(n * sizeof(T));
-    std::memcpy(st, h, n * sizeof(T));
-    CUBBS_CHECK(cudaMemcpyAsync(d, st, n * sizeof(T), cudaMemcpyHostToDevice, rt.stream));
-  }
-  return d;
-}
-
-// Upload the message list and hash it to scalars with api_id || MAP_MSG_TO_SCALAR_AS_HASH_.
-fr *hash_messages(Runtime &rt, const MsgList &ml) {
-  size_t n = ml.ptrs.size();
-  fr *out = rt.arena.alloc<fr>(n ? n : 1);
-  if (!n) return out;
-  uint8_t *h = rt.staging.alloc(ml.bytes + 8 * n);
-  uint32_t *ho = reinterpret_cast<uint32_t *>(h), *hl = ho + n;
-  uint8_t *hb = h + 8 * n;
-  size_t cur = 0;
-  #pragma unroll 1
-  for (size_t i = 0; i < n; i++) {
-    ho[i] = (uint32_t)cur;
-    hl[i] = (uint32_t)ml.lens[i];
-    if (ml.lens[i]) std::memcpy(hb + cur, ml.ptrs[i], ml.lens[i]);
-    cur += ml.lens[i];
-  }
-  uint8_t *d = rt.arena.alloc<uint8_t>(ml.bytes + 8 * n);
-  CUBBS_CHECK(cudaMemcpyAsync(d, h, ml.bytes + 8 * n, cudaMemcpyHostToDevice, rt.stream));
-  static const char MAP_DST[] = "BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_H2G_HM2S_MAP_MSG_TO_SCALAR_AS_HASH_";
-  uint8_t *ddst = upload(rt, reinterpret_cast<const uint8_t *>(MAP_DST), sizeof(MAP_DST) - 1);
-  launch_h2s_flat(rt.stream, d + 8 * n, reinterpret_cast<uint32_t *>(d), reinterpret_cast<uint32_t *>(d) + n,
-                  (uint32_t)n, ddst, sizeof(MAP_DST) - 1, out);
-  return out;
-}
 
 void sort_dedup(const size_t *p, size_t n, std::vector<size_t> &out) {
   out.assign(p, p + n);
@@ -566,13 +533,495 @@ void sort_dedup(const size_t *p, size_t n, std::vector<size_t> &out) {
   out.erase(std::unique(out.begin(), out.end()), out.end());
 }
 
-size_t reserve_for(size_t items, size_t maxL, size_t blob_bytes, size_t msgs) {
-  size_t stride = maxL + 2;
-  return 4096 + blob_bytes * 2 + msgs * 64 + items * (stride * 2 * sizeof(fr) + 16 * sizeof(g1) + 8 * sizeof(fr) +
-                                                      4 * sizeof(g1a) + sizeof(PairJob) + 512);
+enum Op { OP_SIGN = 0, OP_VERIFY = 1, OP_PGEN = 2, OP_PVERIFY = 3 };
+
+// One packed batch of a four-operation call.  plan_*() packs on the host,
+// upload() moves everything to the device once, run() replays the whole device
+// pipeline (this is the timed step of the benchmark), download() maps results.
+struct OpBatch {
+  Op op;
+  size_t n = 0, maxL = 0, maxU = 0, stride = 0, rs_stride = 0, out_total = 0;
+  Blob blob;
+  MsgList ml;
+  std::vector<uint8_t> pts48;       // points to decode (48 B each), npts per item
+  size_t npts_per_item = 0;
+  std::vector<DomainJob> dj;
+  std::vector<uint8_t> items;       // host copy of the per-item device structs
+  size_t item_size = 0;
+  std::vector<const uint8_t *> pks;
+  std::vector<int32_t> code;        // host-side per-item result codes
+  // device buffers
+  uint8_t *dblob = nullptr, *dmsg = nullptr, *dpts48 = nullptr, *ditems0 = nullptr, *ditems = nullptr;
+  DomainJob *ddj = nullptr;
+  fr *msc = nullptr, *domain = nullptr, *rows = nullptr, *jscal = nullptr, *rs = nullptr, *e = nullptr;
+  uint32_t *nterms = nullptr;
+  VarJob *jobs = nullptr;
+  g1a *pts = nullptr, *vpts = nullptr;
+  int32_t *dec = nullptr;
+  g1 *fixed = nullptr, *v = nullptr;
+  PairJob *pj = nullptr;
+  uint8_t *ok = nullptr, *out = nullptr;
+  size_t launches_per_run = 0;
+};
+
+size_t g_h2d_bytes = 0, g_d2h_bytes = 0;  // bytes moved by the last four-operation call
+
+template <typename T> T *upload_to(Runtime &rt, T *d, const T *h, size_t n) {
+  if (n) {
+    g_h2d_bytes += n * sizeof(T);
+    uint8_t *st = rt.staging.alloc(n * sizeof(T));
+    std::memcpy(st, h, n * sizeof(T));
+    CUBBS_CHECK(cudaMemcpyAsync(d, st, n * sizeof(T), cudaMemcpyHostToDevice, rt.stream));
+  }
+  return d;
+}
+template <typename T> T *upload(Runtime &rt, const T *h, size_t n) {
+  return upload_to(rt, rt.arena.alloc<T>(n ? n : 1), h, n);
+}
+
+size_t vars_per_item(Op op) { return op == OP_PVERIFY ? 4 : op == OP_VERIFY ? 1 : op == OP_PGEN ? 7 : 0; }
+size_t fixed_rows_per_item(Op op) { return op == OP_PGEN ? 2 : 1; }
+
+void upload(Runtime &rt, OpBatch &b) {
+  size_t n = b.n, nm = b.ml.count();
+  b.stride = b.maxL + 2;
+  b.rs_stride = b.maxU + 5;
+  size_t fr_rows = fixed_rows_per_item(b.op) * n * b.stride, nv = vars_per_item(b.op) * n;
+  size_t need = 65536 + 2 * b.blob.b.size() + b.ml.bytes.size() + 8 * nm + nm * sizeof(fr) + b.pts48.size() +
+                n * (b.item_size * 2 + sizeof(DomainJob) + 2 * sizeof(fr) + sizeof(PairJob) + 256) +
+                fr_rows * sizeof(fr) + 2 * n * sizeof(uint32_t) + nv * (sizeof(VarJob) + sizeof(fr) + sizeof(g1)) +
+                (b.pts48.size() / 48) * (sizeof(g1a) + 4) + 2 * n * sizeof(g1) + 2 * n * sizeof(g1a) +
+                n * b.rs_stride * sizeof(fr) + b.out_total + 64 * 256;
+  rt.arena.reserve(need);
+  rt.staging.reserve(65536 + 2 * b.blob.b.size() + b.ml.bytes.size() + 8 * nm + b.pts48.size() +
+                     n * (b.item_size + sizeof(DomainJob) + 64));
+  b.dblob = upload(rt, b.blob.b.data(), b.blob.b.size());
+  std::vector<uint8_t> flat(8 * nm + b.ml.bytes.size());
+  if (nm) {
+    std::memcpy(flat.data(), b.ml.offs.data(), 4 * nm);
+    std::memcpy(flat.data() + 4 * nm, b.ml.lens.data(), 4 * nm);
+    if (!b.ml.bytes.empty()) std::memcpy(flat.data() + 8 * nm, b.ml.bytes.data(), b.ml.bytes.size());
+  }
+  b.dmsg = upload(rt, flat.data(), flat.size());
+  b.msc = rt.arena.alloc<fr>(nm ? nm : 1);
+  b.dpts48 = upload(rt, b.pts48.data(), b.pts48.size());
+  size_t npts = b.pts48.size() / 48;
+  b.pts = rt.arena.alloc<g1a>(npts ? npts : 1);
+  b.dec = rt.arena.alloc<int32_t>(npts ? npts : 1);
+  b.ddj = upload(rt, b.dj.data(), n);
+  b.domain = rt.arena.alloc<fr>(n);
+  b.ditems0 = upload(rt, b.items.data(), b.items.size());
+  b.ditems = rt.arena.alloc<uint8_t>(b.items.size());
+  b.rows = rt.arena.alloc<fr>(fr_rows ? fr_rows : 1);
+  b.nterms = rt.arena.alloc<uint32_t>(fixed_rows_per_item(b.op) * n);
+  b.jobs = rt.arena.alloc<VarJob>(nv ? nv : 1);
+  b.jscal = rt.arena.alloc<fr>(nv ? nv : 1);
+  b.v = rt.arena.alloc<g1>(nv ? nv : 1);
+  b.fixed = rt.arena.alloc<g1>(fixed_rows_per_item(b.op) * n);
+  b.pj = rt.arena.alloc<PairJob>(n);
+  b.ok = rt.arena.alloc<uint8_t>(n);
+  b.e = rt.arena.alloc<fr>(n);
+  b.vpts = rt.arena.alloc<g1a>(2 * n);
+  if (b.op == OP_PGEN) b.rs = rt.arena.alloc<fr>(n * b.rs_stride);
+  b.out = rt.arena.alloc<uint8_t>(b.out_total + 1);
+}
+
+static const char MAP_DST_H[] = "BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_H2G_HM2S_MAP_MSG_TO_SCALAR_AS_HASH_";
+
+// Optional per-stage events (benchmark breakdown): stage k ends at ev[k].
+struct StageEvents {
+  cudaEvent_t ev[16];
+  int used = 0;
+  const char *name[16];
+};
+StageEvents *g_stages = nullptr;
+void stage_mark(cudaStream_t s, const char *name) {
+  if (!g_stages || g_stages->used >= 16) return;
+  cudaEventRecord(g_stages->ev[g_stages->used], s);
+  g_stages->name[g_stages->used++] = name;
+}
+
+// The whole device pipeline of one batch (no host work, no transfers).
+void run(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
+  cudaStream_t s = rt.stream;
+  if (g_stages) g_stages->used = 0;
+  stage_mark(s, "start");
+  size_t n = b.n, nm = b.ml.count();
+  uint32_t N = (uint32_t)n, stride = (uint32_t)b.stride;
+  CUBBS_CHECK(cudaMemcpyAsync(b.ditems, b.ditems0, b.items.size(), cudaMemcpyDeviceToDevice, s));
+  size_t launches = 0;
+  if (nm) {
+    launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
+                    reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1, b.msc);
+    launches++;
+  }
+  stage_mark(s, "hash_messages");
+  size_t npts = b.pts48.size() / 48;
+  if (npts) {
+    launch_g1_decode(s, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, true);
+    launches++;
+  }
+  stage_mark(s, "g1_decode");
+  launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, b.domain);
+  launches++;
+  stage_mark(s, "domain");
+  switch (b.op) {
+    case OP_PVERIFY: {
+      PvItem *it = reinterpret_cast<PvItem *>(b.ditems);
+      k_pv_prep<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.rows, stride, b.nterms,
+                                                   b.jobs, b.jscal);
+      stage_mark(s, "scalar_prep");
+      launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed);
+      stage_mark(s, "fixed_msm");
+      launch_var_mul(s, b.pts, b.jobs, b.jscal, 4 * N, b.v);
+      stage_mark(s, "var_mul");
+      k_pv_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.fixed, b.v, b.pts, b.dec,
+                                                   b.pj);
+      stage_mark(s, "challenge");
+      launch_pairing_check(s, b.pj, N, rt.d_lines, b.ok);
+      stage_mark(s, "pairing");
+      launches += 5;
+      break;
+    }
+    case OP_SIGN: {
+      SignItem *it = reinterpret_cast<SignItem *>(b.ditems);
+      k_sign_prep<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms, b.e);
+      launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed);
+      k_sign_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.fixed, b.e, b.out);
+      launches += 3;
+      break;
+    }
+    case OP_VERIFY: {
+      VerifyItem *it = reinterpret_cast<VerifyItem *>(b.ditems);
+      k_verify_prep<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.rows, stride,
+                                                       b.nterms, b.jobs, b.jscal);
+      launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed);
+      launch_var_mul(s, b.pts, b.jobs, b.jscal, N, b.v);
+      k_verify_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.fixed, b.v, b.pts, b.dec, b.pj);
+      launch_pairing_check(s, b.pj, N, rt.d_lines, b.ok);
+      launches += 5;
+      break;
+    }
+    case OP_PGEN: {
+      PgItem *it = reinterpret_cast<PgItem *>(b.ditems);
+      uint32_t rss = (uint32_t)b.rs_stride;
+      k_pg_random<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.rs, rss);
+      stage_mark(s, "random_scalars");
+      k_pg_prep<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rs, rss, b.dec, b.rows, stride,
+                                                   b.nterms);
+      stage_mark(s, "scalar_prep");
+      launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, 2 * N, b.fixed);
+      stage_mark(s, "fixed_msm");
+      k_pg_vars<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.fixed, b.pts, b.dec, b.rs, rss, b.vpts, b.jobs,
+                                                 b.jscal);
+      stage_mark(s, "var_prep");
+      launch_var_mul(s, b.vpts, b.jobs, b.jscal, 7 * N, b.v);
+      stage_mark(s, "var_mul");
+      k_pg_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rs, rss, b.fixed + n, b.v,
+                                                   b.out);
+      stage_mark(s, "finish");
+      launches += 6;
+      break;
+    }
+  }
+  CUBBS_CHECK(cudaGetLastError());
+  b.launches_per_run = launches;
+}
+
+uint8_t *upload_mapdst(Runtime &rt) {
+  return upload(rt, reinterpret_cast<const uint8_t *>(MAP_DST_H), sizeof(MAP_DST_H) - 1);
+}
+
+void finish_pks(Runtime &rt, OpBatch &b, bool need_table = true) {
+  std::vector<int> slots, st;
+  rt.resolve_pks(b.pks, slots, st);
+  for (size_t i = 0; i < b.n; i++) {
+    uint8_t *raw = b.items.data() + i * b.item_size;
+    switch (b.op) {
+      case OP_PVERIFY: {
+        PvItem *p = reinterpret_cast<PvItem *>(raw);
+        p->pk_slot = slots[i];
+        p->pk_status = st[i];
+        if (st[i] == DEC_BAD) p->status = ST_ERROR;
+        break;
+      }
+      case OP_VERIFY: {
+        VerifyItem *p = reinterpret_cast<VerifyItem *>(raw);
+        p->pk_slot = slots[i];
+        p->pk_status = st[i];
+        if (st[i] == DEC_BAD) p->status = ST_ERROR;
+        break;
+      }
+      case OP_SIGN:
+        reinterpret_cast<SignItem *>(raw)->pk_status = st[i];
+        break;
+      case OP_PGEN: {
+        PgItem *p = reinterpret_cast<PgItem *>(raw);
+        p->pk_status = st[i];
+        if (st[i] == DEC_BAD && p->status == ST_OK) {
+          p->status = ST_ERROR;
+          b.code[i] = CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+        }
+        break;
+      }
+    }
+  }
+  if (need_table) rt.ensure_table((int)b.maxL + 2);
+}
+
+// --------------------------------------------------------------------------- planners (host packing)
+int32_t plan_pverify(const CuBbsBbsGpuProofVerifyItem *items, size_t n, OpBatch &b) {
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    if (it.public_key.data == nullptr || it.public_key.len != 96 || (it.proof.len && !it.proof.data) ||
+        (it.header.len && !it.header.data) || (it.presentation_header.len && !it.presentation_header.data) ||
+        (it.disclosed_count && !it.disclosed_messages) || (it.disclosed_indexes.len && !it.disclosed_indexes.data))
+      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+    for (size_t k = 0; k < it.disclosed_count; k++)
+      if (it.disclosed_messages[k].len && !it.disclosed_messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  }
+  b.op = OP_PVERIFY;
+  b.n = n;
+  b.item_size = sizeof(PvItem);
+  b.items.assign(n * sizeof(PvItem), 0);
+  b.pts48.assign(144 * n, 0);
+  b.npts_per_item = 3;
+  b.pks.resize(n);
+  b.code.assign(n, CUBBS_BBS_GPU_SUCCESS);
+  b.dj.resize(n);
+  std::vector<size_t> di;
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    PvItem &p = reinterpret_cast<PvItem *>(b.items.data())[i];
+    b.pks[i] = it.public_key.data;
+    p.status = ST_OK;
+    size_t plen = it.proof.len;
+    sort_dedup(it.disclosed_indexes.data, it.disclosed_indexes.len, di);
+    size_t U = plen >= 272 ? (plen - 240) / 32 - 1 : 0;
+    size_t R = di.size(), L = U + R;
+    bool ok = plen >= 272 && it.disclosed_count == R && L <= MAX_MESSAGES;
+    for (size_t k = 0; k < R && ok; k++) ok = di[k] < L;
+    p.msg_base = (uint32_t)b.ml.count();
+    uint32_t pk_off = b.blob.put(it.public_key.data, 96);
+    if (!ok) {
+      p.status = ST_INVALID;
+      p.proof_off = b.blob.put(nullptr, 0);
+      b.dj[i] = {pk_off, 0, 0, 0};
+      continue;
+    }
+    for (size_t k = 0; k < it.disclosed_count; k++)
+      b.ml.add(it.disclosed_messages[k].data, it.disclosed_messages[k].len);
+    p.U = (uint32_t)U;
+    p.R = (uint32_t)R;
+    p.L = (uint32_t)L;
+    p.proof_off = b.blob.put(it.proof.data, 240 + 32 * (U + 1));
+    p.hdr_off = b.blob.put(it.header.data, it.header.len);
+    p.hdr_len = (uint32_t)it.header.len;
+    p.ph_off = b.blob.put(it.presentation_header.data, it.presentation_header.len);
+    p.ph_len = (uint32_t)it.presentation_header.len;
+    std::vector<uint32_t> d32(di.begin(), di.end());
+    p.idx_off = b.blob.put_u32s(d32);
+    std::memcpy(&b.pts48[144 * i], it.proof.data, 144);
+    b.dj[i] = {pk_off, p.hdr_off, p.hdr_len, p.L};
+    b.maxL = std::max(b.maxL, L);
+  }
+  return CUBBS_BBS_GPU_SUCCESS;
+}
+
+int32_t plan_sign(CuBbsBbsGpuSignItem *items, size_t n, OpBatch &b) {
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    if (it.secret_key.data == nullptr || it.public_key.data == nullptr || (it.header.len && !it.header.data) ||
+        (it.message_count && !it.messages) || it.signature_out.data == nullptr)
+      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+    for (size_t k = 0; k < it.message_count; k++)
+      if (it.messages[k].len && !it.messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  }
+  static const uint8_t zero96[96] = {0};
+  b.op = OP_SIGN;
+  b.n = n;
+  b.item_size = sizeof(SignItem);
+  b.items.assign(n * sizeof(SignItem), 0);
+  b.pks.resize(n);
+  b.code.assign(n, CUBBS_BBS_GPU_SUCCESS);
+  b.dj.resize(n);
+  b.out_total = 80 * n;
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    SignItem &p = reinterpret_cast<SignItem *>(b.items.data())[i];
+    bool shape = it.secret_key.len == 32 && it.public_key.len == 96 && it.message_count <= MAX_MESSAGES;
+    if (shape && it.signature_out.capacity < 80) b.code[i] = CUBBS_BBS_GPU_ERR_INSUFFICIENT_OUTPUT;
+    else if (!shape) b.code[i] = CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+    bool ok = b.code[i] == CUBBS_BBS_GPU_SUCCESS;
+    p.status = ok ? ST_OK : ST_ERROR;
+    b.pks[i] = it.public_key.len == 96 ? it.public_key.data : zero96;
+    p.sk_off = b.blob.put(ok ? it.secret_key.data : zero96, 32);
+    p.pk_off = b.blob.put(b.pks[i], 96);
+    p.hdr_off = b.blob.put(it.header.data, it.header.len);
+    p.hdr_len = (uint32_t)it.header.len;
+    p.msg_base = (uint32_t)b.ml.count();
+    p.L = ok ? (uint32_t)it.message_count : 0;
+    if (ok)
+      for (size_t k = 0; k < it.message_count; k++) b.ml.add(it.messages[k].data, it.messages[k].len);
+    b.dj[i] = {p.pk_off, p.hdr_off, p.hdr_len, p.L};
+    b.maxL = std::max(b.maxL, (size_t)p.L);
+  }
+  return CUBBS_BBS_GPU_SUCCESS;
+}
+
+int32_t plan_verify(const CuBbsBbsGpuVerifyItem *items, size_t n, OpBatch &b) {
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    if (it.public_key.data == nullptr || it.public_key.len != 96 || (it.signature.len && !it.signature.data) ||
+        (it.header.len && !it.header.data) || (it.message_count && !it.messages))
+      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+    for (size_t k = 0; k < it.message_count; k++)
+      if (it.messages[k].len && !it.messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  }
+  static const uint8_t zeros[80] = {0};
+  b.op = OP_VERIFY;
+  b.n = n;
+  b.item_size = sizeof(VerifyItem);
+  b.items.assign(n * sizeof(VerifyItem), 0);
+  b.pks.resize(n);
+  b.code.assign(n, CUBBS_BBS_GPU_SUCCESS);
+  b.dj.resize(n);
+  b.pts48.assign(48 * n, 0);
+  b.npts_per_item = 1;
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    VerifyItem &p = reinterpret_cast<VerifyItem *>(b.items.data())[i];
+    b.pks[i] = it.public_key.data;
+    bool ok = it.signature.len == 80 && it.message_count <= MAX_MESSAGES;
+    p.status = ok ? ST_OK : ST_INVALID;
+    p.sig_off = b.blob.put(ok ? it.signature.data : zeros, 80);
+    if (ok) std::memcpy(&b.pts48[48 * i], it.signature.data, 48);
+    uint32_t pk_off = b.blob.put(it.public_key.data, 96);
+    p.hdr_off = b.blob.put(it.header.data, it.header.len);
+    p.hdr_len = (uint32_t)it.header.len;
+    p.msg_base = (uint32_t)b.ml.count();
+    p.L = ok ? (uint32_t)it.message_count : 0;
+    if (ok)
+      for (size_t k = 0; k < it.message_count; k++) b.ml.add(it.messages[k].data, it.messages[k].len);
+    b.dj[i] = {pk_off, p.hdr_off, p.hdr_len, p.L};
+    b.maxL = std::max(b.maxL, (size_t)p.L);
+  }
+  return CUBBS_BBS_GPU_SUCCESS;
+}
+
+int32_t plan_pgen(CuBbsBbsGpuProofGenItem *items, size_t n, const uint8_t (*seeds)[32], OpBatch &b,
+                  std::vector<uint8_t> &os_seeds) {
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    if (it.public_key.data == nullptr || it.public_key.len != 96 || (it.signature.len && !it.signature.data) ||
+        (it.header.len && !it.header.data) || (it.presentation_header.len && !it.presentation_header.data) ||
+        (it.message_count && !it.messages) || (it.disclosed_indexes.len && !it.disclosed_indexes.data) ||
+        it.proof_out.data == nullptr)
+      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+    for (size_t k = 0; k < it.message_count; k++)
+      if (it.messages[k].len && !it.messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  }
+  if (seeds == nullptr) {  // production blinding: 32 bytes of OS randomness per item
+    os_seeds.resize(32 * n);
+    size_t got = 0;
+    while (got < os_seeds.size()) {
+      ssize_t r = getrandom(os_seeds.data() + got, os_seeds.size() - got, 0);
+      if (r <= 0) return CUBBS_BBS_GPU_ERR_INTERNAL;
+      got += (size_t)r;
+    }
+  }
+  static const uint8_t zeros[80] = {0};
+  b.op = OP_PGEN;
+  b.n = n;
+  b.item_size = sizeof(PgItem);
+  b.items.assign(n * sizeof(PgItem), 0);
+  b.pks.resize(n);
+  b.code.assign(n, CUBBS_BBS_GPU_SUCCESS);
+  b.dj.resize(n);
+  b.pts48.assign(48 * n, 0);
+  b.npts_per_item = 1;
+  std::vector<size_t> di;
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    PgItem &p = reinterpret_cast<PgItem *>(b.items.data())[i];
+    b.pks[i] = it.public_key.data;
+    sort_dedup(it.disclosed_indexes.data, it.disclosed_indexes.len, di);
+    size_t L = it.message_count, R = di.size();
+    bool ok = it.signature.len == 80 && L <= MAX_MESSAGES && R <= L;
+    for (size_t k = 0; k < R && ok; k++) ok = di[k] < L;
+    size_t U = ok ? L - R : 0;
+    size_t need = 272 + 32 * U;
+    if (ok && it.proof_out.capacity < need) {
+      b.code[i] = CUBBS_BBS_GPU_ERR_INSUFFICIENT_OUTPUT;
+      ok = false;
+    } else if (!ok) {
+      b.code[i] = CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+    }
+    p.status = ok ? ST_OK : ST_ERROR;
+    p.sig_off = b.blob.put(ok ? it.signature.data : zeros, 80);
+    if (ok) std::memcpy(&b.pts48[48 * i], it.signature.data, 48);
+    uint32_t pk_off = b.blob.put(it.public_key.data, 96);
+    p.hdr_off = b.blob.put(it.header.data, it.header.len);
+    p.hdr_len = (uint32_t)it.header.len;
+    p.ph_off = b.blob.put(it.presentation_header.data, it.presentation_header.len);
+    p.ph_len = (uint32_t)it.presentation_header.len;
+    std::vector<uint32_t> d32(di.begin(), di.end());
+    p.idx_off = b.blob.put_u32s(d32);
+    p.seed_off = b.blob.put(seeds ? seeds[i] : &os_seeds[32 * i], 32);
+    p.msg_base = (uint32_t)b.ml.count();
+    p.L = ok ? (uint32_t)L : 0;
+    p.R = ok ? (uint32_t)R : 0;
+    p.U = (uint32_t)U;
+    p.out_off = (uint32_t)b.out_total;
+    if (ok) {
+      b.out_total += need;
+      for (size_t k = 0; k < L; k++) b.ml.add(it.messages[k].data, it.messages[k].len);
+    }
+    b.dj[i] = {pk_off, p.hdr_off, p.hdr_len, p.L};
+    b.maxL = std::max(b.maxL, (size_t)p.L);
+    b.maxU = std::max(b.maxU, U);
+  }
+  return CUBBS_BBS_GPU_SUCCESS;
+}
+
+// --------------------------------------------------------------------------- result mapping
+template <typename ItemT> void fetch_items(Runtime &rt, OpBatch &b, std::vector<ItemT> &out) {
+  out.resize(b.n);
+  g_d2h_bytes += b.n * sizeof(ItemT);
+  CUBBS_CHECK(cudaMemcpyAsync(out.data(), b.ditems, b.n * sizeof(ItemT), cudaMemcpyDeviceToHost, rt.stream));
+}
+
+void download_bool(Runtime &rt, OpBatch &b, CuBbsBbsGpuResult *results) {
+  std::vector<uint8_t> hok(b.n);
+  std::vector<int32_t> st(b.n);
+  CUBBS_CHECK(cudaMemcpyAsync(hok.data(), b.ok, b.n, cudaMemcpyDeviceToHost, rt.stream));
+  g_d2h_bytes += b.n;
+  if (b.op == OP_PVERIFY) {
+    std::vector<PvItem> h;
+    fetch_items(rt, b, h);
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    for (size_t i = 0; i < b.n; i++) st[i] = h[i].status;
+  } else {
+    std::vector<VerifyItem> h;
+    fetch_items(rt, b, h);
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    for (size_t i = 0; i < b.n; i++) st[i] = h[i].status;
+  }
+  for (size_t i = 0; i < b.n; i++) {
+    if (st[i] == ST_ERROR) results[i] = {CUBBS_BBS_GPU_ERR_INVALID_INPUT, 0, 0};
+    else results[i] = {CUBBS_BBS_GPU_SUCCESS, (uint8_t)(st[i] == ST_OK && hok[i] ? 1 : 0), 0};
+  }
 }
 
 }  // namespace
+
+// Runs one packed batch through upload + pipeline (used by the ABI entries and the bench).
+static void execute(Runtime &rt, OpBatch &b) {
+  g_h2d_bytes = g_d2h_bytes = 0;
+  upload(rt, b);
+  uint8_t *mapdst = upload_mapdst(rt);
+  run(rt, b, mapdst);
+}
 
 }  // namespace cubbs
 
@@ -583,120 +1032,35 @@ extern "C" int32_t cubbs_bbs_gpu_proof_verify_batch_v2(uint32_t abi, const CuBbs
                                                        size_t n, CuBbsBbsGpuResult *results) {
   if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
-  #pragma unroll 1
-  for (size_t i = 0; i < n; i++) {
-    const auto &it = items[i];
-    if (it.public_key.data == nullptr || it.public_key.len != 96 || (it.proof.len && !it.proof.data) ||
-        (it.header.len && !it.header.data) || (it.presentation_header.len && !it.presentation_header.data) ||
-        (it.disclosed_count && !it.disclosed_messages) ||
-        (it.disclosed_indexes.len && !it.disclosed_indexes.data))
-      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-    #pragma unroll 1
-    for (size_t k = 0; k < it.disclosed_count; k++)
-      if (it.disclosed_messages[k].len && !it.disclosed_messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-  }
   try {
     Runtime &rt = Runtime::get();
     CallScope scope(rt);
-    Blob blob;
-    MsgList ml;
-    std::vector<PvItem> hi(n);
-    std::vector<const uint8_t *> pks(n);
-    size_t maxL = 0;
-    std::vector<size_t> di;
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) {
-      const auto &it = items[i];
-      PvItem &p = hi[i];
-      std::memset(&p, 0, sizeof p);
-      pks[i] = it.public_key.data;
-      p.status = ST_OK;
-      size_t plen = it.proof.len;
-      sort_dedup(it.disclosed_indexes.data, it.disclosed_indexes.len, di);
-      size_t U = plen >= 272 ? (plen - 240) / 32 - 1 : 0;
-      size_t R = di.size(), L = U + R;
-      bool ok = plen >= 272 && it.disclosed_count == R && L <= MAX_MESSAGES;
-      #pragma unroll 1
-      for (size_t k = 0; k < R && ok; k++) ok = di[k] < L;
-      p.msg_base = (uint32_t)ml.ptrs.size();
-      if (!ok) {
-        p.status = ST_INVALID;
-        p.proof_off = blob.put(nullptr, 0);
-        continue;
-      }
-      #pragma unroll 1
-      for (size_t k = 0; k < it.disclosed_count; k++) ml.add(it.disclosed_messages[k].data, it.disclosed_messages[k].len);
-      p.U = (uint32_t)U;
-      p.R = (uint32_t)R;
-      p.L = (uint32_t)L;
-      p.proof_off = blob.put(it.proof.data, 240 + 32 * (U + 1));
-      p.hdr_off = blob.put(it.header.data, it.header.len);
-      p.hdr_len = (uint32_t)it.header.len;
-      p.ph_off = blob.put(it.presentation_header.data, it.presentation_header.len);
-      p.ph_len = (uint32_t)it.presentation_header.len;
-      std::vector<uint32_t> d32(di.begin(), di.end());
-      p.idx_off = blob.put_u32s(d32);
-      maxL = std::max(maxL, L);
-    }
-    std::vector<uint32_t> pk_off(n);
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) pk_off[i] = blob.put(pks[i], 96);
-    std::vector<int> slots, pst;
-    rt.resolve_pks(pks, slots, pst);
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) {
-      hi[i].pk_slot = slots[i];
-      hi[i].pk_status = pst[i];
-      if (pst[i] == DEC_BAD) hi[i].status = ST_ERROR;
-    }
-    rt.ensure_table((int)maxL + 2);
-    size_t stride = maxL + 2;
-    rt.arena.reserve(reserve_for(n, maxL, blob.b.size(), ml.ptrs.size()));
-    rt.staging.reserve(blob.b.size() * 2 + ml.bytes + 16 * ml.ptrs.size() + n * 256 + 65536);
-    cudaStream_t s = rt.stream;
-    uint8_t *dblob = upload(rt, blob.b.data(), blob.b.size());
-    fr *msc = hash_messages(rt, ml);
-    // decode Abar, Bbar, D (items that failed host checks decode a zero buffer -> DEC_BAD)
-    std::vector<uint8_t> pbytes(144 * n, 0);
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++)
-      if (hi[i].status == ST_OK) std::memcpy(&pbytes[144 * i], items[i].proof.data, 144);
-    uint8_t *dp = upload(rt, pbytes.data(), pbytes.size());
-    g1a *pts = rt.arena.alloc<g1a>(3 * n);
-    int32_t *dst = rt.arena.alloc<int32_t>(3 * n);
-    launch_g1_decode(s, dp, 48, (uint32_t)(3 * n), pts, dst, true);
-    std::vector<DomainJob> dj(n);
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) dj[i] = {pk_off[i], hi[i].hdr_off, hi[i].hdr_len, hi[i].L};
-    DomainJob *ddj = upload(rt, dj.data(), n);
-    fr *domain = rt.arena.alloc<fr>(n);
-    launch_domain(s, ddj, (uint32_t)n, dblob, rt.d_gens_c, domain);
-    PvItem *ditems = upload(rt, hi.data(), n);
-    fr *rows = rt.arena.alloc<fr>(n * stride);
-    uint32_t *nterms = rt.arena.alloc<uint32_t>(n);
-    VarJob *jobs = rt.arena.alloc<VarJob>(4 * n);
-    fr *jscal = rt.arena.alloc<fr>(4 * n);
-    k_pv_prep<<<blocks_for(n, 128), 128, 0, s>>>(ditems, (uint32_t)n, dblob, msc, domain, dst, rows,
-                                                 (uint32_t)stride, nterms, jobs, jscal);
-    g1 *t2fix = rt.arena.alloc<g1>(n);
-    launch_fixed_msm(s, rt.table, rows, (uint32_t)stride, nterms, (uint32_t)n, t2fix);
-    g1 *v = rt.arena.alloc<g1>(4 * n);
-    launch_var_mul(s, pts, jobs, jscal, (uint32_t)(4 * n), v);
-    PairJob *pj = rt.arena.alloc<PairJob>(n);
-    k_pv_finish<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, dblob, msc, domain, t2fix, v, pts, dst, pj);
-    uint8_t *ok = rt.arena.alloc<uint8_t>(n);
-    launch_pairing_check(s, pj, (uint32_t)n, rt.d_lines, ok);
-    CUBBS_CHECK(cudaGetLastError());
-    std::vector<uint8_t> hok(n);
-    std::vector<PvItem> hout(n);
-    CUBBS_CHECK(cudaMemcpyAsync(hok.data(), ok, n, cudaMemcpyDeviceToHost, s));
-    CUBBS_CHECK(cudaMemcpyAsync(hout.data(), ditems, n * sizeof(PvItem), cudaMemcpyDeviceToHost, s));
-    CUBBS_CHECK(cudaStreamSynchronize(s));
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) {
-      if (hout[i].status == ST_ERROR) results[i] = {CUBBS_BBS_GPU_ERR_INVALID_INPUT, 0, 0};
-      else results[i] = {CUBBS_BBS_GPU_SUCCESS, (uint8_t)(hout[i].status == ST_OK && hok[i] ? 1 : 0), 0};
-    }
+    OpBatch b;
+    int32_t st = plan_pverify(items, n, b);
+    if (st != CUBBS_BBS_GPU_SUCCESS) return st;
+    finish_pks(rt, b);
+    execute(rt, b);
+    download_bool(rt, b, results);
+    return CUBBS_BBS_GPU_SUCCESS;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}
+
+// ----------------------------------------------------------------------------- Verify
+extern "C" int32_t cubbs_bbs_gpu_verify_batch_v2(uint32_t abi, const CuBbsBbsGpuVerifyItem *items, size_t n,
+                                                 CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
+  try {
+    Runtime &rt = Runtime::get();
+    CallScope scope(rt);
+    OpBatch b;
+    int32_t st = plan_verify(items, n, b);
+    if (st != CUBBS_BBS_GPU_SUCCESS) return st;
+    finish_pks(rt, b);
+    execute(rt, b);
+    download_bool(rt, b, results);
     return CUBBS_BBS_GPU_SUCCESS;
   } catch (const CudaError &) {
     return CUBBS_BBS_GPU_ERR_INTERNAL;
@@ -708,83 +1072,24 @@ extern "C" int32_t cubbs_bbs_gpu_sign_batch_v2(uint32_t abi, CuBbsBbsGpuSignItem
                                                CuBbsBbsGpuResult *results) {
   if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
-  #pragma unroll 1
-  for (size_t i = 0; i < n; i++) {
-    const auto &it = items[i];
-    if (it.secret_key.data == nullptr || it.public_key.data == nullptr || (it.header.len && !it.header.data) ||
-        (it.message_count && !it.messages) || it.signature_out.data == nullptr)
-      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-    #pragma unroll 1
-    for (size_t k = 0; k < it.message_count; k++)
-      if (it.messages[k].len && !it.messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-  }
   try {
     Runtime &rt = Runtime::get();
     CallScope scope(rt);
-    Blob blob;
-    MsgList ml;
-    std::vector<SignItem> hi(n);
-    std::vector<const uint8_t *> pks(n);
-    std::vector<uint8_t> zero96(96, 0);
-    size_t maxL = 0;
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) {
-      const auto &it = items[i];
-      SignItem &p = hi[i];
-      std::memset(&p, 0, sizeof p);
-      bool ok = it.secret_key.len == 32 && it.public_key.len == 96 && it.signature_out.capacity >= 80 &&
-                it.message_count <= MAX_MESSAGES;
-      p.status = ok ? ST_OK : ST_ERROR;
-      pks[i] = it.public_key.len == 96 ? it.public_key.data : zero96.data();
-      p.sk_off = blob.put(ok ? it.secret_key.data : zero96.data(), 32);
-      p.pk_off = blob.put(pks[i], 96);
-      p.hdr_off = blob.put(it.header.data, it.header.len);
-      p.hdr_len = (uint32_t)it.header.len;
-      p.msg_base = (uint32_t)ml.ptrs.size();
-      p.L = ok ? (uint32_t)it.message_count : 0;
-      if (ok)
-        #pragma unroll 1
-        for (size_t k = 0; k < it.message_count; k++) ml.add(it.messages[k].data, it.messages[k].len);
-      maxL = std::max(maxL, (size_t)p.L);
-    }
-    std::vector<int> slots, pst;
-    rt.resolve_pks(pks, slots, pst);
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) hi[i].pk_status = pst[i];
-    rt.ensure_table((int)maxL + 2);
-    size_t stride = maxL + 2;
-    rt.arena.reserve(reserve_for(n, maxL, blob.b.size(), ml.ptrs.size()));
-    rt.staging.reserve(blob.b.size() * 2 + ml.bytes + 16 * ml.ptrs.size() + n * 256 + 65536);
-    cudaStream_t s = rt.stream;
-    uint8_t *dblob = upload(rt, blob.b.data(), blob.b.size());
-    fr *msc = hash_messages(rt, ml);
-    std::vector<DomainJob> dj(n);
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) dj[i] = {hi[i].pk_off, hi[i].hdr_off, hi[i].hdr_len, hi[i].L};
-    DomainJob *ddj = upload(rt, dj.data(), n);
-    fr *domain = rt.arena.alloc<fr>(n);
-    launch_domain(s, ddj, (uint32_t)n, dblob, rt.d_gens_c, domain);
-    SignItem *ditems = upload(rt, hi.data(), n);
-    fr *rows = rt.arena.alloc<fr>(n * stride);
-    uint32_t *nterms = rt.arena.alloc<uint32_t>(n);
-    fr *e = rt.arena.alloc<fr>(n);
-    k_sign_prep<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, dblob, msc, domain, rows, (uint32_t)stride,
-                                                 nterms, e);
-    g1 *A = rt.arena.alloc<g1>(n);
-    launch_fixed_msm(s, rt.table, rows, (uint32_t)stride, nterms, (uint32_t)n, A);
-    uint8_t *sig = rt.arena.alloc<uint8_t>(80 * n);
-    k_sign_finish<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, A, e, sig);
-    CUBBS_CHECK(cudaGetLastError());
+    OpBatch b;
+    int32_t st = plan_sign(items, n, b);
+    if (st != CUBBS_BBS_GPU_SUCCESS) return st;
+    finish_pks(rt, b);
+    execute(rt, b);
     std::vector<uint8_t> hsig(80 * n);
-    std::vector<SignItem> hout(n);
-    CUBBS_CHECK(cudaMemcpyAsync(hsig.data(), sig, 80 * n, cudaMemcpyDeviceToHost, s));
-    CUBBS_CHECK(cudaMemcpyAsync(hout.data(), ditems, n * sizeof(SignItem), cudaMemcpyDeviceToHost, s));
-    CUBBS_CHECK(cudaStreamSynchronize(s));
-    #pragma unroll 1
+    std::vector<SignItem> h;
+    CUBBS_CHECK(cudaMemcpyAsync(hsig.data(), b.out, 80 * n, cudaMemcpyDeviceToHost, rt.stream));
+    g_d2h_bytes += 80 * n;
+    fetch_items(rt, b, h);
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
     for (size_t i = 0; i < n; i++) {
-      if (items[i].signature_out.capacity < 80 && items[i].secret_key.len == 32 && items[i].public_key.len == 96) {
-        results[i] = {CUBBS_BBS_GPU_ERR_INSUFFICIENT_OUTPUT, 0, 0};
-      } else if (hout[i].status != ST_OK) {
+      if (b.code[i] != CUBBS_BBS_GPU_SUCCESS) {
+        results[i] = {b.code[i], 0, 0};
+      } else if (h[i].status != ST_OK) {
         results[i] = {CUBBS_BBS_GPU_ERR_INVALID_INPUT, 0, 0};
       } else {
         std::memcpy(items[i].signature_out.data, &hsig[80 * i], 80);
@@ -798,252 +1103,33 @@ extern "C" int32_t cubbs_bbs_gpu_sign_batch_v2(uint32_t abi, CuBbsBbsGpuSignItem
   }
 }
 
-// ----------------------------------------------------------------------------- Verify
-extern "C" int32_t cubbs_bbs_gpu_verify_batch_v2(uint32_t abi, const CuBbsBbsGpuVerifyItem *items, size_t n,
-                                                 CuBbsBbsGpuResult *results) {
-  if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-  if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
-  #pragma unroll 1
-  for (size_t i = 0; i < n; i++) {
-    const auto &it = items[i];
-    if (it.public_key.data == nullptr || it.public_key.len != 96 || (it.signature.len && !it.signature.data) ||
-        (it.header.len && !it.header.data) || (it.message_count && !it.messages))
-      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-    #pragma unroll 1
-    for (size_t k = 0; k < it.message_count; k++)
-      if (it.messages[k].len && !it.messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-  }
-  try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
-    Blob blob;
-    MsgList ml;
-    std::vector<VerifyItem> hi(n);
-    std::vector<const uint8_t *> pks(n);
-    std::vector<uint8_t> sigA(48 * n, 0);
-    size_t maxL = 0;
-    std::vector<uint32_t> pk_off(n);
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) {
-      const auto &it = items[i];
-      VerifyItem &p = hi[i];
-      std::memset(&p, 0, sizeof p);
-      pks[i] = it.public_key.data;
-      bool ok = it.signature.len == 80 && it.message_count <= MAX_MESSAGES;
-      p.status = ok ? ST_OK : ST_INVALID;
-      static const uint8_t zeros[80] = {0};
-      p.sig_off = blob.put(ok ? it.signature.data : zeros, 80);
-      if (ok) std::memcpy(&sigA[48 * i], it.signature.data, 48);
-      pk_off[i] = blob.put(it.public_key.data, 96);
-      p.hdr_off = blob.put(it.header.data, it.header.len);
-      p.hdr_len = (uint32_t)it.header.len;
-      p.msg_base = (uint32_t)ml.ptrs.size();
-      p.L = ok ? (uint32_t)it.message_count : 0;
-      if (ok)
-        #pragma unroll 1
-        for (size_t k = 0; k < it.message_count; k++) ml.add(it.messages[k].data, it.messages[k].len);
-      maxL = std::max(maxL, (size_t)p.L);
-    }
-    std::vector<int> slots, pst;
-    rt.resolve_pks(pks, slots, pst);
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) {
-      hi[i].pk_slot = slots[i];
-      hi[i].pk_status = pst[i];
-      if (pst[i] == DEC_BAD) hi[i].status = ST_ERROR;
-    }
-    rt.ensure_table((int)maxL + 2);
-    size_t stride = maxL + 2;
-    rt.arena.reserve(reserve_for(n, maxL, blob.b.size(), ml.ptrs.size()));
-    rt.staging.reserve(blob.b.size() * 2 + ml.bytes + 16 * ml.ptrs.size() + n * 256 + 65536);
-    cudaStream_t s = rt.stream;
-    uint8_t *dblob = upload(rt, blob.b.data(), blob.b.size());
-    fr *msc = hash_messages(rt, ml);
-    uint8_t *dsa = upload(rt, sigA.data(), sigA.size());
-    g1a *A = rt.arena.alloc<g1a>(n);
-    int32_t *dst = rt.arena.alloc<int32_t>(n);
-    launch_g1_decode(s, dsa, 48, (uint32_t)n, A, dst, true);
-    std::vector<DomainJob> dj(n);
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) dj[i] = {pk_off[i], hi[i].hdr_off, hi[i].hdr_len, hi[i].L};
-    DomainJob *ddj = upload(rt, dj.data(), n);
-    fr *domain = rt.arena.alloc<fr>(n);
-    launch_domain(s, ddj, (uint32_t)n, dblob, rt.d_gens_c, domain);
-    VerifyItem *ditems = upload(rt, hi.data(), n);
-    fr *rows = rt.arena.alloc<fr>(n * stride);
-    uint32_t *nterms = rt.arena.alloc<uint32_t>(n);
-    VarJob *jobs = rt.arena.alloc<VarJob>(n);
-    fr *jscal = rt.arena.alloc<fr>(n);
-    k_verify_prep<<<blocks_for(n, 128), 128, 0, s>>>(ditems, (uint32_t)n, dblob, msc, domain, dst, rows,
-                                                     (uint32_t)stride, nterms, jobs, jscal);
-    g1 *B = rt.arena.alloc<g1>(n);
-    launch_fixed_msm(s, rt.table, rows, (uint32_t)stride, nterms, (uint32_t)n, B);
-    g1 *v = rt.arena.alloc<g1>(n);
-    launch_var_mul(s, A, jobs, jscal, (uint32_t)n, v);
-    PairJob *pj = rt.arena.alloc<PairJob>(n);
-    k_verify_finish<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, B, v, A, dst, pj);
-    uint8_t *ok = rt.arena.alloc<uint8_t>(n);
-    launch_pairing_check(s, pj, (uint32_t)n, rt.d_lines, ok);
-    CUBBS_CHECK(cudaGetLastError());
-    std::vector<uint8_t> hok(n);
-    std::vector<VerifyItem> hout(n);
-    CUBBS_CHECK(cudaMemcpyAsync(hok.data(), ok, n, cudaMemcpyDeviceToHost, s));
-    CUBBS_CHECK(cudaMemcpyAsync(hout.data(), ditems, n * sizeof(VerifyItem), cudaMemcpyDeviceToHost, s));
-    CUBBS_CHECK(cudaStreamSynchronize(s));
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) {
-      if (hout[i].status == ST_ERROR) results[i] = {CUBBS_BBS_GPU_ERR_INVALID_INPUT, 0, 0};
-      else results[i] = {CUBBS_BBS_GPU_SUCCESS, (uint8_t)(hout[i].status == ST_OK && hok[i] ? 1 : 0), 0};
-    }
-    return CUBBS_BBS_GPU_SUCCESS;
-  } catch (const CudaError &) {
-    return CUBBS_BBS_GPU_ERR_INTERNAL;
-  }
-}
-
 // ----------------------------------------------------------------------------- ProofGen
 static int32_t proof_gen_impl(CuBbsBbsGpuProofGenItem *items, size_t n, const uint8_t (*seeds)[32],
                               CuBbsBbsGpuResult *results) {
-  #pragma unroll 1
-  for (size_t i = 0; i < n; i++) {
-    const auto &it = items[i];
-    if (it.public_key.data == nullptr || it.public_key.len != 96 || (it.signature.len && !it.signature.data) ||
-        (it.header.len && !it.header.data) || (it.presentation_header.len && !it.presentation_header.data) ||
-        (it.message_count && !it.messages) || (it.disclosed_indexes.len && !it.disclosed_indexes.data) ||
-        it.proof_out.data == nullptr)
-      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-    #pragma unroll 1
-    for (size_t k = 0; k < it.message_count; k++)
-      if (it.messages[k].len && !it.messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-  }
-  std::vector<uint8_t> os_seeds;
-  if (seeds == nullptr) {  // production blinding: 32 bytes of OS randomness per item
-    os_seeds.resize(32 * n);
-    size_t got = 0;
-    while (got < os_seeds.size()) {
-      ssize_t r = getrandom(os_seeds.data() + got, os_seeds.size() - got, 0);
-      if (r <= 0) return CUBBS_BBS_GPU_ERR_INTERNAL;
-      got += (size_t)r;
-    }
-  }
   try {
     Runtime &rt = Runtime::get();
     CallScope scope(rt);
-    Blob blob;
-    MsgList ml;
-    std::vector<PgItem> hi(n);
-    std::vector<const uint8_t *> pks(n);
-    std::vector<uint8_t> sigA(48 * n, 0);
-    std::vector<uint32_t> pk_off(n);
-    std::vector<int32_t> code(n, CUBBS_BBS_GPU_SUCCESS);
-    size_t maxL = 0, maxU = 0, out_total = 0;
-    std::vector<size_t> di;
-    #pragma unroll 1
+    OpBatch b;
+    std::vector<uint8_t> os_seeds;
+    int32_t st = plan_pgen(items, n, seeds, b, os_seeds);
+    if (st != CUBBS_BBS_GPU_SUCCESS) return st;
+    finish_pks(rt, b);
+    execute(rt, b);
+    std::vector<uint8_t> hout(b.out_total + 1);
+    std::vector<PgItem> h;
+    CUBBS_CHECK(cudaMemcpyAsync(hout.data(), b.out, b.out_total + 1, cudaMemcpyDeviceToHost, rt.stream));
+    g_d2h_bytes += b.out_total + 1;
+    fetch_items(rt, b, h);
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    const PgItem *hp = reinterpret_cast<const PgItem *>(b.items.data());
     for (size_t i = 0; i < n; i++) {
-      const auto &it = items[i];
-      PgItem &p = hi[i];
-      std::memset(&p, 0, sizeof p);
-      pks[i] = it.public_key.data;
-      sort_dedup(it.disclosed_indexes.data, it.disclosed_indexes.len, di);
-      size_t L = it.message_count, R = di.size();
-      bool ok = it.signature.len == 80 && L <= MAX_MESSAGES && R <= L;
-      #pragma unroll 1
-      for (size_t k = 0; k < R && ok; k++) ok = di[k] < L;
-      size_t U = ok ? L - R : 0;
-      size_t need = 272 + 32 * U;
-      if (ok && it.proof_out.capacity < need) {
-        code[i] = CUBBS_BBS_GPU_ERR_INSUFFICIENT_OUTPUT;
-        ok = false;
-      } else if (!ok) {
-        code[i] = CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-      }
-      p.status = ok ? ST_OK : ST_ERROR;
-      static const uint8_t zeros[80] = {0};
-      p.sig_off = blob.put(ok ? it.signature.data : zeros, 80);
-      if (ok) std::memcpy(&sigA[48 * i], it.signature.data, 48);
-      pk_off[i] = blob.put(it.public_key.data, 96);
-      p.hdr_off = blob.put(it.header.data, it.header.len);
-      p.hdr_len = (uint32_t)it.header.len;
-      p.ph_off = blob.put(it.presentation_header.data, it.presentation_header.len);
-      p.ph_len = (uint32_t)it.presentation_header.len;
-      std::vector<uint32_t> d32(di.begin(), di.end());
-      p.idx_off = blob.put_u32s(d32);
-      p.seed_off = blob.put(seeds ? seeds[i] : &os_seeds[32 * i], 32);
-      p.msg_base = (uint32_t)ml.ptrs.size();
-      p.L = ok ? (uint32_t)L : 0;
-      p.R = ok ? (uint32_t)R : 0;
-      p.U = (uint32_t)U;
-      p.out_off = (uint32_t)out_total;
-      if (ok) {
-        out_total += need;
-        #pragma unroll 1
-        for (size_t k = 0; k < L; k++) ml.add(it.messages[k].data, it.messages[k].len);
-      }
-      maxL = std::max(maxL, (size_t)p.L);
-      maxU = std::max(maxU, U);
-    }
-    std::vector<int> slots, pst;
-    rt.resolve_pks(pks, slots, pst);
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) {
-      hi[i].pk_status = pst[i];
-      if (pst[i] == DEC_BAD && hi[i].status == ST_OK) {
-        hi[i].status = ST_ERROR;
-        code[i] = CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-      }
-    }
-    rt.ensure_table((int)maxL + 2);
-    size_t stride = maxL + 2, rs_stride = maxU + 5;
-    rt.arena.reserve(reserve_for(2 * n, maxL, blob.b.size(), ml.ptrs.size()) + n * rs_stride * sizeof(fr) +
-                     out_total + 14 * n * sizeof(g1));
-    rt.staging.reserve(blob.b.size() * 2 + ml.bytes + 16 * ml.ptrs.size() + n * 256 + out_total + 65536);
-    cudaStream_t s = rt.stream;
-    uint8_t *dblob = upload(rt, blob.b.data(), blob.b.size());
-    fr *msc = hash_messages(rt, ml);
-    uint8_t *dsa = upload(rt, sigA.data(), sigA.size());
-    g1a *A = rt.arena.alloc<g1a>(n);
-    int32_t *dst = rt.arena.alloc<int32_t>(n);
-    launch_g1_decode(s, dsa, 48, (uint32_t)n, A, dst, true);
-    std::vector<DomainJob> dj(n);
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) dj[i] = {pk_off[i], hi[i].hdr_off, hi[i].hdr_len, hi[i].L};
-    DomainJob *ddj = upload(rt, dj.data(), n);
-    fr *domain = rt.arena.alloc<fr>(n);
-    launch_domain(s, ddj, (uint32_t)n, dblob, rt.d_gens_c, domain);
-    PgItem *ditems = upload(rt, hi.data(), n);
-    fr *rs = rt.arena.alloc<fr>(n * rs_stride);
-    k_pg_random<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, dblob, rs, (uint32_t)rs_stride);
-    fr *rows = rt.arena.alloc<fr>(2 * n * stride);
-    uint32_t *nterms = rt.arena.alloc<uint32_t>(2 * n);
-    k_pg_prep<<<blocks_for(n, 128), 128, 0, s>>>(ditems, (uint32_t)n, dblob, msc, domain, rs, (uint32_t)rs_stride,
-                                                 dst, rows, (uint32_t)stride, nterms);
-    g1 *fixed = rt.arena.alloc<g1>(2 * n);
-    launch_fixed_msm(s, rt.table, rows, (uint32_t)stride, nterms, (uint32_t)(2 * n), fixed);
-    g1a *pts = rt.arena.alloc<g1a>(2 * n);
-    VarJob *jobs = rt.arena.alloc<VarJob>(7 * n);
-    fr *jscal = rt.arena.alloc<fr>(7 * n);
-    k_pg_vars<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, dblob, fixed, A, dst, rs, (uint32_t)rs_stride,
-                                               pts, jobs, jscal);
-    g1 *v = rt.arena.alloc<g1>(7 * n);
-    launch_var_mul(s, pts, jobs, jscal, (uint32_t)(7 * n), v);
-    uint8_t *out = rt.arena.alloc<uint8_t>(out_total + 1);
-    k_pg_finish<<<blocks_for(n, 64), 64, 0, s>>>(ditems, (uint32_t)n, dblob, msc, domain, rs, (uint32_t)rs_stride,
-                                                 fixed + n, v, out);
-    CUBBS_CHECK(cudaGetLastError());
-    std::vector<uint8_t> hout_b(out_total + 1);
-    std::vector<PgItem> hout(n);
-    CUBBS_CHECK(cudaMemcpyAsync(hout_b.data(), out, out_total + 1, cudaMemcpyDeviceToHost, s));
-    CUBBS_CHECK(cudaMemcpyAsync(hout.data(), ditems, n * sizeof(PgItem), cudaMemcpyDeviceToHost, s));
-    CUBBS_CHECK(cudaStreamSynchronize(s));
-    #pragma unroll 1
-    for (size_t i = 0; i < n; i++) {
-      if (code[i] != CUBBS_BBS_GPU_SUCCESS) {
-        results[i] = {code[i], 0, 0};
-      } else if (hout[i].status != ST_OK) {
+      if (b.code[i] != CUBBS_BBS_GPU_SUCCESS) {
+        results[i] = {b.code[i], 0, 0};
+      } else if (h[i].status != ST_OK) {
         results[i] = {CUBBS_BBS_GPU_ERR_INVALID_INPUT, 0, 0};
       } else {
-        size_t need = 272 + 32 * (size_t)hi[i].U;
-        std::memcpy(items[i].proof_out.data, &hout_b[hi[i].out_off], need);
+        size_t need = 272 + 32 * (size_t)hp[i].U;
+        std::memcpy(items[i].proof_out.data, &hout[hp[i].out_off], need);
         items[i].proof_out.len = need;
         results[i] = {CUBBS_BBS_GPU_SUCCESS, 0, need};
       }
@@ -1067,6 +1153,98 @@ extern "C" int32_t cubbs_bbs_gpu_proof_gen_seeded_batch_v2(uint32_t abi, CuBbsBb
     return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   return proof_gen_impl(items, n, seeds, results);
+}
+
+// ----------------------------------------------------------------------------- device-resident timing
+// Benchmark entry (outside the reference ABI): packs and uploads one batch of
+// the given operation once, then replays the whole device pipeline warmup +
+// steps times on the library's stream.  Each timed step is bracketed by CUDA
+// events on that stream; between steps a 256 MiB buffer is rewritten to evict
+// L2 (outside the events).  op: 0 Sign, 1 Verify, 2 ProofGen (items seeded by
+// seeds), 3 ProofVerify.  ms_out[k] = duration of step k; *launches = kernels
+// per step.  The results of the last step are returned in results as the ABI
+// call would.
+static char g_stage_names[16][32];
+static float g_stage_ms[16];
+static int g_stage_count = 0;
+
+extern "C" int32_t cubbs_bbs_gpu_bench_device_steps_v2(uint32_t abi, int32_t op, void *items, size_t n,
+                                                       const uint8_t (*seeds)[32], int32_t warmup, int32_t steps,
+                                                       float *ms_out, int32_t *launches, CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || !items || n == 0 || !ms_out || !launches || !results || steps <= 0 || warmup < 0)
+    return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  try {
+    Runtime &rt = Runtime::get();
+    CallScope scope(rt);
+    OpBatch b;
+    std::vector<uint8_t> os_seeds;
+    int32_t st;
+    switch (op) {
+      case 0: st = plan_sign(static_cast<CuBbsBbsGpuSignItem *>(items), n, b); break;
+      case 1: st = plan_verify(static_cast<const CuBbsBbsGpuVerifyItem *>(items), n, b); break;
+      case 2: st = plan_pgen(static_cast<CuBbsBbsGpuProofGenItem *>(items), n, seeds, b, os_seeds); break;
+      case 3: st = plan_pverify(static_cast<const CuBbsBbsGpuProofVerifyItem *>(items), n, b); break;
+      default: return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+    }
+    if (st != CUBBS_BBS_GPU_SUCCESS) return st;
+    finish_pks(rt, b);
+    upload(rt, b);
+    uint8_t *mapdst = upload_mapdst(rt);
+    static uint8_t *flush = nullptr;
+    const size_t FLUSH = (size_t)256 << 20;
+    if (!flush) CUBBS_CHECK(cudaMalloc(&flush, FLUSH));
+    cudaEvent_t e0, e1;
+    CUBBS_CHECK(cudaEventCreate(&e0));
+    CUBBS_CHECK(cudaEventCreate(&e1));
+    for (int k = 0; k < warmup + steps; k++) {
+      CUBBS_CHECK(cudaMemsetAsync(flush, k & 0xff, FLUSH, rt.stream));
+      CUBBS_CHECK(cudaEventRecord(e0, rt.stream));
+      run(rt, b, mapdst);
+      CUBBS_CHECK(cudaEventRecord(e1, rt.stream));
+      CUBBS_CHECK(cudaEventSynchronize(e1));
+      float ms = 0;
+      CUBBS_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+      if (k >= warmup) ms_out[k - warmup] = ms;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    *launches = (int32_t)b.launches_per_run;
+    // one extra untimed replay with per-stage events for the breakdown
+    StageEvents se;
+    for (int k = 0; k < 16; k++) CUBBS_CHECK(cudaEventCreate(&se.ev[k]));
+    g_stages = &se;
+    CUBBS_CHECK(cudaMemsetAsync(flush, 0x5a, FLUSH, rt.stream));
+    run(rt, b, mapdst);
+    g_stages = nullptr;
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    g_stage_count = se.used > 0 ? se.used - 1 : 0;
+    for (int k = 1; k < se.used; k++) {
+      float ms = 0;
+      cudaEventElapsedTime(&ms, se.ev[k - 1], se.ev[k]);
+      g_stage_ms[k - 1] = ms;
+      std::snprintf(g_stage_names[k - 1], 32, "%s", se.name[k]);
+    }
+    for (int k = 0; k < 16; k++) cudaEventDestroy(se.ev[k]);
+    if (op == 1 || op == 3) {
+      download_bool(rt, b, results);
+    } else {
+      std::vector<uint8_t> codes(n);
+      if (op == 0) {
+        std::vector<SignItem> h;
+        fetch_items(rt, b, h);
+        CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+        for (size_t i = 0; i < n; i++) results[i] = {h[i].status == ST_OK ? 0 : 1, 0, 80};
+      } else {
+        std::vector<PgItem> h;
+        fetch_items(rt, b, h);
+        CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+        for (size_t i = 0; i < n; i++) results[i] = {h[i].status == ST_OK ? 0 : 1, 0, 0};
+      }
+    }
+    return CUBBS_BBS_GPU_SUCCESS;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
 }
 
 // Test export: H2S(s_0 || ... || s_{n-1}, api_id || "H2S_") over canonical scalars,
@@ -1153,4 +1331,22 @@ extern "C" int32_t cubbs_bbs_gpu_pairs_h2s_for_test_v2(uint32_t abi, const uint8
 extern "C" int32_t cubbs_bbs_gpu_last_debug_record_for_test_v2(uint8_t *out256) {
   if (!out256) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   return cudaMemcpyFromSymbol(out256, g_debug_record, 256) == cudaSuccess ? 0 : CUBBS_BBS_GPU_ERR_INTERNAL;
+}
+
+// Stage breakdown of the last bench_device_steps call: returns the number of
+// stages; names are written as 32-byte NUL-padded strings.
+extern "C" int32_t cubbs_bbs_gpu_bench_stages_v2(char *names32, float *ms, int32_t cap) {
+  int k = 0;
+  for (; k < g_stage_count && k < cap; k++) {
+    std::memcpy(names32 + 32 * k, g_stage_names[k], 32);
+    ms[k] = g_stage_ms[k];
+  }
+  return k;
+}
+
+extern "C" int32_t cubbs_bbs_gpu_last_transfer_bytes_v2(uint64_t *h2d, uint64_t *d2h) {
+  if (!h2d || !d2h) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  *h2d = g_h2d_bytes;
+  *d2h = g_d2h_bytes;
+  return 0;
 }

@@ -156,3 +156,80 @@ extern "C" int32_t cubbs_bbs_gpu_g1_op_for_test_v2(uint32_t abi, const uint8_t *
     return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   return run_test(1, 0, pts48, k32, n, xy96, kp48, status);
 }
+
+// ------------------------------------------------------------------------- integer-pipe peak
+// Peak 32-bit multiply-add throughput: every thread runs 16 independent
+// mad.lo chains (no carries), so issue rate, not latency, bounds the kernel.
+__global__ void __launch_bounds__(256) k_imad_peak(uint32_t *out, uint32_t iters, uint32_t seed) {
+  uint32_t a[16];
+#pragma unroll
+  for (int k = 0; k < 16; k++) a[k] = seed + threadIdx.x * 16 + k;
+  const uint32_t m = 0x9e3779b9u + blockIdx.x;
+#pragma unroll 1
+  for (uint32_t it = 0; it < iters; it++) {
+#pragma unroll
+    for (int r = 0; r < 8; r++) {
+#pragma unroll
+      for (int k = 0; k < 16; k++) asm volatile("mad.lo.u32 %0, %0, %1, %2;" : "+r"(a[k]) : "r"(m), "r"(k + 1));
+    }
+  }
+  uint32_t x = 0;
+#pragma unroll
+  for (int k = 0; k < 16; k++) x ^= a[k];
+  if (x == 0x12345678u) out[0] = x;  // keeps the chains live
+}
+
+// Fp Montgomery products per second at full occupancy (4 independent products per thread).
+__global__ void __launch_bounds__(256) k_fpmul_rate(fp *out, uint32_t iters) {
+  fp a = fp_one(), b = fp_one(), c = fp_one(), d = fp_one();
+  a.w[0] += threadIdx.x; b.w[1] += blockIdx.x; c.w[2] += 3; d.w[3] += 5;
+  fp k = fp_one();
+  k.w[4] ^= threadIdx.x * 7u;
+#pragma unroll 1
+  for (uint32_t it = 0; it < iters; it++) {
+    a = fp_mul(a, k);
+    b = fp_mul(b, k);
+    c = fp_mul(c, k);
+    d = fp_mul(d, k);
+  }
+  if (fp_is_zero(a) && fp_is_zero(b) && fp_is_zero(c) && fp_is_zero(d)) out[0] = a;
+}
+
+// Returns the measured IMAD rate (1e12 multiply-adds per second) and the Fp
+// Montgomery product rate (1e9 products per second) on the current device.
+extern "C" int32_t cubbs_bbs_gpu_int_peaks_v2(double *tera_imad, double *giga_fpmul) {
+  if (!tera_imad || !giga_fpmul) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  try {
+    Runtime &rt = Runtime::get();
+    CallScope scope(rt);
+    uint32_t *o = rt.arena.alloc<uint32_t>(4);
+    fp *of = rt.arena.alloc<fp>(1);
+    int blocks = rt.sm_count * 8;
+    cudaEvent_t e0, e1;
+    CUBBS_CHECK(cudaEventCreate(&e0));
+    CUBBS_CHECK(cudaEventCreate(&e1));
+    const uint32_t iters = 4096;
+    k_imad_peak<<<blocks, 256, 0, rt.stream>>>(o, 64, 1);  // warm-up
+    CUBBS_CHECK(cudaEventRecord(e0, rt.stream));
+    k_imad_peak<<<blocks, 256, 0, rt.stream>>>(o, iters, 2);
+    CUBBS_CHECK(cudaEventRecord(e1, rt.stream));
+    CUBBS_CHECK(cudaEventSynchronize(e1));
+    float ms = 0;
+    CUBBS_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+    *tera_imad = (double)blocks * 256 * iters * 8 * 16 / (ms * 1e-3) / 1e12;
+    const uint32_t fiters = 256;
+    k_fpmul_rate<<<blocks, 256, 0, rt.stream>>>(of, 8);
+    CUBBS_CHECK(cudaEventRecord(e0, rt.stream));
+    k_fpmul_rate<<<blocks, 256, 0, rt.stream>>>(of, fiters);
+    CUBBS_CHECK(cudaEventRecord(e1, rt.stream));
+    CUBBS_CHECK(cudaEventSynchronize(e1));
+    CUBBS_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+    *giga_fpmul = (double)blocks * 256 * fiters * 4 / (ms * 1e-3) / 1e9;
+    CUBBS_CHECK(cudaGetLastError());
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return 0;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}
