@@ -17,6 +17,8 @@ LIB_PATH = _HERE / "lib" / "libcubbs_bbs_cuda.so"
 ABI_VERSION = 2
 
 SUCCESS, ERR_INVALID_INPUT, ERR_INSUFFICIENT_OUTPUT, ERR_INTERNAL = 0, 1, 2, 3
+ERR_NOALLOC_LIMIT = 4          # cubbs_bbs_gpu_g1_msm_noalloc_v2 only: too many terms
+NOALLOC_MSM_MAX_TERMS = 4096   # term limit of cubbs_bbs_gpu_g1_msm_noalloc_v2
 BACKEND_KIND_CUDA = 1
 API_ID = b"BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_H2G_HM2S_"
 MAP_DST = API_ID + b"MAP_MSG_TO_SCALAR_AS_HASH_"
@@ -162,6 +164,7 @@ def lib():
             "cubbs_bbs_gpu_sha256_batch_for_test_v2": [U32, P, P, P, S, P],
             "cubbs_bbs_gpu_expand_xmd_sha256_48_batch_for_test_v2": [U32, P, P, P, S, P, S, P],
             "cubbs_bbs_gpu_hash_to_scalar_sha256_batch_for_test_v2": [U32, P, P, P, S, P, S, P],
+            "cubbs_bbs_gpu_g1_msm_noalloc_v2": [U32, P, P, S, P, P],
         }
         for name in _SYMBOLS:
             fn = getattr(_LIB, name)
@@ -183,7 +186,7 @@ _SYMBOLS = [
     "cubbs_bbs_gpu_pairing_eq_batch_v2", "cubbs_bbs_gpu_pairing_eq_aggregate_v2",
     "cubbs_bbs_gpu_proof_gen_t2_prepare_batch_v2", "cubbs_bbs_gpu_sha256_batch_for_test_v2",
     "cubbs_bbs_gpu_expand_xmd_sha256_48_batch_for_test_v2",
-    "cubbs_bbs_gpu_hash_to_scalar_sha256_batch_for_test_v2",
+    "cubbs_bbs_gpu_hash_to_scalar_sha256_batch_for_test_v2", "cubbs_bbs_gpu_g1_msm_noalloc_v2",
 ]
 
 
@@ -363,6 +366,21 @@ def g1_msm_batch(msms):
     _call("cubbs_bbs_gpu_g1_msm_batch_v2", ABI_VERSION, items, len(msms), res)
     return [(res[i].code, outs[i].raw[:48]) for i in range(len(msms))]
 
+
+def g1_msm_noalloc(points, scalars):
+    """One MSM through the allocation-free entry point (fixed scratch array in
+    the library, at most NOALLOC_MSM_MAX_TERMS terms).  Returns (rc, code,
+    point48): rc is the call's return value, code the per-item result code."""
+    n = len(points)
+    pb = ctypes.create_string_buffer(b"".join(points), max(1, 48 * n))
+    sb = ctypes.create_string_buffer(b"".join(scalars), max(1, 32 * n))
+    out = ctypes.create_string_buffer(48)
+    res = Result()
+    rc = lib().cubbs_bbs_gpu_g1_msm_noalloc_v2(ABI_VERSION, ctypes.cast(pb, ctypes.c_void_p),
+                                               ctypes.cast(sb, ctypes.c_void_p), n,
+                                               ctypes.cast(out, ctypes.c_void_p),
+                                               ctypes.cast(ctypes.pointer(res), ctypes.c_void_p))
+    return rc, res.code, out.raw[:48]
 
 def g1_msm_common_points(points, rows, fused=False, packed_scale=None):
     """One group: common points, rows of scalars.  packed_scale: optional per-row

@@ -293,6 +293,27 @@ int32_t cubbs_bbs_gpu_prepare_b_batch_v2(uint32_t abi_version, CuBbsBbsGpuPrepar
 /* reference :263-266 */
 int32_t cubbs_bbs_gpu_g1_msm_batch_v2(uint32_t abi_version, CuBbsBbsGpuG1MsmItem *items,
                                       size_t item_count, CuBbsBbsGpuResult *results);
+
+/* Addition with no counterpart in the reference: one G1 MSM that allocates
+ * nothing.  out = sum_k scalar_k * point_k over term_count terms, given as
+ * contiguous 48-byte compressed points and 32-byte big-endian scalars; same
+ * result and per-item codes as one item of cubbs_bbs_gpu_g1_msm_batch_v2
+ * (result.value = route 4).  Every device buffer is a slice of one fixed
+ * scratch array in the library (under 2 MiB), so the call makes no device or
+ * pinned allocation: for callers that must not allocate while they run (a
+ * reserved-memory budget, code inside an allocator, work recorded ahead of
+ * time).  Limits: term_count <= CUBBS_BBS_GPU_NOALLOC_MSM_MAX_TERMS, else
+ * CUBBS_BBS_GPU_ERR_NOALLOC_LIMIT (returned and in result.code) with no CUDA
+ * call made.  The first call on a device does one-time set-up with that
+ * device current (looks up the scratch address; the driver may load the
+ * module and size the thread stack): make it before any stream capture.
+ * All calls share the scratch array, so overlapping calls would race; the
+ * library serialises them with a lock and each call is synchronous. */
+#define CUBBS_BBS_GPU_NOALLOC_MSM_MAX_TERMS 4096u
+#define CUBBS_BBS_GPU_ERR_NOALLOC_LIMIT 4
+int32_t cubbs_bbs_gpu_g1_msm_noalloc_v2(uint32_t abi_version, const uint8_t *points48,
+                                        const uint8_t *scalars32, size_t term_count,
+                                        uint8_t *point_out48, CuBbsBbsGpuResult *result);
 /* reference :268-271 */
 int32_t cubbs_bbs_gpu_g1_msm_common_points_batch_v2(uint32_t abi_version,
                                                     CuBbsBbsGpuG1MsmCommonPointsBatchItem *items,
