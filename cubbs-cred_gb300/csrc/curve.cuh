@@ -18,7 +18,10 @@ DEV g1 g1_from_aff(const g1a &a) { g1 r; r.X = a.x; r.Y = a.y; r.ZZ = fp_one(); 
 DEV g1 g1_neg(const g1 &p) { g1 r = p; r.Y = fp_neg(p.Y); return r; }
 DEV g1a g1a_neg(const g1a &p) { g1a r = p; r.y = fp_neg(p.y); return r; }
 
-DEVNI g1 g1_dbl(g1 p) {
+DEVNI g1 g1_dbl(g1 p);
+DEVNI g1 g1_dbl_aff(g1a p);
+
+DEV g1 g1_dbl_inl(g1 p) {
   if (g1_is_inf(p)) return p;
   fp U = fp_dbl(p.Y);
   fp V = fp_sqr(U);
@@ -33,7 +36,7 @@ DEVNI g1 g1_dbl(g1 p) {
   r.ZZZ = fp_mul(W, p.ZZZ);
   return r;
 }
-DEVNI g1 g1_dbl_aff(g1a p) {
+DEV g1 g1_dbl_aff_inl(g1a p) {
   fp U = fp_dbl(p.y);
   fp V = fp_sqr(U);
   fp W = fp_mul(U, V);
@@ -48,7 +51,7 @@ DEVNI g1 g1_dbl_aff(g1a p) {
   return r;
 }
 // p + q with q affine
-DEVNI g1 g1_add_aff(g1 p, g1a q) {
+DEV g1 g1_add_aff_inl(g1 p, g1a q) {
   if (g1_is_inf(p)) return g1_from_aff(q);
   fp U2 = fp_mul(q.x, p.ZZ);
   fp S2 = fp_mul(q.y, p.ZZZ);
@@ -68,7 +71,7 @@ DEVNI g1 g1_add_aff(g1 p, g1a q) {
   r.ZZZ = fp_mul(p.ZZZ, PPP);
   return r;
 }
-DEVNI g1 g1_add(g1 p, g1 q) {
+DEV g1 g1_add_inl(g1 p, g1 q) {
   if (g1_is_inf(p)) return q;
   if (g1_is_inf(q)) return p;
   fp U1 = fp_mul(p.X, q.ZZ);
@@ -91,6 +94,12 @@ DEVNI g1 g1_add(g1 p, g1 q) {
   r.ZZZ = fp_mul(fp_mul(p.ZZZ, q.ZZZ), PPP);
   return r;
 }
+// Out-of-line entry points (one copy per translation unit keeps compile
+// times bounded); hot loops call the _inl forms directly.
+DEVNI g1 g1_dbl(g1 p) { return g1_dbl_inl(p); }
+DEVNI g1 g1_dbl_aff(g1a p) { return g1_dbl_aff_inl(p); }
+DEVNI g1 g1_add_aff(g1 p, g1a q) { return g1_add_aff_inl(p, q); }
+DEVNI g1 g1_add(g1 p, g1 q) { return g1_add_inl(p, q); }
 // affine conversion with a single inversion; returns false for infinity
 DEV bool g1_to_aff(g1 p, g1a &out) {
   if (g1_is_inf(p)) return false;

@@ -53,7 +53,8 @@ DEV g1 zabs_unrolled_bits(g1 p) {
   return acc;
 }
 
-// op 0: Fp product of canonical BE inputs; op 1: Fp inverse; op 2: Fp sqrt (0 if none)
+// op 0: Fp product of canonical BE inputs; op 1: Fp inverse; op 2: Fp sqrt (0 if none);
+// op 3: variable-time Fp inverse
 __global__ void k_fp_test(const uint8_t *a, const uint8_t *b, uint32_t n, int op, uint8_t *out, int32_t *st) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -62,6 +63,7 @@ __global__ void k_fp_test(const uint8_t *a, const uint8_t *b, uint32_t n, int op
   if (ok) {
     if (op == 0) r = fp_mul(x, y);
     else if (op == 1) r = fp_inv(x);
+    else if (op == 3) r = fp_inv_vartime(x);
     else ok = fp_sqrt(x, r);
   }
   st[i] = ok ? 0 : 1;
@@ -141,7 +143,8 @@ static int32_t run_test(int kind, int op, const uint8_t *a, const uint8_t *b, si
   }
 }
 
-// op: 0 mul, 1 inverse, 2 sqrt.  Inputs and outputs are 48-byte big-endian canonical.
+// op: 0 mul, 1 inverse, 2 sqrt, 3 variable-time inverse.  Inputs and outputs are 48-byte
+// big-endian canonical.
 extern "C" int32_t cubbs_bbs_gpu_fp_op_for_test_v2(uint32_t abi, int32_t op, const uint8_t *a, const uint8_t *b,
                                                    size_t n, uint8_t *out, int32_t *status) {
   if (abi != CUBBS_BBS_GPU_ABI_VERSION || (n && (!a || !b || !out || !status))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
@@ -193,6 +196,130 @@ __global__ void __launch_bounds__(256) k_fpmul_rate(fp *out, uint32_t iters) {
     d = fp_mul(d, k);
   }
   if (fp_is_zero(a) && fp_is_zero(b) && fp_is_zero(c) && fp_is_zero(d)) out[0] = a;
+}
+
+// Code-size variants of the Fp product for the latency probe.
+DEVNI fp fp_mul_call(fp a, fp b) { return fp_mul_inl(a, b); }
+DEV fp fp_mul_rolled(const fp &a, fp b) {
+  uint32_t t[13];
+#pragma unroll
+  for (int j = 0; j < 13; j++) t[j] = 0;
+#pragma unroll 1
+  for (int i = 0; i < 12; i++) {
+    fp_cios_row(t, a.w, b.w[0]);
+#pragma unroll
+    for (int j = 0; j < 12; j++) t[j] = t[j + 1];
+    t[12] = 0;
+#pragma unroll
+    for (int j = 0; j < 11; j++) b.w[j] = b.w[j + 1];
+  }
+  fp r;
+  fp_reduce_once(r.w, t);
+  return r;
+}
+#define G1_DBL_WITH(NAME, MUL)                                   \
+  DEVNI g1 NAME(g1 p) {                                          \
+    if (g1_is_inf(p)) return p;                                  \
+    fp U = fp_dbl(p.Y);                                          \
+    fp V = MUL(U, U);                                            \
+    fp W = MUL(U, V);                                            \
+    fp S = MUL(p.X, V);                                          \
+    fp X2 = MUL(p.X, p.X);                                       \
+    fp M = fp_add(fp_dbl(X2), X2);                               \
+    g1 r;                                                        \
+    r.X = fp_sub(fp_sub(MUL(M, M), S), S);                       \
+    r.Y = fp_sub(MUL(M, fp_sub(S, r.X)), MUL(W, p.Y));           \
+    r.ZZ = MUL(V, p.ZZ);                                         \
+    r.ZZZ = MUL(W, p.ZZZ);                                       \
+    return r;                                                    \
+  }
+G1_DBL_WITH(g1_dbl_call, fp_mul_call)
+G1_DBL_WITH(g1_dbl_rolled, fp_mul_rolled)
+
+// Single-warp latency of dependent chains, in SM cycles per operation
+// (clock64 around n iterations; every lane runs the same chain).
+//   0 fp_mul (out of line)   1 three independent fp_mul chains (cycles per iteration)
+//   2 fp_add   3 fp2_mul   4 fp2_sqr   5 fp12_sqr   6 fp12_mul
+//   7 fp12_mul_line   8 g1_dbl   9 g1_add_aff   10 g1_add   11 fr_mul
+//   12 g1_dbl_inl   13 g1_add_aff_inl   14 fp2_mul_inl   15 fp_sqr chain of 64 (one fp_pow step)
+//   16 inlined fp_mul   17 three independent inlined fp_mul chains
+//   18/19 out-of-line fp_mul (1 / 3 chains)   20/21 rolled-loop fp_mul (1 / 3 chains)
+//   22 g1_dbl over out-of-line fp_mul   23 g1_dbl over rolled fp_mul
+__global__ void __launch_bounds__(32) k_latency_probe(double *cyc, fp *sink, uint32_t n) {
+  fp a = fp_one(), b = fp_one(), c = fp_one(), k = fp_one();
+  a.w[0] += threadIdx.x + 3;
+  b.w[1] += 7;
+  c.w[2] += 11;
+  k.w[3] ^= 0x55u;
+  fp2 x2 = {a, b}, k2 = {b, c};
+  fp12 f, g;
+  f.c0 = {x2, k2, x2};
+  f.c1 = {k2, x2, k2};
+  g = f;
+  g1 P = {a, b, fp_one(), fp_one()};
+  g1a Q = {c, k};
+  g1 Rr = {k, c, fp_one(), fp_one()};
+  fr s = fr_one(), sk = fr_one();
+  sk.w[1] ^= 0x1234u;
+  long long t0, t1;
+  const int R = 24;
+  double res[R];
+#define LAT(IDX, ITERS, BODY)                          \
+  t0 = clock64();                                      \
+  _Pragma("unroll 1") for (uint32_t it = 0; it < (ITERS); it++) { BODY; } \
+  t1 = clock64();                                      \
+  res[IDX] = (double)(t1 - t0) / (ITERS);
+  LAT(0, n, a = fp_mul(a, k));
+  LAT(1, n, a = fp_mul(a, k); b = fp_mul(b, k); c = fp_mul(c, k));
+  LAT(2, n, a = fp_add(a, k));
+  LAT(3, n, x2 = fp2_mul(x2, k2));
+  LAT(4, n, x2 = fp2_sqr(x2));
+  LAT(5, n / 8, f = fp12_sqr(f));
+  LAT(6, n / 8, f = fp12_mul(f, g));
+  LAT(7, n / 8, f = fp12_mul_line(f, k2, x2, c));
+  LAT(8, n / 4, P = g1_dbl(P));
+  LAT(9, n / 4, P = g1_add_aff(P, Q));
+  LAT(10, n / 4, P = g1_add(P, Rr));
+  LAT(11, n, s = fr_mul(s, sk));
+  LAT(12, n / 4, P = g1_dbl_inl(P));
+  LAT(13, n / 4, P = g1_add_aff_inl(P, Q));
+  LAT(14, n, x2 = fp2_mul_inl(x2, k2));
+  LAT(15, n / 64, _Pragma("unroll 1") for (int q = 0; q < 64; q++) b = fp_sqr(b));
+  LAT(16, n, a = fp_mul_inl(a, k));
+  LAT(17, n, a = fp_mul_inl(a, k); b = fp_mul_inl(b, k); c = fp_mul_inl(c, k));
+  LAT(18, n, a = fp_mul_call(a, k));
+  LAT(19, n, a = fp_mul_call(a, k); b = fp_mul_call(b, k); c = fp_mul_call(c, k));
+  LAT(20, n, a = fp_mul_rolled(a, k));
+  LAT(21, n, a = fp_mul_rolled(a, k); b = fp_mul_rolled(b, k); c = fp_mul_rolled(c, k));
+  LAT(22, n / 4, P = g1_dbl_call(P));
+  LAT(23, n / 4, P = g1_dbl_rolled(P));
+#undef LAT
+  if (threadIdx.x == 0)
+    for (int i = 0; i < R; i++) cyc[i] = res[i];
+  fp acc = fp_add(fp_add(a, b), fp_add(c, x2.c0));
+  acc = fp_add(acc, fp_add(f.c0.c0.c0, P.X));
+  acc.w[0] ^= s.w[0];
+  sink[threadIdx.x] = acc;
+}
+
+// Fills cycles[0..cap) with the per-operation latencies of k_latency_probe;
+// returns how many were written.
+extern "C" int32_t cubbs_bbs_gpu_latency_probe_for_test_v2(double *cycles, int32_t cap) {
+  if (!cycles || cap < 24) return -1;
+  try {
+    Runtime &rt = Runtime::get();
+    CallScope scope(rt);
+    double *d = rt.arena.alloc<double>(24);
+    fp *sink = rt.arena.alloc<fp>(32);
+    k_latency_probe<<<1, 32, 0, rt.stream>>>(d, sink, 64);  // warm-up
+    k_latency_probe<<<1, 32, 0, rt.stream>>>(d, sink, 512);
+    CUBBS_CHECK(cudaGetLastError());
+    CUBBS_CHECK(cudaMemcpyAsync(cycles, d, 24 * sizeof(double), cudaMemcpyDeviceToHost, rt.stream));
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    return 24;
+  } catch (const CudaError &) {
+    return -2;
+  }
 }
 
 // Returns the measured IMAD rate (1e12 multiply-adds per second) and the Fp

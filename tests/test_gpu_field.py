@@ -29,6 +29,15 @@ def test_fp_inv_sqrt(gpu, oracle):
         assert st == 0 and oracle.fp_mul(r, r) == s
 
 
+def test_fp_inv_vartime_matches_fermat(gpu, oracle):
+    a = rand_fp(oracle, b"vinv", 48) + [(1).to_bytes(48, "big"), (oracle.P_MOD - 1).to_bytes(48, "big"),
+                                        (2).to_bytes(48, "big"), bytes(48)]
+    fermat = gpu.fp_op_for_test(1, a, a)
+    binary = gpu.fp_op_for_test(3, a, a)
+    assert [r for _, r in binary] == [r for _, r in fermat]
+    assert binary[-1][1] == bytes(48)
+
+
 def test_g1_decode_and_mul(gpu, oracle):
     p1, gens = oracle.generators(8)
     pts = [p1] + gens
