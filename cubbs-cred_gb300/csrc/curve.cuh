@@ -100,10 +100,12 @@ DEVNI g1 g1_dbl(g1 p) { return g1_dbl_inl(p); }
 DEVNI g1 g1_dbl_aff(g1a p) { return g1_dbl_aff_inl(p); }
 DEVNI g1 g1_add_aff(g1 p, g1a q) { return g1_add_aff_inl(p, q); }
 DEVNI g1 g1_add(g1 p, g1 q) { return g1_add_inl(p, q); }
-// affine conversion with a single inversion; returns false for infinity
+// affine conversion with a single inversion; returns false for infinity.  The
+// points converted are public (proof and signature components, MSM outputs),
+// so the inverse is the variable-time one.
 DEV bool g1_to_aff(g1 p, g1a &out) {
   if (g1_is_inf(p)) return false;
-  fp t = fp_inv(fp_mul(p.ZZ, p.ZZZ));
+  fp t = fp_inv_vartime(fp_mul(p.ZZ, p.ZZZ));
   out.x = fp_mul(p.X, fp_mul(t, p.ZZZ));  // X / ZZ
   out.y = fp_mul(p.Y, fp_mul(t, p.ZZ));   // Y / ZZZ
   return true;

@@ -40,7 +40,7 @@ void launch_pk_prepare(cudaStream_t s, const uint8_t *pks96, uint32_t n, int slo
 
 // One pairing check per 16-lane team (4 teams per 64-thread block); see
 // pairing_team.cuh.  The B * xP factors of the lines are computed by lanes
-// that are idle in the preceding round.
+// that have no product of their own in the preceding round.
 __global__ void __launch_bounds__(64) k_pairing_check_team(const PairJob *jobs, uint32_t n, const line2 *lines,
                                                            uint8_t *ok) {
   __shared__ PtShared smem[64 / PT_LANES];
@@ -69,24 +69,21 @@ __global__ void __launch_bounds__(64) k_pairing_check_team(const PairJob *jobs, 
 #pragma unroll 1
   for (int i = 62; i >= 0; i--) {
     const bool bit = zabs_bit(i) != 0;
-    pt_sqr(c, PT_F, [&](int s) {  // B * xP of this step's doubling lines
-      const int p = s >> 1;
-      if (skip[p]) return;
-      const fp2 b = L[p][idx].b;
-      const fp v = fp_mul((s & 1) ? b.c1 : b.c0, c.sm->PX[p]);
-      if (s & 1) c.sm->BX[p].c1 = v;
-      else c.sm->BX[p].c0 = v;
+    pt_sqr(c, PT_F, [&](int s, fp2 &x, fp2 &y) -> fp2 * {  // B * xP of this step's doubling lines
+      if (s >= 2 || skip[s]) return nullptr;
+      x = L[s][idx].b;
+      y.c0 = c.sm->PX[s];
+      return &c.sm->BX[s];
     });
 #pragma unroll 1
     for (int p = 0; p < 2; p++) {
       if (skip[p]) continue;
       const fp2 A = L[p][idx].a;
-      pt_line(c, PT_F, A, &c.sm->BX[p], &c.sm->PY[p], [&](int s) {  // B * xP of the addition line
-        if (!bit || s >= 2) return;
-        const fp2 b = L[p][idx + 1].b;
-        const fp v = fp_mul(s ? b.c1 : b.c0, c.sm->PX[p]);
-        if (s) c.sm->BXA[p].c1 = v;
-        else c.sm->BXA[p].c0 = v;
+      pt_line(c, PT_F, A, &c.sm->BX[p], &c.sm->PY[p], [&](int s, fp2 &x, fp2 &y) -> fp2 * {
+        if (!bit || s != 0) return nullptr;  // B * xP of the addition line
+        x = L[p][idx + 1].b;
+        y.c0 = c.sm->PX[p];
+        return &c.sm->BXA[p];
       });
     }
     idx++;
@@ -95,7 +92,7 @@ __global__ void __launch_bounds__(64) k_pairing_check_team(const PairJob *jobs, 
       for (int p = 0; p < 2; p++) {
         if (skip[p]) continue;
         const fp2 A = L[p][idx].a;
-        pt_line(c, PT_F, A, &c.sm->BXA[p], &c.sm->PY[p], [](int) {});
+        pt_line(c, PT_F, A, &c.sm->BXA[p], &c.sm->PY[p], [](int, fp2 &, fp2 &) -> fp2 * { return nullptr; });
       }
       idx++;
     }

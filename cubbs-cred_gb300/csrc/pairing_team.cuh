@@ -91,27 +91,35 @@ DEVNI void pt_frob(PtCtx c, int dst, int src) {
   c.sync();
 }
 
-// S = S^2 (general Fp12 squaring, Miller loop).  Lanes 12..15 run `side`
-// (the B*xP products of the next lines) in the product round.
+// Every lane of a round selects its operands (cheap, divergent) and then all
+// lanes make the same fp2_mul call, so the products of a round run as one
+// SIMT instruction stream.  `side(s, x, y)` lets the lanes beyond the
+// operation's own products compute other Fp2 products (the B * xP factors of
+// the next lines) in the same call: it sets the operands and returns where to
+// store the product, or nullptr.
+
+// S = S^2 (general Fp12 squaring, Miller loop); side lanes 12..15.
 template <typename Side>
 DEV void pt_sqr(const PtCtx &c, int s, Side side) {
   fp2 *S = c.sm->S[s];
   const int l = c.lane;
-  if (l < 12) {
-    fp2 x, y;
-    if (l < 6) {  // ab = c0 * c1
-      pt_kara_pick(l, S[0], S[1], S[2], S[3], S[4], S[5], x, y);
-    } else {      // (c0 + c1) * (c0 + v c1),  v c1 = (xi c12, c10, c11)
-      fp2 a0 = fp2_add(S[0], S[3]), a1 = fp2_add(S[1], S[4]), a2 = fp2_add(S[2], S[5]);
-      fp2 b0 = fp2_add(S[0], fp2_mul_xi(S[5])), b1 = fp2_add(S[1], S[3]), b2 = fp2_add(S[2], S[4]);
-      pt_kara_pick(l - 6, a0, a1, a2, b0, b1, b2, x, y);
-    }
-    c.sm->Z[l] = fp2_mul(x, y);
+  fp2 x = fp2_zero(), y = fp2_zero();
+  fp2 *dst = nullptr;
+  if (l < 6) {  // ab = c0 * c1
+    pt_kara_pick(l, S[0], S[1], S[2], S[3], S[4], S[5], x, y);
+    dst = &c.sm->Z[l];
+  } else if (l < 12) {  // (c0 + c1) * (c0 + v c1),  v c1 = (xi c12, c10, c11)
+    fp2 a0 = fp2_add(S[0], S[3]), a1 = fp2_add(S[1], S[4]), a2 = fp2_add(S[2], S[5]);
+    fp2 b0 = fp2_add(S[0], fp2_mul_xi(S[5])), b1 = fp2_add(S[1], S[3]), b2 = fp2_add(S[2], S[4]);
+    pt_kara_pick(l - 6, a0, a1, a2, b0, b1, b2, x, y);
+    dst = &c.sm->Z[l];
   } else {
-    side(l - 12);
+    dst = side(l - 12, x, y);
   }
+  const fp2 z = fp2_mul(x, y);
+  if (dst) *dst = z;
   c.sync();
-  if (l < 6) c.sm->W[l] = pt_kara_assemble(l % 3, c.sm->Z + (l < 3 ? 0 : 6));  // r = ab, t = ...
+  if (l < 6) c.sm->W[l] = pt_kara_assemble(l % 3, c.sm->Z + (l < 3 ? 0 : 6));  // r = ab, t
   c.sync();
   if (l < 6) {
     const fp2 *r = c.sm->W, *t = c.sm->W + 3;
@@ -127,41 +135,41 @@ DEV void pt_sqr(const PtCtx &c, int s, Side side) {
   c.sync();
 }
 
-// S *= A + (B xP) v + yP v w  with Bx = B xP from shared memory.
-// Lanes 13..15 run `side` in the product round.
+// S *= A + (B xP) v + yP v w  with Bx = B xP from shared memory; side lanes 13..15.
 template <typename Side>
 DEV void pt_line(const PtCtx &c, int s, const fp2 &A, const fp2 *Bxp, const fp *yPp, Side side) {
   fp2 *S = c.sm->S[s];
   const int l = c.lane;
-  if (l < 13) {
-    fp2 z;
-    if (l < 5) {  // t0 = f0 * (A, Bx, 0)
-      fp2 Bx = *Bxp;
-      switch (l) {
-        case 0: z = fp2_mul(S[0], A); break;
-        case 1: z = fp2_mul(S[1], Bx); break;
-        case 2: z = fp2_mul(S[2], Bx); break;
-        case 3: z = fp2_mul(fp2_add(S[0], S[1]), fp2_add(A, Bx)); break;
-        default: z = fp2_mul(S[2], A); break;
-      }
-    } else if (l < 8) {  // t1 = f1 * yP v : products f12 yP, f10 yP, f11 yP
-      const int src[3] = {5, 3, 4};
-      z = fp2_mul_fp(S[src[l - 5]], *yPp);
-    } else {  // t2 = (f0 + f1) * (A, Bx + yP, 0)
-      fp2 B2 = *Bxp;
-      B2.c0 = fp_add(B2.c0, *yPp);
-      switch (l) {
-        case 8: z = fp2_mul(fp2_add(S[0], S[3]), A); break;
-        case 9: z = fp2_mul(fp2_add(S[1], S[4]), B2); break;
-        case 10: z = fp2_mul(fp2_add(S[2], S[5]), B2); break;
-        case 11: z = fp2_mul(fp2_add(fp2_add(S[0], S[3]), fp2_add(S[1], S[4])), fp2_add(A, B2)); break;
-        default: z = fp2_mul(fp2_add(S[2], S[5]), A); break;
-      }
+  fp2 x = fp2_zero(), y = fp2_zero();
+  fp2 *dst = l < 13 ? &c.sm->Z[l] : nullptr;
+  if (l < 5) {  // t0 = f0 * (A, Bx, 0)
+    const fp2 Bx = *Bxp;
+    switch (l) {
+      case 0: x = S[0]; y = A; break;
+      case 1: x = S[1]; y = Bx; break;
+      case 2: x = S[2]; y = Bx; break;
+      case 3: x = fp2_add(S[0], S[1]); y = fp2_add(A, Bx); break;
+      default: x = S[2]; y = A; break;
     }
-    c.sm->Z[l] = z;
+  } else if (l < 8) {  // t1 = f1 * yP v : products f12 yP, f10 yP, f11 yP
+    const int src[3] = {5, 3, 4};
+    x = S[src[l - 5]];
+    y.c0 = *yPp;
+  } else if (l < 13) {  // t2 = (f0 + f1) * (A, Bx + yP, 0)
+    fp2 B2 = *Bxp;
+    B2.c0 = fp_add(B2.c0, *yPp);
+    switch (l) {
+      case 8: x = fp2_add(S[0], S[3]); y = A; break;
+      case 9: x = fp2_add(S[1], S[4]); y = B2; break;
+      case 10: x = fp2_add(S[2], S[5]); y = B2; break;
+      case 11: x = fp2_add(fp2_add(S[0], S[3]), fp2_add(S[1], S[4])); y = fp2_add(A, B2); break;
+      default: x = fp2_add(S[2], S[5]); y = A; break;
+    }
   } else {
-    side(l - 13);
+    dst = side(l - 13, x, y);
   }
+  const fp2 z = fp2_mul(x, y);
+  if (dst) *dst = z;
   c.sync();
   if (l < 6) {
     const fp2 *Z = c.sm->Z;

@@ -55,6 +55,8 @@ void Runtime::init() {
   CUBBS_CHECK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
   CUBBS_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   CUBBS_CHECK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
   // The kernels are register heavy; give them room for local-memory spills.
   CUBBS_CHECK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
   table_w = env_int("CUBBS_BBS_TABLE_WINDOW", 8);

@@ -73,6 +73,7 @@ struct Runtime {
   std::mutex mu;
   int device = 0;
   cudaStream_t stream = nullptr, stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // stream -> stream2 -> stream
   DeviceArena arena;
   HostStaging staging;
   // generators: d_gens[0] = P1, d_gens[1] = Q1, d_gens[1 + i] = H_i
