@@ -568,7 +568,7 @@ struct OpBatch {
   size_t launches_per_run = 0;
 };
 
-size_t g_h2d_bytes = 0, g_d2h_bytes = 0;  // bytes moved by the last four-operation call
+thread_local size_t g_h2d_bytes = 0, g_d2h_bytes = 0;  // bytes moved by this thread's last four-operation call
 
 template <typename T> T *upload_to(Runtime &rt, T *d, const T *h, size_t n) {
   if (n) {
@@ -640,7 +640,7 @@ struct StageEvents {
   cudaEvent_t side[2];  // the pairing kernel on the second stream
   bool side_used = false;
 };
-StageEvents *g_stages = nullptr;
+thread_local StageEvents *g_stages = nullptr;
 void stage_mark(cudaStream_t s, const char *name) {
   if (!g_stages || g_stages->used >= 16) return;
   cudaEventRecord(g_stages->ev[g_stages->used], s);
@@ -1051,8 +1051,8 @@ extern "C" int32_t cubbs_bbs_gpu_proof_verify_batch_v2(uint32_t abi, const CuBbs
   if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     OpBatch b;
     int32_t st = plan_pverify(items, n, b);
     if (st != CUBBS_BBS_GPU_SUCCESS) return st;
@@ -1071,8 +1071,8 @@ extern "C" int32_t cubbs_bbs_gpu_verify_batch_v2(uint32_t abi, const CuBbsBbsGpu
   if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     OpBatch b;
     int32_t st = plan_verify(items, n, b);
     if (st != CUBBS_BBS_GPU_SUCCESS) return st;
@@ -1091,8 +1091,8 @@ extern "C" int32_t cubbs_bbs_gpu_sign_batch_v2(uint32_t abi, CuBbsBbsGpuSignItem
   if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     OpBatch b;
     int32_t st = plan_sign(items, n, b);
     if (st != CUBBS_BBS_GPU_SUCCESS) return st;
@@ -1125,8 +1125,8 @@ extern "C" int32_t cubbs_bbs_gpu_sign_batch_v2(uint32_t abi, CuBbsBbsGpuSignItem
 static int32_t proof_gen_impl(CuBbsBbsGpuProofGenItem *items, size_t n, const uint8_t (*seeds)[32],
                               CuBbsBbsGpuResult *results) {
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     OpBatch b;
     std::vector<uint8_t> os_seeds;
     int32_t st = plan_pgen(items, n, seeds, b, os_seeds);
@@ -1192,8 +1192,8 @@ extern "C" int32_t cubbs_bbs_gpu_bench_device_steps_v2(uint32_t abi, int32_t op,
   if (!abi_ok(abi) || !items || n == 0 || !ms_out || !launches || !results || steps <= 0 || warmup < 0)
     return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     OpBatch b;
     std::vector<uint8_t> os_seeds;
     int32_t st;
@@ -1291,8 +1291,8 @@ __global__ void k_h2s_scalars_test(const uint8_t *be, uint32_t n, fr *out) {
 extern "C" int32_t cubbs_bbs_gpu_h2s_scalars_for_test_v2(uint32_t abi, const uint8_t *be, size_t n, uint8_t *out32) {
   if (abi != CUBBS_BBS_GPU_ABI_VERSION || !be || !out32 || n == 0) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     uint8_t *d = rt.arena.alloc<uint8_t>(32 * n);
     fr *o = rt.arena.alloc<fr>(1);
     CUBBS_CHECK(cudaMemcpy(d, be, 32 * n, cudaMemcpyHostToDevice));
@@ -1333,8 +1333,8 @@ extern "C" int32_t cubbs_bbs_gpu_pairs_h2s_for_test_v2(uint32_t abi, const uint8
                                                        uint8_t *out32, uint32_t *echo) {
   if (abi != CUBBS_BBS_GPU_ABI_VERSION) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     uint8_t *d = rt.arena.alloc<uint8_t>(blob_len + 1);
     uint8_t *dm = rt.arena.alloc<uint8_t>(32 * R + 1);
     uint32_t *de = rt.arena.alloc<uint32_t>(R + 1);

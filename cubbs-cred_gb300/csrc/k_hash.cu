@@ -203,8 +203,8 @@ static int32_t flat_test_call(uint32_t abi, const uint8_t *messages, const size_
     return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     std::vector<const uint8_t *> ptrs(n);
     size_t total = 0;
     #pragma unroll 1
@@ -290,8 +290,8 @@ extern "C" int32_t cubbs_bbs_gpu_messages_to_scalar_batch_v2(uint32_t abi,
     total += lens[i];
   }
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     rt.staging.reserve(total + 16 * n + 4096);
     rt.arena.reserve(total + 64 * n + 4096);
     FlatMsgs f = stage_flat(rt, ptrs.data(), lens.data(), n);
@@ -322,6 +322,7 @@ extern "C" int32_t cubbs_bbs_gpu_messages_to_scalar_batch_v2(uint32_t abi,
 // call's scalars stay on the device for later resident calls.
 static fr *g_resident = nullptr;
 static size_t g_resident_cap = 0, g_resident_count = 0;
+static std::mutex g_resident_mu;  // one resident set per process
 
 static void be_from_raw(const uint32_t *raw, uint8_t *o) {
   for (int w = 0; w < 8; w++)
@@ -356,8 +357,9 @@ extern "C" int32_t cubbs_bbs_gpu_sign_e_from_resident_scalars_batch_v2(
     }
   }
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    std::lock_guard<std::mutex> resident_lock(g_resident_mu);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     if (!raw) {
       for (size_t i = 0; i < n; i++)
         if (items[i].message_scalar_offset + items[i].message_count > g_resident_count)

@@ -106,14 +106,9 @@ template <typename T> T *upload(Runtime &rt, const T *h, size_t n) {
 }
 
 // Host copy of the compressed generators [P1, Q1, H1, ...] for prefix detection.
-std::vector<uint8_t> &host_gens_c(Runtime &rt, int count) {
-  static std::vector<uint8_t> cache;
-  if ((int)(cache.size() / 48) < count) {
-    rt.ensure_generators(std::max(count, rt.gen_count));
-    cache.resize((size_t)rt.gen_count * 48);
-    CUBBS_CHECK(cudaMemcpy(cache.data(), rt.d_gens_c, cache.size(), cudaMemcpyDeviceToHost));
-  }
-  return cache;
+const std::vector<uint8_t> &host_gens_c(Runtime &rt, int count) {
+  rt.ensure_generators(count);
+  return rt.host_gens_c();
 }
 
 // Plan of output rows made of (a) an optional fixed-base part over a prefix of
@@ -223,7 +218,7 @@ void run_plan(Runtime &rt, Plan &pl, std::vector<uint8_t> &out48, std::vector<ui
 // Is points[0..K) == [P1, Q1, H1, ...][0..K)?
 bool is_generator_prefix(Runtime &rt, const CuBbsBbsGpuByteSlice *points, size_t K) {
   if (K == 0 || K > 16386) return false;
-  std::vector<uint8_t> &g = host_gens_c(rt, (int)K);
+  const std::vector<uint8_t> &g = host_gens_c(rt, (int)K);
   for (size_t k = 0; k < K; k++)
     if (points[k].len != 48 || std::memcmp(points[k].data, &g[48 * k], 48) != 0) return false;
   return true;
@@ -313,8 +308,8 @@ extern "C" int32_t cubbs_bbs_gpu_g1_msm_batch_v2(uint32_t abi, CuBbsBbsGpuG1MsmI
   }
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   ABI_GUARD_BEGIN
-  Runtime &rt = Runtime::get();
-  CallScope scope(rt);
+  CallScope scope;
+  Runtime &rt = scope.rt;
   Plan pl;
   pl.rows = n;
   for (size_t i = 0; i < n; i++) {
@@ -355,8 +350,8 @@ static int32_t common_points_entry(uint32_t abi, CuBbsBbsGpuG1MsmCommonPointsBat
     }
   }
   ABI_GUARD_BEGIN
-  Runtime &rt = Runtime::get();
-  CallScope scope(rt);
+  CallScope scope;
+  Runtime &rt = scope.rt;
   size_t cursor = 0;
   for (size_t g = 0; g < groups; g++) {
     auto &it = items[g];
@@ -452,8 +447,8 @@ extern "C" int32_t cubbs_bbs_gpu_g1_msm_common_points_plus_variable_batch_v2(
       if (it.points[k].len != 48 || !it.points[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   }
   ABI_GUARD_BEGIN
-  Runtime &rt = Runtime::get();
-  CallScope scope(rt);
+  CallScope scope;
+  Runtime &rt = scope.rt;
   size_t cursor = 0;
   for (size_t g = 0; g < groups; g++) {
     auto &it = items[g];
@@ -494,8 +489,8 @@ extern "C" int32_t cubbs_bbs_gpu_proof_verify_msm_pair_batch_v2(uint32_t abi, Cu
     }
   }
   ABI_GUARD_BEGIN
-  Runtime &rt = Runtime::get();
-  CallScope scope(rt);
+  CallScope scope;
+  Runtime &rt = scope.rt;
   size_t cursor = 0;
   for (size_t g = 0; g < groups; g++) {
     auto &it = items[g];
@@ -558,8 +553,8 @@ extern "C" int32_t cubbs_bbs_gpu_g1_dual_msm_same_points_lanes_batch_v2(uint32_t
         return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   }
   ABI_GUARD_BEGIN
-  Runtime &rt = Runtime::get();
-  CallScope scope(rt);
+  CallScope scope;
+  Runtime &rt = scope.rt;
   for (size_t i = 0; i < n; i++) {
     auto &it = items[i];
     // rows: lane j of lhs = row j, lane j of rhs = row lanes + j; lane j sums terms k = j (mod lanes)
@@ -625,8 +620,8 @@ extern "C" int32_t cubbs_bbs_gpu_g1_add_batch_v2(uint32_t abi, CuBbsBbsGpuG1AddI
   }
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   ABI_GUARD_BEGIN
-  Runtime &rt = Runtime::get();
-  CallScope scope(rt);
+  CallScope scope;
+  Runtime &rt = scope.rt;
   // lhs + rhs as a 2-term MSM with unit scalars
   Plan pl;
   pl.rows = n;
@@ -664,8 +659,8 @@ extern "C" int32_t cubbs_bbs_gpu_prepare_b_batch_v2(uint32_t abi, CuBbsBbsGpuPre
   }
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   ABI_GUARD_BEGIN
-  Runtime &rt = Runtime::get();
-  CallScope scope(rt);
+  CallScope scope;
+  Runtime &rt = scope.rt;
   size_t maxL = 0;
   for (size_t i = 0; i < n; i++) maxL = std::max(maxL, items[i].message_count);
   rt.ensure_table((int)maxL + 2);
@@ -731,8 +726,8 @@ extern "C" int32_t cubbs_bbs_gpu_proof_gen_t2_prepare_batch_v2(uint32_t abi, CuB
   }
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   ABI_GUARD_BEGIN
-  Runtime &rt = Runtime::get();
-  CallScope scope(rt);
+  CallScope scope;
+  Runtime &rt = scope.rt;
   // rows per item: d = B s0 ; abar = A s1 ; bbar = B s2 - A s3 ; t1 = A s4 + B s5
   Plan pl;
   pl.rows = 4 * n;
@@ -792,8 +787,8 @@ extern "C" int32_t cubbs_bbs_gpu_pairing_eq_batch_v2(uint32_t abi, const CuBbsBb
   }
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   ABI_GUARD_BEGIN
-  Runtime &rt = Runtime::get();
-  CallScope scope(rt);
+  CallScope scope;
+  Runtime &rt = scope.rt;
   std::vector<const uint8_t *> g2(2 * n);
   for (size_t i = 0; i < n; i++) {
     g2[2 * i] = items[i].lhs_g2.data;
@@ -867,8 +862,8 @@ extern "C" int32_t cubbs_bbs_gpu_pairing_eq_aggregate_v2(uint32_t abi, const CuB
     return CUBBS_BBS_GPU_SUCCESS;
   }
   ABI_GUARD_BEGIN
-  Runtime &rt = Runtime::get();
-  CallScope scope(rt);
+  CallScope scope;
+  Runtime &rt = scope.rt;
   // group G1 terms by G2 point: for lhs pair, (coef, lhs_g1); for rhs pair, (coef, -rhs_g1)
   std::vector<std::string> keys;
   std::unordered_map<std::string, size_t> key_idx;
@@ -948,6 +943,71 @@ extern "C" int32_t cubbs_bbs_gpu_pairing_eq_aggregate_v2(uint32_t abi, const CuB
   CUBBS_CHECK(cudaMemcpyAsync(&hok, dok, 1, cudaMemcpyDeviceToHost, rt.stream));
   CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
   *result = {CUBBS_BBS_GPU_SUCCESS, hok, 0};
+  return CUBBS_BBS_GPU_SUCCESS;
+  ABI_GUARD_END
+}
+
+// ----------------------------------------------------------------------------- fixed-base MSM autotuner
+// Batched fixed-base MSMs over the first `terms` resident generators
+// [P1, Q1, H1, ...]: rows x terms canonical big-endian scalars.  For every
+// window width w in [w_lo, w_hi] the table is rebuilt with width w and the
+// MSM kernel is timed with CUDA events over `steps` launches (256 MiB L2
+// flush before each); ms_per_w[w - w_lo] gets the mean, and the width with
+// the lowest time stays as the process's table width (*best_w).  The
+// reference sweeps its comb width by term count (prepare_b_msm.cu:315-329).
+extern "C" int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi, const uint8_t *scalars_be, size_t rows,
+                                                       size_t terms, int32_t w_lo, int32_t w_hi, int32_t steps,
+                                                       float *ms_per_w, int32_t *best_w) {
+  if (!abi_ok(abi) || !scalars_be || rows == 0 || terms == 0 || terms > 1024 || w_lo < 4 || w_hi > 13 ||
+      w_lo > w_hi || steps <= 0 || !ms_per_w || !best_w)
+    return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  ABI_GUARD_BEGIN
+  CallScope scope;
+  Runtime &rt = scope.rt;
+  cudaStream_t s = rt.stream;
+  const size_t n = rows * terms;
+  rt.arena.reserve(n * (32 + sizeof(fr) + 4) + rows * (sizeof(g1) + 4) + 65536);
+  rt.staging.reserve(n * 32 + rows * 4 + 65536);
+  uint8_t *dbe = upload(rt, scalars_be, n * 32);
+  fr *sc = rt.arena.alloc<fr>(n);
+  int32_t *st = rt.arena.alloc<int32_t>(n);
+  k_parse_scalars<<<blocks_for(n, 128), 128, 0, s>>>(dbe, (uint32_t)n, sc, st);
+  std::vector<uint32_t> nt(rows, (uint32_t)terms);
+  uint32_t *dnt = upload(rt, nt.data(), rows);
+  g1 *out = rt.arena.alloc<g1>(rows);
+  static uint8_t *flush = nullptr;
+  const size_t FLUSH = (size_t)256 << 20;
+  if (!flush) CUBBS_CHECK(cudaMalloc(&flush, FLUSH));
+  cudaEvent_t e0, e1;
+  CUBBS_CHECK(cudaEventCreate(&e0));
+  CUBBS_CHECK(cudaEventCreate(&e1));
+  float best = 0;
+  int bw = w_lo;
+  for (int w = w_lo; w <= w_hi; w++) {
+    rt.set_table_window(w, (int)terms);
+    launch_fixed_msm(s, rt.table, sc, (uint32_t)terms, dnt, (uint32_t)rows, out);  // warm-up
+    float total = 0;
+    for (int k = 0; k < steps; k++) {
+      CUBBS_CHECK(cudaMemsetAsync(flush, k & 0xff, FLUSH, s));
+      CUBBS_CHECK(cudaEventRecord(e0, s));
+      launch_fixed_msm(s, rt.table, sc, (uint32_t)terms, dnt, (uint32_t)rows, out);
+      CUBBS_CHECK(cudaEventRecord(e1, s));
+      CUBBS_CHECK(cudaEventSynchronize(e1));
+      float ms = 0;
+      CUBBS_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+      total += ms;
+    }
+    ms_per_w[w - w_lo] = total / steps;
+    if (w == w_lo || ms_per_w[w - w_lo] < best) {
+      best = ms_per_w[w - w_lo];
+      bw = w;
+    }
+  }
+  CUBBS_CHECK(cudaGetLastError());
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  rt.set_table_window(bw, (int)terms);
+  *best_w = bw;
   return CUBBS_BBS_GPU_SUCCESS;
   ABI_GUARD_END
 }

@@ -122,8 +122,8 @@ static int32_t run_test(int kind, int op, const uint8_t *a, const uint8_t *b, si
                         int32_t *status) {
   if (n == 0) return 0;
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     size_t asz = kind == 0 ? 48 : 48, bsz = kind == 0 ? 48 : 32;
     uint8_t *da = rt.arena.alloc<uint8_t>(asz * n), *db = rt.arena.alloc<uint8_t>(bsz * n);
     uint8_t *d1 = rt.arena.alloc<uint8_t>(96 * n), *d2 = rt.arena.alloc<uint8_t>(48 * (13 + 64) * n);
@@ -307,8 +307,8 @@ __global__ void __launch_bounds__(32) k_latency_probe(double *cyc, fp *sink, uin
 extern "C" int32_t cubbs_bbs_gpu_latency_probe_for_test_v2(double *cycles, int32_t cap) {
   if (!cycles || cap < 24) return -1;
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     double *d = rt.arena.alloc<double>(24);
     fp *sink = rt.arena.alloc<fp>(32);
     k_latency_probe<<<1, 32, 0, rt.stream>>>(d, sink, 64);  // warm-up
@@ -327,8 +327,8 @@ extern "C" int32_t cubbs_bbs_gpu_latency_probe_for_test_v2(double *cycles, int32
 extern "C" int32_t cubbs_bbs_gpu_int_peaks_v2(double *tera_imad, double *giga_fpmul) {
   if (!tera_imad || !giga_fpmul) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     uint32_t *o = rt.arena.alloc<uint32_t>(4);
     fp *of = rt.arena.alloc<fp>(1);
     int blocks = rt.sm_count * 8;

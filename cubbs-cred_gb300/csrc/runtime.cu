@@ -34,9 +34,9 @@ void HostStaging::reserve(size_t bytes) {
   used = 0;
 }
 
-Runtime &Runtime::get() {
-  static Runtime rt;
-  return rt;
+SharedState &SharedState::get() {
+  static SharedState s;
+  return s;
 }
 
 static int env_int(const char *name, int dflt) {
@@ -45,7 +45,8 @@ static int env_int(const char *name, int dflt) {
   return std::atoi(v);
 }
 
-void Runtime::init() {
+void SharedState::init() {
+  std::lock_guard<std::mutex> g(init_mu);
   if (initialised) return;
   int ndev = 0;
   CUBBS_CHECK(cudaGetDeviceCount(&ndev));
@@ -53,30 +54,27 @@ void Runtime::init() {
   device = env_int("CUBBS_BBS_DEVICE", 0);
   CUBBS_CHECK(cudaSetDevice(device));
   CUBBS_CHECK(cudaDeviceGetAttribute(&sm_count, cudaDevAttrMultiProcessorCount, device));
-  CUBBS_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
-  CUBBS_CHECK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
-  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
-  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+  CUBBS_CHECK(cudaStreamCreateWithFlags(&prep, cudaStreamNonBlocking));
   // The kernels are register heavy; give them room for local-memory spills.
   CUBBS_CHECK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
   table_w = env_int("CUBBS_BBS_TABLE_WINDOW", 8);
   if (table_w < 4 || table_w > 16) table_w = 8;
+  workspaces = env_int("CUBBS_BBS_WORKSPACES", 4);
+  if (workspaces < 1 || workspaces > 64) workspaces = 4;
   line_capacity = 2 + 1024;
   CUBBS_CHECK(cudaMalloc(&d_lines, (size_t)line_capacity * MILLER_LINES * sizeof(line2)));
   CUBBS_CHECK(cudaMalloc(&d_pk_aff, (size_t)line_capacity * sizeof(g2a)));
-  launch_p2_lines(stream, d_lines);
+  launch_p2_lines(prep, d_lines);
   CUBBS_CHECK(cudaGetLastError());
-  CUBBS_CHECK(cudaStreamSynchronize(stream));
+  CUBBS_CHECK(cudaStreamSynchronize(prep));
   line_used = 2;
   slot_info.assign(2, PkSlot{DEC_OK});
-  arena.reserve((size_t)256 << 20);
-  staging.reserve((size_t)64 << 20);
   initialised = true;
 }
 
 // Build generators up to d_gens[count) on the device: P1 is decoded from its
 // published encoding; Q1, H1, ... come from the seed chain + hash_to_curve.
-void Runtime::ensure_generators(int count) {
+void SharedState::grow_generators(int count) {
   if (count <= gen_count) return;
   int ncap = gen_capacity ? gen_capacity : 256;
   while (ncap < count) ncap *= 2;
@@ -86,9 +84,9 @@ void Runtime::ensure_generators(int count) {
     CUBBS_CHECK(cudaMalloc(&ng, (size_t)ncap * sizeof(g1a)));
     CUBBS_CHECK(cudaMalloc(&nc, (size_t)ncap * 48 + 48));
     if (gen_count) {
-      CUBBS_CHECK(cudaMemcpyAsync(ng, d_gens, (size_t)gen_count * sizeof(g1a), cudaMemcpyDeviceToDevice, stream));
-      CUBBS_CHECK(cudaMemcpyAsync(nc, d_gens_c, (size_t)gen_count * 48 + 48, cudaMemcpyDeviceToDevice, stream));
-      CUBBS_CHECK(cudaStreamSynchronize(stream));
+      CUBBS_CHECK(cudaDeviceSynchronize());  // no call may still read the old arrays
+      CUBBS_CHECK(cudaMemcpy(ng, d_gens, (size_t)gen_count * sizeof(g1a), cudaMemcpyDeviceToDevice));
+      CUBBS_CHECK(cudaMemcpy(nc, d_gens_c, (size_t)gen_count * 48 + 48, cudaMemcpyDeviceToDevice));
       cudaFree(d_gens);
       cudaFree(d_gens_c);
     }
@@ -99,29 +97,31 @@ void Runtime::ensure_generators(int count) {
   static uint8_t *d_seed_state = nullptr;
   if (!d_seed_state) CUBBS_CHECK(cudaMalloc(&d_seed_state, 64));
   if (gen_count == 0) {
-    launch_decode_p1(stream, d_gens, d_gens_c);
+    launch_decode_p1(prep, d_gens, d_gens_c);
     gen_count = 1;
   }
   int first = gen_count;  // 1-based generator number == d_gens index
   int n = count - gen_count;
   uint8_t *seeds = nullptr;
   CUBBS_CHECK(cudaMalloc(&seeds, (size_t)n * 48));
-  launch_make_generator_seeds(stream, first, n, d_seed_state, seeds);
-  launch_hash_generators(stream, first, n, seeds, d_gens, d_gens_c);
+  launch_make_generator_seeds(prep, first, n, d_seed_state, seeds);
+  launch_hash_generators(prep, first, n, seeds, d_gens, d_gens_c);
   CUBBS_CHECK(cudaGetLastError());
-  CUBBS_CHECK(cudaStreamSynchronize(stream));
+  CUBBS_CHECK(cudaStreamSynchronize(prep));
   cudaFree(seeds);
   gen_count = count;
+  h_gens_c.resize((size_t)gen_count * 48);
+  CUBBS_CHECK(cudaMemcpy(h_gens_c.data(), d_gens_c, h_gens_c.size(), cudaMemcpyDeviceToHost));
 }
 
 // Fixed-base window table over d_gens[0..gens).  Rebuilt (all generators)
 // when it must grow; built in generator chunks to bound the scratch.
-void Runtime::ensure_table(int gens) {
+void SharedState::grow_table(int gens) {
   if (table.entries && table.gens >= gens && table.w == table_w) return;
   int want = 1;
   while (want < gens) want *= 2;
   if (want < 64) want = 64;
-  ensure_generators(want);
+  grow_generators(want);
   FixedTable t;
   t.w = table_w;
   t.nwin = 255 / t.w + 1;
@@ -142,70 +142,177 @@ void Runtime::ensure_table(int gens) {
   for (int g0 = 0; g0 < want; g0 += chunk) {
     int g1n = std::min(want, g0 + chunk);
     // the kernel indexes scratch by (g - g0) * nwin + k
-    launch_build_table(stream, d_gens, g0, g1n, t, scratch, prod);
+    launch_build_table(prep, d_gens, g0, g1n, t, scratch, prod);
     CUBBS_CHECK(cudaGetLastError());
-    CUBBS_CHECK(cudaStreamSynchronize(stream));
+    CUBBS_CHECK(cudaStreamSynchronize(prep));
   }
   cudaFree(scratch);
   cudaFree(prod);
-  if (table.entries) cudaFree(table.entries);
+  if (table.entries) {
+    CUBBS_CHECK(cudaDeviceSynchronize());
+    cudaFree(table.entries);
+  }
   table = t;
+}
+
+// Decode, check and line-precompute public keys not seen before.
+void SharedState::add_pks(const std::vector<std::string> &keys) {
+  std::vector<std::string> fresh;
+  for (const auto &k : keys)
+    if (!pk_slots.count(k)) fresh.push_back(k);
+  if (fresh.empty()) return;
+  if (line_used + (int)fresh.size() > line_capacity) {
+    int ncap = line_capacity;
+    while (ncap < line_used + (int)fresh.size()) ncap *= 2;
+    line2 *nl = nullptr;
+    g2a *na = nullptr;
+    CUBBS_CHECK(cudaMalloc(&nl, (size_t)ncap * MILLER_LINES * sizeof(line2)));
+    CUBBS_CHECK(cudaMalloc(&na, (size_t)ncap * sizeof(g2a)));
+    CUBBS_CHECK(cudaDeviceSynchronize());
+    CUBBS_CHECK(cudaMemcpy(nl, d_lines, (size_t)line_used * MILLER_LINES * sizeof(line2), cudaMemcpyDeviceToDevice));
+    CUBBS_CHECK(cudaMemcpy(na, d_pk_aff, (size_t)line_used * sizeof(g2a), cudaMemcpyDeviceToDevice));
+    cudaFree(d_lines);
+    cudaFree(d_pk_aff);
+    d_lines = nl;
+    d_pk_aff = na;
+    line_capacity = ncap;
+  }
+  std::vector<uint8_t> h(96 * fresh.size());
+  for (size_t i = 0; i < fresh.size(); i++) std::memcpy(h.data() + 96 * i, fresh[i].data(), 96);
+  uint8_t *d = nullptr;
+  int32_t *dst = nullptr;
+  CUBBS_CHECK(cudaMalloc(&d, h.size()));
+  CUBBS_CHECK(cudaMalloc(&dst, 4 * fresh.size()));
+  CUBBS_CHECK(cudaMemcpyAsync(d, h.data(), h.size(), cudaMemcpyHostToDevice, prep));
+  launch_pk_prepare(prep, d, (uint32_t)fresh.size(), line_used, d_pk_aff, d_lines, dst);
+  CUBBS_CHECK(cudaGetLastError());
+  std::vector<int32_t> st(fresh.size());
+  CUBBS_CHECK(cudaMemcpyAsync(st.data(), dst, 4 * fresh.size(), cudaMemcpyDeviceToHost, prep));
+  CUBBS_CHECK(cudaStreamSynchronize(prep));
+  cudaFree(d);
+  cudaFree(dst);
+  for (size_t i = 0; i < fresh.size(); i++) {
+    pk_slots[fresh[i]] = line_used + (int)i;
+    slot_info.push_back(PkSlot{st[i]});
+  }
+  line_used += (int)fresh.size();
+}
+
+Runtime::Runtime(SharedState &s)
+    : sh(s), device(s.device), sm_count(s.sm_count), gen_count(s.gen_count), d_gens(s.d_gens),
+      d_gens_c(s.d_gens_c), table(s.table), table_w(s.table_w), d_lines(s.d_lines) {
+  CUBBS_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+  CUBBS_CHECK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
+  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
+  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+  arena.reserve((size_t)256 << 20);
+  staging.reserve((size_t)64 << 20);
+}
+
+// Growth from inside a call: drop the shared hold, grow under the exclusive
+// lock (the grow functions re-check), take the shared hold again.
+void Runtime::ensure_generators(int count) {
+  if (count <= sh.gen_count) return;
+  lock->unlock();
+  {
+    std::unique_lock<std::shared_mutex> ex(sh.mu);
+    sh.grow_generators(count);
+  }
+  lock->lock();
+}
+
+void Runtime::ensure_table(int gens) {
+  if (sh.table.entries && sh.table.gens >= gens && sh.table.w == sh.table_w) return;
+  lock->unlock();
+  {
+    std::unique_lock<std::shared_mutex> ex(sh.mu);
+    sh.grow_table(gens);
+  }
+  lock->lock();
+}
+
+void Runtime::set_table_window(int w, int gens) {
+  lock->unlock();
+  {
+    std::unique_lock<std::shared_mutex> ex(sh.mu);
+    sh.table_w = w;
+    sh.grow_table(std::max(gens, sh.table.gens));
+  }
+  lock->lock();
 }
 
 void Runtime::resolve_pks(const std::vector<const uint8_t *> &pk_ptrs, std::vector<int> &slots,
                           std::vector<int> &status) {
+  std::vector<std::string> keys(pk_ptrs.size());
+  bool missing = false;
+  for (size_t i = 0; i < pk_ptrs.size(); i++) {
+    keys[i].assign(reinterpret_cast<const char *>(pk_ptrs[i]), 96);
+    if (!missing && !sh.pk_slots.count(keys[i])) missing = true;
+  }
+  if (missing) {
+    lock->unlock();
+    {
+      std::unique_lock<std::shared_mutex> ex(sh.mu);
+      sh.add_pks(keys);
+    }
+    lock->lock();
+  }
   slots.assign(pk_ptrs.size(), -1);
   status.assign(pk_ptrs.size(), DEC_BAD);
-  std::vector<std::string> fresh;
-  std::unordered_map<std::string, int> fresh_idx;
-  for (size_t i = 0; i < pk_ptrs.size(); i++) {
-    std::string key(reinterpret_cast<const char *>(pk_ptrs[i]), 96);
-    if (pk_slots.count(key) || fresh_idx.count(key)) continue;
-    fresh_idx[key] = (int)fresh.size();
-    fresh.push_back(key);
-  }
-  if (!fresh.empty()) {
-    if (line_used + (int)fresh.size() > line_capacity) {
-      int ncap = line_capacity;
-      while (ncap < line_used + (int)fresh.size()) ncap *= 2;
-      line2 *nl = nullptr;
-      g2a *na = nullptr;
-      CUBBS_CHECK(cudaMalloc(&nl, (size_t)ncap * MILLER_LINES * sizeof(line2)));
-      CUBBS_CHECK(cudaMalloc(&na, (size_t)ncap * sizeof(g2a)));
-      CUBBS_CHECK(cudaMemcpy(nl, d_lines, (size_t)line_used * MILLER_LINES * sizeof(line2), cudaMemcpyDeviceToDevice));
-      CUBBS_CHECK(cudaMemcpy(na, d_pk_aff, (size_t)line_used * sizeof(g2a), cudaMemcpyDeviceToDevice));
-      cudaFree(d_lines);
-      cudaFree(d_pk_aff);
-      d_lines = nl;
-      d_pk_aff = na;
-      line_capacity = ncap;
-    }
-    std::vector<uint8_t> h(96 * fresh.size());
-    for (size_t i = 0; i < fresh.size(); i++) std::memcpy(h.data() + 96 * i, fresh[i].data(), 96);
-    uint8_t *d = nullptr;
-    int32_t *dst = nullptr;
-    CUBBS_CHECK(cudaMalloc(&d, h.size()));
-    CUBBS_CHECK(cudaMalloc(&dst, 4 * fresh.size()));
-    CUBBS_CHECK(cudaMemcpyAsync(d, h.data(), h.size(), cudaMemcpyHostToDevice, stream));
-    launch_pk_prepare(stream, d, (uint32_t)fresh.size(), line_used, d_pk_aff, d_lines, dst);
-    CUBBS_CHECK(cudaGetLastError());
-    std::vector<int32_t> st(fresh.size());
-    CUBBS_CHECK(cudaMemcpyAsync(st.data(), dst, 4 * fresh.size(), cudaMemcpyDeviceToHost, stream));
-    CUBBS_CHECK(cudaStreamSynchronize(stream));
-    cudaFree(d);
-    cudaFree(dst);
-    for (size_t i = 0; i < fresh.size(); i++) {
-      pk_slots[fresh[i]] = line_used + (int)i;
-      slot_info.push_back(PkSlot{st[i]});
-    }
-    line_used += (int)fresh.size();
-  }
-  for (size_t i = 0; i < pk_ptrs.size(); i++) {
-    std::string key(reinterpret_cast<const char *>(pk_ptrs[i]), 96);
-    int s = pk_slots[key];
+  for (size_t i = 0; i < keys.size(); i++) {
+    int s = sh.pk_slots.at(keys[i]);
     slots[i] = s;
-    status[i] = slot_info[s].status;
+    status[i] = sh.slot_info[s].status;
   }
+}
+
+// ---------------------------------------------------------------- workspace pool
+namespace {
+std::mutex g_pool_mu;
+std::condition_variable g_pool_cv;
+std::vector<std::unique_ptr<Runtime>> g_pool;
+std::vector<bool> g_busy;
+
+Runtime &acquire_workspace() {
+  SharedState &sh = SharedState::get();
+  sh.init();
+  CUBBS_CHECK(cudaSetDevice(sh.device));
+  std::unique_lock<std::mutex> lk(g_pool_mu);
+  for (;;) {
+    for (size_t i = 0; i < g_pool.size(); i++)
+      if (!g_busy[i]) {
+        g_busy[i] = true;
+        return *g_pool[i];
+      }
+    if ((int)g_pool.size() < sh.workspaces) {
+      g_pool.emplace_back(new Runtime(sh));
+      g_busy.push_back(true);
+      return *g_pool.back();
+    }
+    g_pool_cv.wait(lk);
+  }
+}
+
+void release_workspace(Runtime &rt) {
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    for (size_t i = 0; i < g_pool.size(); i++)
+      if (g_pool[i].get() == &rt) g_busy[i] = false;
+  }
+  g_pool_cv.notify_one();
+}
+}  // namespace
+
+CallScope::CallScope() : rt(acquire_workspace()), lock(rt.sh.mu) {
+  rt.lock = &lock;
+  rt.arena.reset();
+  rt.staging.reset();
+}
+
+CallScope::~CallScope() {
+  rt.lock = nullptr;
+  lock.unlock();
+  release_workspace(rt);
 }
 
 }  // namespace cubbs
@@ -221,8 +328,8 @@ extern "C" int32_t cubbs_bbs_gpu_backend_info_v2(uint32_t abi, CuBbsBbsGpuBacken
   info->backend_kind = CUBBS_BBS_GPU_BACKEND_KIND_UNKNOWN;
   info->hardware_acceleration = 0;
   try {
-    Runtime &rt = Runtime::get();
-    CallScope scope(rt);
+    CallScope scope;
+    Runtime &rt = scope.rt;
     uint32_t *d = rt.arena.alloc<uint32_t>(1);
     k_canary<<<1, 1, 0, rt.stream>>>(d);
     CUBBS_CHECK(cudaGetLastError());

@@ -5,7 +5,10 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <condition_variable>
+#include <memory>
 #include <mutex>
+#include <shared_mutex>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -69,18 +72,24 @@ struct PkSlot {
   int status = DEC_BAD;  // DEC_OK / DEC_INF / DEC_BAD
 };
 
-struct Runtime {
-  std::mutex mu;
+// Process-wide prepared state shared by every call: generators, the
+// fixed-base window table and the Miller lines of -P2, P2 and every public
+// key seen.  Calls hold `mu` shared while their kernels may read the state;
+// growing it (more generators, a wider table, new keys) takes `mu` exclusive,
+// so nothing is reallocated under a running call.
+struct SharedState {
+  std::shared_mutex mu;
+  std::mutex init_mu;
+  bool initialised = false;
   int device = 0;
-  cudaStream_t stream = nullptr, stream2 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // stream -> stream2 -> stream
-  DeviceArena arena;
-  HostStaging staging;
+  int sm_count = 0;
+  cudaStream_t prep = nullptr;  // stream that builds prepared state
   // generators: d_gens[0] = P1, d_gens[1] = Q1, d_gens[1 + i] = H_i
-  int gen_count = 0;      // entries of d_gens built (P1 included)
+  int gen_count = 0;            // entries of d_gens built (P1 included)
   int gen_capacity = 0;
   g1a *d_gens = nullptr;
   uint8_t *d_gens_c = nullptr;  // compressed, same indexing as d_gens
+  std::vector<uint8_t> h_gens_c;  // host copy of d_gens_c[0..gen_count)
   FixedTable table;
   int table_w = 8;
   // Miller lines: slot 0 = -P2, slot 1 = P2, slots >= 2 = public keys
@@ -89,28 +98,57 @@ struct Runtime {
   int line_capacity = 0, line_used = 0;
   std::unordered_map<std::string, int> pk_slots;
   std::vector<PkSlot> slot_info;
-  bool initialised = false;
-  int sm_count = 0;
+  int workspaces = 4;           // concurrent calls (CUBBS_BBS_WORKSPACES)
 
-  static Runtime &get();
-  void init();                             // device, streams, -P2/P2 lines
-  void ensure_generators(int count);       // d_gens[0..count) (P1 + count-1 generators)
-  void ensure_table(int gens);             // fixed-base table covering d_gens[0..gens)
+  static SharedState &get();
+  void init();                              // device, prep stream, -P2/P2 lines
+  // the following run with mu held exclusively
+  void grow_generators(int count);
+  void grow_table(int gens);
+  void add_pks(const std::vector<std::string> &fresh);
+};
+
+// One call's workspace: arena, pinned staging, two streams and the events
+// that fork and join them.  Workspaces come from a pool (CallScope), so calls
+// from several host threads run concurrently on the device.  The prepared
+// state is reached through the reference members below.
+struct Runtime {
+  SharedState &sh;
+  int &device;
+  int &sm_count;
+  int &gen_count;
+  g1a *&d_gens;
+  uint8_t *&d_gens_c;
+  FixedTable &table;
+  int &table_w;
+  line2 *&d_lines;
+  cudaStream_t stream = nullptr, stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // stream -> stream2 -> stream
+  DeviceArena arena;
+  HostStaging staging;
+  std::shared_lock<std::shared_mutex> *lock = nullptr;  // the running call's shared hold
+
+  explicit Runtime(SharedState &s);
+  void ensure_generators(int count);  // d_gens[0..count) (P1 + count-1 generators)
+  void ensure_table(int gens);        // fixed-base table covering d_gens[0..gens)
+  void set_table_window(int w, int gens);  // rebuild the table with window width w
   // Resolve public keys to line slots (decoding + subgroup check + lines on the
   // device for new keys).  pk_ptrs[i] -> slot index; status per key.
   void resolve_pks(const std::vector<const uint8_t *> &pk_ptrs, std::vector<int> &slots,
                    std::vector<int> &status);
+  const std::vector<uint8_t> &host_gens_c() const { return sh.h_gens_c; }
 };
 
-// Lock + reset helper for ABI calls.
+// Takes a free workspace from the pool (waiting while all are busy), makes the
+// device current on the calling thread, holds the prepared state shared and
+// resets the workspace's arena and staging.  Released on destruction.
 struct CallScope {
   Runtime &rt;
-  std::lock_guard<std::mutex> lock;
-  explicit CallScope(Runtime &r) : rt(r), lock(r.mu) {
-    rt.init();
-    rt.arena.reset();
-    rt.staging.reset();
-  }
+  std::shared_lock<std::shared_mutex> lock;
+  CallScope();
+  ~CallScope();
+  CallScope(const CallScope &) = delete;
+  CallScope &operator=(const CallScope &) = delete;
 };
 
 inline unsigned blocks_for(size_t n, unsigned tpb) { return (unsigned)((n + tpb - 1) / tpb); }
