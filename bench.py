@@ -153,6 +153,104 @@ def cpu_oracle_proof_verify(items, seconds_budget, threads):
     return sample / dt, sample, dt
 
 
+def fixed_msm_section(pkg, rank):
+    """C2: 4096 independent 12-term fixed-base MSMs (bases P1, Q1, H1..H10, scalars
+    uniform mod r).  The autotuner rebuilds the resident table for window widths
+    4..12 and keeps the fastest; e2e goes through the common-points ABI call."""
+    rows, terms = 4096, 12
+    seed = b"cubbs-bench-c2-%d" % rank
+    scal = [(int.from_bytes(drbg(seed, b"s", i, 48), "big") % R_MOD).to_bytes(32, "big") for i in range(rows * terms)]
+    ms_w, best_w = pkg.fixed_msm_autotune(b"".join(scal), rows, terms, 4, 12, steps=3)
+    best_ms = ms_w[best_w - 4]
+    g = json.loads((ROOT / "tests" / "golden" / "cfrg_bls12381_sha256.json").read_text())["generators"]
+    gens = [bytes.fromhex(x) for x in [g["P1"], g["Q1"]] + g["MsgGenerators"]][:terms]
+    call = pkg.prepared_common_points_call(gens, [scal[r * terms:(r + 1) * terms] for r in range(rows)])
+    for _ in range(3):
+        call()
+    e2e = []
+    for _ in range(5):
+        t0 = time.perf_counter()
+        out = call()
+        e2e.append(time.perf_counter() - t0)
+    assert all(c == 0 for c, _, _ in out)
+    return {"workload": "4096 fixed-base G1 MSMs x 12 terms over [P1, Q1, H1..H10], affine out",
+            "msms_per_s": round(rows / (best_ms / 1e3), 1), "kernel_ms": round(best_ms, 4),
+            "window_sweep_ms": {str(w): round(ms, 4) for w, ms in zip(range(4, 13), ms_w)},
+            "autotuned_window": best_w,
+            "e2e_msms_per_s": round(rows / statistics.mean(e2e), 1)}
+
+
+def serving_section(pkg, rank):
+    """C5: Poisson arrivals of a 40/40/10/10 Sign/Verify/ProofGen/ProofVerify mix,
+    L ~ U{5,10,20,50,100,200}, disclosure ~ U[0.1, 0.9], 256 keypairs with their
+    public-key lines device-resident; p50/p99 latency and ops/s of the serving queue
+    (continuous batching) against plain fixed-size batches (256 requests, 2 ms)."""
+    import random
+    keys = json.loads((ROOT / "tests" / "golden" / "keypairs256.json").read_text())
+    keys = [(bytes.fromhex(k["sk"]), bytes.fromhex(k["pk"])) for k in keys]
+    rng = random.Random(1000 + rank)
+    seed = b"cubbs-bench-c5-%d" % rank
+    P = 2048
+    plan = []
+    for i in range(P):
+        u = rng.random()
+        op = pkg.OP_SIGN if u < 0.4 else pkg.OP_VERIFY if u < 0.8 else pkg.OP_PROOF_GEN if u < 0.9 else pkg.OP_PROOF_VERIFY
+        L = rng.choice((5, 10, 20, 50, 100, 200))
+        f = rng.uniform(0.1, 0.9)
+        plan.append((op, L, max(1, round(f * L)), rng.randrange(256)))
+    # signatures for everything that needs one, then proofs (this library, untimed)
+    base = []
+    for i, (op, L, R, kidx) in enumerate(plan):
+        msgs = [drbg(seed, b"m%d" % i, j, 64) for j in range(L)]
+        order = sorted(range(L), key=lambda j: drbg(seed, b"d%d" % i, j, 8))
+        base.append({"msgs": msgs, "hdr": drbg(seed, b"h", i, 64), "ph": drbg(seed, b"p", i, 64),
+                     "di": sorted(order[:R]), "seed": drbg(seed, b"b", i, 32), "sk": keys[kidx][0],
+                     "pk": keys[kidx][1]})
+    need = [i for i, (op, *_ ) in enumerate(plan) if op != pkg.OP_SIGN]
+    sigs = pkg.sign_batch([(base[i]["sk"], base[i]["pk"], base[i]["hdr"], base[i]["msgs"]) for i in need])
+    sig_of = {i: s for i, (_, s) in zip(need, sigs)}
+    pv = [i for i, (op, *_ ) in enumerate(plan) if op == pkg.OP_PROOF_VERIFY]
+    proofs = pkg.proof_gen_batch([(base[i]["pk"], sig_of[i], base[i]["hdr"], base[i]["ph"], base[i]["msgs"],
+                                   base[i]["di"]) for i in pv], seeds=[base[i]["seed"] for i in pv])
+    proof_of = {i: p for i, (_, p) in zip(pv, proofs)}
+    pool = []
+    for i, (op, L, R, _) in enumerate(plan):
+        b = base[i]
+        if op == pkg.OP_SIGN:
+            pool.append((op, (b["sk"], b["pk"], b["hdr"], b["msgs"]), None))
+        elif op == pkg.OP_VERIFY:
+            pool.append((op, (b["pk"], sig_of[i], b["hdr"], b["msgs"]), None))
+        elif op == pkg.OP_PROOF_GEN:
+            pool.append((op, (b["pk"], sig_of[i], b["hdr"], b["ph"], b["msgs"], b["di"]), b["seed"]))
+        else:
+            pool.append((op, (b["pk"], proof_of[i], b["hdr"], b["ph"], [b["msgs"][j] for j in b["di"]], b["di"], L),
+                         None))
+    # warm the prepared state (256 keys' lines, generator tables) untimed
+    res, _, _ = pkg.serve_replay(pool, [(i, 0) for i in range(P)], mode=pkg.SERVE_QUEUE)
+    assert all(c == 0 for c, _, _ in res)
+    assert all(v == 1 for (op, _, _), (c, v, _) in zip(pool, res) if op in (pkg.OP_VERIFY, pkg.OP_PROOF_VERIFY))
+    out = []
+    for rate in (5000, 20000, 50000, 100000, 200000):
+        count = max(2000, min(40000, int(rate * 0.4)))
+        t, schedule = 0.0, []
+        for _ in range(count):
+            t += rng.expovariate(rate)
+            schedule.append((rng.randrange(P), int(t * 1e9)))
+        row = {"rate_req_s": rate, "requests": count}
+        for name, mode in (("served", pkg.SERVE_QUEUE), ("plain", pkg.SERVE_PLAIN)):
+            res, lat, wall = pkg.serve_replay(pool, schedule, mode=mode, plain_batch=256, plain_timeout_us=2000)
+            assert all(c == 0 for c, _, _ in res)
+            lat_ms = sorted(x / 1e6 for x in lat)
+            row[name] = {"p50_ms": round(lat_ms[len(lat_ms) // 2], 3),
+                         "p99_ms": round(lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))], 3),
+                         "ops_per_s": round(count / wall, 1)}
+        out.append(row)
+    return {"workload": "Poisson arrivals, 40/40/10/10 Sign/Verify/ProofGen/ProofVerify, L~U{5..200}, "
+                        "disclosure~U[0.1,0.9], 256 device-resident keys; served = continuous batching "
+                        "(4 slots, HBM budget 1 GiB), plain = batches of 256 or 2 ms, one at a time",
+            "rates": out}
+
+
 def reference_arm(args):
     """The reference's CPU implementation of the path (oracle port), rank 0 only."""
     rank = int(os.environ.get("RANK", "0"))
@@ -205,6 +303,7 @@ def main():
     ap.add_argument("--R", type=int, default=50)
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--quick", action="store_true", help="headline only (no C2/C5 sections)")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     if args.impl == "reference":
@@ -279,6 +378,13 @@ def main():
     assert all(c == 0 and v for c, v in out)
     h2d, d2h = pkg.last_transfer_bytes()
 
+    # ---------------- C2: 4096 fixed-base MSMs of 12 terms over [P1, Q1, H1..H10];
+    # the window width of the resident table is swept by the autotuner
+    c2 = fixed_msm_section(pkg, rank) if not args.quick else None
+
+    # ---------------- C5: serving queue vs plain batches under Poisson arrivals
+    c5 = serving_section(pkg, rank) if not args.quick else None
+
     pv_step = statistics.mean(pv_ms)
     e2e_step = statistics.mean(e2e) * 1e3
     if dist is not None:
@@ -341,6 +447,8 @@ def main():
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": pv_launch * args.steps,
             "clocks": clocks,
+            "fixed_base_msm_c2": c2,
+            "serving_c5": c5,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

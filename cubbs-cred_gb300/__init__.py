@@ -415,6 +415,61 @@ def g1_msm_common_points(points, rows, fused=False, packed_scale=None):
     return [(res[r].code, res[r].value, bufs[r].raw[:48]) for r in range(R)]
 
 
+def prepared_common_points_call(points, rows):
+    """Builds one common-points group (packed big-endian scalar rows) once and
+    returns call() -> [(code, route, point48)] making one synchronous
+    cubbs_bbs_gpu_g1_msm_common_points_batch_v2 call on it."""
+    k = _Keep()
+    R = len(rows)
+    outs = (ByteBuffer * max(1, R))()
+    bufs = []
+    for r in range(R):
+        ob, buf = k.out(48)
+        bufs.append(buf)
+        outs[r] = ob
+    blob = b"".join(b"".join(row) for row in rows)
+    b = ctypes.create_string_buffer(blob, max(1, len(blob)))
+    k.refs.append(b)
+    item = G1MsmCommonPointsBatchItem()
+    item.points = k.slices(points)
+    item.term_count = len(points)
+    item.scalar_rows = None
+    item.scalar_rows_be = ctypes.cast(b, ctypes.c_void_p)
+    item.scalar_row_stride = len(points) * 32
+    item.output_count = R
+    item.point_outs = ctypes.cast(outs, ctypes.c_void_p)
+    res = (Result * max(1, R))()
+    fn = lib().cubbs_bbs_gpu_g1_msm_common_points_batch_v2
+    ip, rp = ctypes.cast(ctypes.pointer(item), ctypes.c_void_p), ctypes.cast(res, ctypes.c_void_p)
+
+    def call():
+        rc = fn(ABI_VERSION, ip, 1, rp)
+        if rc:
+            raise RuntimeError(f"common points call returned {rc}")
+        _ = k
+        return [(res[r].code, res[r].value, bufs[r].raw[:48]) for r in range(R)]
+    return call
+
+
+def fixed_msm_autotune(scalars_be, rows, terms, w_lo=4, w_hi=12, steps=3):
+    """Times the fixed-base MSM kernel over rows x terms scalars (bases: the first
+    `terms` resident generators) for table window widths w_lo..w_hi; the fastest
+    width stays in use.  Returns ([ms per width], best width)."""
+    nw = w_hi - w_lo + 1
+    ms = (ctypes.c_float * nw)()
+    best = ctypes.c_int32(0)
+    sb = ctypes.create_string_buffer(scalars_be, len(scalars_be))
+    fn = lib().cubbs_bbs_gpu_fixed_msm_autotune_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int32,
+                   ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+    rc = fn(ABI_VERSION, ctypes.cast(sb, ctypes.c_void_p), rows, terms, w_lo, w_hi, steps,
+            ctypes.cast(ms, ctypes.c_void_p), ctypes.cast(ctypes.pointer(best), ctypes.c_void_p))
+    if rc:
+        raise RuntimeError(f"fixed_msm_autotune returned {rc}")
+    return list(ms), best.value
+
+
 def g1_msm_common_points_plus_variable(points, rows, var_points, var_scalars):
     k = _Keep()
     R = len(rows)
@@ -607,6 +662,84 @@ def _op_items(op, reqs, k):
         items[i] = ProofVerifyItem(k.bytes(pk), k.bytes(proof), k.bytes(hdr), k.bytes(ph), k.slices(dmsgs),
                                    len(dmsgs), k.index(didx), L)
     return items
+
+
+class ServeConfig(ctypes.Structure):
+    _fields_ = [("max_inflight", ctypes.c_uint32), ("max_batch_items", ctypes.c_uint32),
+                ("hbm_budget_bytes", ctypes.c_uint64)]
+
+
+SERVE_QUEUE, SERVE_PLAIN = 0, 1
+
+
+def serve_replay(pool, schedule, mode=SERVE_QUEUE, max_inflight=0, max_batch_items=0, hbm_budget_bytes=0,
+                 plain_batch=256, plain_timeout_us=2000):
+    """Replays single requests through the serving queue (mode 0) or through plain
+    fixed-size batches (mode 1).  pool: list of (op, req, seed or None), req shaped
+    as for the batch helpers (OP_SIGN ... OP_PROOF_VERIFY); schedule: list of
+    (pool index, arrival offset in ns), offsets non-decreasing.  A pool entry may be
+    scheduled more than once (its output buffer is then shared).  Returns
+    (results, latencies_ns, wall_s), results[i] = (code, value, output bytes or None)."""
+    k = _Keep()
+    P, n = len(pool), len(schedule)
+    pool_ptr = [0] * P
+    outs = [None] * P
+    arrays = []
+    for op in (OP_SIGN, OP_VERIFY, OP_PROOF_GEN, OP_PROOF_VERIFY):
+        idxs = [i for i, (o, _, _) in enumerate(pool) if o == op]
+        if not idxs:
+            continue
+        reqs = [pool[i][1] for i in idxs]
+        if op == OP_SIGN:
+            items = (SignItem * len(reqs))()
+            bufs = []
+            for j, (sk, pk, hdr, msgs) in enumerate(reqs):
+                ob, buf = k.out(80)
+                bufs.append(buf)
+                items[j] = SignItem(k.bytes(sk), k.bytes(pk), k.bytes(hdr), k.slices(msgs), len(msgs), ob)
+        elif op == OP_PROOF_GEN:
+            items, bufs = _proof_gen_items(k, reqs)
+        else:
+            items, bufs = _op_items(op, reqs, k), None
+        arrays.append(items)
+        for j, i in enumerate(idxs):
+            pool_ptr[i] = ctypes.addressof(items[j])
+            if bufs is not None:
+                outs[i] = (items, j, bufs[j])
+    ptrs = (ctypes.c_void_p * max(1, n))(*[pool_ptr[i] for i, _ in schedule])
+    ops = (ctypes.c_int32 * max(1, n))(*[pool[i][0] for i, _ in schedule])
+    seeds = ctypes.create_string_buffer(32 * max(1, n))
+    has_seed = False
+    for s, (i, _) in enumerate(schedule):
+        if pool[i][2] is not None:
+            ctypes.memmove(ctypes.addressof(seeds) + 32 * s, pool[i][2], 32)
+            has_seed = True
+    arr = (ctypes.c_uint64 * max(1, n))(*[a for _, a in schedule])
+    lat = (ctypes.c_uint64 * max(1, n))()
+    res = (Result * max(1, n))()
+    wall = ctypes.c_double(0)
+    cfg = ServeConfig(max_inflight, max_batch_items, hbm_budget_bytes)
+    fn = lib().cubbs_bbs_gpu_serve_replay
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_uint32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_uint32,
+                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    rc = fn(ABI_VERSION, mode, ctypes.cast(ctypes.pointer(cfg), ctypes.c_void_p), ctypes.cast(ops, ctypes.c_void_p),
+            ctypes.cast(ptrs, ctypes.c_void_p), ctypes.cast(seeds, ctypes.c_void_p) if has_seed else None,
+            ctypes.cast(arr, ctypes.c_void_p), n, plain_batch, plain_timeout_us, ctypes.cast(lat, ctypes.c_void_p),
+            ctypes.cast(res, ctypes.c_void_p), ctypes.cast(ctypes.pointer(wall), ctypes.c_void_p))
+    if rc:
+        raise RuntimeError(f"serve_replay returned {rc}")
+    results = []
+    for s, (i, _) in enumerate(schedule):
+        out = None
+        if outs[i] is not None:
+            items, j, buf = outs[i]
+            ln = items[j].signature_out.len if pool[i][0] == OP_SIGN else items[j].proof_out.len
+            out = buf.raw[:ln]
+        results.append((res[s].code, res[s].value, out))
+    del arrays
+    return results, [lat[s] for s in range(n)], wall.value
 
 
 def bench_device_steps(op, reqs, warmup, steps, seeds=None):

@@ -359,6 +359,40 @@ int32_t cubbs_bbs_gpu_proof_gen_t2_prepare_batch_v2(uint32_t abi_version,
                                                     size_t item_count,
                                                     CuBbsBbsGpuResult *results);
 
+/* Serving queue (no counterpart in the reference ABI): continuous batching of
+ * single requests of the four operations.  Up to max_inflight batches run at
+ * once on separate device workspaces; a free slot takes the operation whose
+ * oldest request waited longest, as many of its requests as fit in
+ * max_batch_items and in the device-memory budget left by the running batches.
+ * Items and their buffers are caller-owned and must stay alive until the
+ * request's wait returns.  op: 0 Sign, 1 Verify, 2 ProofGen, 3 ProofVerify;
+ * seed32 (ProofGen only, nullable) selects seeded blinding as in
+ * cubbs_bbs_gpu_proof_gen_seeded_batch_v2, else OS randomness.  The result of
+ * a request equals the result of the same request in a batch of its own. */
+typedef struct CuBbsBbsGpuServeConfig {
+  uint32_t max_inflight;     /* 0: one per device workspace (CUBBS_BBS_WORKSPACES, default 4) */
+  uint32_t max_batch_items;  /* 0: 1024 */
+  uint64_t hbm_budget_bytes; /* device bytes admitted across running batches; 0: 1 GiB */
+} CuBbsBbsGpuServeConfig;
+
+int32_t cubbs_bbs_gpu_serve_create(uint32_t abi_version, const CuBbsBbsGpuServeConfig *config,
+                                   void **server);
+int32_t cubbs_bbs_gpu_serve_submit(void *server, int32_t op, void *item, const uint8_t *seed32,
+                                   uint64_t *ticket);
+int32_t cubbs_bbs_gpu_serve_wait(void *server, uint64_t ticket, CuBbsBbsGpuResult *result);
+int32_t cubbs_bbs_gpu_serve_destroy(void *server);
+/* Load replay for benchmarks and tests: request i arrives arrival_ns[i] after
+ * the start (non-decreasing); mode 0 serves through the queue, mode 1 through
+ * plain fixed-size batches (plain_batch requests, flushed after
+ * plain_timeout_us, one batch at a time).  latency_ns[i] = completion minus
+ * scheduled arrival; wall_s = start to last completion. */
+int32_t cubbs_bbs_gpu_serve_replay(uint32_t abi_version, int32_t mode,
+                                   const CuBbsBbsGpuServeConfig *config, const int32_t *ops,
+                                   void *const *items, const uint8_t (*seeds)[32],
+                                   const uint64_t *arrival_ns, size_t count, uint32_t plain_batch,
+                                   uint32_t plain_timeout_us, uint64_t *latency_ns,
+                                   CuBbsBbsGpuResult *results, double *wall_s);
+
 /* Test exports outside the reference header (reference cubbs_bbs_cuda.cu:53,117,230). */
 int32_t cubbs_bbs_gpu_sha256_batch_for_test_v2(uint32_t abi_version, const uint8_t *messages,
                                                const size_t *offsets, const size_t *lengths,
