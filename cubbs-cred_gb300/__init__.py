@@ -451,6 +451,27 @@ def prepared_common_points_call(points, rows):
     return call
 
 
+def msm_uneven_bench(n_msms=16384, k_min=2, k_max=257, seed=4, tune=True, warmup=3, steps=5):
+    """Uneven variable-base MSM benchmark (points u*P1 and scalars generated on the
+    device from `seed`).  Returns dict(ms=[per replay], decode_ms, chunk=[per size
+    class], window=[per size class], checked, mismatch)."""
+    ms = (ctypes.c_float * steps)()
+    dec = ctypes.c_float(0)
+    tun = (ctypes.c_uint32 * 8)()
+    chk, mm = ctypes.c_uint32(0), ctypes.c_uint32(0)
+    fn = lib().cubbs_bbs_gpu_msm_uneven_bench_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_uint32, ctypes.c_size_t, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
+                   ctypes.c_int32, ctypes.c_int32, ctypes.c_int32] + [ctypes.c_void_p] * 5
+    rc = fn(ABI_VERSION, n_msms, k_min, k_max, seed, 1 if tune else 0, warmup, steps, ctypes.cast(ms, ctypes.c_void_p),
+            ctypes.cast(ctypes.pointer(dec), ctypes.c_void_p), ctypes.cast(tun, ctypes.c_void_p),
+            ctypes.cast(ctypes.pointer(chk), ctypes.c_void_p), ctypes.cast(ctypes.pointer(mm), ctypes.c_void_p))
+    if rc:
+        raise RuntimeError(f"msm_uneven_bench returned {rc}")
+    return {"ms": list(ms), "decode_ms": dec.value, "chunk": list(tun[:4]), "window": list(tun[4:]),
+            "checked": chk.value, "mismatch": mm.value}
+
+
 def fixed_msm_autotune(scalars_be, rows, terms, w_lo=4, w_hi=12, steps=3):
     """Times the fixed-base MSM kernel over rows x terms scalars (bases: the first
     `terms` resident generators) for table window widths w_lo..w_hi; the fastest

@@ -141,10 +141,20 @@ void run_plan(Runtime &rt, Plan &pl, std::vector<uint8_t> &out48, std::vector<ui
   cudaStream_t s = rt.stream;
   size_t R = pl.rows, npts = pl.points_be.size() / 48, nvar = pl.var_point.size();
   size_t nfix = pl.has_fixed ? R * pl.fixed_stride : 0;
+  // Many variable-only rows: the persistent bucket-method engine (k_msm.cu)
+  // instead of one GLV multiplication per term plus a row sum.
+  const bool engine = !pl.has_fixed && R >= 32 && nvar >= 8 * R;
+  MsmPlan mp;
+  if (engine) {
+    std::vector<uint32_t> K(R);
+    for (size_t r = 0; r < R; r++) K[r] = pl.var_start[r + 1] - pl.var_start[r];
+    mp.build(K, rt.sh.msm_tuning);
+  }
+  const size_t eng_bytes = engine ? MsmDevice::arena_bytes(mp) : 0;
   rt.arena.reserve(8192 + npts * (sizeof(g1a) + 64) + nvar * (sizeof(g1) + sizeof(fr) + 48) +
-                   nfix * (sizeof(fr) + 40) + R * (2 * sizeof(g1) + 128));
+                   nfix * (sizeof(fr) + 40) + R * (2 * sizeof(g1) + 128) + eng_bytes);
   rt.staging.reserve(65536 + pl.points_be.size() + pl.var_scalars_be.size() + pl.fixed_scalars_be.size() +
-                     R * 128 + nvar * 16);
+                     R * 128 + nvar * 16 + eng_bytes);
   if (pl.has_fixed) rt.ensure_table((int)pl.fixed_stride);
   // decode points
   uint8_t *dpb = upload(rt, pl.points_be.data(), pl.points_be.size());
@@ -194,13 +204,20 @@ void run_plan(Runtime &rt, Plan &pl, std::vector<uint8_t> &out48, std::vector<ui
     jobs[j] = {p, (uint32_t)(hpst[p] != DEC_OK ? 1 : 0)};
   }
   VarJob *djobs = upload(rt, jobs.data(), nvar);
-  g1 *v = rt.arena.alloc<g1>(nvar);
-  launch_var_mul(s, pts, djobs, vsc, (uint32_t)nvar, v);
-  uint32_t *dstart = upload(rt, pl.var_start.data(), R + 1);
-  g1 *res = rt.arena.alloc<g1>(R);
-  if (R) k_row_sum<<<blocks_for(R * 32, 128), 128, 0, s>>>(fixed, v, dstart, (uint32_t)R, res);
   uint8_t *dout = rt.arena.alloc<uint8_t>(48 * R);
-  launch_g1_compress(s, res, (uint32_t)R, dout);
+  if (engine) {
+    MsmDevice md;
+    md.upload(rt, mp, s);
+    launch_msm_prep(s, md, pts, djobs, vsc);
+    launch_msm_main(s, md, pts, djobs, rt.sm_count, nullptr, dout);
+  } else {
+    g1 *v = rt.arena.alloc<g1>(nvar);
+    launch_var_mul(s, pts, djobs, vsc, (uint32_t)nvar, v);
+    uint32_t *dstart = upload(rt, pl.var_start.data(), R + 1);
+    g1 *res = rt.arena.alloc<g1>(R);
+    if (R) k_row_sum<<<blocks_for(R * 32, 128), 128, 0, s>>>(fixed, v, dstart, (uint32_t)R, res);
+    launch_g1_compress(s, res, (uint32_t)R, dout);
+  }
   CUBBS_CHECK(cudaGetLastError());
   out48.resize(48 * R);
   if (R) CUBBS_CHECK(cudaMemcpyAsync(out48.data(), dout, 48 * R, cudaMemcpyDeviceToHost, s));

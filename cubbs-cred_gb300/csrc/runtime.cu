@@ -241,6 +241,15 @@ void Runtime::set_table_window(int w, int gens) {
   lock->lock();
 }
 
+void Runtime::set_msm_tuning(const MsmTuning &t) {
+  lock->unlock();
+  {
+    std::unique_lock<std::shared_mutex> ex(sh.mu);
+    sh.msm_tuning = t;
+  }
+  lock->lock();
+}
+
 void Runtime::resolve_pks(const std::vector<const uint8_t *> &pk_ptrs, std::vector<int> &slots,
                           std::vector<int> &status) {
   std::vector<std::string> keys(pk_ptrs.size());

@@ -72,6 +72,29 @@ struct PkSlot {
   int status = DEC_BAD;  // DEC_OK / DEC_INF / DEC_BAD
 };
 
+// Uneven variable-base MSMs (k_msm.cu): chunks of t terms per lane, bucket
+// method of window c; t and c per size class of the term count K.
+#define MSM_CLASSES 4  // K <= 8, <= 32, <= 96, larger
+struct MsmTuning {
+  uint32_t chunk[MSM_CLASSES] = {8, 16, 32, 48};
+  uint32_t window[MSM_CLASSES] = {4, 4, 5, 5};
+};
+struct MsmChunk {
+  uint32_t first, count;  // term range
+  uint32_t slot;          // partial index (0xffffffff: padding)
+  uint32_t pad;
+};
+int msm_size_class(uint32_t K);
+struct MsmPlan {
+  std::vector<uint32_t> start;    // term offsets of the MSMs (n + 1)
+  uint32_t terms = 0;
+  std::vector<uint8_t> term_c;    // window width per term
+  std::vector<MsmChunk> chunks;   // units of 32, grouped by window width
+  std::vector<uint8_t> unit_c;
+  std::vector<uint32_t> pstart;   // partial offsets of the MSMs (n + 1)
+  uint32_t nparts = 0;
+  void build(const std::vector<uint32_t> &K, const MsmTuning &tune);
+};
 // Process-wide prepared state shared by every call: generators, the
 // fixed-base window table and the Miller lines of -P2, P2 and every public
 // key seen.  Calls hold `mu` shared while their kernels may read the state;
@@ -99,6 +122,7 @@ struct SharedState {
   std::unordered_map<std::string, int> pk_slots;
   std::vector<PkSlot> slot_info;
   int workspaces = 4;           // concurrent calls (CUBBS_BBS_WORKSPACES)
+  MsmTuning msm_tuning;         // uneven-MSM chunk length / window per size class
 
   static SharedState &get();
   void init();                              // device, prep stream, -P2/P2 lines
@@ -132,6 +156,7 @@ struct Runtime {
   void ensure_generators(int count);  // d_gens[0..count) (P1 + count-1 generators)
   void ensure_table(int gens);        // fixed-base table covering d_gens[0..gens)
   void set_table_window(int w, int gens);  // rebuild the table with window width w
+  void set_msm_tuning(const MsmTuning &t);
   // Resolve public keys to line slots (decoding + subgroup check + lines on the
   // device for new keys).  pk_ptrs[i] -> slot index; status per key.
   void resolve_pks(const std::vector<const uint8_t *> &pk_ptrs, std::vector<int> &slots,
@@ -187,6 +212,21 @@ struct VarJob {
 void launch_var_mul(cudaStream_t s, const g1a *points, const VarJob *jobs, const fr *scalars, uint32_t n,
                     g1 *out);
 void launch_g1_compress(cudaStream_t s, const g1 *pts, uint32_t n, uint8_t *out48);
+struct MsmDevice {
+  uint32_t n = 0, nterms = 0, nchunks = 0, nunits = 0;
+  uint8_t *term_c = nullptr, *unit_c = nullptr;
+  MsmChunk *chunks = nullptr;
+  uint32_t *pstart = nullptr, *koff = nullptr, *counter = nullptr;
+  g1a *phi = nullptr;
+  g1 *partials = nullptr;
+  void upload(Runtime &rt, const MsmPlan &p, cudaStream_t s);
+  static size_t arena_bytes(const MsmPlan &p);
+};
+// term j of the flat term list uses point jobs[j].point (skipped when flags & 1)
+// and scalar scalars[j]; MSM i owns terms [start[i], start[i+1]).
+void launch_msm_prep(cudaStream_t s, const MsmDevice &d, const g1a *pts, const VarJob *jobs, const fr *scalars);
+void launch_msm_main(cudaStream_t s, const MsmDevice &d, const g1a *pts, const VarJob *jobs, int sm_count, g1 *out,
+                     uint8_t *out48);
 void launch_pk_prepare(cudaStream_t s, const uint8_t *pks96, uint32_t n, int slot0, g2a *pk_aff,
                        line2 *lines, int32_t *status);
 void launch_p2_lines(cudaStream_t s, line2 *lines);

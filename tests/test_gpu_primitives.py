@@ -189,3 +189,28 @@ def test_pairing_eq_aggregate(gpu, oracle):
     assert gpu.pairing_eq_aggregate(good) == (0, True)
     bad = good[:2] + [(p[2], pk, p[2], pk2, c[2])]
     assert gpu.pairing_eq_aggregate(bad) == (0, False)
+
+
+def test_g1_msm_batch_uneven_engine(gpu, oracle):
+    """64 MSMs of uneven length take the persistent bucket-method engine."""
+    import random
+    rng = random.Random(11)
+    seed = b"msm-uneven"
+    p1, _ = oracle.generators(1)
+    msms = []
+    for i in range(64):
+        K = rng.randint(2, 40)
+        pts = [oracle.g1_mul(p1, scalar(seed, b"pt%d" % i, k)) for k in range(K)]
+        scs = [scalar(seed, b"k%d" % i, k) for k in range(K)]
+        if i == 5:
+            pts[1] = bytes([0xC0]) + bytes(47)  # identity term
+        if i == 9:
+            scs[0] = bytes(32)                  # zero scalar
+        msms.append((pts, scs))
+    got = gpu.g1_msm_batch(msms)
+    assert [(c, p) for c, p in got] == [(0, oracle.g1_msm(pts, scs)) for pts, scs in msms]
+
+
+def test_msm_uneven_bench_self_check(gpu):
+    r = gpu.msm_uneven_bench(n_msms=512, k_min=2, k_max=257, seed=9, tune=False, warmup=1, steps=1)
+    assert r["checked"] == 64 and r["mismatch"] == 0 and r["ms"][0] > 0
