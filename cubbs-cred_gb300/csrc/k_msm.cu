@@ -374,7 +374,8 @@ MsmWork make_work(Runtime &rt, cudaStream_t s, uint64_t seed, const std::vector<
   return w;
 }
 
-// mean ms of `reps` engine runs (prep + persistent launch + reduction) on `w` with `tune`
+// mean ms of `reps` engine runs (prep + persistent launch + reduction) on `w` with `tune`;
+// the kernels are the same for every candidate, so no warm-up run is needed
 float time_engine(Runtime &rt, cudaStream_t s, const MsmWork &w, const MsmTuning &tune, int reps, uint8_t *out48,
                   cudaEvent_t e0, cudaEvent_t e1) {
   MsmPlan p;
@@ -382,8 +383,6 @@ float time_engine(Runtime &rt, cudaStream_t s, const MsmWork &w, const MsmTuning
   size_t mark = rt.arena.used;
   MsmDevice d;
   d.upload(rt, p, s);
-  launch_msm_prep(s, d, w.pts, w.jobs, w.sc);
-  launch_msm_main(s, d, w.pts, w.jobs, rt.sm_count, nullptr, out48);  // warm-up
   CUBBS_CHECK(cudaEventRecord(e0, s));
   for (int r = 0; r < reps; r++) {
     launch_msm_prep(s, d, w.pts, w.jobs, w.sc);
@@ -435,34 +434,36 @@ extern "C" int32_t cubbs_bbs_gpu_msm_uneven_bench_v2(uint32_t abi, size_t n_msms
     cudaEvent_t e0, e1;
     CUBBS_CHECK(cudaEventCreate(&e0));
     CUBBS_CHECK(cudaEventCreate(&e1));
-    // ---- autotune on per-class samples
+    // ---- autotune: coordinate descent over the size classes on a sample with the
+    // workload's own K distribution (all classes share the device, as in the run)
     MsmTuning best = rt.sh.msm_tuning;
     if (tune) {
-      const uint32_t lo[MSM_CLASSES] = {2, 9, 33, 97}, hi[MSM_CLASSES] = {8, 32, 96, 257};
-      const uint32_t chunks[] = {2, 4, 8, 16, 32, 64, 128, 256};
+      const uint32_t lo[MSM_CLASSES] = {2, 9, 33, 97}, hi[MSM_CLASSES] = {8, 32, 96, 0xffffffffu};
+      const uint32_t chunks[] = {2, 4, 8, 16, 32, 64};
+      const size_t ns = std::min<size_t>(n_msms, 4096);
+      size_t mark = rt.arena.used;
+      MsmWork w = make_work(rt, s, seed ^ 0x77ull, draw_k(seed + 99, ns, k_min, k_max));
+      uint8_t *o = rt.arena.alloc<uint8_t>(48 * ns);
+      time_engine(rt, s, w, best, 1, o, e0, e1);  // first launch of the kernels, untimed
+      float cur = time_engine(rt, s, w, best, 1, o, e0, e1);
       for (int cls = 0; cls < MSM_CLASSES; cls++) {
         const uint32_t a = std::max(lo[cls], k_min), b = std::min(hi[cls], k_max);
         if (a > b) continue;
-        size_t mark = rt.arena.used;
-        MsmWork w = make_work(rt, s, seed ^ (0x51ull + cls), draw_k(seed + 17 + cls, 1024, a, b));
-        uint8_t *o = rt.arena.alloc<uint8_t>(48 * 1024);
-        float bms = 0;
         for (uint32_t t : chunks) {
           if (t > 2 * b) continue;
-          for (int c = 4; c <= 7; c++) {
+          for (int c = 4; c <= 6; c++) {
             MsmTuning cand = best;
             cand.chunk[cls] = t;
             cand.window[cls] = (uint32_t)c;
-            float ms = time_engine(rt, s, w, cand, 2, o, e0, e1);
-            if (bms == 0 || ms < bms) {
-              bms = ms;
-              best.chunk[cls] = t;
-              best.window[cls] = (uint32_t)c;
+            const float ms = time_engine(rt, s, w, cand, 1, o, e0, e1);
+            if (ms < cur) {
+              cur = ms;
+              best = cand;
             }
           }
         }
-        rt.arena.used = mark;
       }
+      rt.arena.used = mark;
       rt.set_msm_tuning(best);
     }
     for (int c = 0; c < MSM_CLASSES; c++) {
