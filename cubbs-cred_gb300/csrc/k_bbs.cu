@@ -65,17 +65,14 @@ struct PvItem {
   int32_t status;  // host-side status
 };
 
-// Parse the scalars of the proof, build the T2 fixed-base row and the four
-// variable-base jobs (Bbar*c, Abar*e^, D*r1^, D*r3^).
-__global__ void __launch_bounds__(128) k_pv_prep(PvItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
-                                                 const fr *domain, const int32_t *dec_status, fr *rows,
-                                                 uint32_t stride, uint32_t *nterms, VarJob *jobs, fr *jscal) {
+// Parse the scalars of the proof and build its T2 fixed-base row.  Needs no
+// decoded point, so the fixed-base MSM can run while the points decode.
+__global__ void __launch_bounds__(128) k_pv_rows(PvItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
+                                                 const fr *domain, fr *rows, uint32_t stride, uint32_t *nterms) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   PvItem it = items[i];
   bool ok = it.status == ST_OK && it.pk_status != DEC_BAD;
-  #pragma unroll 1
-  for (int k = 0; k < 3 && ok; k++) ok = dec_status[3 * i + k] != DEC_BAD;
   const uint8_t *pr = blob + it.proof_off;
   fr ecap, r1cap, r3cap, c;
   if (ok) ok = fr_raw_from_be32(pr + 144, ecap) && fr_raw_from_be32(pr + 176, r1cap) &&
@@ -89,7 +86,6 @@ __global__ void __launch_bounds__(128) k_pv_prep(PvItem *items, uint32_t n, cons
   if (!ok) {
     items[i].status = ST_INVALID;
     nterms[i] = 0;
-    for (int k = 0; k < 4; k++) jobs[4 * i + k] = {0, 1};
     return;
   }
   nterms[i] = it.L + 2;
@@ -108,6 +104,28 @@ __global__ void __launch_bounds__(128) k_pv_prep(PvItem *items, uint32_t n, cons
       row[2 + m] = t;
       u++;
     }
+  }
+}
+
+// The four variable-base jobs of each proof (Bbar*c, Abar*e^, D*r1^, D*r3^),
+// from the untouched input items and the decoded points; a proof whose points
+// or scalars do not decode gets jobs at infinity (k_pv_rows and k_pv_finish
+// mark it invalid).
+__global__ void __launch_bounds__(128) k_pv_jobs(const PvItem *items0, uint32_t n, const uint8_t *blob,
+                                                 const int32_t *dec_status, VarJob *jobs, fr *jscal) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PvItem it = items0[i];
+  bool ok = it.status == ST_OK && it.pk_status != DEC_BAD;
+  #pragma unroll 1
+  for (int k = 0; k < 3 && ok; k++) ok = dec_status[3 * i + k] != DEC_BAD;
+  const uint8_t *pr = blob + it.proof_off;
+  fr ecap, r1cap, r3cap, c;
+  if (ok) ok = fr_raw_from_be32(pr + 144, ecap) && fr_raw_from_be32(pr + 176, r1cap) &&
+               fr_raw_from_be32(pr + 208, r3cap) && fr_raw_from_be32(pr + 240 + 32 * it.U, c);
+  if (!ok) {
+    for (int k = 0; k < 4; k++) jobs[4 * i + k] = {0, 1};
+    return;
   }
   // points: 3i+0 Abar, 3i+1 Bbar, 3i+2 D
   uint32_t fa = dec_status[3 * i] == DEC_INF, fb = dec_status[3 * i + 1] == DEC_INF, fd = dec_status[3 * i + 2] == DEC_INF;
@@ -146,11 +164,16 @@ __global__ void __launch_bounds__(128) k_pv_pairjobs(const PvItem *items0, uint3
 
 // T1, T2 -> compressed; recompute the challenge (a mismatch marks the item invalid).
 __global__ void __launch_bounds__(64) k_pv_finish(PvItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
-                                                  const fr *domain, const g1 *t2fix, const g1 *v) {
+                                                  const fr *domain, const int32_t *dec_status, const g1 *t2fix,
+                                                  const g1 *v) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   PvItem it = items[i];
   if (it.status != ST_OK) return;
+  if (dec_status[3 * i] == DEC_BAD || dec_status[3 * i + 1] == DEC_BAD || dec_status[3 * i + 2] == DEC_BAD) {
+    items[i].status = ST_INVALID;
+    return;
+  }
   g1 T1 = g1_add(g1_add(v[4 * i], v[4 * i + 1]), v[4 * i + 2]);
   g1 T2 = g1_add(t2fix[i], v[4 * i + 3]);
   uint8_t t1c[48], t2c[48];
@@ -364,17 +387,17 @@ __global__ void __launch_bounds__(64) k_pg_random(const PgItem *items, uint32_t 
   }
 }
 
-// rows 0..n-1: B = P1 + Q1 domain + sum H_i m_i ; rows n..2n-1: T2 fixed part sum_{j in U} H_j m~_j
+// rows 0..n-1: B = P1 + Q1 domain + sum H_i m_i ; rows n..2n-1: T2 fixed part sum_{j in U} H_j m~_j.
+// Needs no decoded signature point (k_pg_vars rejects a signature whose A does
+// not decode), so the signature decode runs beside it.
 __global__ void __launch_bounds__(128) k_pg_prep(PgItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
-                                                 const fr *domain, const fr *rs, uint32_t rs_stride,
-                                                 const int32_t *dec_status, fr *rows, uint32_t stride,
-                                                 uint32_t *nterms) {
+                                                 const fr *domain, const fr *rs, uint32_t rs_stride, fr *rows,
+                                                 uint32_t stride, uint32_t *nterms) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   PgItem it = items[i];
   fr e;
-  bool ok = it.status == ST_OK && it.pk_status != DEC_BAD && dec_status[i] != DEC_BAD &&
-            fr_raw_from_be32(blob + it.sig_off + 48, e);
+  bool ok = it.status == ST_OK && it.pk_status != DEC_BAD && fr_raw_from_be32(blob + it.sig_off + 48, e);
   if (!ok) {
     items[i].status = ST_ERROR;
     nterms[i] = 0;
@@ -407,7 +430,7 @@ __global__ void __launch_bounds__(128) k_pg_prep(PgItem *items, uint32_t n, cons
 
 // Variable-base jobs on B (affine) and A: D = r2 B, Abar = r1r2 A,
 // Bbar = r1r2 B - e r1r2 A, T1 = r1~ r2 B + e~ r1r2 A, T2 += r3~ r2 B.
-__global__ void __launch_bounds__(64) k_pg_vars(const PgItem *items, uint32_t n, const uint8_t *blob, const g1 *Bx,
+__global__ void __launch_bounds__(64) k_pg_vars(PgItem *items, uint32_t n, const uint8_t *blob, const g1 *Bx,
                                                 const g1a *A, const int32_t *dec_status, const fr *rs,
                                                 uint32_t rs_stride, g1a *pts, VarJob *jobs, fr *jscal) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -415,6 +438,10 @@ __global__ void __launch_bounds__(64) k_pg_vars(const PgItem *items, uint32_t n,
   PgItem it = items[i];
   for (int k = 0; k < 7; k++) jobs[7 * i + k] = {2 * i, 1};
   if (it.status != ST_OK) return;
+  if (dec_status[i] == DEC_BAD) {  // signature A does not decode
+    items[i].status = ST_ERROR;
+    return;
+  }
   g1a b;
   bool binf = !g1_to_aff(Bx[i], b);
   pts[2 * i] = A[i];
@@ -632,115 +659,165 @@ void upload(Runtime &rt, OpBatch &b) {
 
 static const char MAP_DST_H[] = "BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_H2G_HM2S_MAP_MSG_TO_SCALAR_AS_HASH_";
 
-// Optional per-stage events (benchmark breakdown): stage k ends at ev[k].
+// Optional per-kernel spans (benchmark breakdown): span k runs from a[k] to
+// b[k], both recorded on the stream the kernel is launched on, so kernels that
+// run side by side on different streams are timed each on its own stream.
 struct StageEvents {
-  cudaEvent_t ev[16];
-  int used = 0;
+  cudaEvent_t a[16], b[16];
   const char *name[16];
-  cudaEvent_t side[2];  // the pairing kernel on the second stream
-  bool side_used = false;
+  int used = 0;
 };
 thread_local StageEvents *g_stages = nullptr;
-void stage_mark(cudaStream_t s, const char *name) {
-  if (!g_stages || g_stages->used >= 16) return;
-  cudaEventRecord(g_stages->ev[g_stages->used], s);
-  g_stages->name[g_stages->used++] = name;
+int span_begin(cudaStream_t s) {
+  if (!g_stages || g_stages->used >= 16) return -1;
+  CUBBS_CHECK(cudaEventRecord(g_stages->a[g_stages->used], s));
+  return g_stages->used++;
+}
+void span_end(cudaStream_t s, int k, const char *name) {
+  if (!g_stages || k < 0) return;
+  CUBBS_CHECK(cudaEventRecord(g_stages->b[k], s));
+  g_stages->name[k] = name;
+}
+#define SPAN(stream, label, ...)          \
+  do {                                    \
+    const int _k = span_begin(stream);    \
+    __VA_ARGS__;                          \
+    span_end(stream, _k, label);          \
+  } while (0)
+
+// ProofVerify on three streams.  Decoding Abar, Bbar, D (stream2) is
+// independent of the message hash, the domain and the T2 fixed-base MSM
+// (stream); the variable-base terms follow the decode on stream2 and the
+// pairing follows it on stream3.  Each of these kernels fills only part of the
+// GPU, so running them side by side shortens the step.
+void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
+  cudaStream_t s = rt.stream, s2 = rt.stream2, s3 = rt.stream3;
+  size_t n = b.n, nm = b.ml.count(), npts = b.pts48.size() / 48;
+  uint32_t N = (uint32_t)n, stride = (uint32_t)b.stride;
+  PvItem *it = reinterpret_cast<PvItem *>(b.ditems);
+  const PvItem *it0 = reinterpret_cast<const PvItem *>(b.ditems0);
+  CUBBS_CHECK(cudaEventRecord(rt.ev_fork, s));
+  CUBBS_CHECK(cudaStreamWaitEvent(s2, rt.ev_fork, 0));
+  SPAN(s2, "g1_decode", launch_g1_decode(s2, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, true));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_mid, s2));
+  CUBBS_CHECK(cudaStreamWaitEvent(s3, rt.ev_mid, 0));
+  SPAN(s3, "pairing_kernel",
+       k_pv_pairjobs<<<blocks_for(n, 128), 128, 0, s3>>>(it0, N, b.pts, b.dec, b.pj);
+       launch_pairing_check(s3, b.pj, N, rt.d_lines, b.ok));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_join, s3));
+  SPAN(s2, "var_mul",
+       k_pv_jobs<<<blocks_for(n, 128), 128, 0, s2>>>(it0, N, b.dblob, b.dec, b.jobs, b.jscal);
+       launch_var_mul(s2, b.pts, b.jobs, b.jscal, 4 * N, b.v));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_side, s2));
+  if (nm)
+    SPAN(s, "hash_messages",
+         launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
+                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1,
+                         b.msc));
+  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, b.domain));
+  SPAN(s, "scalar_prep",
+       k_pv_rows<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms));
+  SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
+  CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_side, 0));
+  SPAN(s, "challenge",
+       k_pv_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.fixed, b.v));
+  CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_join, 0));
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 1 : 0) + 8;
+}
+
+// ProofGen on three streams: the signature decode (stream3) and the blinding
+// scalars (stream2) run beside the message hash, the domain and the B / T2
+// fixed-base MSMs; the variable-base terms need all of them.
+void run_pgen(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
+  cudaStream_t s = rt.stream, s2 = rt.stream2, s3 = rt.stream3;
+  size_t n = b.n, nm = b.ml.count(), npts = b.pts48.size() / 48;
+  uint32_t N = (uint32_t)n, stride = (uint32_t)b.stride, rss = (uint32_t)b.rs_stride;
+  PgItem *it = reinterpret_cast<PgItem *>(b.ditems);
+  const PgItem *it0 = reinterpret_cast<const PgItem *>(b.ditems0);
+  CUBBS_CHECK(cudaEventRecord(rt.ev_fork, s));
+  CUBBS_CHECK(cudaStreamWaitEvent(s2, rt.ev_fork, 0));
+  CUBBS_CHECK(cudaStreamWaitEvent(s3, rt.ev_fork, 0));
+  SPAN(s3, "g1_decode", launch_g1_decode(s3, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, true));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_join, s3));
+  SPAN(s2, "random_scalars", k_pg_random<<<blocks_for(n, 64), 64, 0, s2>>>(it0, N, b.dblob, b.rs, rss));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_side, s2));
+  if (nm)
+    SPAN(s, "hash_messages",
+         launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
+                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1,
+                         b.msc));
+  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, b.domain));
+  CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_side, 0));
+  SPAN(s, "scalar_prep",
+       k_pg_prep<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rs, rss, b.rows, stride,
+                                                    b.nterms));
+  SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, 2 * N, b.fixed));
+  CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_join, 0));
+  SPAN(s, "var_prep",
+       k_pg_vars<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.fixed, b.pts, b.dec, b.rs, rss, b.vpts, b.jobs,
+                                                  b.jscal));
+  SPAN(s, "var_mul", launch_var_mul(s, b.vpts, b.jobs, b.jscal, 7 * N, b.v));
+  SPAN(s, "finish",
+       k_pg_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rs, rss, b.fixed + n, b.v,
+                                                    b.out));
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 1 : 0) + 7;
 }
 
 // The whole device pipeline of one batch (no host work, no transfers).
 void run(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   cudaStream_t s = rt.stream;
-  if (g_stages) g_stages->used = 0;
-  stage_mark(s, "start");
   size_t n = b.n, nm = b.ml.count();
   uint32_t N = (uint32_t)n, stride = (uint32_t)b.stride;
   CUBBS_CHECK(cudaMemcpyAsync(b.ditems, b.ditems0, b.items.size(), cudaMemcpyDeviceToDevice, s));
+  if (b.op == OP_PVERIFY || b.op == OP_PGEN) {
+    if (b.op == OP_PVERIFY) run_pverify(rt, b, dmapdst);
+    else run_pgen(rt, b, dmapdst);
+    CUBBS_CHECK(cudaGetLastError());
+    return;
+  }
   size_t launches = 0;
   if (nm) {
-    launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
-                    reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1, b.msc);
+    SPAN(s, "hash_messages",
+         launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
+                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1,
+                         b.msc));
     launches++;
   }
-  stage_mark(s, "hash_messages");
   size_t npts = b.pts48.size() / 48;
   if (npts) {
-    launch_g1_decode(s, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, true);
+    SPAN(s, "g1_decode", launch_g1_decode(s, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, true));
     launches++;
   }
-  stage_mark(s, "g1_decode");
-  launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, b.domain);
+  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, b.domain));
   launches++;
-  stage_mark(s, "domain");
   switch (b.op) {
-    case OP_PVERIFY: {
-      // The pairing needs only the decoded Abar, Bbar and the key's lines: it
-      // runs on the second stream beside the MSMs and the challenge.
-      PvItem *it = reinterpret_cast<PvItem *>(b.ditems);
-      CUBBS_CHECK(cudaEventRecord(rt.ev_fork, s));
-      CUBBS_CHECK(cudaStreamWaitEvent(rt.stream2, rt.ev_fork, 0));
-      k_pv_pairjobs<<<blocks_for(n, 128), 128, 0, rt.stream2>>>(reinterpret_cast<const PvItem *>(b.ditems0), N,
-                                                                 b.pts, b.dec, b.pj);
-      if (g_stages) CUBBS_CHECK(cudaEventRecord(g_stages->side[0], rt.stream2));
-      launch_pairing_check(rt.stream2, b.pj, N, rt.d_lines, b.ok);
-      if (g_stages) {
-        CUBBS_CHECK(cudaEventRecord(g_stages->side[1], rt.stream2));
-        g_stages->side_used = true;
-      }
-      CUBBS_CHECK(cudaEventRecord(rt.ev_join, rt.stream2));
-      k_pv_prep<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.rows, stride, b.nterms,
-                                                   b.jobs, b.jscal);
-      stage_mark(s, "scalar_prep");
-      launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed);
-      stage_mark(s, "fixed_msm");
-      launch_var_mul(s, b.pts, b.jobs, b.jscal, 4 * N, b.v);
-      stage_mark(s, "var_mul");
-      k_pv_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.fixed, b.v);
-      stage_mark(s, "challenge");
-      CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_join, 0));
-      stage_mark(s, "pairing_join");
-      launches += 6;
+    case OP_PVERIFY:
       break;
-    }
     case OP_SIGN: {
       SignItem *it = reinterpret_cast<SignItem *>(b.ditems);
-      k_sign_prep<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms, b.e);
-      launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed);
-      k_sign_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.fixed, b.e, b.out);
+      SPAN(s, "scalar_prep",
+           k_sign_prep<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms,
+                                                        b.e));
+      SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
+      SPAN(s, "finish", k_sign_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.fixed, b.e, b.out));
       launches += 3;
       break;
     }
     case OP_VERIFY: {
       VerifyItem *it = reinterpret_cast<VerifyItem *>(b.ditems);
-      k_verify_prep<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.rows, stride,
-                                                       b.nterms, b.jobs, b.jscal);
-      launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed);
-      launch_var_mul(s, b.pts, b.jobs, b.jscal, N, b.v);
-      k_verify_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.fixed, b.v, b.pts, b.dec, b.pj);
-      launch_pairing_check(s, b.pj, N, rt.d_lines, b.ok);
+      SPAN(s, "scalar_prep",
+           k_verify_prep<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.rows,
+                                                            stride, b.nterms, b.jobs, b.jscal));
+      SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
+      SPAN(s, "var_mul", launch_var_mul(s, b.pts, b.jobs, b.jscal, N, b.v));
+      SPAN(s, "finish",
+           k_verify_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.fixed, b.v, b.pts, b.dec, b.pj));
+      SPAN(s, "pairing", launch_pairing_check(s, b.pj, N, rt.d_lines, b.ok));
       launches += 5;
       break;
     }
-    case OP_PGEN: {
-      PgItem *it = reinterpret_cast<PgItem *>(b.ditems);
-      uint32_t rss = (uint32_t)b.rs_stride;
-      k_pg_random<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.rs, rss);
-      stage_mark(s, "random_scalars");
-      k_pg_prep<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rs, rss, b.dec, b.rows, stride,
-                                                   b.nterms);
-      stage_mark(s, "scalar_prep");
-      launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, 2 * N, b.fixed);
-      stage_mark(s, "fixed_msm");
-      k_pg_vars<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.fixed, b.pts, b.dec, b.rs, rss, b.vpts, b.jobs,
-                                                 b.jscal);
-      stage_mark(s, "var_prep");
-      launch_var_mul(s, b.vpts, b.jobs, b.jscal, 7 * N, b.v);
-      stage_mark(s, "var_mul");
-      k_pg_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rs, rss, b.fixed + n, b.v,
-                                                   b.out);
-      stage_mark(s, "finish");
-      launches += 6;
+    case OP_PGEN:
       break;
-    }
   }
   CUBBS_CHECK(cudaGetLastError());
   b.launches_per_run = launches;
@@ -1227,31 +1304,28 @@ extern "C" int32_t cubbs_bbs_gpu_bench_device_steps_v2(uint32_t abi, int32_t op,
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     *launches = (int32_t)b.launches_per_run;
-    // one extra untimed replay with per-stage events for the breakdown
+    // one extra untimed replay with per-kernel spans for the breakdown
     StageEvents se;
-    for (int k = 0; k < 16; k++) CUBBS_CHECK(cudaEventCreate(&se.ev[k]));
-    for (int k = 0; k < 2; k++) CUBBS_CHECK(cudaEventCreate(&se.side[k]));
+    for (int k = 0; k < 16; k++) {
+      CUBBS_CHECK(cudaEventCreate(&se.a[k]));
+      CUBBS_CHECK(cudaEventCreate(&se.b[k]));
+    }
     g_stages = &se;
     CUBBS_CHECK(cudaMemsetAsync(flush, 0x5a, FLUSH, rt.stream));
     run(rt, b, mapdst);
     g_stages = nullptr;
     CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
-    g_stage_count = se.used > 0 ? se.used - 1 : 0;
-    for (int k = 1; k < se.used; k++) {
+    g_stage_count = se.used;
+    for (int k = 0; k < se.used; k++) {
       float ms = 0;
-      cudaEventElapsedTime(&ms, se.ev[k - 1], se.ev[k]);
-      g_stage_ms[k - 1] = ms;
-      std::snprintf(g_stage_names[k - 1], 32, "%s", se.name[k]);
+      CUBBS_CHECK(cudaEventElapsedTime(&ms, se.a[k], se.b[k]));
+      g_stage_ms[k] = ms;
+      std::snprintf(g_stage_names[k], 32, "%s", se.name[k]);
     }
-    if (se.side_used && g_stage_count < 16) {  // stream-2 kernel, reported after the main-stream stages
-      float ms = 0;
-      cudaEventElapsedTime(&ms, se.side[0], se.side[1]);
-      g_stage_ms[g_stage_count] = ms;
-      std::snprintf(g_stage_names[g_stage_count], 32, "%s", "pairing_kernel");
-      g_stage_count++;
+    for (int k = 0; k < 16; k++) {
+      cudaEventDestroy(se.a[k]);
+      cudaEventDestroy(se.b[k]);
     }
-    for (int k = 0; k < 16; k++) cudaEventDestroy(se.ev[k]);
-    for (int k = 0; k < 2; k++) cudaEventDestroy(se.side[k]);
     if (op == 1 || op == 3) {
       download_bool(rt, b, results);
     } else {

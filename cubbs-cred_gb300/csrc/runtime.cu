@@ -205,6 +205,9 @@ Runtime::Runtime(SharedState &s)
   CUBBS_CHECK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
+  CUBBS_CHECK(cudaStreamCreateWithFlags(&stream3, cudaStreamNonBlocking));
+  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_mid, cudaEventDisableTiming));
+  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_side, cudaEventDisableTiming));
   arena.reserve((size_t)256 << 20);
   staging.reserve((size_t)64 << 20);
 }

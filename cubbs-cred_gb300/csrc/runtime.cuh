@@ -146,8 +146,9 @@ struct Runtime {
   FixedTable &table;
   int &table_w;
   line2 *&d_lines;
-  cudaStream_t stream = nullptr, stream2 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;  // stream -> stream2 -> stream
+  cudaStream_t stream = nullptr, stream2 = nullptr, stream3 = nullptr;
+  // stream -> stream2 (ev_fork), stream2 -> stream3 (ev_mid), back to stream (ev_side, ev_join)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_mid = nullptr, ev_side = nullptr;
   DeviceArena arena;
   HostStaging staging;
   std::shared_lock<std::shared_mutex> *lock = nullptr;  // the running call's shared hold
