@@ -622,7 +622,8 @@ def pairing_eq_aggregate(reqs):
 
 
 def fp_op_for_test(op, a_list, b_list):
-    """Device Fp op (0 mul, 1 inverse, 2 sqrt, 3 variable-time inverse) on 48-byte BE canonical inputs."""
+    """Device Fp op (0 mul, 1 inverse, 2 sqrt, 3 variable-time inverse, 4 CIOS mul) on
+    48-byte BE canonical inputs."""
     n = len(a_list)
     a = ctypes.create_string_buffer(b"".join(a_list), max(1, 48 * n))
     b = ctypes.create_string_buffer(b"".join(b_list), max(1, 48 * n))

@@ -54,7 +54,7 @@ DEV g1 zabs_unrolled_bits(g1 p) {
 }
 
 // op 0: Fp product of canonical BE inputs; op 1: Fp inverse; op 2: Fp sqrt (0 if none);
-// op 3: variable-time Fp inverse
+// op 3: variable-time Fp inverse; op 4: Fp product by CIOS carry chains
 __global__ void k_fp_test(const uint8_t *a, const uint8_t *b, uint32_t n, int op, uint8_t *out, int32_t *st) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -62,6 +62,7 @@ __global__ void k_fp_test(const uint8_t *a, const uint8_t *b, uint32_t n, int op
   bool ok = fp_from_be48(a + 48 * (size_t)i, x) && fp_from_be48(b + 48 * (size_t)i, y);
   if (ok) {
     if (op == 0) r = fp_mul(x, y);
+    else if (op == 4) r = fp_mul_cios(x, y);
     else if (op == 1) r = fp_inv(x);
     else if (op == 3) r = fp_inv_vartime(x);
     else ok = fp_sqrt(x, r);
@@ -198,6 +199,22 @@ __global__ void __launch_bounds__(256) k_fpmul_rate(fp *out, uint32_t iters) {
   if (fp_is_zero(a) && fp_is_zero(b) && fp_is_zero(c) && fp_is_zero(d)) out[0] = a;
 }
 
+// CIOS products per second (same shape as k_fpmul_rate).
+__global__ void __launch_bounds__(256) k_fpmul_cios_rate(fp *out, uint32_t iters) {
+  fp a = fp_one(), b = fp_one(), c = fp_one(), d = fp_one();
+  a.w[0] += threadIdx.x; b.w[1] += blockIdx.x; c.w[2] += 3; d.w[3] += 5;
+  fp k = fp_one();
+  k.w[4] ^= threadIdx.x * 7u;
+#pragma unroll 1
+  for (uint32_t it = 0; it < iters; it++) {
+    a = fp_mul_cios(a, k);
+    b = fp_mul_cios(b, k);
+    c = fp_mul_cios(c, k);
+    d = fp_mul_cios(d, k);
+  }
+  if (fp_is_zero(a) && fp_is_zero(b) && fp_is_zero(c) && fp_is_zero(d)) out[0] = a;
+}
+
 // Code-size variants of the Fp product for the latency probe.
 DEVNI fp fp_mul_call(fp a, fp b) { return fp_mul_inl(a, b); }
 DEV fp fp_mul_rolled(const fp &a, fp b) {
@@ -235,6 +252,7 @@ DEV fp fp_mul_rolled(const fp &a, fp b) {
   }
 G1_DBL_WITH(g1_dbl_call, fp_mul_call)
 G1_DBL_WITH(g1_dbl_rolled, fp_mul_rolled)
+G1_DBL_WITH(g1_dbl_cios, fp_mul_cios)
 
 // Single-warp latency of dependent chains, in SM cycles per operation
 // (clock64 around n iterations; every lane runs the same chain).
@@ -245,6 +263,8 @@ G1_DBL_WITH(g1_dbl_rolled, fp_mul_rolled)
 //   16 inlined fp_mul   17 three independent inlined fp_mul chains
 //   18/19 out-of-line fp_mul (1 / 3 chains)   20/21 rolled-loop fp_mul (1 / 3 chains)
 //   22 g1_dbl over out-of-line fp_mul   23 g1_dbl over rolled fp_mul
+//   24/25 CIOS fp_mul out of line (1 / 3 chains)   26 CIOS inlined
+//   27 g1_dbl over CIOS fp_mul
 __global__ void __launch_bounds__(32) k_latency_probe(double *cyc, fp *sink, uint32_t n) {
   fp a = fp_one(), b = fp_one(), c = fp_one(), k = fp_one();
   a.w[0] += threadIdx.x + 3;
@@ -262,7 +282,7 @@ __global__ void __launch_bounds__(32) k_latency_probe(double *cyc, fp *sink, uin
   fr s = fr_one(), sk = fr_one();
   sk.w[1] ^= 0x1234u;
   long long t0, t1;
-  const int R = 24;
+  const int R = 28;
   double res[R];
 #define LAT(IDX, ITERS, BODY)                          \
   t0 = clock64();                                      \
@@ -293,6 +313,10 @@ __global__ void __launch_bounds__(32) k_latency_probe(double *cyc, fp *sink, uin
   LAT(21, n, a = fp_mul_rolled(a, k); b = fp_mul_rolled(b, k); c = fp_mul_rolled(c, k));
   LAT(22, n / 4, P = g1_dbl_call(P));
   LAT(23, n / 4, P = g1_dbl_rolled(P));
+  LAT(24, n, a = fp_mul_cios(a, k));
+  LAT(25, n, a = fp_mul_cios(a, k); b = fp_mul_cios(b, k); c = fp_mul_cios(c, k));
+  LAT(26, n, a = fp_mul_cios_inl(a, k));
+  LAT(27, n / 4, P = g1_dbl_cios(P));
 #undef LAT
   if (threadIdx.x == 0)
     for (int i = 0; i < R; i++) cyc[i] = res[i];
@@ -305,20 +329,59 @@ __global__ void __launch_bounds__(32) k_latency_probe(double *cyc, fp *sink, uin
 // Fills cycles[0..cap) with the per-operation latencies of k_latency_probe;
 // returns how many were written.
 extern "C" int32_t cubbs_bbs_gpu_latency_probe_for_test_v2(double *cycles, int32_t cap) {
-  if (!cycles || cap < 24) return -1;
+  if (!cycles || cap < 28) return -1;
   try {
     CallScope scope;
     Runtime &rt = scope.rt;
-    double *d = rt.arena.alloc<double>(24);
+    double *d = rt.arena.alloc<double>(28);
     fp *sink = rt.arena.alloc<fp>(32);
     k_latency_probe<<<1, 32, 0, rt.stream>>>(d, sink, 64);  // warm-up
     k_latency_probe<<<1, 32, 0, rt.stream>>>(d, sink, 512);
     CUBBS_CHECK(cudaGetLastError());
-    CUBBS_CHECK(cudaMemcpyAsync(cycles, d, 24 * sizeof(double), cudaMemcpyDeviceToHost, rt.stream));
+    CUBBS_CHECK(cudaMemcpyAsync(cycles, d, 28 * sizeof(double), cudaMemcpyDeviceToHost, rt.stream));
     CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
-    return 24;
+    return 28;
   } catch (const CudaError &) {
     return -2;
+  }
+}
+
+// Fp products per second (1e9) of the carry-save product (fp_mul) and the
+// CIOS product with `wps[k]` warps per SM (blocks of 32 threads,
+// sm_count * wps[k] blocks): rates[2k] carry-save, rates[2k + 1] CIOS.
+extern "C" int32_t cubbs_bbs_gpu_fpmul_rates_for_test_v2(const int32_t *wps, int32_t n, double *rates) {
+  if (!wps || !rates || n <= 0 || n > 8) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  for (int k = 0; k < n; k++)
+    if (wps[k] < 1 || wps[k] > 64) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  try {
+    CallScope scope;
+    Runtime &rt = scope.rt;
+    fp *of = rt.arena.alloc<fp>(1);
+    cudaEvent_t e0, e1;
+    CUBBS_CHECK(cudaEventCreate(&e0));
+    CUBBS_CHECK(cudaEventCreate(&e1));
+    const uint32_t iters = 128;
+    for (int k = 0; k < n; k++) {
+      const int blocks = rt.sm_count * wps[k];
+      for (int v = 0; v < 2; v++) {
+        for (int rep = 0; rep < 2; rep++) {  // the first run is a warm-up
+          CUBBS_CHECK(cudaEventRecord(e0, rt.stream));
+          if (v == 0) k_fpmul_rate<<<blocks, 32, 0, rt.stream>>>(of, iters);
+          else k_fpmul_cios_rate<<<blocks, 32, 0, rt.stream>>>(of, iters);
+          CUBBS_CHECK(cudaEventRecord(e1, rt.stream));
+          CUBBS_CHECK(cudaEventSynchronize(e1));
+        }
+        float ms = 0;
+        CUBBS_CHECK(cudaEventElapsedTime(&ms, e0, e1));
+        rates[2 * k + v] = (double)blocks * 32 * iters * 4 / (ms * 1e-3) / 1e9;
+      }
+    }
+    CUBBS_CHECK(cudaGetLastError());
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return 0;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
   }
 }
 

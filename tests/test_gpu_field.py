@@ -17,6 +17,17 @@ def test_fp_mul(gpu, oracle):
     assert [g[1] for g in got] == [oracle.fp_mul(x, y) for x, y in zip(a, b)]
 
 
+def test_fp_mul_carry_save(gpu, oracle):
+    """The carry-save product (fp_mul) equals the CIOS product and the oracle, edge operands included."""
+    edge = [oracle.P_MOD - 1, oracle.P_MOD - 2, 1, 0, 2, (1 << 380) % oracle.P_MOD, (1 << 352) - 1]
+    a = rand_fp(oracle, b"csa", 2048) + [x.to_bytes(48, "big") for x in edge for _ in edge]
+    b = rand_fp(oracle, b"csb", 2048) + [y.to_bytes(48, "big") for _ in edge for y in edge]
+    cs = gpu.fp_op_for_test(0, a, b)
+    cios = gpu.fp_op_for_test(4, a, b)
+    assert [g[1] for g in cs] == [g[1] for g in cios]
+    assert [g[1] for g in cs] == [oracle.fp_mul(x, y) for x, y in zip(a, b)]
+
+
 def test_fp_inv_sqrt(gpu, oracle):
     a = rand_fp(oracle, b"inv", 16)
     inv = gpu.fp_op_for_test(1, a, a)
