@@ -139,6 +139,48 @@ def gen_field(name, mod, n):
     return "\n".join(out)
 
 
+def gen_lazy(name, mod, n):
+    """Unreduced sums for short signed sums of reduced values (at most 6 terms
+    of [0, mod], so every partial sum stays below 6 mod < 2^(32n)):
+    {name}_acc_add (plain add), {name}_from_mod (mod - a) and {name}_csub{k}
+    (subtract k*mod when the value is at least k*mod, k = 4, 2, 1), which bring
+    a value below 8 mod back to [0, mod)."""
+    assert 6 * mod < 1 << (32 * n)
+    out = []
+    w = out.append
+    outs = ", ".join(f'"=&r"(r[{i}])' for i in range(n))
+    ins2 = ", ".join(f'"r"(a[{i}])' for i in range(n)) + ", " + ", ".join(f'"r"(b[{i}])' for i in range(n))
+    ins1 = ", ".join(f'"r"(a[{i}])' for i in range(n))
+    body = [f"add.cc.u32 %0, %{n}, %{2 * n};"]
+    for j in range(1, n):
+        body.append(f"add{'c.cc' if j < n - 1 else 'c'}.u32 %{j}, %{n + j}, %{2 * n + j};")
+    w(f"__device__ __forceinline__ void {name}_acc_add(uint32_t *r, const uint32_t *a, const uint32_t *b) {{")
+    w(f'  asm("' + "\\n\\t".join(body) + f'" : {outs} : {ins2});')
+    w("}")
+    ml = limbs(mod, n)
+    body = [f"sub.cc.u32 %0, 0x{ml[0]:08x}, %{n};"]
+    for j in range(1, n):
+        body.append(f"sub{'c.cc' if j < n - 1 else 'c'}.u32 %{j}, 0x{ml[j]:08x}, %{n + j};")
+    w(f"__device__ __forceinline__ void {name}_from_mod(uint32_t *r, const uint32_t *a) {{")
+    w(f'  asm("' + "\\n\\t".join(body) + f'" : {outs} : {ins1});')
+    w("}")
+    for k in (4, 2, 1):
+        kl = limbs(k * mod, n)
+        body = ["{ .reg .u32 d<%d>; .reg .u32 bw; .reg .pred ge;" % n, f"sub.cc.u32 d0, %{n}, 0x{kl[0]:08x};"]
+        for j in range(1, n):
+            body.append(f"subc.cc.u32 d{j}, %{n + j}, 0x{kl[j]:08x};")
+        body.append("subc.u32 bw, 0, 0;")
+        body.append("setp.eq.u32 ge, bw, 0;")
+        for j in range(n):
+            body.append(f"selp.u32 %{j}, d{j}, %{n + j}, ge;")
+        body.append("}")
+        w(f"__device__ __forceinline__ void {name}_csub{k}(uint32_t *r, const uint32_t *a) {{")
+        w(f'  asm("' + "\\n\\t".join(body) + f'" : {outs} : {ins1});')
+        w("}")
+    w("")
+    return "\n".join(out)
+
+
 def main():
     text = [
         "// GENERATED by gen_field_ptx.py -- do not edit by hand.",
@@ -147,6 +189,7 @@ def main():
         "#include <stdint.h>",
         "",
         gen_field("fp", P, 12),
+        gen_lazy("fp", P, 12),
         gen_field("fr", R, 8),
     ]
     dst = pathlib.Path(__file__).with_name("field_ptx.cuh")
