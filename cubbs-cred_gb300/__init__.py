@@ -660,6 +660,22 @@ def g1_op_for_test(points, scalars):
     return [(st[i], xy.raw[96 * i:96 * i + 96], kp.raw[48 * i:48 * i + 48], diag[i], chain[i]) for i in range(n)]
 
 
+def g1_subgroup_for_test(points):
+    """Unchecked device decode plus the separate subgroup kernel -> [(decode status, outside G1)]."""
+    n = len(points)
+    p = ctypes.create_string_buffer(b"".join(points), max(1, 48 * n))
+    st = (ctypes.c_int32 * max(1, n))()
+    out = (ctypes.c_int32 * max(1, n))()
+    fn = lib().cubbs_bbs_gpu_g1_subgroup_for_test_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
+    rc = fn(ABI_VERSION, ctypes.cast(p, ctypes.c_void_p), n, ctypes.cast(st, ctypes.c_void_p),
+            ctypes.cast(out, ctypes.c_void_p))
+    if rc:
+        raise RuntimeError(f"g1_subgroup_for_test returned {rc}")
+    return [(st[i], out[i]) for i in range(n)]
+
+
 # --------------------------------------------------------------------------- benchmark helpers
 OP_SIGN, OP_VERIFY, OP_PROOF_GEN, OP_PROOF_VERIFY = 0, 1, 2, 3
 

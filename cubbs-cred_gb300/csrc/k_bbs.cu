@@ -164,13 +164,14 @@ __global__ void __launch_bounds__(128) k_pv_pairjobs(const PvItem *items0, uint3
 
 // T1, T2 -> compressed; recompute the challenge (a mismatch marks the item invalid).
 __global__ void __launch_bounds__(64) k_pv_finish(PvItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
-                                                  const fr *domain, const int32_t *dec_status, const g1 *t2fix,
-                                                  const g1 *v) {
+                                                  const fr *domain, const int32_t *dec_status,
+                                                  const int32_t *outside_g1, const g1 *t2fix, const g1 *v) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   PvItem it = items[i];
   if (it.status != ST_OK) return;
-  if (dec_status[3 * i] == DEC_BAD || dec_status[3 * i + 1] == DEC_BAD || dec_status[3 * i + 2] == DEC_BAD) {
+  if (dec_status[3 * i] == DEC_BAD || dec_status[3 * i + 1] == DEC_BAD || dec_status[3 * i + 2] == DEC_BAD ||
+      outside_g1[3 * i] || outside_g1[3 * i + 1] || outside_g1[3 * i + 2]) {
     items[i].status = ST_INVALID;
     return;
   }
@@ -588,7 +589,7 @@ struct OpBatch {
   uint32_t *nterms = nullptr;
   VarJob *jobs = nullptr;
   g1a *pts = nullptr, *vpts = nullptr;
-  int32_t *dec = nullptr;
+  int32_t *dec = nullptr, *sub = nullptr;  // decode status; 1 = decoded outside G1 (ProofVerify)
   g1 *fixed = nullptr, *v = nullptr;
   PairJob *pj = nullptr;
   uint8_t *ok = nullptr, *out = nullptr;
@@ -621,7 +622,7 @@ void upload(Runtime &rt, OpBatch &b) {
   size_t need = 65536 + 2 * b.blob.b.size() + b.ml.bytes.size() + 8 * nm + nm * sizeof(fr) + b.pts48.size() +
                 n * (b.item_size * 2 + sizeof(DomainJob) + 2 * sizeof(fr) + sizeof(PairJob) + 256) +
                 fr_rows * sizeof(fr) + 2 * n * sizeof(uint32_t) + nv * (sizeof(VarJob) + sizeof(fr) + sizeof(g1)) +
-                (b.pts48.size() / 48) * (sizeof(g1a) + 4) + 2 * n * sizeof(g1) + 2 * n * sizeof(g1a) +
+                (b.pts48.size() / 48) * (sizeof(g1a) + 8) + 2 * n * sizeof(g1) + 2 * n * sizeof(g1a) +
                 n * b.rs_stride * sizeof(fr) + b.out_total + 64 * 256;
   rt.arena.reserve(need);
   rt.staging.reserve(65536 + 2 * b.blob.b.size() + b.ml.bytes.size() + 8 * nm + b.pts48.size() +
@@ -639,6 +640,7 @@ void upload(Runtime &rt, OpBatch &b) {
   size_t npts = b.pts48.size() / 48;
   b.pts = rt.arena.alloc<g1a>(npts ? npts : 1);
   b.dec = rt.arena.alloc<int32_t>(npts ? npts : 1);
+  b.sub = rt.arena.alloc<int32_t>(npts ? npts : 1);
   b.ddj = upload(rt, b.dj.data(), n);
   b.domain = rt.arena.alloc<fr>(n);
   b.ditems0 = upload(rt, b.items.data(), b.items.size());
@@ -685,11 +687,14 @@ void span_end(cudaStream_t s, int k, const char *name) {
     span_end(stream, _k, label);          \
   } while (0)
 
-// ProofVerify on three streams.  Decoding Abar, Bbar, D (stream2) is
+// ProofVerify on four streams.  Decoding Abar, Bbar, D (stream2) is
 // independent of the message hash, the domain and the T2 fixed-base MSM
 // (stream); the variable-base terms follow the decode on stream2 and the
-// pairing follows it on stream3.  Each of these kernels fills only part of the
-// GPU, so running them side by side shortens the step.
+// pairing follows it on stream3.  The decode leaves out the subgroup check,
+// which runs on stream4 beside the pairing and the variable-base terms: those
+// need only the affine points, and the challenge kernel rejects every proof
+// with a point outside G1 before any result is read.  Each of these kernels
+// fills only part of the GPU, so running them side by side shortens the step.
 void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   cudaStream_t s = rt.stream, s2 = rt.stream2, s3 = rt.stream3;
   size_t n = b.n, nm = b.ml.count(), npts = b.pts48.size() / 48;
@@ -698,8 +703,11 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   const PvItem *it0 = reinterpret_cast<const PvItem *>(b.ditems0);
   CUBBS_CHECK(cudaEventRecord(rt.ev_fork, s));
   CUBBS_CHECK(cudaStreamWaitEvent(s2, rt.ev_fork, 0));
-  SPAN(s2, "g1_decode", launch_g1_decode(s2, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, true));
+  SPAN(s2, "g1_decode", launch_g1_decode(s2, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, false));
   CUBBS_CHECK(cudaEventRecord(rt.ev_mid, s2));
+  CUBBS_CHECK(cudaStreamWaitEvent(rt.stream4, rt.ev_mid, 0));
+  SPAN(rt.stream4, "g1_subgroup", launch_g1_subgroup(rt.stream4, b.pts, b.dec, (uint32_t)npts, b.sub));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_sub, rt.stream4));
   CUBBS_CHECK(cudaStreamWaitEvent(s3, rt.ev_mid, 0));
   SPAN(s3, "pairing_kernel",
        k_pv_pairjobs<<<blocks_for(n, 128), 128, 0, s3>>>(it0, N, b.pts, b.dec, b.pj);
@@ -719,10 +727,11 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
        k_pv_rows<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms));
   SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_side, 0));
+  CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_sub, 0));
   SPAN(s, "challenge",
-       k_pv_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.fixed, b.v));
+       k_pv_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.sub, b.fixed, b.v));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_join, 0));
-  b.launches_per_run = (nm ? 1 : 0) + (npts ? 1 : 0) + 8;
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 8;
 }
 
 // ProofGen on three streams: the signature decode (stream3) and the blinding

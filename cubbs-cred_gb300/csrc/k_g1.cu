@@ -155,6 +155,16 @@ __global__ void __launch_bounds__(128) k_g1_compress(const g1 *pts, uint32_t n, 
   for (int k = 0; k < 48; k++) out[48 * (size_t)i + k] = b[k];
 }
 
+// Subgroup check of points decoded without it: bad[i] = 1 when point i
+// decoded to an affine point outside G1 (status DEC_OK), else 0.
+__global__ void __launch_bounds__(32) k_g1_subgroup(const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  bad[i] = (status[i] == DEC_OK && !g1_in_subgroup(pts[i])) ? 1 : 0;
+}
+void launch_g1_subgroup(cudaStream_t s, const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad) {
+  if (n) k_g1_subgroup<<<blocks_for(n, 32), 32, 0, s>>>(pts, status, n, bad);
+}
 void launch_g1_decode(cudaStream_t s, const uint8_t *pts48, uint32_t stride, uint32_t n, g1a *out, int32_t *status,
                       bool check_subgroup) {
   if (n) k_g1_decode<<<blocks_for(n, 128), 128, 0, s>>>(pts48, stride, n, out, status, check_subgroup);

@@ -161,6 +161,32 @@ extern "C" int32_t cubbs_bbs_gpu_g1_op_for_test_v2(uint32_t abi, const uint8_t *
   return run_test(1, 0, pts48, k32, n, xy96, kp48, status);
 }
 
+// Decode without the subgroup check, then the separate subgroup kernel (the
+// ProofVerify split): status[i] = decode status, outside[i] = 1 when point i
+// decoded to a point outside G1.
+extern "C" int32_t cubbs_bbs_gpu_g1_subgroup_for_test_v2(uint32_t abi, const uint8_t *pts48, size_t n,
+                                                         int32_t *status, int32_t *outside) {
+  if (abi != CUBBS_BBS_GPU_ABI_VERSION || n == 0 || !pts48 || !status || !outside)
+    return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  try {
+    CallScope scope;
+    Runtime &rt = scope.rt;
+    uint8_t *d = rt.arena.alloc<uint8_t>(48 * n);
+    g1a *pts = rt.arena.alloc<g1a>(n);
+    int32_t *st = rt.arena.alloc<int32_t>(n), *bad = rt.arena.alloc<int32_t>(n);
+    CUBBS_CHECK(cudaMemcpyAsync(d, pts48, 48 * n, cudaMemcpyHostToDevice, rt.stream));
+    launch_g1_decode(rt.stream, d, 48, (uint32_t)n, pts, st, false);
+    launch_g1_subgroup(rt.stream, pts, st, (uint32_t)n, bad);
+    CUBBS_CHECK(cudaGetLastError());
+    CUBBS_CHECK(cudaMemcpyAsync(status, st, 4 * n, cudaMemcpyDeviceToHost, rt.stream));
+    CUBBS_CHECK(cudaMemcpyAsync(outside, bad, 4 * n, cudaMemcpyDeviceToHost, rt.stream));
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    return 0;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}
+
 // ------------------------------------------------------------------------- integer-pipe peak
 // Peak 32-bit multiply-add throughput: every thread runs 16 independent
 // mad.lo chains (no carries), so issue rate, not latency, bounds the kernel.

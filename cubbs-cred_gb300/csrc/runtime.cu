@@ -208,6 +208,8 @@ Runtime::Runtime(SharedState &s)
   CUBBS_CHECK(cudaStreamCreateWithFlags(&stream3, cudaStreamNonBlocking));
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_mid, cudaEventDisableTiming));
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_side, cudaEventDisableTiming));
+  CUBBS_CHECK(cudaStreamCreateWithFlags(&stream4, cudaStreamNonBlocking));
+  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_sub, cudaEventDisableTiming));
   arena.reserve((size_t)256 << 20);
   staging.reserve((size_t)64 << 20);
 }

@@ -146,9 +146,10 @@ struct Runtime {
   FixedTable &table;
   int &table_w;
   line2 *&d_lines;
-  cudaStream_t stream = nullptr, stream2 = nullptr, stream3 = nullptr;
-  // stream -> stream2 (ev_fork), stream2 -> stream3 (ev_mid), back to stream (ev_side, ev_join)
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_mid = nullptr, ev_side = nullptr;
+  cudaStream_t stream = nullptr, stream2 = nullptr, stream3 = nullptr, stream4 = nullptr;
+  // stream -> stream2 (ev_fork), stream2 -> stream3, stream4 (ev_mid), back to stream
+  // (ev_side, ev_join, ev_sub)
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_mid = nullptr, ev_side = nullptr, ev_sub = nullptr;
   DeviceArena arena;
   HostStaging staging;
   std::shared_lock<std::shared_mutex> *lock = nullptr;  // the running call's shared hold
@@ -200,6 +201,7 @@ void launch_decode_p1(cudaStream_t s, g1a *gens, uint8_t *gens_c);
 void launch_build_table(cudaStream_t s, const g1a *gens, int g0, int g1n, FixedTable t, g1 *scratch_xyzz,
                         fp *scratch_prod);
 // decode N compressed G1 points: status DEC_*; affine out
+void launch_g1_subgroup(cudaStream_t s, const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad);
 void launch_g1_decode(cudaStream_t s, const uint8_t *pts48, uint32_t stride, uint32_t n, g1a *out,
                       int32_t *status, bool check_subgroup);
 // fixed-base MSM rows: scalars raw Fr [row * stride + g] for g < nterms[row]

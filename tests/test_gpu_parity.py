@@ -177,6 +177,54 @@ def test_proof_verify_tampered(gpu, oracle):
     assert want[-2] is True and not any(want[:4])
 
 
+def _on_curve_outside_g1(oracle, tag):
+    """Compressed encoding of a point of E(Fp): y^2 = x^3 + 4 whose x comes from a
+    hash; such a point lies in G1 with probability 1/h, h ~ 2^126."""
+    P = oracle.P_MOD
+    ctr = 0
+    while True:
+        x = int.from_bytes(drbg(b"non-g1", tag, ctr, 64), "big") % P
+        ctr += 1
+        rhs = (x * x * x + 4) % P
+        y = pow(rhs, (P + 1) // 4, P)
+        if y * y % P == rhs:
+            b = bytearray(x.to_bytes(48, "big"))
+            b[0] |= 0x80 | (0x20 if y > P - y else 0)
+            return bytes(b)
+
+
+def test_proof_verify_rejects_points_outside_g1(gpu, oracle):
+    """Abar, Bbar or D on the curve but outside G1: rejected like the oracle does."""
+    seed = b"proof-non-g1"
+    sk, pk = keypair(oracle, seed)
+    msgs = messages(seed, 0, 16, 32)
+    sig = oracle.sign(sk, pk, b"h", msgs)[0]
+    di = [0, 4, 9]
+    proof = oracle.proof_gen(pk, sig, b"h", b"p", msgs, di, seed=b"g" * 32)
+    dm = [msgs[j] for j in di]
+    bad = [proof[:48 * k] + _on_curve_outside_g1(oracle, b"%d" % k) + proof[48 * (k + 1):] for k in range(3)]
+    reqs = [(pk, f, b"h", b"p", dm, di, 16) for f in bad + [proof]]
+    got = [v for _, v in gpu.proof_verify_batch(reqs)]
+    want = [oracle.proof_verify(pk, f, b"h", b"p", dm, di) == 0 for f in bad + [proof]]
+    assert want == [False, False, False, True]
+    assert got == want
+
+
+def test_split_subgroup_check(gpu, golden, oracle):
+    """The unchecked decode plus the separate subgroup kernel used by ProofVerify:
+    G1 points pass, curve points outside G1 are flagged, undecodable ones fail decode."""
+    g = golden["generators"]
+    in_g1 = [h(x) for x in [g["P1"], g["Q1"]] + g["MsgGenerators"]]
+    sk, pk = keypair(oracle, b"subgroup")
+    in_g1 += [oracle.sign(sk, pk, b"", messages(b"subgroup", i, 3, 32))[0][:48] for i in range(4)]
+    outside = [_on_curve_outside_g1(oracle, b"s%d" % i) for i in range(8)]
+    undecodable = [bytes([in_g1[0][0] ^ 0x01]) + in_g1[0][1:]]
+    got = gpu.g1_subgroup_for_test(in_g1 + outside + undecodable)
+    assert got[:len(in_g1)] == [(0, 0)] * len(in_g1)
+    assert got[len(in_g1):len(in_g1) + len(outside)] == [(0, 1)] * len(outside)
+    assert got[-1][0] == 2 and got[-1][1] == 0
+
+
 def test_sign_e_resident(gpu, oracle):
     import ctypes
     seed = b"sign-e"
