@@ -161,6 +161,27 @@ DEV bool g1_in_subgroup(g1a a) {
   return fp_eq(t.X, fp_mul(bx, t.ZZ)) && fp_eq(t.Y, fp_mul(ny, t.ZZZ));
 }
 
+// Warp-wide sum of one XYZZ point per lane (the result is valid on lane 0).
+DEV g1 shfl_down_g1(const g1 &p, int delta) {
+  g1 r;
+#pragma unroll
+  for (int i = 0; i < 12; i++) {
+    r.X.w[i] = __shfl_down_sync(0xffffffffu, p.X.w[i], delta);
+    r.Y.w[i] = __shfl_down_sync(0xffffffffu, p.Y.w[i], delta);
+    r.ZZ.w[i] = __shfl_down_sync(0xffffffffu, p.ZZ.w[i], delta);
+    r.ZZZ.w[i] = __shfl_down_sync(0xffffffffu, p.ZZZ.w[i], delta);
+  }
+  return r;
+}
+DEV g1 warp_sum_g1(g1 acc) {
+  #pragma unroll 1
+  for (int d = 16; d > 0; d >>= 1) {
+    g1 o = shfl_down_g1(acc, d);
+    acc = g1_add(acc, o);
+  }
+  return acc;
+}
+
 // Decode status values
 #define DEC_OK 0
 #define DEC_INF 1

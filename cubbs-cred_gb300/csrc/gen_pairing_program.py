@@ -677,14 +677,17 @@ def emit(progs):
         for ptype, entries in p.phases:
             types.append(ptype)
             row = []
+            # every lane of a LIN phase runs the phase's largest term count;
+            # shorter sums are padded with the zero slot
+            width = max((len(a) for _, op, a in entries if op == "lin"), default=0)
             for l in range(LANES):
-                u = [NONE, ptype << 8, 0, 0, 0, 0, 0, 0]
+                u = [NONE, ptype << 8 | width, 0, 0, 0, 0, 0, 0]
                 if l < len(entries):
                     out, op, args = entries[l]
                     u[0] = out
                     if op == "lin":
-                        u[1] |= len(args)
-                        for t, (sg, sl) in enumerate(args):
+                        padded = list(args) + [(1, ZERO_SLOT)] * (width - len(args))
+                        for t, (sg, sl) in enumerate(padded):
                             assert sl < 0x8000
                             u[2 + t] = sl | (0x8000 if sg < 0 else 0)
                     else:
@@ -696,7 +699,8 @@ def emit(progs):
     first.append(len(types))
     lines.append("#define PP_NPHASE %d" % len(types))
     lines.append("__device__ const uint16_t PP_PROG_FIRST[PP_NPROG + 1] = {" + ", ".join(map(str, first)) + "};")
-    lines.append("// entry per (phase, lane): u16 out (PP_NONE: idle lane), u16 phase type << 8 | term count,")
+    lines.append("// entry per (phase, lane): u16 out (PP_NONE: idle lane), u16 phase type << 8 | term count")
+    lines.append("// (LIN: the same count on every lane of the phase, short sums padded with the zero slot),")
     lines.append("// then u16 x 6 terms (LIN; bit 15: subtract) or operand slots (MUL: a, b; INV: a)")
     lines.append("__device__ const uint4 PP_ENTRY[PP_NPHASE * PP_LANES] = {")
     lines += ents

@@ -162,6 +162,139 @@ __global__ void __launch_bounds__(128) k_pv_pairjobs(const PvItem *items0, uint3
   pj[i] = job;
 }
 
+// ---------------------------------------------------------------- aggregated pairing checks
+// Proofs under one public key are checked together, as the reference's GPU
+// engine does for ProofVerify batches of 128 or more
+// (crates/cubbs-bbs/src/gpu_engine.rs:2095-2108, execution.rs:3797-3801;
+// protocol form core_proof_pairing_verify_batch, proof.rs:2656-2710): with
+// random coefficients rho_i,
+//     e(sum rho_i Abar_i, PK) * e(sum rho_i Bbar_i, -P2) == 1
+// holds for a group whose items all pass their own check, and fails with
+// probability at least 1 - 2^-63 when one item of the group fails its own
+// check.  rho_i = a_i + b_i lambda with a_i in [2^31, 2^32), b_i in [0, 2^32)
+// drawn per call from OS randomness (lambda = z^2 is the eigenvalue of the GLV
+// endomorphism, so the 2^63 values are distinct below r, and
+// rho_i P = a_i P + b_i phi(P) costs 31 doublings); every pairing value lies in
+// the order-r subgroup of Fp12*.  A group that fails is checked item by item,
+// so every item's result equals its own check.
+struct AggSeed {
+  uint32_t w[8];
+};
+
+// (a_i, b_i) = the first 8 bytes of SHA-256(seed || I2OSP(i, 4)), big-endian,
+// with the top bit of a_i set.
+DEV void agg_rho(const AggSeed &seed, uint32_t i, uint32_t &a, uint32_t &b) {
+  sha_ctx c;
+  sha_init(c);
+  uint8_t m[36];
+  for (int k = 0; k < 8; k++)
+    for (int j = 0; j < 4; j++) m[4 * k + j] = (uint8_t)(seed.w[k] >> (8 * j));
+  for (int j = 0; j < 4; j++) m[32 + j] = (uint8_t)(i >> (24 - 8 * j));
+  sha_bytes(c, m, 36);
+  uint8_t h[32];
+  sha_final(c, h);
+  a = ((uint32_t)h[0] << 24 | (uint32_t)h[1] << 16 | (uint32_t)h[2] << 8 | h[3]) | 0x80000000u;
+  b = (uint32_t)h[4] << 24 | (uint32_t)h[5] << 16 | (uint32_t)h[6] << 8 | h[7];
+}
+
+// a P + b phi(P) for affine P (Shamir's trick over the 32 bits of a and b).
+// Every step adds one of {P, phi(P), P + phi(P)} or nothing and keeps the sum
+// by a select, so lanes with different scalars never diverge.
+DEV g1 g1_mul_rho(const g1a &p, uint32_t a, uint32_t b) {
+  const g1 P = g1_from_aff(p);
+  const g1 E = g1_endo(P);
+  const g1 PE = g1_add(P, E);
+  g1 acc = (b >> 31) ? PE : P;  // bit 31 of a is set
+#pragma unroll 1
+  for (int i = 30; i >= 0; i--) {
+    acc = g1_dbl(acc);
+    const uint32_t sel = ((a >> i) & 1) | (((b >> i) & 1) << 1);
+    const g1 t = sel == 1 ? P : sel == 2 ? E : PE;
+    const g1 sum = g1_add(acc, t);
+    if (sel) acc = sum;
+  }
+  return acc;
+}
+
+// One thread per (item, point): scaled[2i] = rho_i Abar_i, scaled[2i+1] = rho_i Bbar_i
+// for items of an aggregated group whose points decoded (infinity otherwise).
+__global__ void __launch_bounds__(32) k_agg_scale(const PvItem *items0, uint32_t n, const g1a *pts,
+                                                  const int32_t *dec, const int32_t *group_of, AggSeed seed,
+                                                  g1 *scaled) {
+  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= 2 * n) return;
+  const uint32_t i = t >> 1, which = t & 1;
+  const PvItem it = items0[i];
+  bool use = group_of[i] >= 0 && it.status == ST_OK && it.pk_status == DEC_OK;
+  #pragma unroll 1
+  for (int k = 0; k < 3 && use; k++) use = dec[3 * i + k] != DEC_BAD;
+  const int32_t d = dec[3 * i + which];
+  uint32_t ra, rb;
+  agg_rho(seed, i, ra, rb);
+  scaled[t] = (use && d == DEC_OK) ? g1_mul_rho(pts[3 * i + which], ra, rb) : g1_inf();
+}
+
+// Grid (groups, 2): block (g, 0) sums the scaled Abar of group g's items (in
+// perm[goff[g] .. goff[g+1])), block (g, 1) the scaled Bbar; each writes its
+// half of the group's pairing job in affine form (the job's flags start at 0).
+__global__ void __launch_bounds__(512) k_agg_sum(const g1 *scaled, const uint32_t *perm, const uint32_t *goff,
+                                                 const int32_t *gslot, PairJob *gjobs) {
+  __shared__ g1 part[16];
+  const uint32_t g = blockIdx.x, which = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  g1 a = g1_inf();
+  #pragma unroll 1
+  for (uint32_t k = goff[g] + threadIdx.x; k < goff[g + 1]; k += blockDim.x) a = g1_add(a, scaled[2 * perm[k] + which]);
+  a = warp_sum_g1(a);
+  if (lane == 0) part[warp] = a;
+  __syncthreads();
+  if (warp == 0) {
+    a = lane < 16 ? part[lane] : g1_inf();
+    a = warp_sum_g1(a);
+    if (lane == 0) {
+      g1a aff;
+      const bool finite = g1_to_aff(a, aff);
+      PairJob &j = gjobs[g];
+      if (which == 0) {
+        j.pa = aff;
+        j.slot_a = gslot[g];
+        j.slot_b = 0;
+        j.active = 1;
+      } else {
+        j.pb = aff;
+      }
+      if (!finite) atomicOr(&j.flags, which == 0 ? 1u : 2u);
+    }
+  }
+}
+
+// Per-item pairing jobs after the group checks: an item of a group whose check
+// passed is valid for the pairing (ok = 1, job skipped); any other item that
+// decoded gets its own check.
+__global__ void __launch_bounds__(128) k_pv_pairjobs_agg(const PvItem *items0, uint32_t n, const g1a *pts,
+                                                         const int32_t *dec_status, const int32_t *group_of,
+                                                         const uint8_t *group_ok, PairJob *pj, uint8_t *ok) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PvItem it = items0[i];
+  PairJob job;
+  job.slot_a = it.pk_slot < 0 ? 0 : it.pk_slot;
+  job.slot_b = 0;
+  job.pa = pts[3 * i];
+  job.pb = pts[3 * i + 1];
+  job.flags = 0;
+  bool valid = it.status == ST_OK && it.pk_status != DEC_BAD;
+  #pragma unroll 1
+  for (int k = 0; k < 3; k++) valid = valid && dec_status[3 * i + k] != DEC_BAD;
+  job.active = valid ? 1 : 0;
+  if (valid && group_of[i] >= 0 && group_ok[group_of[i]]) {
+    job.active = 2;
+    ok[i] = 1;
+  }
+  if (dec_status[3 * i] == DEC_INF || it.pk_status == DEC_INF) job.flags |= 1;
+  if (dec_status[3 * i + 1] == DEC_INF) job.flags |= 2;
+  pj[i] = job;
+}
+
 // T1, T2 -> compressed; recompute the challenge (a mismatch marks the item invalid).
 __global__ void __launch_bounds__(64) k_pv_finish(PvItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
                                                   const fr *domain, const int32_t *dec_status,
@@ -590,6 +723,14 @@ struct OpBatch {
   VarJob *jobs = nullptr;
   g1a *pts = nullptr, *vpts = nullptr;
   int32_t *dec = nullptr, *sub = nullptr;  // decode status; 1 = decoded outside G1 (ProofVerify)
+  // ProofVerify pairing groups (items under one public key, checked together)
+  std::vector<int32_t> h_group_of, h_gslot;
+  std::vector<uint32_t> h_perm, h_goff;
+  int32_t *group_of = nullptr, *gslot = nullptr;
+  uint32_t *perm = nullptr, *goff = nullptr;
+  PairJob *gjobs = nullptr;
+  uint8_t *gok = nullptr;
+  g1 *scaled = nullptr;
   g1 *fixed = nullptr, *v = nullptr;
   PairJob *pj = nullptr;
   uint8_t *ok = nullptr, *out = nullptr;
@@ -614,6 +755,50 @@ template <typename T> T *upload(Runtime &rt, const T *h, size_t n) {
 size_t vars_per_item(Op op) { return op == OP_PVERIFY ? 4 : op == OP_VERIFY ? 1 : op == OP_PGEN ? 7 : 0; }
 size_t fixed_rows_per_item(Op op) { return op == OP_PGEN ? 2 : 1; }
 
+// Pairing groups of a ProofVerify batch: the items that are well formed so far,
+// by public-key slot; a batch of at least 128 items checks every key with at
+// least 16 items as one group (the reference aggregates batches of 128 or more:
+// crates/cubbs-bbs/src/execution.rs:3797-3801).  Other items are checked alone.
+const size_t AGG_MIN_BATCH = 128, AGG_MIN_GROUP = 16;
+void plan_groups(Runtime &rt, OpBatch &b) {
+  const size_t n = b.n;
+  b.h_group_of.assign(n, -1);
+  b.h_perm.clear();
+  b.h_goff.assign(1, 0);
+  b.h_gslot.clear();
+  if (n >= AGG_MIN_BATCH) {
+    std::unordered_map<int32_t, std::vector<uint32_t>> by_slot;
+    std::vector<int32_t> order;
+    for (size_t i = 0; i < n; i++) {
+      const PvItem &p = reinterpret_cast<const PvItem *>(b.items.data())[i];
+      if (p.status != ST_OK || p.pk_status != DEC_OK) continue;
+      auto &v = by_slot[p.pk_slot];
+      if (v.empty()) order.push_back(p.pk_slot);
+      v.push_back((uint32_t)i);
+    }
+    for (int32_t slot : order) {
+      const auto &v = by_slot[slot];
+      if (v.size() < AGG_MIN_GROUP) continue;
+      for (uint32_t i : v) {
+        b.h_group_of[i] = (int32_t)b.h_gslot.size();
+        b.h_perm.push_back(i);
+      }
+      b.h_gslot.push_back(slot);
+      b.h_goff.push_back((uint32_t)b.h_perm.size());
+    }
+  }
+  const size_t G = b.h_gslot.size();
+  b.group_of = upload(rt, b.h_group_of.data(), n);
+  if (G) {
+    b.perm = upload(rt, b.h_perm.data(), b.h_perm.size());
+    b.goff = upload(rt, b.h_goff.data(), G + 1);
+    b.gslot = upload(rt, b.h_gslot.data(), G);
+    b.gjobs = rt.arena.alloc<PairJob>(G);
+    b.gok = rt.arena.alloc<uint8_t>(G);
+    b.scaled = rt.arena.alloc<g1>(2 * n);
+  }
+}
+
 void upload(Runtime &rt, OpBatch &b) {
   size_t n = b.n, nm = b.ml.count();
   b.stride = b.maxL + 2;
@@ -623,10 +808,11 @@ void upload(Runtime &rt, OpBatch &b) {
                 n * (b.item_size * 2 + sizeof(DomainJob) + 2 * sizeof(fr) + sizeof(PairJob) + 256) +
                 fr_rows * sizeof(fr) + 2 * n * sizeof(uint32_t) + nv * (sizeof(VarJob) + sizeof(fr) + sizeof(g1)) +
                 (b.pts48.size() / 48) * (sizeof(g1a) + 8) + 2 * n * sizeof(g1) + 2 * n * sizeof(g1a) +
-                n * b.rs_stride * sizeof(fr) + b.out_total + 64 * 256;
+                n * b.rs_stride * sizeof(fr) + b.out_total + n * (2 * sizeof(g1) + 16 + sizeof(PairJob) + 8) +
+                64 * 256;
   rt.arena.reserve(need);
   rt.staging.reserve(65536 + 2 * b.blob.b.size() + b.ml.bytes.size() + 8 * nm + b.pts48.size() +
-                     n * (b.item_size + sizeof(DomainJob) + 64));
+                     n * (b.item_size + sizeof(DomainJob) + 96));
   b.dblob = upload(rt, b.blob.b.data(), b.blob.b.size());
   std::vector<uint8_t> flat(8 * nm + b.ml.bytes.size());
   if (nm) {
@@ -656,6 +842,7 @@ void upload(Runtime &rt, OpBatch &b) {
   b.e = rt.arena.alloc<fr>(n);
   b.vpts = rt.arena.alloc<g1a>(2 * n);
   if (b.op == OP_PGEN) b.rs = rt.arena.alloc<fr>(n * b.rs_stride);
+  if (b.op == OP_PVERIFY) plan_groups(rt, b);
   b.out = rt.arena.alloc<uint8_t>(b.out_total + 1);
 }
 
@@ -709,9 +896,29 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   SPAN(rt.stream4, "g1_subgroup", launch_g1_subgroup(rt.stream4, b.pts, b.dec, (uint32_t)npts, b.sub));
   CUBBS_CHECK(cudaEventRecord(rt.ev_sub, rt.stream4));
   CUBBS_CHECK(cudaStreamWaitEvent(s3, rt.ev_mid, 0));
-  SPAN(s3, "pairing_kernel",
-       k_pv_pairjobs<<<blocks_for(n, 128), 128, 0, s3>>>(it0, N, b.pts, b.dec, b.pj);
-       launch_pairing_check(s3, b.pj, N, rt.d_lines, b.ok));
+  const uint32_t G = (uint32_t)b.h_gslot.size();
+  if (G) {
+    AggSeed seed;
+    size_t got = 0;
+    while (got < sizeof(seed)) {
+      ssize_t r = getrandom(reinterpret_cast<uint8_t *>(&seed) + got, sizeof(seed) - got, 0);
+      if (r <= 0) throw CudaError(cudaErrorUnknown, "getrandom");
+      got += (size_t)r;
+    }
+    SPAN(s3, "pairing_aggregate",
+         k_agg_scale<<<blocks_for(2 * n, 32), 32, 0, s3>>>(it0, N, b.pts, b.dec, b.group_of, seed, b.scaled);
+         CUBBS_CHECK(cudaMemsetAsync(b.gjobs, 0, G * sizeof(PairJob), s3));
+         k_agg_sum<<<dim3(G, 2), 512, 0, s3>>>(b.scaled, b.perm, b.goff, b.gslot, b.gjobs);
+         launch_pairing_check(s3, b.gjobs, G, rt.d_lines, b.gok));
+    SPAN(s3, "pairing_kernel",
+         k_pv_pairjobs_agg<<<blocks_for(n, 128), 128, 0, s3>>>(it0, N, b.pts, b.dec, b.group_of, b.gok, b.pj,
+                                                                b.ok);
+         launch_pairing_check(s3, b.pj, N, rt.d_lines, b.ok));
+  } else {
+    SPAN(s3, "pairing_kernel",
+         k_pv_pairjobs<<<blocks_for(n, 128), 128, 0, s3>>>(it0, N, b.pts, b.dec, b.pj);
+         launch_pairing_check(s3, b.pj, N, rt.d_lines, b.ok));
+  }
   CUBBS_CHECK(cudaEventRecord(rt.ev_join, s3));
   SPAN(s2, "var_mul",
        k_pv_jobs<<<blocks_for(n, 128), 128, 0, s2>>>(it0, N, b.dblob, b.dec, b.jobs, b.jscal);
@@ -731,7 +938,7 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   SPAN(s, "challenge",
        k_pv_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.sub, b.fixed, b.v));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_join, 0));
-  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 8;
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 8 + (G ? 3 : 0);
 }
 
 // ProofGen on three streams: the signature decode (stream3) and the blinding

@@ -76,26 +76,6 @@ DEV uint32_t scalar_bits(const fr &s, int pos, int w) {
   return (uint32_t)(v & ((1u << w) - 1));
 }
 
-DEV g1 shfl_down_g1(const g1 &p, int delta) {
-  g1 r;
-#pragma unroll
-  for (int i = 0; i < 12; i++) {
-    r.X.w[i] = __shfl_down_sync(0xffffffffu, p.X.w[i], delta);
-    r.Y.w[i] = __shfl_down_sync(0xffffffffu, p.Y.w[i], delta);
-    r.ZZ.w[i] = __shfl_down_sync(0xffffffffu, p.ZZ.w[i], delta);
-    r.ZZZ.w[i] = __shfl_down_sync(0xffffffffu, p.ZZZ.w[i], delta);
-  }
-  return r;
-}
-DEV g1 warp_sum_g1(g1 acc) {
-  #pragma unroll 1
-  for (int d = 16; d > 0; d >>= 1) {
-    g1 o = shfl_down_g1(acc, d);
-    acc = g1_add(acc, o);
-  }
-  return acc;
-}
-
 // Fixed-base MSM: row r = sum_g scalars[r*stride + g] * G_g, g < nterms[r].
 // One warp per row; lane l takes generators l, l+32, ...; per generator the
 // scalar is recoded into signed w-bit digits on the fly and each nonzero digit

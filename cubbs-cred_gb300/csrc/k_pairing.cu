@@ -48,8 +48,8 @@ __global__ void __launch_bounds__(32) k_pairing_check_warp(const PairJob *jobs, 
   const uint32_t item = blockIdx.x;
   if (item >= n) return;
   const PairJob &j = jobs[item];
-  if (!j.active) {
-    if (lane == 0) ok[item] = 0;
+  if (j.active != 1) {  // 0: not evaluated (result 0); 2: settled before the launch (ok[item] kept)
+    if (lane == 0 && j.active == 0) ok[item] = 0;
     return;
   }
   const bool skip[2] = {(j.flags & 1) != 0, (j.flags & 2) != 0};
@@ -57,6 +57,41 @@ __global__ void __launch_bounds__(32) k_pairing_check_warp(const PairJob *jobs, 
   const g1a P[2] = {j.pa, j.pb};
   const bool one = pp::pairing_check(sl, lane, P, L, skip);
   if (lane == 0) ok[item] = one ? 1 : 0;
+}
+
+// Latency probe: SM cycles of one run of each pairing program on a lone warp
+// (slots filled with Montgomery one; the values do not change the path).
+__global__ void __launch_bounds__(32) k_pp_probe(double *cycles, int reps) {
+  extern __shared__ __align__(16) uint8_t pp_smem[];
+  fp *sl = reinterpret_cast<fp *>(pp_smem);
+  const int lane = threadIdx.x;
+  for (int i = lane; i < PP_SLOTS; i += 32) pp::st(sl, i, fp_one());
+  __syncwarp();
+  for (int prog = 0; prog < PP_NPROG; prog++) {
+    const long long t0 = clock64();
+#pragma unroll 1
+    for (int r = 0; r < reps; r++) pp::run(sl, lane, prog);
+    const long long t1 = clock64();
+    if (lane == 0) cycles[prog] = (double)(t1 - t0) / reps;
+  }
+}
+
+extern "C" int32_t cubbs_bbs_gpu_pairing_probe_for_test_v2(double *cycles, int32_t cap) {
+  if (!cycles || cap < PP_NPROG) return -1;
+  try {
+    CallScope scope;
+    Runtime &rt = scope.rt;
+    double *d = rt.arena.alloc<double>(PP_NPROG);
+    const size_t smem = (size_t)PP_SLOTS * sizeof(fp);
+    k_pp_probe<<<1, 32, smem, rt.stream>>>(d, 2);  // warm-up
+    k_pp_probe<<<1, 32, smem, rt.stream>>>(d, 16);
+    CUBBS_CHECK(cudaGetLastError());
+    CUBBS_CHECK(cudaMemcpyAsync(cycles, d, PP_NPROG * sizeof(double), cudaMemcpyDeviceToHost, rt.stream));
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    return PP_NPROG;
+  } catch (const CudaError &) {
+    return -2;
+  }
 }
 
 void launch_pairing_check(cudaStream_t s, const PairJob *jobs, uint32_t n, const line2 *lines, uint8_t *ok) {

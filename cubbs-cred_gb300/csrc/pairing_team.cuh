@@ -45,31 +45,43 @@ DEV uint32_t term(const uint4 &e, int t) {
   return (t & 1) ? w >> 16 : w & 0xffffu;
 }
 
-// Signed sum of at most six reduced slots: every partial sum is a plain
-// 12-limb sum of values in [0, p] (a subtracted term x enters as p - x), so it
-// stays below 6p < 2^384; conditional subtractions of 4p, 2p and p (as many as
-// the term count needs) reduce it once at the end.
-DEV fp lin(const fp *sl, const uint4 &e, int n) {
-  fp acc;
-  {
-    const uint32_t tv = term(e, 0);
+// Signed sum of N reduced slots (N is the same on every lane of a phase): a
+// subtracted term x enters as p - x, every term is loaded and prepared before
+// the sums, and the terms are added as a pairwise tree of plain 12-limb
+// additions (every partial sum stays below N p <= 6p < 2^384); conditional
+// subtractions of 4p, 2p and p, as many as N needs, reduce the result once.
+// No branch depends on the lane.
+template <int N> DEV fp lin_n(const fp *sl, const uint4 &e) {
+  fp v[N];
+#pragma unroll
+  for (int t = 0; t < N; t++) {
+    const uint32_t tv = term(e, t);
     const fp x = ld(sl, tv & 0x7fffu);
-    if (tv & 0x8000u) fp_from_mod(acc.w, x.w);
-    else acc = x;
+    fp y;
+    fp_from_mod(y.w, x.w);
+    const bool neg = (tv & 0x8000u) != 0;
+#pragma unroll
+    for (int k = 0; k < 12; k++) v[t].w[k] = neg ? y.w[k] : x.w[k];
   }
 #pragma unroll
-  for (int t = 1; t < 6; t++) {
-    if (t < n) {
-      const uint32_t tv = term(e, t);
-      fp y = ld(sl, tv & 0x7fffu);
-      if (tv & 0x8000u) fp_from_mod(y.w, y.w);
-      fp_acc_add(acc.w, acc.w, y.w);
-    }
+  for (int w = 1; w < N; w *= 2) {
+#pragma unroll
+    for (int t = 0; t + w < N; t += 2 * w) fp_acc_add(v[t].w, v[t].w, v[t + w].w);
   }
-  if (n >= 4) fp_csub4(acc.w, acc.w);
-  if (n >= 2) fp_csub2(acc.w, acc.w);
-  fp_csub1(acc.w, acc.w);
-  return acc;
+  if (N >= 4) fp_csub4(v[0].w, v[0].w);
+  if (N >= 2) fp_csub2(v[0].w, v[0].w);
+  fp_csub1(v[0].w, v[0].w);
+  return v[0];
+}
+DEV fp lin(const fp *sl, const uint4 &e, int n) {
+  switch (n) {
+    case 1: return lin_n<1>(sl, e);
+    case 2: return lin_n<2>(sl, e);
+    case 3: return lin_n<3>(sl, e);
+    case 4: return lin_n<4>(sl, e);
+    case 5: return lin_n<5>(sl, e);
+    default: return lin_n<6>(sl, e);
+  }
 }
 
 // Runs program `prog` on the slot array of this warp's check.  The table

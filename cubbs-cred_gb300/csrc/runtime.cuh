@@ -239,7 +239,7 @@ struct PairJob {
   g1a pa, pb;
   int32_t slot_a, slot_b;
   uint32_t flags;
-  uint32_t active;  // 0: not evaluated (result 0)
+  uint32_t active;  // 1: evaluate; 0: not evaluated (result 0); 2: result already written
 };
 void launch_pairing_check(cudaStream_t s, const PairJob *jobs, uint32_t n, const line2 *lines, uint8_t *ok);
 

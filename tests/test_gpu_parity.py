@@ -225,6 +225,45 @@ def test_split_subgroup_check(gpu, golden, oracle):
     assert got[-1][0] == 2 and got[-1][1] == 0
 
 
+def _pv_items(oracle, seed, count, L, fake=()):
+    """`count` ProofVerify items under one key; items in `fake` are proofs made
+    from the signature of other messages, which pass the challenge check and
+    fail only the pairing check."""
+    sk, pk = keypair(oracle, seed)
+    items = []
+    for i in range(count):
+        msgs = messages(seed, i, L, 32)
+        sig = oracle.sign(sk, pk, b"h", msgs)[0]
+        if i in fake:
+            sig = oracle.sign(sk, pk, b"h", messages(seed + b"-other", i, L, 32))[0][:48] + sig[48:]
+        di = disclosed_subset(seed, i, L, L // 2)
+        proof = oracle.proof_gen(pk, sig, b"h", b"p", msgs, di, seed=drbg(seed, b"s", i, 32))
+        items.append((pk, proof, b"h", b"p", [msgs[j] for j in di], di, L))
+    return items
+
+
+def test_proof_verify_aggregated_groups(gpu, oracle):
+    """Batches of 128 or more check each key's proofs (16 or more) as one group;
+    a group that fails is checked item by item.  Every verdict equals the
+    oracle's and the verdict of the same item in a batch too small to group."""
+    big = _pv_items(oracle, b"agg-a", 136, 6, fake={5, 77, 130})
+    small = _pv_items(oracle, b"agg-b", 10, 6, fake={3})
+    clean = _pv_items(oracle, b"agg-c", 20, 6)
+    items = big + small + clean
+    items[40] = items[40][:3] + (b"p!",) + items[40][4:]   # challenge mismatch
+    want = [oracle.proof_verify(pk, pr, hd, ph, dm, di) == 0 for pk, pr, hd, ph, dm, di, _ in items]
+    assert want.count(False) == 5
+    got = [v for _, v in gpu.proof_verify_batch(items)]
+    assert got == want
+    alone = []
+    for k in range(0, len(items), 50):
+        alone += [v for _, v in gpu.proof_verify_batch(items[k:k + 50])]
+    assert alone == want
+    # all valid: every group check passes
+    ok_items = [it for it, w in zip(items, want) if w]
+    assert all(v for _, v in gpu.proof_verify_batch(ok_items))
+
+
 def test_sign_e_resident(gpu, oracle):
     import ctypes
     seed = b"sign-e"
