@@ -472,7 +472,18 @@ def msm_uneven_bench(n_msms=16384, k_min=2, k_max=257, seed=4, tune=True, warmup
             "checked": chk.value, "mismatch": mm.value}
 
 
-def fixed_msm_autotune(scalars_be, rows, terms, w_lo=4, w_hi=12, steps=3):
+def table_window():
+    """Window width of the resident fixed-base table (0 before it is built)."""
+    w = ctypes.c_int32(0)
+    fn = lib().cubbs_bbs_gpu_table_window_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_void_p]
+    if fn(ctypes.cast(ctypes.pointer(w), ctypes.c_void_p)):
+        raise RuntimeError("table_window failed")
+    return w.value
+
+
+def fixed_msm_autotune(scalars_be, rows, terms, w_lo=4, w_hi=16, steps=3):
     """Times the fixed-base MSM kernel over rows x terms scalars (bases: the first
     `terms` resident generators) for table window widths w_lo..w_hi; the fastest
     width stays in use.  Returns ([ms per width], best width)."""

@@ -975,7 +975,7 @@ extern "C" int32_t cubbs_bbs_gpu_pairing_eq_aggregate_v2(uint32_t abi, const CuB
 extern "C" int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi, const uint8_t *scalars_be, size_t rows,
                                                        size_t terms, int32_t w_lo, int32_t w_hi, int32_t steps,
                                                        float *ms_per_w, int32_t *best_w) {
-  if (!abi_ok(abi) || !scalars_be || rows == 0 || terms == 0 || terms > 1024 || w_lo < 4 || w_hi > 13 ||
+  if (!abi_ok(abi) || !scalars_be || rows == 0 || terms == 0 || terms > 1024 || w_lo < 4 || w_hi > 16 ||
       w_lo > w_hi || steps <= 0 || !ms_per_w || !best_w)
     return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   ABI_GUARD_BEGIN
@@ -1027,4 +1027,16 @@ extern "C" int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi, const uint8
   *best_w = bw;
   return CUBBS_BBS_GPU_SUCCESS;
   ABI_GUARD_END
+}
+
+// Window width of the resident fixed-base table (0 before the first table is built).
+extern "C" int32_t cubbs_bbs_gpu_table_window_v2(int32_t *w) {
+  if (!w) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  try {
+    CallScope scope;
+    *w = scope.rt.table.entries ? scope.rt.table.w : 0;
+    return CUBBS_BBS_GPU_SUCCESS;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
 }

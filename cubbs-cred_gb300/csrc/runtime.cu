@@ -57,8 +57,8 @@ void SharedState::init() {
   CUBBS_CHECK(cudaStreamCreateWithFlags(&prep, cudaStreamNonBlocking));
   // The kernels are register heavy; give them room for local-memory spills.
   CUBBS_CHECK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
-  table_w = env_int("CUBBS_BBS_TABLE_WINDOW", 8);
-  if (table_w < 4 || table_w > 16) table_w = 8;
+  table_w = env_int("CUBBS_BBS_TABLE_WINDOW", 0);  // 0: chosen by table_window_for
+  if (table_w != 0 && (table_w < 4 || table_w > 16)) table_w = 0;
   workspaces = env_int("CUBBS_BBS_WORKSPACES", 4);
   if (workspaces < 1 || workspaces > 64) workspaces = 4;
   line_capacity = 2 + 1024;
@@ -116,14 +116,33 @@ void SharedState::grow_generators(int count) {
 
 // Fixed-base window table over d_gens[0..gens).  Rebuilt (all generators)
 // when it must grow; built in generator chunks to bound the scratch.
+// Window width of a table over `gens` generators: the explicit setting, else
+// the widest w in 8..16 whose table (gens * ceil(256/w) * 2^(w-1) affine
+// points) fits in TABLE_BUDGET.  A wider window costs fewer mixed additions
+// per term (16 at w = 16, 32 at w = 8); the entries are read at random, one
+// 96-byte point per addition, from HBM.
+static const size_t TABLE_BUDGET = (size_t)16 << 30;
+int SharedState::table_window_for(int gens) const {
+  if (table_w) return table_w;
+  for (int w = 16; w > 8; w--) {
+    const size_t bytes = (size_t)gens * (255 / w + 1) * ((size_t)1 << (w - 1)) * sizeof(g1a);
+    if (bytes <= TABLE_BUDGET) return w;
+  }
+  return 8;
+}
+
+bool SharedState::table_covers(int gens) const {
+  return table.entries && table.gens >= gens && (table_w == 0 || table.w == table_w);
+}
+
 void SharedState::grow_table(int gens) {
-  if (table.entries && table.gens >= gens && table.w == table_w) return;
+  if (table_covers(gens)) return;
   int want = 1;
   while (want < gens) want *= 2;
   if (want < 64) want = 64;
   grow_generators(want);
   FixedTable t;
-  t.w = table_w;
+  t.w = table_window_for(want);
   t.nwin = 255 / t.w + 1;
   t.half = 1 << (t.w - 1);
   t.gens = want;
@@ -131,9 +150,9 @@ void SharedState::grow_table(int gens) {
   g1a *entries = nullptr;
   CUBBS_CHECK(cudaMalloc(&entries, (size_t)want * per_gen * sizeof(g1a)));
   t.entries = entries;
-  // chunk so that the XYZZ + prefix scratch stays below ~1 GiB
+  // chunk so that the XYZZ + prefix scratch stays below ~8 GiB
   size_t per_gen_scratch = per_gen * (sizeof(g1) + sizeof(fp));
-  int chunk = (int)std::max<size_t>(1, ((size_t)1 << 30) / per_gen_scratch);
+  int chunk = (int)std::max<size_t>(1, ((size_t)8 << 30) / per_gen_scratch);
   if (chunk > want) chunk = want;
   g1 *scratch = nullptr;
   fp *prod = nullptr;
@@ -227,7 +246,7 @@ void Runtime::ensure_generators(int count) {
 }
 
 void Runtime::ensure_table(int gens) {
-  if (sh.table.entries && sh.table.gens >= gens && sh.table.w == sh.table_w) return;
+  if (sh.table_covers(gens)) return;
   lock->unlock();
   {
     std::unique_lock<std::shared_mutex> ex(sh.mu);

@@ -114,7 +114,7 @@ struct SharedState {
   uint8_t *d_gens_c = nullptr;  // compressed, same indexing as d_gens
   std::vector<uint8_t> h_gens_c;  // host copy of d_gens_c[0..gen_count)
   FixedTable table;
-  int table_w = 8;
+  int table_w = 0;              // fixed-base window width; 0 = widest that fits the table budget
   // Miller lines: slot 0 = -P2, slot 1 = P2, slots >= 2 = public keys
   line2 *d_lines = nullptr;
   g2a *d_pk_aff = nullptr;
@@ -129,6 +129,8 @@ struct SharedState {
   // the following run with mu held exclusively
   void grow_generators(int count);
   void grow_table(int gens);
+  int table_window_for(int gens) const;
+  bool table_covers(int gens) const;
   void add_pks(const std::vector<std::string> &fresh);
 };
 
@@ -157,7 +159,7 @@ struct Runtime {
   explicit Runtime(SharedState &s);
   void ensure_generators(int count);  // d_gens[0..count) (P1 + count-1 generators)
   void ensure_table(int gens);        // fixed-base table covering d_gens[0..gens)
-  void set_table_window(int w, int gens);  // rebuild the table with window width w
+  void set_table_window(int w, int gens);  // rebuild the table with window width w (0: automatic)
   void set_msm_tuning(const MsmTuning &t);
   // Resolve public keys to line slots (decoding + subgroup check + lines on the
   // device for new keys).  pk_ptrs[i] -> slot index; status per key.
