@@ -110,6 +110,82 @@ DEV bool g1_to_aff(g1 p, g1a &out) {
   out.y = fp_mul(p.Y, fp_mul(t, p.ZZ));   // Y / ZZZ
   return true;
 }
+// Fp value of another lane (full-warp shuffles).
+DEV fp shfl_fp(const fp &a, int src) {
+  fp r;
+#pragma unroll
+  for (int i = 0; i < 12; i++) r.w[i] = __shfl_sync(0xffffffffu, a.w[i], src);
+  return r;
+}
+DEV fp shfl_up_fp(const fp &a, int d) {
+  fp r;
+#pragma unroll
+  for (int i = 0; i < 12; i++) r.w[i] = __shfl_up_sync(0xffffffffu, a.w[i], d);
+  return r;
+}
+DEV fp shfl_down_fp(const fp &a, int d) {
+  fp r;
+#pragma unroll
+  for (int i = 0; i < 12; i++) r.w[i] = __shfl_down_sync(0xffffffffu, a.w[i], d);
+  return r;
+}
+// v^-1 for one value per lane of a full warp (Montgomery's simultaneous
+// inversion): inclusive prefix and suffix products by shuffles (5 products
+// each), one variable-time inverse of the whole product on lane 31, then
+// v_l^-1 = (v_0 .. v_{l-1}) (v_{l+1} .. v_31) / (v_0 .. v_31).  A zero value
+// counts as 1 and gets 0.  Every lane of the warp must call it.
+DEV fp warp_batch_inv(const fp &v_in) {
+  const int lane = threadIdx.x & 31;
+  const bool zero = fp_is_zero(v_in);
+  const fp one = fp_one();
+  const fp v = zero ? one : v_in;
+  fp pre = v, suf = v;
+#pragma unroll 1
+  for (int d = 1; d < 32; d *= 2) {
+    fp o = shfl_up_fp(pre, d);
+    pre = fp_mul(pre, lane >= d ? o : one);
+    fp q = shfl_down_fp(suf, d);
+    suf = fp_mul(suf, lane + d < 32 ? q : one);
+  }
+  fp inv_all = fp_zero();
+  if (lane == 31) inv_all = fp_inv_vartime(pre);
+  inv_all = shfl_fp(inv_all, 31);
+  fp before = shfl_up_fp(pre, 1), after = shfl_down_fp(suf, 1);
+  if (lane == 0) before = one;
+  if (lane == 31) after = one;
+  const fp r = fp_mul(fp_mul(before, after), inv_all);
+  return zero ? fp_zero() : r;
+}
+// Affine forms of N points per lane with one warp-batched inversion (the
+// inverses of the lane's N values ZZ ZZZ come from the inverse of their
+// product and in-lane prefix / suffix products); fin[k] is false for infinity.
+// Every lane of the warp must call it.
+template <int N> DEV void warp_to_aff(const g1 *p, g1a *a, bool *fin) {
+  const fp one = fp_one();
+  fp z[N], pre[N], suf[N];
+#pragma unroll
+  for (int k = 0; k < N; k++) {
+    fin[k] = !g1_is_inf(p[k]);
+    z[k] = fin[k] ? fp_mul(p[k].ZZ, p[k].ZZZ) : one;
+  }
+  pre[0] = z[0];
+#pragma unroll
+  for (int k = 1; k < N; k++) pre[k] = fp_mul(pre[k - 1], z[k]);
+  suf[N - 1] = z[N - 1];
+#pragma unroll
+  for (int k = N - 2; k >= 0; k--) suf[k] = fp_mul(suf[k + 1], z[k]);
+  const fp t = warp_batch_inv(pre[N - 1]);
+#pragma unroll
+  for (int k = 0; k < N; k++) {
+    fp ik = t;  // 1 / (ZZ_k ZZZ_k) = t * prod_{j != k} z_j
+    if (k > 0) ik = fp_mul(ik, pre[k - 1]);
+    if (k < N - 1) ik = fp_mul(ik, suf[k + 1]);
+    a[k].x = fp_mul(p[k].X, fp_mul(ik, p[k].ZZZ));
+    a[k].y = fp_mul(p[k].Y, fp_mul(ik, p[k].ZZ));
+  }
+}
+DEV void g1_compress_aff_or_inf(const g1a &a, bool finite, uint8_t out[48]);
+
 DEV bool g1_eq(const g1 &p, const g1 &q) {
   bool pi = g1_is_inf(p), qi = g1_is_inf(q);
   if (pi || qi) return pi && qi;
@@ -129,6 +205,15 @@ DEV void g1_compress_aff(const g1a &a, uint8_t out[48]) {
   fp_to_be48(a.x, out);
   out[0] |= 0x80;
   if (fp_lex_largest(a.y)) out[0] |= 0x20;
+}
+DEV void g1_compress_aff_or_inf(const g1a &a, bool finite, uint8_t out[48]) {
+  if (!finite) {
+    out[0] = 0xc0;
+    #pragma unroll 1
+    for (int i = 1; i < 48; i++) out[i] = 0;
+    return;
+  }
+  g1_compress_aff(a, out);
 }
 DEV void g1_compress(g1 p, uint8_t out[48]) {
   g1a a;

@@ -299,20 +299,33 @@ __global__ void __launch_bounds__(128) k_pv_pairjobs_agg(const PvItem *items0, u
 __global__ void __launch_bounds__(64) k_pv_finish(PvItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
                                                   const fr *domain, const int32_t *dec_status,
                                                   const int32_t *outside_g1, const g1 *t2fix, const g1 *v) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  PvItem it = items[i];
-  if (it.status != ST_OK) return;
-  if (dec_status[3 * i] == DEC_BAD || dec_status[3 * i + 1] == DEC_BAD || dec_status[3 * i + 2] == DEC_BAD ||
-      outside_g1[3 * i] || outside_g1[3 * i + 1] || outside_g1[3 * i + 2]) {
-    items[i].status = ST_INVALID;
-    return;
+  // every lane of the warp reaches the shared affine conversion below
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool act = i < n;
+  PvItem it;
+  if (act) {
+    it = items[i];
+    act = it.status == ST_OK;
+    if (act && (dec_status[3 * i] == DEC_BAD || dec_status[3 * i + 1] == DEC_BAD ||
+                dec_status[3 * i + 2] == DEC_BAD || outside_g1[3 * i] || outside_g1[3 * i + 1] ||
+                outside_g1[3 * i + 2])) {
+      items[i].status = ST_INVALID;
+      act = false;
+    }
   }
-  g1 T1 = g1_add(g1_add(v[4 * i], v[4 * i + 1]), v[4 * i + 2]);
-  g1 T2 = g1_add(t2fix[i], v[4 * i + 3]);
+  g1 T1 = g1_inf(), T2 = g1_inf();
+  if (act) {
+    T1 = g1_add(g1_add(v[4 * i], v[4 * i + 1]), v[4 * i + 2]);
+    T2 = g1_add(t2fix[i], v[4 * i + 3]);
+  }
+  const g1 T[2] = {T1, T2};
+  g1a aff[2];
+  bool fin[2];
+  warp_to_aff<2>(T, aff, fin);
+  if (!act) return;
   uint8_t t1c[48], t2c[48];
-  g1_compress(T1, t1c);
-  g1_compress(T2, t2c);
+  g1_compress_aff_or_inf(aff[0], fin[0], t1c);
+  g1_compress_aff_or_inf(aff[1], fin[1], t2c);
   const uint8_t *pr = blob + it.proof_off;
   const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
   sha_ctx c;
@@ -598,22 +611,30 @@ __global__ void __launch_bounds__(64) k_pg_vars(PgItem *items, uint32_t n, const
 __global__ void __launch_bounds__(64) k_pg_finish(PgItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
                                                   const fr *domain, const fr *rs, uint32_t rs_stride,
                                                   const g1 *t2fix, const g1 *v, uint8_t *out) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  PgItem it = items[i];
-  if (it.status != ST_OK) return;
-  const g1 *vi = v + 7 * (size_t)i;
+  // every lane of the warp reaches the shared affine conversion below
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool act = i < n && items[i].status == ST_OK;
+  g1 P[5] = {g1_inf(), g1_inf(), g1_inf(), g1_inf(), g1_inf()};  // Abar, Bbar, D, T1, T2
+  if (act) {
+    const g1 *vi = v + 7 * (size_t)i;
+    P[0] = vi[1];
+    P[1] = g1_add(vi[2], vi[3]);
+    P[2] = vi[0];
+    P[3] = g1_add(vi[4], vi[5]);
+    P[4] = g1_add(t2fix[i], vi[6]);
+  }
+  g1a aff[5];
+  bool fin[5];
+  warp_to_aff<5>(P, aff, fin);
+  if (!act) return;
+  const PgItem it = items[i];
   uint8_t *o = out + it.out_off;
-  g1 D = vi[0], Abar = vi[1];
-  g1 Bbar = g1_add(vi[2], vi[3]);
-  g1 T1 = g1_add(vi[4], vi[5]);
-  g1 T2 = g1_add(t2fix[i], vi[6]);
-  g1_compress(Abar, o);
-  g1_compress(Bbar, o + 48);
-  g1_compress(D, o + 96);
+  g1_compress_aff_or_inf(aff[0], fin[0], o);
+  g1_compress_aff_or_inf(aff[1], fin[1], o + 48);
+  g1_compress_aff_or_inf(aff[2], fin[2], o + 96);
   uint8_t t1c[48], t2c[48];
-  g1_compress(T1, t1c);
-  g1_compress(T2, t2c);
+  g1_compress_aff_or_inf(aff[3], fin[3], t1c);
+  g1_compress_aff_or_inf(aff[4], fin[4], t2c);
   const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
   sha_ctx c;
   xmd_begin(c);
