@@ -200,29 +200,31 @@ DEV void agg_rho(const AggSeed &seed, uint32_t i, uint32_t &a, uint32_t &b) {
 // a P + b phi(P) for affine P (Shamir's trick over the 32 bits of a and b).
 // Every step adds one of {P, phi(P), P + phi(P)} or nothing and keeps the sum
 // by a select, so lanes with different scalars never diverge.
-DEV g1 g1_mul_rho(const g1a &p, uint32_t a, uint32_t b) {
+// On a lane pair (both lanes return the result; a pair holds one point).
+DEV g1 g1_mul_rho(const LanePair &lp, const g1a &p, uint32_t a, uint32_t b) {
   const g1 P = g1_from_aff(p);
   const g1 E = g1_endo(P);
-  const g1 PE = g1_add(P, E);
+  const g1 PE = g1_add_pair(lp, P, E);
   g1 acc = (b >> 31) ? PE : P;  // bit 31 of a is set
 #pragma unroll 1
   for (int i = 30; i >= 0; i--) {
-    acc = g1_dbl(acc);
+    acc = g1_dbl_pair(lp, acc);
     const uint32_t sel = ((a >> i) & 1) | (((b >> i) & 1) << 1);
     const g1 t = sel == 1 ? P : sel == 2 ? E : PE;
-    const g1 sum = g1_add(acc, t);
+    const g1 sum = g1_add_pair(lp, acc, t);
     if (sel) acc = sum;
   }
   return acc;
 }
 
-// One thread per (item, point): scaled[2i] = rho_i Abar_i, scaled[2i+1] = rho_i Bbar_i
+// One lane pair per (item, point): scaled[2i] = rho_i Abar_i, scaled[2i+1] = rho_i Bbar_i
 // for items of an aggregated group whose points decoded (infinity otherwise).
 __global__ void __launch_bounds__(32) k_agg_scale(const PvItem *items0, uint32_t n, const g1a *pts,
                                                   const int32_t *dec, const int32_t *group_of, AggSeed seed,
                                                   g1 *scaled) {
-  uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= 2 * n) return;
+  const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 1;
+  if (t >= 2 * n) return;  // both lanes of a pair leave together
+  const LanePair lp = LanePair::here();
   const uint32_t i = t >> 1, which = t & 1;
   const PvItem it = items0[i];
   bool use = group_of[i] >= 0 && it.status == ST_OK && it.pk_status == DEC_OK;
@@ -231,7 +233,8 @@ __global__ void __launch_bounds__(32) k_agg_scale(const PvItem *items0, uint32_t
   const int32_t d = dec[3 * i + which];
   uint32_t ra, rb;
   agg_rho(seed, i, ra, rb);
-  scaled[t] = (use && d == DEC_OK) ? g1_mul_rho(pts[3 * i + which], ra, rb) : g1_inf();
+  const g1 r = (use && d == DEC_OK) ? g1_mul_rho(lp, pts[3 * i + which], ra, rb) : g1_inf();
+  if (lp.role == 0) scaled[t] = r;
 }
 
 // Grid (groups, 2): block (g, 0) sums the scaled Abar of group g's items (in
@@ -927,7 +930,7 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
       got += (size_t)r;
     }
     SPAN(s3, "pairing_aggregate",
-         k_agg_scale<<<blocks_for(2 * n, 32), 32, 0, s3>>>(it0, N, b.pts, b.dec, b.group_of, seed, b.scaled);
+         k_agg_scale<<<blocks_for(4 * n, 32), 32, 0, s3>>>(it0, N, b.pts, b.dec, b.group_of, seed, b.scaled);
          CUBBS_CHECK(cudaMemsetAsync(b.gjobs, 0, G * sizeof(PairJob), s3));
          k_agg_sum<<<dim3(G, 2), 512, 0, s3>>>(b.scaled, b.perm, b.goff, b.gslot, b.gjobs);
          launch_pairing_check(s3, b.gjobs, G, rt.d_lines, b.gok));

@@ -115,6 +115,22 @@ __global__ void __launch_bounds__(128) k_fixed_msm(FixedTable t, const fr *scala
   if (lane == 0) out[row] = acc;
 }
 
+// One lane pair per job (g1_mul_glv_pair): the pair splits each point
+// operation's products, halving the latency of a job.
+__global__ void __launch_bounds__(128) k_var_mul_pair(const g1a *points, const VarJob *jobs, const fr *scalars,
+                                                      uint32_t n, g1 *out) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t >> 1;
+  if (i >= n) return;  // both lanes of a pair leave together
+  const LanePair lp = LanePair::here();
+  const VarJob j = jobs[i];
+  if (j.flags & 1) {
+    if (lp.role == 0) out[i] = g1_inf();
+    return;
+  }
+  const g1 r = g1_mul_glv_pair(lp, points[j.point], scalars[i]);
+  if (lp.role == 0) out[i] = r;
+}
 __global__ void __launch_bounds__(128) k_var_mul(const g1a *points, const VarJob *jobs, const fr *scalars,
                                                  uint32_t n, g1 *out) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -137,13 +153,25 @@ __global__ void __launch_bounds__(128) k_g1_compress(const g1 *pts, uint32_t n, 
 
 // Subgroup check of points decoded without it: bad[i] = 1 when point i
 // decoded to an affine point outside G1 (status DEC_OK), else 0.
-__global__ void __launch_bounds__(32) k_g1_subgroup(const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad) {
+__global__ void __launch_bounds__(32) k_g1_subgroup_lane(const g1a *pts, const int32_t *status, uint32_t n,
+                                                          int32_t *bad) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   bad[i] = (status[i] == DEC_OK && !g1_in_subgroup(pts[i])) ? 1 : 0;
 }
-void launch_g1_subgroup(cudaStream_t s, const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad) {
-  if (n) k_g1_subgroup<<<blocks_for(n, 32), 32, 0, s>>>(pts, status, n, bad);
+// One lane pair per point.
+__global__ void __launch_bounds__(32) k_g1_subgroup(const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad) {
+  const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 1;
+  if (i >= n) return;  // both lanes of a pair leave together
+  const LanePair lp = LanePair::here();
+  const bool outside = status[i] == DEC_OK && !g1_in_subgroup_pair(lp, pts[i]);
+  if (lp.role == 0) bad[i] = outside ? 1 : 0;
+}
+void launch_g1_subgroup(cudaStream_t s, const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad,
+                        bool pairs) {
+  if (!n) return;
+  if (pairs) k_g1_subgroup<<<blocks_for(2 * (size_t)n, 32), 32, 0, s>>>(pts, status, n, bad);
+  else k_g1_subgroup_lane<<<blocks_for(n, 32), 32, 0, s>>>(pts, status, n, bad);
 }
 void launch_g1_decode(cudaStream_t s, const uint8_t *pts48, uint32_t stride, uint32_t n, g1a *out, int32_t *status,
                       bool check_subgroup) {
@@ -157,8 +185,11 @@ void launch_fixed_msm(cudaStream_t s, const FixedTable &t, const fr *scalars, ui
                       const uint32_t *nterms, uint32_t rows, g1 *out) {
   if (rows) k_fixed_msm<<<blocks_for((size_t)rows * 32, 128), 128, 0, s>>>(t, scalars, stride, nterms, rows, out);
 }
-void launch_var_mul(cudaStream_t s, const g1a *points, const VarJob *jobs, const fr *scalars, uint32_t n, g1 *out) {
-  if (n) k_var_mul<<<blocks_for(n, 128), 128, 0, s>>>(points, jobs, scalars, n, out);
+void launch_var_mul(cudaStream_t s, const g1a *points, const VarJob *jobs, const fr *scalars, uint32_t n, g1 *out,
+                    bool pairs) {
+  if (!n) return;
+  if (pairs) k_var_mul_pair<<<blocks_for(2 * (size_t)n, 128), 128, 0, s>>>(points, jobs, scalars, n, out);
+  else k_var_mul<<<blocks_for(n, 128), 128, 0, s>>>(points, jobs, scalars, n, out);
 }
 void launch_g1_compress(cudaStream_t s, const g1 *pts, uint32_t n, uint8_t *out48) {
   if (n) k_g1_compress<<<blocks_for(n, 128), 128, 0, s>>>(pts, n, out48);

@@ -224,7 +224,13 @@ Runtime::Runtime(SharedState &s)
   CUBBS_CHECK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_join, cudaEventDisableTiming));
-  CUBBS_CHECK(cudaStreamCreateWithFlags(&stream3, cudaStreamNonBlocking));
+  {
+    // stream3 carries the ProofVerify pairing chain, the step's critical path:
+    // its blocks go first when the block scheduler picks between streams
+    int lo = 0, hi = 0;
+    CUBBS_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    CUBBS_CHECK(cudaStreamCreateWithPriority(&stream3, cudaStreamNonBlocking, hi));
+  }
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_mid, cudaEventDisableTiming));
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_side, cudaEventDisableTiming));
   CUBBS_CHECK(cudaStreamCreateWithFlags(&stream4, cudaStreamNonBlocking));

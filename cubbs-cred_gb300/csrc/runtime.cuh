@@ -203,7 +203,8 @@ void launch_decode_p1(cudaStream_t s, g1a *gens, uint8_t *gens_c);
 void launch_build_table(cudaStream_t s, const g1a *gens, int g0, int g1n, FixedTable t, g1 *scratch_xyzz,
                         fp *scratch_prod);
 // decode N compressed G1 points: status DEC_*; affine out
-void launch_g1_subgroup(cudaStream_t s, const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad);
+void launch_g1_subgroup(cudaStream_t s, const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad,
+                        bool pairs = true);
 void launch_g1_decode(cudaStream_t s, const uint8_t *pts48, uint32_t stride, uint32_t n, g1a *out,
                       int32_t *status, bool check_subgroup);
 // fixed-base MSM rows: scalars raw Fr [row * stride + g] for g < nterms[row]
@@ -215,7 +216,8 @@ struct VarJob {
   uint32_t flags;  // bit0: point is infinity (result infinity)
 };
 void launch_var_mul(cudaStream_t s, const g1a *points, const VarJob *jobs, const fr *scalars, uint32_t n,
-                    g1 *out);
+                    g1 *out,
+                    bool pairs = true);
 void launch_g1_compress(cudaStream_t s, const g1 *pts, uint32_t n, uint8_t *out48);
 struct MsmDevice {
   uint32_t n = 0, nterms = 0, nchunks = 0, nunits = 0;
