@@ -853,11 +853,14 @@ def prepared_call(op, reqs):
             OP_PROOF_VERIFY: "cubbs_bbs_gpu_proof_verify_batch_v2"}[op]
     fn = getattr(lib(), name)
     ip, rp = ctypes.cast(items, ctypes.c_void_p), ctypes.cast(res, ctypes.c_void_p)
+    import numpy as np
+    view = np.frombuffer(res, dtype=np.dtype({"names": ["code", "value"], "formats": ["<i4", "u1"],
+                                              "offsets": [0, 4], "itemsize": ctypes.sizeof(Result)}))
 
     def call():
         rc = fn(ABI_VERSION, ip, n, rp)
         if rc:
             raise RuntimeError(f"{name} returned {rc}")
         _ = k  # keep the buffers alive with the closure
-        return [(res[i].code, res[i].value) for i in range(n)]
+        return list(zip(view["code"].tolist(), view["value"].tolist()))
     return call

@@ -15,6 +15,8 @@
 #include <sys/random.h>
 
 #include <algorithm>
+#include <chrono>
+#include <thread>
 #include <cstdio>
 #include <cstring>
 
@@ -687,37 +689,63 @@ bool abi_ok(uint32_t v) { return v == CUBBS_BBS_GPU_ABI_VERSION; }
 const size_t MAX_MESSAGES = 16384;  // generators kept resident: L + 2 <= 16386
 
 // Growable host byte blob (packed inputs for one batch).
+// Packed bytes of a batch, written straight into pinned host memory (the
+// workspace's pack buffer) so that one DMA moves them to the device.
+struct PinnedBytes {
+  uint8_t *base = nullptr;
+  size_t used = 0, cap = 0;
+  void bind(HostStaging &pack, size_t bytes) {
+    base = pack.alloc(bytes ? bytes : 16);
+    cap = bytes;
+    used = 0;
+  }
+  uint8_t *grab(size_t n) {
+    if (used + n > cap) throw CudaError(cudaErrorMemoryAllocation, "packed batch larger than planned");
+    uint8_t *p = base + used;
+    used += n;
+    return p;
+  }
+  size_t size() const { return used; }
+  const uint8_t *data() const { return base; }
+};
+
 struct Blob {
-  std::vector<uint8_t> b;
+  PinnedBytes b;
   uint32_t put(const uint8_t *p, size_t n) {
     uint32_t off = (uint32_t)b.size();
-    if (n) b.insert(b.end(), p, p + n);
+    if (n) std::memcpy(b.grab(n), p, n);
     return off;
   }
   uint32_t put_u32s(const std::vector<uint32_t> &v) {
-    while (b.size() & 3) b.push_back(0);
+    if (b.size() & 3) std::memset(b.grab(4 - (b.size() & 3)), 0, 4 - (b.size() & 3));
     uint32_t off = (uint32_t)b.size();
-    const uint8_t *p = reinterpret_cast<const uint8_t *>(v.data());
-    b.insert(b.end(), p, p + 4 * v.size());
+    if (!v.empty()) std::memcpy(b.grab(4 * v.size()), v.data(), 4 * v.size());
     return off;
   }
+  // bytes that put() / put_u32s() of n bytes may take (alignment included)
+  static size_t room(size_t n) { return n + 4; }
 };
 
-// Flat message list: [offsets u32 * n][lengths u32 * n][bytes].
+// Flat message list: [offsets u32 * n][lengths u32 * n][bytes]; the bytes are pinned.
 struct MsgList {
   std::vector<uint32_t> offs, lens;
-  std::vector<uint8_t> bytes;
+  PinnedBytes bytes;
   uint32_t add(const uint8_t *p, size_t n) {
     offs.push_back((uint32_t)bytes.size());
     lens.push_back((uint32_t)n);
-    if (n) bytes.insert(bytes.end(), p, p + n);
+    if (n) std::memcpy(bytes.grab(n), p, n);
     return (uint32_t)(offs.size() - 1);
   }
   size_t count() const { return offs.size(); }
 };
 
+// Sorted, de-duplicated disclosed indexes (proof.rs:961-963); callers
+// usually pass them sorted already, which needs no sort.
 void sort_dedup(const size_t *p, size_t n, std::vector<size_t> &out) {
   out.assign(p, p + n);
+  bool strictly_increasing = true;
+  for (size_t k = 1; k < n && strictly_increasing; k++) strictly_increasing = p[k - 1] < p[k];
+  if (strictly_increasing) return;
   std::sort(out.begin(), out.end());
   out.erase(std::unique(out.begin(), out.end()), out.end());
 }
@@ -728,6 +756,17 @@ enum Op { OP_SIGN = 0, OP_VERIFY = 1, OP_PGEN = 2, OP_PVERIFY = 3 };
 // upload() moves everything to the device once, run() replays the whole device
 // pipeline (this is the timed step of the benchmark), download() maps results.
 struct OpBatch {
+  explicit OpBatch(Runtime &rt) : pack(&rt.pack) {}
+  HostStaging *pack;  // pinned buffer the blob and the message bytes are packed into
+  // Binds the blob and the message bytes to the pack buffer (called by the
+  // planners once they know the sizes, before packing).
+  void bind(size_t blob_bytes, size_t msg_bytes, size_t msg_count) {
+    pack->reserve(blob_bytes + msg_bytes + 64);
+    blob.b.bind(*pack, blob_bytes);
+    ml.bytes.bind(*pack, msg_bytes);
+    ml.offs.reserve(msg_count);
+    ml.lens.reserve(msg_count);
+  }
   Op op;
   size_t n = 0, maxL = 0, maxU = 0, stride = 0, rs_stride = 0, out_total = 0;
   Blob blob;
@@ -835,16 +874,23 @@ void upload(Runtime &rt, OpBatch &b) {
                 n * b.rs_stride * sizeof(fr) + b.out_total + n * (2 * sizeof(g1) + 16 + sizeof(PairJob) + 8) +
                 64 * 256;
   rt.arena.reserve(need);
-  rt.staging.reserve(65536 + 2 * b.blob.b.size() + b.ml.bytes.size() + 8 * nm + b.pts48.size() +
-                     n * (b.item_size + sizeof(DomainJob) + 96));
-  b.dblob = upload(rt, b.blob.b.data(), b.blob.b.size());
-  std::vector<uint8_t> flat(8 * nm + b.ml.bytes.size());
-  if (nm) {
-    std::memcpy(flat.data(), b.ml.offs.data(), 4 * nm);
-    std::memcpy(flat.data() + 4 * nm, b.ml.lens.data(), 4 * nm);
-    if (!b.ml.bytes.empty()) std::memcpy(flat.data() + 8 * nm, b.ml.bytes.data(), b.ml.bytes.size());
+  rt.staging.reserve(65536 + 8 * nm + b.pts48.size() + n * (b.item_size + sizeof(DomainJob) + 96));
+  // the blob and the message bytes are already pinned: DMA them directly
+  b.dblob = rt.arena.alloc<uint8_t>(b.blob.b.size() ? b.blob.b.size() : 1);
+  if (b.blob.b.size()) {
+    CUBBS_CHECK(cudaMemcpyAsync(b.dblob, b.blob.b.data(), b.blob.b.size(), cudaMemcpyHostToDevice, rt.stream));
+    g_h2d_bytes += b.blob.b.size();
   }
-  b.dmsg = upload(rt, flat.data(), flat.size());
+  b.dmsg = rt.arena.alloc<uint8_t>(8 * nm + b.ml.bytes.size() + 1);
+  if (nm) {
+    upload_to(rt, reinterpret_cast<uint32_t *>(b.dmsg), b.ml.offs.data(), nm);
+    upload_to(rt, reinterpret_cast<uint32_t *>(b.dmsg) + nm, b.ml.lens.data(), nm);
+    if (b.ml.bytes.size()) {
+      CUBBS_CHECK(cudaMemcpyAsync(b.dmsg + 8 * nm, b.ml.bytes.data(), b.ml.bytes.size(), cudaMemcpyHostToDevice,
+                                  rt.stream));
+      g_h2d_bytes += b.ml.bytes.size();
+    }
+  }
   b.msc = rt.arena.alloc<fr>(nm ? nm : 1);
   b.dpts48 = upload(rt, b.pts48.data(), b.pts48.size());
   size_t npts = b.pts48.size() / 48;
@@ -1115,6 +1161,27 @@ int32_t plan_pverify(const CuBbsBbsGpuProofVerifyItem *items, size_t n, OpBatch 
     for (size_t k = 0; k < it.disclosed_count; k++)
       if (it.disclosed_messages[k].len && !it.disclosed_messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   }
+  // Every item gets a fixed slot of the blob ([PK][proof][header][ph][pad][indexes u32])
+  // and of the message list, from prefix sums of its sizes, so that worker
+  // threads can pack disjoint items straight into the pinned buffer.  An item
+  // rejected by the shape checks keeps its message slots as empty messages.
+  std::vector<size_t> blob_at(n + 1), msg_at(n + 1), byte_at(n + 1);
+  blob_at[0] = msg_at[0] = byte_at[0] = 0;
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    const size_t slot = 96 + it.proof.len + it.header.len + it.presentation_header.len + 3 + 4 * it.disclosed_indexes.len;
+    blob_at[i + 1] = blob_at[i] + ((slot + 3) & ~(size_t)3);
+    msg_at[i + 1] = msg_at[i] + it.disclosed_count;
+    size_t bytes = 0;
+    for (size_t k = 0; k < it.disclosed_count; k++) bytes += it.disclosed_messages[k].len;
+    byte_at[i + 1] = byte_at[i] + bytes;
+  }
+  if (blob_at[n] >= 0xffffffffull || byte_at[n] >= 0xffffffffull) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  b.bind(blob_at[n], byte_at[n], msg_at[n]);
+  b.blob.b.used = blob_at[n];
+  b.ml.bytes.used = byte_at[n];
+  b.ml.offs.resize(msg_at[n]);
+  b.ml.lens.resize(msg_at[n]);
   b.op = OP_PVERIFY;
   b.n = n;
   b.item_size = sizeof(PvItem);
@@ -1124,42 +1191,80 @@ int32_t plan_pverify(const CuBbsBbsGpuProofVerifyItem *items, size_t n, OpBatch 
   b.pks.resize(n);
   b.code.assign(n, CUBBS_BBS_GPU_SUCCESS);
   b.dj.resize(n);
-  std::vector<size_t> di;
-  for (size_t i = 0; i < n; i++) {
-    const auto &it = items[i];
-    PvItem &p = reinterpret_cast<PvItem *>(b.items.data())[i];
-    b.pks[i] = it.public_key.data;
-    p.status = ST_OK;
-    size_t plen = it.proof.len;
-    sort_dedup(it.disclosed_indexes.data, it.disclosed_indexes.len, di);
-    size_t U = plen >= 272 ? (plen - 240) / 32 - 1 : 0;
-    size_t R = di.size(), L = U + R;
-    bool ok = plen >= 272 && it.disclosed_count == R && L <= MAX_MESSAGES;
-    for (size_t k = 0; k < R && ok; k++) ok = di[k] < L;
-    p.msg_base = (uint32_t)b.ml.count();
-    uint32_t pk_off = b.blob.put(it.public_key.data, 96);
-    if (!ok) {
-      p.status = ST_INVALID;
-      p.proof_off = b.blob.put(nullptr, 0);
-      b.dj[i] = {pk_off, 0, 0, 0};
-      continue;
+  auto pack_range = [&](size_t i0, size_t i1, size_t &maxL) {
+    std::vector<size_t> di;
+    uint8_t *blob = b.blob.b.base;
+    for (size_t i = i0; i < i1; i++) {
+      const auto &it = items[i];
+      PvItem &p = reinterpret_cast<PvItem *>(b.items.data())[i];
+      b.pks[i] = it.public_key.data;
+      p.status = ST_OK;
+      const size_t plen = it.proof.len;
+      sort_dedup(it.disclosed_indexes.data, it.disclosed_indexes.len, di);
+      const size_t U = plen >= 272 ? (plen - 240) / 32 - 1 : 0;
+      const size_t R = di.size(), L = U + R;
+      bool ok = plen >= 272 && it.disclosed_count == R && L <= MAX_MESSAGES;
+      for (size_t k = 0; k < R && ok; k++) ok = di[k] < L;
+      p.msg_base = (uint32_t)msg_at[i];
+      size_t at = blob_at[i];
+      const uint32_t pk_off = (uint32_t)at;
+      std::memcpy(blob + at, it.public_key.data, 96);
+      at += 96;
+      if (!ok) {
+        p.status = ST_INVALID;
+        p.proof_off = (uint32_t)at;
+        b.dj[i] = {pk_off, 0, 0, 0};
+        for (size_t k = msg_at[i]; k < msg_at[i + 1]; k++) {
+          b.ml.offs[k] = (uint32_t)byte_at[i];
+          b.ml.lens[k] = 0;
+        }
+        continue;
+      }
+      size_t bat = byte_at[i];
+      for (size_t k = 0; k < it.disclosed_count; k++) {
+        const size_t ln = it.disclosed_messages[k].len;
+        b.ml.offs[msg_at[i] + k] = (uint32_t)bat;
+        b.ml.lens[msg_at[i] + k] = (uint32_t)ln;
+        if (ln) std::memcpy(b.ml.bytes.base + bat, it.disclosed_messages[k].data, ln);
+        bat += ln;
+      }
+      p.U = (uint32_t)U;
+      p.R = (uint32_t)R;
+      p.L = (uint32_t)L;
+      const size_t used = 240 + 32 * (U + 1);
+      p.proof_off = (uint32_t)at;
+      std::memcpy(blob + at, it.proof.data, used);
+      at += used;
+      p.hdr_off = (uint32_t)at;
+      p.hdr_len = (uint32_t)it.header.len;
+      if (it.header.len) std::memcpy(blob + at, it.header.data, it.header.len);
+      at += it.header.len;
+      p.ph_off = (uint32_t)at;
+      p.ph_len = (uint32_t)it.presentation_header.len;
+      if (it.presentation_header.len) std::memcpy(blob + at, it.presentation_header.data, it.presentation_header.len);
+      at += it.presentation_header.len;
+      at = (at + 3) & ~(size_t)3;
+      p.idx_off = (uint32_t)at;
+      for (size_t k = 0; k < R; k++) {
+        const uint32_t v = (uint32_t)di[k];
+        std::memcpy(blob + at + 4 * k, &v, 4);
+      }
+      std::memcpy(&b.pts48[144 * i], it.proof.data, 144);
+      b.dj[i] = {pk_off, p.hdr_off, p.hdr_len, p.L};
+      maxL = std::max(maxL, L);
     }
-    for (size_t k = 0; k < it.disclosed_count; k++)
-      b.ml.add(it.disclosed_messages[k].data, it.disclosed_messages[k].len);
-    p.U = (uint32_t)U;
-    p.R = (uint32_t)R;
-    p.L = (uint32_t)L;
-    p.proof_off = b.blob.put(it.proof.data, 240 + 32 * (U + 1));
-    p.hdr_off = b.blob.put(it.header.data, it.header.len);
-    p.hdr_len = (uint32_t)it.header.len;
-    p.ph_off = b.blob.put(it.presentation_header.data, it.presentation_header.len);
-    p.ph_len = (uint32_t)it.presentation_header.len;
-    std::vector<uint32_t> d32(di.begin(), di.end());
-    p.idx_off = b.blob.put_u32s(d32);
-    std::memcpy(&b.pts48[144 * i], it.proof.data, 144);
-    b.dj[i] = {pk_off, p.hdr_off, p.hdr_len, p.L};
-    b.maxL = std::max(b.maxL, L);
+  };
+  const size_t threads = n >= 256 ? std::min<size_t>(8, n / 128) : 1;
+  std::vector<size_t> maxLs(threads, 0);
+  if (threads == 1) {
+    pack_range(0, n, maxLs[0]);
+  } else {
+    std::vector<std::thread> pool;
+    for (size_t t = 0; t < threads; t++)
+      pool.emplace_back(pack_range, n * t / threads, n * (t + 1) / threads, std::ref(maxLs[t]));
+    for (auto &th : pool) th.join();
   }
+  for (size_t m : maxLs) b.maxL = std::max(b.maxL, m);
   return CUBBS_BBS_GPU_SUCCESS;
 }
 
@@ -1171,6 +1276,16 @@ int32_t plan_sign(CuBbsBbsGpuSignItem *items, size_t n, OpBatch &b) {
       return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
     for (size_t k = 0; k < it.message_count; k++)
       if (it.messages[k].len && !it.messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  }
+  {
+    size_t blob = 0, msg = 0, count = 0;
+    for (size_t i = 0; i < n; i++) {
+      const auto &it = items[i];
+      blob += Blob::room(32) + Blob::room(96) + Blob::room(it.header.len);
+      for (size_t k = 0; k < it.message_count; k++) msg += it.messages[k].len;
+      count += it.message_count;
+    }
+    b.bind(blob, msg, count);
   }
   static const uint8_t zero96[96] = {0};
   b.op = OP_SIGN;
@@ -1212,6 +1327,16 @@ int32_t plan_verify(const CuBbsBbsGpuVerifyItem *items, size_t n, OpBatch &b) {
       return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
     for (size_t k = 0; k < it.message_count; k++)
       if (it.messages[k].len && !it.messages[k].data) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  }
+  {
+    size_t blob = 0, msg = 0, count = 0;
+    for (size_t i = 0; i < n; i++) {
+      const auto &it = items[i];
+      blob += Blob::room(80) + Blob::room(96) + Blob::room(it.header.len);
+      for (size_t k = 0; k < it.message_count; k++) msg += it.messages[k].len;
+      count += it.message_count;
+    }
+    b.bind(blob, msg, count);
   }
   static const uint8_t zeros[80] = {0};
   b.op = OP_VERIFY;
@@ -1265,6 +1390,17 @@ int32_t plan_pgen(CuBbsBbsGpuProofGenItem *items, size_t n, const uint8_t (*seed
       got += (size_t)r;
     }
   }
+  {
+    size_t blob = 0, msg = 0, count = 0;
+    for (size_t i = 0; i < n; i++) {
+      const auto &it = items[i];
+      blob += Blob::room(80) + Blob::room(96) + Blob::room(it.header.len) + Blob::room(it.presentation_header.len) +
+              Blob::room(4 * it.disclosed_indexes.len) + Blob::room(32);
+      for (size_t k = 0; k < it.message_count; k++) msg += it.messages[k].len;
+      count += it.message_count;
+    }
+    b.bind(blob, msg, count);
+  }
   static const uint8_t zeros[80] = {0};
   b.op = OP_PGEN;
   b.n = n;
@@ -1276,6 +1412,7 @@ int32_t plan_pgen(CuBbsBbsGpuProofGenItem *items, size_t n, const uint8_t (*seed
   b.pts48.assign(48 * n, 0);
   b.npts_per_item = 1;
   std::vector<size_t> di;
+  std::vector<uint32_t> d32;
   for (size_t i = 0; i < n; i++) {
     const auto &it = items[i];
     PgItem &p = reinterpret_cast<PgItem *>(b.items.data())[i];
@@ -1300,7 +1437,7 @@ int32_t plan_pgen(CuBbsBbsGpuProofGenItem *items, size_t n, const uint8_t (*seed
     p.hdr_len = (uint32_t)it.header.len;
     p.ph_off = b.blob.put(it.presentation_header.data, it.presentation_header.len);
     p.ph_len = (uint32_t)it.presentation_header.len;
-    std::vector<uint32_t> d32(di.begin(), di.end());
+    d32.assign(di.begin(), di.end());
     p.idx_off = b.blob.put_u32s(d32);
     p.seed_off = b.blob.put(seeds ? seeds[i] : &os_seeds[32 * i], 32);
     p.msg_base = (uint32_t)b.ml.count();
@@ -1370,12 +1507,47 @@ extern "C" int32_t cubbs_bbs_gpu_proof_verify_batch_v2(uint32_t abi, const CuBbs
   try {
     CallScope scope;
     Runtime &rt = scope.rt;
-    OpBatch b;
+    OpBatch b(rt);
     int32_t st = plan_pverify(items, n, b);
     if (st != CUBBS_BBS_GPU_SUCCESS) return st;
     finish_pks(rt, b);
     execute(rt, b);
     download_bool(rt, b, results);
+    return CUBBS_BBS_GPU_SUCCESS;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}
+
+// Test export: host-side phase times (ms) of one ProofVerify call, in order:
+// workspace, plan, public keys, upload, device pipeline, results.
+extern "C" int32_t cubbs_bbs_gpu_proof_verify_phases_for_test_v2(const CuBbsBbsGpuProofVerifyItem *items, size_t n,
+                                                                 CuBbsBbsGpuResult *results, double *ms6) {
+  if (!items || !results || !ms6 || n == 0) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  using clk = std::chrono::steady_clock;
+  try {
+    auto t0 = clk::now();
+    CallScope scope;
+    Runtime &rt = scope.rt;
+    auto t1 = clk::now();
+    OpBatch b(rt);
+    int32_t st = plan_pverify(items, n, b);
+    if (st != CUBBS_BBS_GPU_SUCCESS) return st;
+    auto t2 = clk::now();
+    finish_pks(rt, b);
+    auto t3 = clk::now();
+    g_h2d_bytes = g_d2h_bytes = 0;
+    upload(rt, b);
+    uint8_t *mapdst = upload_mapdst(rt);
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    auto t4 = clk::now();
+    run(rt, b, mapdst);
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    auto t5 = clk::now();
+    download_bool(rt, b, results);
+    auto t6 = clk::now();
+    const clk::time_point t[7] = {t0, t1, t2, t3, t4, t5, t6};
+    for (int k = 0; k < 6; k++) ms6[k] = std::chrono::duration<double, std::milli>(t[k + 1] - t[k]).count();
     return CUBBS_BBS_GPU_SUCCESS;
   } catch (const CudaError &) {
     return CUBBS_BBS_GPU_ERR_INTERNAL;
@@ -1390,7 +1562,7 @@ extern "C" int32_t cubbs_bbs_gpu_verify_batch_v2(uint32_t abi, const CuBbsBbsGpu
   try {
     CallScope scope;
     Runtime &rt = scope.rt;
-    OpBatch b;
+    OpBatch b(rt);
     int32_t st = plan_verify(items, n, b);
     if (st != CUBBS_BBS_GPU_SUCCESS) return st;
     finish_pks(rt, b);
@@ -1410,7 +1582,7 @@ extern "C" int32_t cubbs_bbs_gpu_sign_batch_v2(uint32_t abi, CuBbsBbsGpuSignItem
   try {
     CallScope scope;
     Runtime &rt = scope.rt;
-    OpBatch b;
+    OpBatch b(rt);
     int32_t st = plan_sign(items, n, b);
     if (st != CUBBS_BBS_GPU_SUCCESS) return st;
     finish_pks(rt, b);
@@ -1444,7 +1616,7 @@ static int32_t proof_gen_impl(CuBbsBbsGpuProofGenItem *items, size_t n, const ui
   try {
     CallScope scope;
     Runtime &rt = scope.rt;
-    OpBatch b;
+    OpBatch b(rt);
     std::vector<uint8_t> os_seeds;
     int32_t st = plan_pgen(items, n, seeds, b, os_seeds);
     if (st != CUBBS_BBS_GPU_SUCCESS) return st;
@@ -1511,7 +1683,7 @@ extern "C" int32_t cubbs_bbs_gpu_bench_device_steps_v2(uint32_t abi, int32_t op,
   try {
     CallScope scope;
     Runtime &rt = scope.rt;
-    OpBatch b;
+    OpBatch b(rt);
     std::vector<uint8_t> os_seeds;
     int32_t st;
     switch (op) {

@@ -237,6 +237,7 @@ Runtime::Runtime(SharedState &s)
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_sub, cudaEventDisableTiming));
   arena.reserve((size_t)256 << 20);
   staging.reserve((size_t)64 << 20);
+  pack.reserve((size_t)64 << 20);
 }
 
 // Growth from inside a call: drop the shared hold, grow under the exclusive
@@ -346,6 +347,7 @@ CallScope::CallScope() : rt(acquire_workspace()), lock(rt.sh.mu) {
   rt.lock = &lock;
   rt.arena.reset();
   rt.staging.reset();
+  rt.pack.reset();
 }
 
 CallScope::~CallScope() {

@@ -154,6 +154,7 @@ struct Runtime {
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_mid = nullptr, ev_side = nullptr, ev_sub = nullptr;
   DeviceArena arena;
   HostStaging staging;
+  HostStaging pack;  // pinned: the packed batch bytes, copied to the device without a host copy
   std::shared_lock<std::shared_mutex> *lock = nullptr;  // the running call's shared hold
 
   explicit Runtime(SharedState &s);

@@ -245,14 +245,16 @@ def _pv_items(oracle, seed, count, L, fake=()):
 def test_proof_verify_aggregated_groups(gpu, oracle):
     """Batches of 128 or more check each key's proofs (16 or more) as one group;
     a group that fails is checked item by item.  Every verdict equals the
-    oracle's and the verdict of the same item in a batch too small to group."""
-    big = _pv_items(oracle, b"agg-a", 136, 6, fake={5, 77, 130})
+    oracle's and the verdict of the same item in a batch too small to group.
+    266 items also take the multi-threaded packing of the call."""
+    big = _pv_items(oracle, b"agg-a", 236, 6, fake={5, 77, 130, 201})
     small = _pv_items(oracle, b"agg-b", 10, 6, fake={3})
     clean = _pv_items(oracle, b"agg-c", 20, 6)
     items = big + small + clean
     items[40] = items[40][:3] + (b"p!",) + items[40][4:]   # challenge mismatch
+    items[150] = items[150][:1] + (items[150][1][:200],) + items[150][2:]  # too short: rejected by shape
     want = [oracle.proof_verify(pk, pr, hd, ph, dm, di) == 0 for pk, pr, hd, ph, dm, di, _ in items]
-    assert want.count(False) == 5
+    assert want.count(False) == 7
     got = [v for _, v in gpu.proof_verify_batch(items)]
     assert got == want
     alone = []
