@@ -242,19 +242,46 @@ __global__ void __launch_bounds__(32) k_agg_scale(const PvItem *items0, uint32_t
 // Grid (groups, 2): block (g, 0) sums the scaled Abar of group g's items (in
 // perm[goff[g] .. goff[g+1])), block (g, 1) the scaled Bbar; each writes its
 // half of the group's pairing job in affine form (the job's flags start at 0).
-__global__ void __launch_bounds__(512) k_agg_sum(const g1 *scaled, const uint32_t *perm, const uint32_t *goff,
+// 256 threads = 128 lane pairs: every pair sums a strided share of the items,
+// then the pairs' sums are added by shuffles within each warp and through
+// shared memory across the 8 warps.
+DEV g1 shfl_down_g1_all(const g1 &p, int delta) {
+  g1 r;
+#pragma unroll
+  for (int i = 0; i < 12; i++) {
+    r.X.w[i] = __shfl_down_sync(0xffffffffu, p.X.w[i], delta);
+    r.Y.w[i] = __shfl_down_sync(0xffffffffu, p.Y.w[i], delta);
+    r.ZZ.w[i] = __shfl_down_sync(0xffffffffu, p.ZZ.w[i], delta);
+    r.ZZZ.w[i] = __shfl_down_sync(0xffffffffu, p.ZZZ.w[i], delta);
+  }
+  return r;
+}
+// Sum of the 16 pairs' points of a warp (valid on lanes 0 and 1).
+DEV g1 warp_sum_pairs(const LanePair &lp, g1 acc) {
+#pragma unroll 1
+  for (int d = 2; d < 32; d *= 2) {
+    const g1 o = shfl_down_g1_all(acc, d);
+    const bool has = ((threadIdx.x & 31) + d) < 32;
+    const g1 sum = g1_add_pair(lp, acc, o);
+    if (has) acc = sum;
+  }
+  return acc;
+}
+__global__ void __launch_bounds__(256) k_agg_sum(const g1 *scaled, const uint32_t *perm, const uint32_t *goff,
                                                  const int32_t *gslot, PairJob *gjobs) {
-  __shared__ g1 part[16];
+  __shared__ g1 part[8];
   const uint32_t g = blockIdx.x, which = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const LanePair lp = LanePair::here();
   g1 a = g1_inf();
   #pragma unroll 1
-  for (uint32_t k = goff[g] + threadIdx.x; k < goff[g + 1]; k += blockDim.x) a = g1_add(a, scaled[2 * perm[k] + which]);
-  a = warp_sum_g1(a);
+  for (uint32_t k = goff[g] + (threadIdx.x >> 1); k < goff[g + 1]; k += blockDim.x >> 1)
+    a = g1_add_pair(lp, a, scaled[2 * perm[k] + which]);
+  a = warp_sum_pairs(lp, a);
   if (lane == 0) part[warp] = a;
   __syncthreads();
   if (warp == 0) {
-    a = lane < 16 ? part[lane] : g1_inf();
-    a = warp_sum_g1(a);
+    a = lane < 16 ? part[lane >> 1] : g1_inf();
+    a = warp_sum_pairs(lp, a);
     if (lane == 0) {
       g1a aff;
       const bool finite = g1_to_aff(a, aff);
@@ -978,7 +1005,7 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
     SPAN(s3, "pairing_aggregate",
          k_agg_scale<<<blocks_for(4 * n, 32), 32, 0, s3>>>(it0, N, b.pts, b.dec, b.group_of, seed, b.scaled);
          CUBBS_CHECK(cudaMemsetAsync(b.gjobs, 0, G * sizeof(PairJob), s3));
-         k_agg_sum<<<dim3(G, 2), 512, 0, s3>>>(b.scaled, b.perm, b.goff, b.gslot, b.gjobs);
+         k_agg_sum<<<dim3(G, 2), 256, 0, s3>>>(b.scaled, b.perm, b.goff, b.gslot, b.gjobs);
          launch_pairing_check(s3, b.gjobs, G, rt.d_lines, b.gok));
     SPAN(s3, "pairing_kernel",
          k_pv_pairjobs_agg<<<blocks_for(n, 128), 128, 0, s3>>>(it0, N, b.pts, b.dec, b.group_of, b.gok, b.pj,
