@@ -360,9 +360,21 @@ def prog_add(g):
     return reg_out(REG_F, sym_reg(g, REG_F) * (sym_line(g, 0) * sym_line(g, 1)))
 
 
+def prog_dbl1(g):
+    return reg_out(REG_F, sym_reg(g, REG_F).sqr() * sym_line(g, 0))
+
+
+def prog_add1(g):
+    return reg_out(REG_F, sym_reg(g, REG_F) * sym_line(g, 0))
+
+
 PROGRAMS = {
     "DBL": prog_dbl,
     "ADD": prog_add,
+    # one pair's Miller loop (a warp per pair; the warps' values are multiplied after)
+    "DBL1": prog_dbl1,
+    "ADD1": prog_add1,
+    "MUL_F_F_X": lambda g: reg_out(REG_F, sym_reg(g, REG_F) * sym_reg(g, REG_X)),
     "CONJ_F": lambda g: reg_out(REG_F, sym_reg(g, REG_F, conj=True)),
     "INV_U_F": lambda g: reg_out(REG_U, sym_reg(g, REG_F).inv()),
     "EASY1_T": lambda g: reg_out(REG_T, sym_reg(g, REG_F, conj=True) * sym_reg(g, REG_U)),
@@ -623,6 +635,9 @@ def expected(name, s):
     table = {
         "DBL": (REG_F, lambda: wmul(wmul(F, F), lam)),
         "ADD": (REG_F, lambda: wmul(F, lam)),
+        "DBL1": (REG_F, lambda: wmul(wmul(F, F), line(0))),
+        "ADD1": (REG_F, lambda: wmul(F, line(0))),
+        "MUL_F_F_X": (REG_F, lambda: wmul(F, X)),
         "CONJ_F": (REG_F, lambda: wconj(F)),
         "INV_U_F": (REG_U, lambda: wpow(F, P ** 12 - 2)),
         "EASY1_T": (REG_T, lambda: wmul(wconj(F), U)),

@@ -1006,7 +1006,7 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
          k_agg_scale<<<blocks_for(4 * n, 32), 32, 0, s3>>>(it0, N, b.pts, b.dec, b.group_of, seed, b.scaled);
          CUBBS_CHECK(cudaMemsetAsync(b.gjobs, 0, G * sizeof(PairJob), s3));
          k_agg_sum<<<dim3(G, 2), 256, 0, s3>>>(b.scaled, b.perm, b.goff, b.gslot, b.gjobs);
-         launch_pairing_check(s3, b.gjobs, G, rt.d_lines, b.gok));
+         launch_pairing_check_split(s3, b.gjobs, G, rt.d_lines, b.gok));
     SPAN(s3, "pairing_kernel",
          k_pv_pairjobs_agg<<<blocks_for(n, 128), 128, 0, s3>>>(it0, N, b.pts, b.dec, b.group_of, b.gok, b.pj,
                                                                 b.ok);

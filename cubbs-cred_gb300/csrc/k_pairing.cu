@@ -59,6 +59,45 @@ __global__ void __launch_bounds__(32) k_pairing_check_warp(const PairJob *jobs, 
   if (lane == 0) ok[item] = one ? 1 : 0;
 }
 
+// One pairing check per block of two warps (for the few group checks of an
+// aggregated batch, where one check's latency is the step's critical path):
+// warp w runs the Miller loop of pair w, then warp 0 multiplies the two values
+// and runs the final exponentiation.  Dynamic shared memory: 2 * PP_SLOTS Fp slots.
+__global__ void __launch_bounds__(64) k_pairing_check_split(const PairJob *jobs, uint32_t n, const line2 *lines,
+                                                            uint8_t *ok) {
+  extern __shared__ __align__(16) uint8_t pp_smem[];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  fp *sl = reinterpret_cast<fp *>(pp_smem) + warp * PP_SLOTS;
+  const uint32_t item = blockIdx.x;
+  if (item >= n) return;
+  const PairJob &j = jobs[item];
+  if (j.active != 1) {  // 0: not evaluated (result 0); 2: settled before the launch (ok[item] kept)
+    if (threadIdx.x == 0 && j.active == 0) ok[item] = 0;
+    return;
+  }
+  const bool skip = (j.flags >> warp) & 1;
+  const line2 *L = lines + (size_t)(warp ? j.slot_b : j.slot_a) * MILLER_LINES;
+  pp::miller_one(sl, lane, warp ? j.pb : j.pa, L, skip);
+  __syncthreads();
+  if (warp != 0) return;
+  if (lane < 12) pp::st(sl, PP_REG(PP_REG_X) + lane, pp::ld(sl + PP_SLOTS, PP_REG(PP_REG_F) + lane));
+  __syncwarp();
+  pp::run(sl, lane, PP_MUL_F_F_X);
+  pp::run(sl, lane, PP_CONJ_F);  // z < 0
+  const bool one = pp::final_exp_is_one(sl, lane);
+  if (lane == 0) ok[item] = one ? 1 : 0;
+}
+
+void launch_pairing_check_split(cudaStream_t s, const PairJob *jobs, uint32_t n, const line2 *lines, uint8_t *ok) {
+  const size_t smem = 2 * (size_t)PP_SLOTS * sizeof(fp);
+  static const bool attr = [smem] {
+    CUBBS_CHECK(cudaFuncSetAttribute(k_pairing_check_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    return true;
+  }();
+  (void)attr;
+  if (n) k_pairing_check_split<<<n, 64, smem, s>>>(jobs, n, lines, ok);
+}
+
 // Latency probe: SM cycles of one run of each pairing program on a lone warp
 // (slots filled with Montgomery one; the values do not change the path).
 __global__ void __launch_bounds__(32) k_pp_probe(double *cycles, int reps) {

@@ -193,4 +193,53 @@ DEV bool pairing_check(fp *sl, int lane, const g1a *P, const line2 *const *L, co
   return final_exp_is_one(sl, lane);
 }
 
+// ---- one pair per warp
+// The Miller loop of a single pair (P, lines L) into register F of this warp's
+// slot array; a skipped pair leaves F = 1.  Also loads the Frobenius constants
+// and the zero slot, so the warp can run the final exponentiation after.
+DEV void miller_one(fp *sl, int lane, const g1a &P, const line2 *L, bool skip) {
+  if (lane < 10) {
+    const fp2 g[6] = C_FROB_GAMMA;
+    const fp2 &ge = g[1 + (lane >> 1)];
+    st(sl, PP_GAMMA_BASE + lane, (lane & 1) ? ge.c1 : ge.c0);
+  } else if (lane < 12) {
+    st(sl, PP_PT_BASE + lane - 10, skip ? fp_zero() : ((lane & 1) ? P.y : P.x));
+  } else if (lane == 14) {
+    st(sl, PP_ZERO_SLOT, fp_zero());
+  } else if (lane >= 16 && lane < 28) {
+    st(sl, PP_REG(PP_REG_F) + lane - 16, lane == 16 ? fp_one() : fp_zero());
+  }
+  __syncwarp();
+  int idx = 0;
+#pragma unroll 1
+  for (int i = 62; i >= 0; i--) {
+    if (lane < 4) {
+      fp v;
+      if (skip) v = lane == 0 ? fp_one() : fp_zero();
+      else {
+        const line2 &l = L[idx];
+        v = lane == 0 ? l.a.c0 : lane == 1 ? l.a.c1 : lane == 2 ? l.b.c0 : l.b.c1;
+      }
+      st(sl, PP_LINE_BASE + lane, v);
+    }
+    __syncwarp();
+    idx++;
+    run(sl, lane, PP_DBL1);
+    if (zabs_bit(i)) {
+      if (lane < 4) {
+        fp v;
+        if (skip) v = lane == 0 ? fp_one() : fp_zero();
+        else {
+          const line2 &l = L[idx];
+          v = lane == 0 ? l.a.c0 : lane == 1 ? l.a.c1 : lane == 2 ? l.b.c0 : l.b.c1;
+        }
+        st(sl, PP_LINE_BASE + lane, v);
+      }
+      __syncwarp();
+      idx++;
+      run(sl, lane, PP_ADD1);
+    }
+  }
+}
+
 }  // namespace pp

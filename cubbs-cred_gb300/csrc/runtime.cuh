@@ -247,5 +247,7 @@ struct PairJob {
   uint32_t active;  // 1: evaluate; 0: not evaluated (result 0); 2: result already written
 };
 void launch_pairing_check(cudaStream_t s, const PairJob *jobs, uint32_t n, const line2 *lines, uint8_t *ok);
+// the same check with one warp per pair (lower latency for a few checks)
+void launch_pairing_check_split(cudaStream_t s, const PairJob *jobs, uint32_t n, const line2 *lines, uint8_t *ok);
 
 }  // namespace cubbs
