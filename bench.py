@@ -51,6 +51,13 @@ MODEL_M = {
 }
 
 
+# DRAM bytes per launch of a stage's kernel at this workload, from one ncu capture
+# (dram__bytes_read.sum + dram__bytes_write.sum): k_fixed_msm read 12.77 MB for
+# 512 rows x 12 terms x 16 windows at L = 10; table reads scale with rows x terms,
+# so a 1024 x 102-term launch moves 12.82 MB x (1024 x 102) / (512 x 12) = 218 MB.
+TRAFFIC_BYTES = {"fixed_msm": 12.82e6 * (1024 * 102) / (512 * 12)}
+
+
 def drbg(seed: bytes, label: bytes, i: int, n: int) -> bytes:
     out, ctr = b"", 0
     while len(out) < n:
@@ -425,9 +432,14 @@ def main():
     roof = None
     if model:
         achieved = n * model * IMAD_PER_M / (stage[1] / 1e3) / 1e12
+        traffic = TRAFFIC_BYTES.get(stage[0])
+        if traffic is not None and (n, L) != (1024, 100):
+            traffic = None  # measured for the 1024-proof, L = 100 workload only
         roof = {"bound": "imad", "kernel": stage[0], "achieved": round(achieved, 3), "peak": round(tera_imad, 3),
                 "unit": "T IMAD/s (32-bit integer multiply-add)", "frac": round(achieved / tera_imad, 4),
-                "traffic": None, "peak_source": "measured in this run (k_imad_peak, 16 independent mad.lo chains)",
+                "traffic": round(traffic) if traffic else None,
+                "traffic_unit": "bytes per launch (ncu capture, scaled by table reads)",
+                "peak_source": "measured in this run (k_imad_peak, 16 independent mad.lo chains)",
                 "model_m_per_op": model, "stage_ms": round(stage[1], 3)}
     whole = n * MODEL_M["proof_verify"]["total"] * IMAD_PER_M / (pv_step / 1e3) / 1e12
 
