@@ -17,6 +17,9 @@
 #include <algorithm>
 #include <chrono>
 #include <thread>
+#include <mutex>
+#include <condition_variable>
+#include <functional>
 #include <cstdio>
 #include <cstring>
 
@@ -766,6 +769,90 @@ struct MsgList {
   size_t count() const { return offs.size(); }
 };
 
+// Host workers that pack large batches: created once, they wait for work
+// between calls.  One parallel_for runs at a time; a call that finds the pool
+// busy (another host thread is packing) runs its ranges on its own thread.
+class PackPool {
+ public:
+  static PackPool &get() {
+    static PackPool pool;
+    return pool;
+  }
+  // Runs fn(r) for r = 0..ranges-1 on the workers and the calling thread.
+  void parallel_for(size_t ranges, const std::function<void(size_t)> &fn) {
+    std::unique_lock<std::mutex> owner(run_mu_, std::try_to_lock);
+    if (!owner.owns_lock() || workers_.empty()) {
+      for (size_t r = 0; r < ranges; r++) fn(r);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      fn_ = &fn;
+      ranges_ = ranges;
+      next_ = 0;
+      done_ = 0;
+      gen_++;
+    }
+    cv_.notify_all();
+    drain();
+    std::unique_lock<std::mutex> lk(mu_);
+    done_cv_.wait(lk, [&] { return done_ == ranges_; });
+    fn_ = nullptr;
+  }
+
+ private:
+  PackPool() {
+    const unsigned hw = std::thread::hardware_concurrency();
+    const unsigned n = hw > 1 ? std::min(7u, hw - 1) : 0;
+    for (unsigned k = 0; k < n; k++) workers_.emplace_back([this] { worker(); });
+  }
+  ~PackPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto &t : workers_) t.join();
+  }
+  // Takes ranges until none are left.
+  void drain() {
+    for (;;) {
+      size_t r;
+      const std::function<void(size_t)> *fn;
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (!fn_ || next_ >= ranges_) return;
+        r = next_++;
+        fn = fn_;
+      }
+      (*fn)(r);
+      {
+        std::lock_guard<std::mutex> lk(mu_);
+        if (++done_ == ranges_) done_cv_.notify_all();
+      }
+    }
+  }
+  void worker() {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(mu_);
+        cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+        if (stop_) return;
+        seen = gen_;
+      }
+      drain();
+    }
+  }
+  std::vector<std::thread> workers_;
+  std::mutex run_mu_, mu_;
+  std::condition_variable cv_, done_cv_;
+  const std::function<void(size_t)> *fn_ = nullptr;
+  size_t ranges_ = 0, next_ = 0, done_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
 // Sorted, de-duplicated disclosed indexes (proof.rs:961-963); callers
 // usually pass them sorted already, which needs no sort.
 void sort_dedup(const size_t *p, size_t n, std::vector<size_t> &out) {
@@ -1281,16 +1368,10 @@ int32_t plan_pverify(const CuBbsBbsGpuProofVerifyItem *items, size_t n, OpBatch 
       maxL = std::max(maxL, L);
     }
   };
-  const size_t threads = n >= 256 ? std::min<size_t>(8, n / 128) : 1;
-  std::vector<size_t> maxLs(threads, 0);
-  if (threads == 1) {
-    pack_range(0, n, maxLs[0]);
-  } else {
-    std::vector<std::thread> pool;
-    for (size_t t = 0; t < threads; t++)
-      pool.emplace_back(pack_range, n * t / threads, n * (t + 1) / threads, std::ref(maxLs[t]));
-    for (auto &th : pool) th.join();
-  }
+  const size_t ranges = n >= 256 ? std::min<size_t>(16, n / 64) : 1;
+  std::vector<size_t> maxLs(ranges, 0);
+  if (ranges == 1) pack_range(0, n, maxLs[0]);
+  else PackPool::get().parallel_for(ranges, [&](size_t r) { pack_range(n * r / ranges, n * (r + 1) / ranges, maxLs[r]); });
   for (size_t m : maxLs) b.maxL = std::max(b.maxL, m);
   return CUBBS_BBS_GPU_SUCCESS;
 }
