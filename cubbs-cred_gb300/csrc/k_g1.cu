@@ -76,15 +76,12 @@ DEV uint32_t scalar_bits(const fr &s, int pos, int w) {
   return (uint32_t)(v & ((1u << w) - 1));
 }
 
-// Fixed-base MSM: row r = sum_g scalars[r*stride + g] * G_g, g < nterms[r].
-// One warp per row; lane l takes generators l, l+32, ...; per generator the
-// scalar is recoded into signed w-bit digits on the fly and each nonzero digit
-// costs one table lookup and one mixed addition.
-__global__ void __launch_bounds__(128) k_fixed_msm(FixedTable t, const fr *scalars, uint32_t stride,
-                                                   const uint32_t *nterms, uint32_t rows, g1 *out) {
-  uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-  int lane = threadIdx.x & 31;
-  if (row >= rows) return;  // whole warp exits together
+// One MSM row on one warp (all lanes call it): lane l takes generators
+// l, l+32, ...; per generator the scalar is recoded into signed w-bit digits
+// on the fly and each nonzero digit costs one table lookup and one mixed
+// addition; the lanes' sums are added by shuffles.
+DEV void fixed_msm_row(const FixedTable &t, const fr *scalars, uint32_t stride, const uint32_t *nterms, uint32_t row,
+                       int lane, g1 *out) {
   uint32_t n = nterms[row];
   g1 acc = g1_inf();
   const uint32_t full = 1u << t.w;
@@ -113,6 +110,17 @@ __global__ void __launch_bounds__(128) k_fixed_msm(FixedTable t, const fr *scala
   }
   acc = warp_sum_g1(acc);
   if (lane == 0) out[row] = acc;
+}
+
+// Fixed-base MSM: row r = sum_g scalars[r*stride + g] * G_g, g < nterms[r]; the
+// grid's warps take rows in a grid-stride loop.
+__global__ void __launch_bounds__(128) k_fixed_msm(FixedTable t, const fr *scalars, uint32_t stride,
+                                                   const uint32_t *nterms, uint32_t rows, g1 *out) {
+  const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  #pragma unroll 1
+  for (uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < rows; row += warps)  // per warp
+    fixed_msm_row(t, scalars, stride, nterms, row, lane, out);
 }
 
 // One lane pair per job (g1_mul_glv_pair): the pair splits each point
@@ -183,6 +191,8 @@ void launch_build_table(cudaStream_t s, const g1a *gens, int g0, int g1n, FixedT
 }
 void launch_fixed_msm(cudaStream_t s, const FixedTable &t, const fr *scalars, uint32_t stride,
                       const uint32_t *nterms, uint32_t rows, g1 *out) {
+  // one warp per row: fewer warps with several rows each lengthen the MSM more than they
+  // relieve the kernels that share its SMs (measured in the ProofVerify step)
   if (rows) k_fixed_msm<<<blocks_for((size_t)rows * 32, 128), 128, 0, s>>>(t, scalars, stride, nterms, rows, out);
 }
 void launch_var_mul(cudaStream_t s, const g1a *points, const VarJob *jobs, const fr *scalars, uint32_t n, g1 *out,
