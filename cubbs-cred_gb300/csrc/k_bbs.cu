@@ -449,20 +449,19 @@ struct VerifyItem {
   int32_t status;
 };
 
-__global__ void __launch_bounds__(128) k_verify_prep(VerifyItem *items, uint32_t n, const uint8_t *blob,
-                                                     const fr *msc, const fr *domain, const int32_t *dec_status,
-                                                     fr *rows, uint32_t stride, uint32_t *nterms, VarJob *jobs,
-                                                     fr *jscal) {
+// B-MSM row of each signature (needs no decoded point, so the fixed-base MSM
+// runs while the signature's A decodes).
+__global__ void __launch_bounds__(128) k_verify_rows(VerifyItem *items, uint32_t n, const uint8_t *blob,
+                                                     const fr *msc, const fr *domain, fr *rows, uint32_t stride,
+                                                     uint32_t *nterms) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   VerifyItem it = items[i];
   fr e;
-  bool ok = it.status == ST_OK && it.pk_status != DEC_BAD && dec_status[i] != DEC_BAD &&
-            fr_raw_from_be32(blob + it.sig_off + 48, e);
+  bool ok = it.status == ST_OK && it.pk_status != DEC_BAD && fr_raw_from_be32(blob + it.sig_off + 48, e);
   if (!ok) {
     if (items[i].status == ST_OK) items[i].status = ST_INVALID;
     nterms[i] = 0;
-    jobs[i] = {i, 1};
     return;
   }
   fr *row = rows + (size_t)i * stride;
@@ -471,36 +470,57 @@ __global__ void __launch_bounds__(128) k_verify_prep(VerifyItem *items, uint32_t
   row[1] = domain[i];
   #pragma unroll 1
   for (uint32_t k = 0; k < it.L; k++) row[2 + k] = msc[it.msg_base + k];
-  jobs[i] = {i, dec_status[i] == DEC_INF ? 1u : 0u};
-  jscal[i] = frr_neg(e);
 }
 
-__global__ void __launch_bounds__(64) k_verify_finish(const VerifyItem *items, uint32_t n, const g1 *B,
-                                                      const g1 *v, const g1a *A, const int32_t *dec_status,
-                                                      PairJob *pj) {
+// The variable-base job -e * A of each signature, from the untouched input
+// items and the decoded A (a signature that does not decode gets a job at
+// infinity; k_verify_finish rejects it).
+__global__ void __launch_bounds__(128) k_verify_jobs(const VerifyItem *items0, uint32_t n, const uint8_t *blob,
+                                                     const int32_t *dec_status, VarJob *jobs, fr *jscal) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  VerifyItem it = items[i];
+  const VerifyItem it = items0[i];
+  fr e;
+  const bool ok = it.status == ST_OK && dec_status[i] != DEC_BAD && fr_raw_from_be32(blob + it.sig_off + 48, e);
+  jobs[i] = {i, (!ok || dec_status[i] == DEC_INF) ? 1u : 0u};
+  jscal[i] = ok ? frr_neg(e) : fr_zero();
+}
+
+// Pairing job of each signature: e(A, PK) * e(B - e A, -P2) == 1; every lane
+// of the warp reaches the shared affine conversion.
+__global__ void __launch_bounds__(64) k_verify_finish(VerifyItem *items, uint32_t n, const g1 *B, const g1 *v,
+                                                      const g1a *A, const int32_t *dec_status,
+                                                      const int32_t *outside_g1, PairJob *pj) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool act = i < n;
+  VerifyItem it;
+  if (act) {
+    it = items[i];
+    act = it.status == ST_OK;
+    if (act && (dec_status[i] == DEC_BAD || outside_g1[i])) {
+      items[i].status = ST_INVALID;
+      act = false;
+    }
+  }
+  g1 C = g1_inf();
+  if (act) C = g1_add(B[i], v[i]);  // B - e A
+  g1a ca[1];
+  bool fin[1];
+  warp_to_aff<1>(&C, ca, fin);
+  if (i >= n) return;
   PairJob job;
   job.active = 0;
   job.flags = 0;
   job.slot_a = it.pk_slot < 0 ? 0 : it.pk_slot;
   job.slot_b = 0;
   job.pa = A[i];
-  if (it.status != ST_OK) {
-    job.pb = A[i];
-    pj[i] = job;
-    return;
+  job.pb = A[i];
+  if (act) {
+    if (fin[0]) job.pb = ca[0];
+    else job.flags |= 2;
+    if (dec_status[i] == DEC_INF || it.pk_status == DEC_INF) job.flags |= 1;
+    job.active = 1;
   }
-  g1 C = g1_add(B[i], v[i]);  // B - e A
-  g1a ca;
-  if (!g1_to_aff(C, ca)) {
-    ca = A[i];
-    job.flags |= 2;
-  }
-  job.pb = ca;
-  if (dec_status[i] == DEC_INF || it.pk_status == DEC_INF) job.flags |= 1;
-  job.active = 1;
   pj[i] = job;
 }
 
@@ -1163,15 +1183,56 @@ void run_pgen(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   b.launches_per_run = (nm ? 1 : 0) + (npts ? 1 : 0) + 7;
 }
 
+// Verify on three streams, as ProofVerify: the signature decode (stream2, no
+// subgroup check) and its GLV term run beside the message hash, the domain and
+// the B-MSM (stream); the subgroup check runs on stream4; the pairing checks
+// follow the finish kernel.  Small batches take the two-warp pairing kernel
+// (lower latency per check).
+void run_verify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
+  cudaStream_t s = rt.stream, s2 = rt.stream2, s4 = rt.stream4;
+  size_t n = b.n, nm = b.ml.count(), npts = b.pts48.size() / 48;
+  uint32_t N = (uint32_t)n, stride = (uint32_t)b.stride;
+  VerifyItem *it = reinterpret_cast<VerifyItem *>(b.ditems);
+  const VerifyItem *it0 = reinterpret_cast<const VerifyItem *>(b.ditems0);
+  CUBBS_CHECK(cudaEventRecord(rt.ev_fork, s));
+  CUBBS_CHECK(cudaStreamWaitEvent(s2, rt.ev_fork, 0));
+  SPAN(s2, "g1_decode", launch_g1_decode(s2, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, false));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_mid, s2));
+  CUBBS_CHECK(cudaStreamWaitEvent(s4, rt.ev_mid, 0));
+  SPAN(s4, "g1_subgroup", launch_g1_subgroup(s4, b.pts, b.dec, (uint32_t)npts, b.sub));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_sub, s4));
+  SPAN(s2, "var_mul",
+       k_verify_jobs<<<blocks_for(n, 128), 128, 0, s2>>>(it0, N, b.dblob, b.dec, b.jobs, b.jscal);
+       launch_var_mul(s2, b.pts, b.jobs, b.jscal, N, b.v));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_side, s2));
+  if (nm)
+    SPAN(s, "hash_messages",
+         launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
+                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1,
+                         b.msc));
+  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, b.domain));
+  SPAN(s, "scalar_prep",
+       k_verify_rows<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms));
+  SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
+  CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_side, 0));
+  CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_sub, 0));
+  SPAN(s, "finish",
+       k_verify_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.fixed, b.v, b.pts, b.dec, b.sub, b.pj));
+  if (n <= 256) SPAN(s, "pairing", launch_pairing_check_split(s, b.pj, N, rt.d_lines, b.ok));
+  else SPAN(s, "pairing", launch_pairing_check(s, b.pj, N, rt.d_lines, b.ok));
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 7;
+}
+
 // The whole device pipeline of one batch (no host work, no transfers).
 void run(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   cudaStream_t s = rt.stream;
   size_t n = b.n, nm = b.ml.count();
   uint32_t N = (uint32_t)n, stride = (uint32_t)b.stride;
   CUBBS_CHECK(cudaMemcpyAsync(b.ditems, b.ditems0, b.items.size(), cudaMemcpyDeviceToDevice, s));
-  if (b.op == OP_PVERIFY || b.op == OP_PGEN) {
+  if (b.op == OP_PVERIFY || b.op == OP_PGEN || b.op == OP_VERIFY) {
     if (b.op == OP_PVERIFY) run_pverify(rt, b, dmapdst);
-    else run_pgen(rt, b, dmapdst);
+    else if (b.op == OP_PGEN) run_pgen(rt, b, dmapdst);
+    else run_verify(rt, b, dmapdst);
     CUBBS_CHECK(cudaGetLastError());
     return;
   }
@@ -1203,19 +1264,8 @@ void run(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
       launches += 3;
       break;
     }
-    case OP_VERIFY: {
-      VerifyItem *it = reinterpret_cast<VerifyItem *>(b.ditems);
-      SPAN(s, "scalar_prep",
-           k_verify_prep<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.rows,
-                                                            stride, b.nterms, b.jobs, b.jscal));
-      SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
-      SPAN(s, "var_mul", launch_var_mul(s, b.pts, b.jobs, b.jscal, N, b.v));
-      SPAN(s, "finish",
-           k_verify_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.fixed, b.v, b.pts, b.dec, b.pj));
-      SPAN(s, "pairing", launch_pairing_check(s, b.pj, N, rt.d_lines, b.ok));
-      launches += 5;
+    case OP_VERIFY:
       break;
-    }
     case OP_PGEN:
       break;
   }
