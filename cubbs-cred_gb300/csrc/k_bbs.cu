@@ -589,12 +589,11 @@ __global__ void __launch_bounds__(64) k_pg_random(const PgItem *items, uint32_t 
   }
 }
 
-// rows 0..n-1: B = P1 + Q1 domain + sum H_i m_i ; rows n..2n-1: T2 fixed part sum_{j in U} H_j m~_j.
-// Needs no decoded signature point (k_pg_vars rejects a signature whose A does
-// not decode), so the signature decode runs beside it.
-__global__ void __launch_bounds__(128) k_pg_prep(PgItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
-                                                 const fr *domain, const fr *rs, uint32_t rs_stride, fr *rows,
-                                                 uint32_t stride, uint32_t *nterms) {
+// Row i: B = P1 + Q1 domain + sum H_i m_i.  Needs neither the decoded signature
+// point (k_pg_vars rejects a signature whose A does not decode) nor the blinding
+// scalars, so the B-MSM starts as soon as the messages are hashed.
+__global__ void __launch_bounds__(128) k_pg_rows_b(PgItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
+                                                   const fr *domain, fr *rows, uint32_t stride, uint32_t *nterms) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   PgItem it = items[i];
@@ -603,15 +602,30 @@ __global__ void __launch_bounds__(128) k_pg_prep(PgItem *items, uint32_t n, cons
   if (!ok) {
     items[i].status = ST_ERROR;
     nterms[i] = 0;
-    nterms[n + i] = 0;
     return;
   }
   fr *rb = rows + (size_t)i * stride;
-  fr *rt = rows + (size_t)(n + i) * stride;
   nterms[i] = it.L + 2;
-  nterms[n + i] = it.L + 2;
   rb[0] = frr_one();
   rb[1] = domain[i];
+  #pragma unroll 1
+  for (uint32_t m = 0; m < it.L; m++) rb[2 + m] = msc[it.msg_base + m];
+}
+
+// Row n + i: the fixed part of T2, sum_{j not disclosed} H_j m~_j, from the
+// untouched input items and the blinding scalars.
+__global__ void __launch_bounds__(128) k_pg_rows_t2(const PgItem *items0, uint32_t n, const uint8_t *blob,
+                                                    const fr *rs, uint32_t rs_stride, fr *rows, uint32_t stride,
+                                                    uint32_t *nterms) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PgItem it = items0[i];
+  if (it.status != ST_OK) {
+    nterms[n + i] = 0;
+    return;
+  }
+  fr *rt = rows + (size_t)(n + i) * stride;
+  nterms[n + i] = it.L + 2;
   rt[0] = fr_zero();
   rt[1] = fr_zero();
   const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
@@ -619,7 +633,6 @@ __global__ void __launch_bounds__(128) k_pg_prep(PgItem *items, uint32_t n, cons
   uint32_t k = 0, u = 0;
   #pragma unroll 1
   for (uint32_t m = 0; m < it.L; m++) {
-    rb[2 + m] = msc[it.msg_base + m];
     if (k < it.R && idx[k] == m) {
       rt[2 + m] = fr_zero();
       k++;
@@ -633,14 +646,14 @@ __global__ void __launch_bounds__(128) k_pg_prep(PgItem *items, uint32_t n, cons
 // Variable-base jobs on B (affine) and A: D = r2 B, Abar = r1r2 A,
 // Bbar = r1r2 B - e r1r2 A, T1 = r1~ r2 B + e~ r1r2 A, T2 += r3~ r2 B.
 __global__ void __launch_bounds__(64) k_pg_vars(PgItem *items, uint32_t n, const uint8_t *blob, const g1 *Bx,
-                                                const g1a *A, const int32_t *dec_status, const fr *rs,
-                                                uint32_t rs_stride, g1a *pts, VarJob *jobs, fr *jscal) {
+                                                const g1a *A, const int32_t *dec_status, const int32_t *outside_g1,
+                                                const fr *rs, uint32_t rs_stride, g1a *pts, VarJob *jobs, fr *jscal) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   PgItem it = items[i];
   for (int k = 0; k < 7; k++) jobs[7 * i + k] = {2 * i, 1};
   if (it.status != ST_OK) return;
-  if (dec_status[i] == DEC_BAD) {  // signature A does not decode
+  if (dec_status[i] == DEC_BAD || outside_g1[i]) {  // signature A does not decode to a point of G1
     items[i].status = ST_ERROR;
     return;
   }
@@ -1145,9 +1158,10 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 8 + (G ? 3 : 0);
 }
 
-// ProofGen on three streams: the signature decode (stream3) and the blinding
-// scalars (stream2) run beside the message hash, the domain and the B / T2
-// fixed-base MSMs; the variable-base terms need all of them.
+// ProofGen on three streams: the signature decode (stream3) runs beside
+// everything before the variable-base terms; the B-MSM follows the message hash
+// and the domain (stream) while the blinding scalars and the T2 fixed-base MSM
+// run on stream2; the variable-base terms need all of them.
 void run_pgen(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   cudaStream_t s = rt.stream, s2 = rt.stream2, s3 = rt.stream3;
   size_t n = b.n, nm = b.ml.count(), npts = b.pts48.size() / 48;
@@ -1157,9 +1171,13 @@ void run_pgen(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   CUBBS_CHECK(cudaEventRecord(rt.ev_fork, s));
   CUBBS_CHECK(cudaStreamWaitEvent(s2, rt.ev_fork, 0));
   CUBBS_CHECK(cudaStreamWaitEvent(s3, rt.ev_fork, 0));
-  SPAN(s3, "g1_decode", launch_g1_decode(s3, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, true));
+  SPAN(s3, "g1_decode", launch_g1_decode(s3, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, false));
+  SPAN(s3, "g1_subgroup", launch_g1_subgroup(s3, b.pts, b.dec, (uint32_t)npts, b.sub));
   CUBBS_CHECK(cudaEventRecord(rt.ev_join, s3));
   SPAN(s2, "random_scalars", k_pg_random<<<blocks_for(n, 64), 64, 0, s2>>>(it0, N, b.dblob, b.rs, rss));
+  SPAN(s2, "fixed_msm_t2",
+       k_pg_rows_t2<<<blocks_for(n, 128), 128, 0, s2>>>(it0, N, b.dblob, b.rs, rss, b.rows, stride, b.nterms);
+       launch_fixed_msm(s2, rt.table, b.rows + (size_t)n * stride, stride, b.nterms + n, N, b.fixed + n));
   CUBBS_CHECK(cudaEventRecord(rt.ev_side, s2));
   if (nm)
     SPAN(s, "hash_messages",
@@ -1167,20 +1185,19 @@ void run_pgen(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
                          reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1,
                          b.msc));
   SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, b.domain));
+  SPAN(s, "fixed_msm",
+       k_pg_rows_b<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms);
+       launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_side, 0));
-  SPAN(s, "scalar_prep",
-       k_pg_prep<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rs, rss, b.rows, stride,
-                                                    b.nterms));
-  SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, 2 * N, b.fixed));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_join, 0));
   SPAN(s, "var_prep",
-       k_pg_vars<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.fixed, b.pts, b.dec, b.rs, rss, b.vpts, b.jobs,
-                                                  b.jscal));
+       k_pg_vars<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.fixed, b.pts, b.dec, b.sub, b.rs, rss, b.vpts,
+                                                  b.jobs, b.jscal));
   SPAN(s, "var_mul", launch_var_mul(s, b.vpts, b.jobs, b.jscal, 7 * N, b.v));
   SPAN(s, "finish",
        k_pg_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rs, rss, b.fixed + n, b.v,
                                                     b.out));
-  b.launches_per_run = (nm ? 1 : 0) + (npts ? 1 : 0) + 7;
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 9;
 }
 
 // Verify on three streams, as ProofVerify: the signature decode (stream2, no
