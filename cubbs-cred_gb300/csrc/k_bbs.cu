@@ -563,22 +563,47 @@ __global__ void __launch_bounds__(64) k_pg_random(const PgItem *items, uint32_t 
     sha_byte(c, 0);
     sha_bytes(c, dst, DST_MOCK_LEN);
     sha_byte(c, DST_MOCK_LEN);
-    uint8_t b0[32], bi[32];
+    uint8_t b0[32];
     sha_final(c, b0);
+    // b_i = SHA-256((b_0 xor b_(i-1)) || I2OSP(i, 1) || DST || I2OSP(68, 1)): 102 bytes
+    // in two blocks.  Block 1 is 8 words of b_0 xor b_(i-1), then i and DST[0..30];
+    // block 2 (DST[31..67], the DST length, the padding, the bit length 816) is the
+    // same for every i.
+    uint32_t x0[8], bi[8] = {0, 0, 0, 0, 0, 0, 0, 0}, tail1[7], blk2[16];
+    for (int k = 0; k < 8; k++)
+      x0[k] = (uint32_t)b0[4 * k] << 24 | (uint32_t)b0[4 * k + 1] << 16 | (uint32_t)b0[4 * k + 2] << 8 | b0[4 * k + 3];
+    const uint32_t dst3 = (uint32_t)dst[0] << 16 | (uint32_t)dst[1] << 8 | dst[2];
+    for (int k = 0; k < 7; k++)
+      tail1[k] = (uint32_t)dst[3 + 4 * k] << 24 | (uint32_t)dst[4 + 4 * k] << 16 | (uint32_t)dst[5 + 4 * k] << 8 |
+                 dst[6 + 4 * k];
+    {
+      uint8_t t[64];
+      for (int k = 0; k < 37; k++) t[k] = dst[31 + k];
+      t[37] = DST_MOCK_LEN;
+      t[38] = 0x80;
+      for (int k = 39; k < 64; k++) t[k] = 0;
+      t[62] = (uint8_t)((102 * 8) >> 8);
+      t[63] = (uint8_t)(102 * 8);
+      for (int k = 0; k < 16; k++)
+        blk2[k] = (uint32_t)t[4 * k] << 24 | (uint32_t)t[4 * k + 1] << 16 | (uint32_t)t[4 * k + 2] << 8 | t[4 * k + 3];
+    }
     uint8_t okm[48];
     uint32_t fill = 0, produced = 0;
     uint32_t ell = (nbytes + 31) / 32;
     #pragma unroll 1
     for (uint32_t b = 1; b <= ell; b++) {
-      sha_ctx s;
-      sha_init(s);
-      for (int j = 0; j < 32; j++) sha_byte(s, b == 1 ? b0[j] : (uint8_t)(b0[j] ^ bi[j]));
-      sha_byte(s, (uint8_t)b);
-      sha_bytes(s, dst, DST_MOCK_LEN);
-      sha_byte(s, DST_MOCK_LEN);
-      sha_final(s, bi);
+      uint32_t h[8] = {0x6a09e667u, 0xbb67ae85u, 0x3c6ef372u, 0xa54ff53au,
+                       0x510e527fu, 0x9b05688cu, 0x1f83d9abu, 0x5be0cd19u};
+      uint32_t w[16];
+      for (int k = 0; k < 8; k++) w[k] = x0[k] ^ bi[k];  // bi = 0 before b_1
+      w[8] = b << 24 | dst3;
+      for (int k = 0; k < 7; k++) w[9 + k] = tail1[k];
+      sha256_compress(h, w);
+      for (int k = 0; k < 16; k++) w[k] = blk2[k];
+      sha256_compress(h, w);
+      for (int k = 0; k < 8; k++) bi[k] = h[k];
       for (int j = 0; j < 32; j++) {
-        okm[fill++] = bi[j];
+        okm[fill++] = (uint8_t)(bi[j >> 2] >> (24 - 8 * (j & 3)));
         if (fill == 48) {
           out[c0 + produced] = fr_raw_from_okm(okm);
           produced++;
