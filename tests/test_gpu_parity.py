@@ -145,6 +145,39 @@ def test_proof_roundtrip_random(gpu, oracle, L, R):
     assert [v for _, v in ver] == [True, False] * len(reqs)
 
 
+def test_proof_gen_chunked_random_scalars(gpu, oracle):
+    """L = 200 with 10 disclosed: 5 + U = 195 blinding scalars exceed one
+    expand_message call (255 x 32 bytes), so they are drawn in chunks; bytes equal
+    the oracle's, and the proofs verify (generators beyond the first 128)."""
+    seed = b"proof-chunked"
+    sk, pk = keypair(oracle, seed)
+    reqs, seeds = [], []
+    for i in range(3):
+        msgs = messages(seed, i, 200, 32)
+        sig = oracle.sign(sk, pk, b"h", msgs)[0]
+        di = disclosed_subset(seed, i, 200, 10)
+        reqs.append((pk, sig, b"h", b"p", msgs, di))
+        seeds.append(drbg(seed, b"seed", i, 32))
+    got = gpu.proof_gen_batch(reqs, seeds=seeds)
+    for (pk_, sig, hdr, ph, msgs, di), sd, (code, proof) in zip(reqs, seeds, got):
+        assert code == 0 and proof == oracle.proof_gen(pk_, sig, hdr, ph, msgs, di, seed=sd)
+    ver = gpu.proof_verify_batch([(pk_, proof, hdr, ph, [msgs[j] for j in di], di, 200)
+                                  for (pk_, sig, hdr, ph, msgs, di), (_, proof) in zip(reqs, got)])
+    assert all(c == 0 and v for c, v in ver)
+
+
+def test_empty_batches(gpu):
+    """A batch of zero items succeeds without touching the device."""
+    import ctypes
+    lib = gpu.lib()
+    res = (gpu.Result * 1)()
+    for name in ("sign", "verify", "proof_gen", "proof_verify"):
+        fn = getattr(lib, "cubbs_bbs_gpu_%s_batch_v2" % name)
+        fn.restype = ctypes.c_int32
+        fn.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+        assert fn(2, None, 0, ctypes.cast(res, ctypes.c_void_p)) == 0, name
+
+
 def test_proof_gen_os_randomness_verifies(gpu, oracle):
     seed = b"proof-os"
     sk, pk = keypair(oracle, seed)
