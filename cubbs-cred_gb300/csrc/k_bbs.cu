@@ -431,14 +431,19 @@ __global__ void __launch_bounds__(64) k_sign_prep(SignItem *items, uint32_t n, c
 
 __global__ void __launch_bounds__(64) k_sign_finish(SignItem *items, uint32_t n, const g1 *A, const fr *e,
                                                     uint8_t *sig) {
-  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  if (items[i].status != ST_OK) return;
-  if (g1_is_inf(A[i])) {  // "A == Identity_G1" (signature.rs:653-657)
+  // every lane of the warp reaches the shared affine conversion below
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  bool act = i < n && items[i].status == ST_OK;
+  if (act && g1_is_inf(A[i])) {  // "A == Identity_G1" (signature.rs:653-657)
     items[i].status = ST_ERROR;
-    return;
+    act = false;
   }
-  g1_compress(A[i], sig + 80 * (size_t)i);
+  const g1 p = act ? A[i] : g1_inf();
+  g1a a[1];
+  bool fin[1];
+  warp_to_aff<1>(&p, a, fin);
+  if (!act) return;
+  g1_compress_aff_or_inf(a[0], fin[0], sig + 80 * (size_t)i);
   fr_raw_to_be32(e[i], sig + 80 * (size_t)i + 48);
 }
 
