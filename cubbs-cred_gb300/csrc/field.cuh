@@ -153,108 +153,169 @@ DEV fp fp_inv(fp a) {
                           0xf38512bfu, 0x64774b84u, 0x434bacd7u, 0x4b1ba7b6u, 0x397fe69au, 0x1a0111eau};
   return fp_pow_window(a, e);
 }
-// Variable-time inverse for public values (binary extended Euclid on the
-// Montgomery residue y = aR: y^-1 = a^-1 R^-1, and one product with R^3 mod p
-// gives the Montgomery form a^-1 R).  About 2 x 381 shift/subtract steps on a
-// single thread instead of the ~450 dependent products of a^(p-2).
-DEVNI fp fp_inv_vartime(fp a) {
-  if (fp_is_zero(a)) return a;
-  const fp pm = FP_MOD_INIT;
-  uint32_t u[12], v[12], x1[12], x2[12];
+// Variable-time inverse for public values: the optimized binary GCD of
+// T. Pornin, "Optimized Binary GCD for Modular Inversion" (IACR ePrint
+// 2020/972).  Each outer iteration runs 30 binary-GCD divsteps on 64-bit
+// approximations of (a, b) (the low 31 bits and the top 33 bits of the longer
+// value's length), then applies the resulting 2x2 matrix of factors in
+// [-2^30, 2^30] to the full 381-bit a, b (exact division by 2^30) and to the
+// companions u, v (Montgomery division by 2^30 mod p).  The invariants
+// a c = y u and b c = y v (mod p), with u = c = R^2 mod p at the start, end at
+// b = 1, v = R^2 / y; for the Montgomery residue y = aR that is a^-1 R, the
+// Montgomery form of the inverse.  2 * 381 - 1 divsteps suffice (Pornin,
+// section 3), so at most 26 outer iterations run; 32 only bound the loop.
+// The accumulators stay inside int64: |a_i f| + |b_i g| < 2^63, and with the
+// Montgomery term k p_i < 2^62 added, |u_i f| + |v_i g| + k p_i < 3 * 2^62.
+namespace inv_detail {
+constexpr uint32_t FP_NEG_PINV = 0xfffcfffdu;  // -p^-1 mod 2^32
+
+// out = (a f + b g) / 2^30, exact; returns true when that was negative, in
+// which case out holds its absolute value.
+DEV bool lin_div30(const uint32_t *a, const uint32_t *b, int32_t f, int32_t g, uint32_t *out) {
+  uint32_t r[13];
+  int64_t c = 0;
 #pragma unroll
   for (int i = 0; i < 12; i++) {
-    u[i] = a.w[i];
-    v[i] = pm.w[i];
-    x1[i] = 0;
-    x2[i] = 0;
+    const int64_t acc = c + (int64_t)a[i] * f + (int64_t)b[i] * g;
+    r[i] = (uint32_t)acc;
+    c = acc >> 32;
   }
-  x1[0] = 1;
-  auto is_one = [](const uint32_t *x) {
-    uint32_t o = x[0] ^ 1u;
+  r[12] = (uint32_t)c;
 #pragma unroll
-    for (int i = 1; i < 12; i++) o |= x[i];
-    return o == 0;
-  };
-  auto is_zero = [](const uint32_t *x) {
-    uint32_t o = 0;
-#pragma unroll
-    for (int i = 0; i < 12; i++) o |= x[i];
-    return o == 0;
-  };
-  auto shr1 = [](uint32_t *x) {
-#pragma unroll
-    for (int i = 0; i < 11; i++) x[i] = (x[i] >> 1) | (x[i + 1] << 31);
-    x[11] >>= 1;
-  };
-  // x = x / 2 mod p  (x < p; x + p < 2^382 fits in 12 words)
-  auto half_mod = [&](uint32_t *x) {
-    if (x[0] & 1) {
-      uint64_t c = 0;
-#pragma unroll
-      for (int i = 0; i < 12; i++) {
-        c += (uint64_t)x[i] + pm.w[i];
-        x[i] = (uint32_t)c;
-        c >>= 32;
-      }
-    }
-    shr1(x);
-  };
-  auto geq = [](const uint32_t *x, const uint32_t *y) {
-    for (int i = 11; i >= 0; i--)
-      if (x[i] != y[i]) return x[i] > y[i];
-    return true;
-  };
-  auto sub = [](uint32_t *x, const uint32_t *y) {  // x -= y, returns borrow
-    int64_t b = 0;
+  for (int i = 0; i < 12; i++) out[i] = __funnelshift_r(r[i], r[i + 1], 30);
+  const bool neg = c < 0;
+  if (neg) {
+    uint64_t t = 1;
 #pragma unroll
     for (int i = 0; i < 12; i++) {
-      b += (int64_t)x[i] - y[i];
-      x[i] = (uint32_t)b;
-      b >>= 32;
+      t += (uint32_t)~out[i];
+      out[i] = (uint32_t)t;
+      t >>= 32;
     }
-    return b != 0;
-  };
-  // x = x - y mod p
-  auto sub_mod = [&](uint32_t *x, const uint32_t *y) {
-    if (sub(x, y)) {
-      uint64_t c = 0;
+  }
+  return neg;
+}
+
+// out = (u f + v g) / 2^30 mod p, for u, v in [0, p); out in [0, p).
+DEV void mod_div30(const uint32_t *u, const uint32_t *v, int32_t f, int32_t g, uint32_t *out) {
+  const fp pm = FP_MOD_INIT;
+  const uint32_t k = ((u[0] * (uint32_t)f + v[0] * (uint32_t)g) * FP_NEG_PINV) & 0x3fffffffu;
+  uint32_t r[13];
+  int64_t c = 0;
 #pragma unroll
-      for (int i = 0; i < 12; i++) {
-        c += (uint64_t)x[i] + pm.w[i];
-        x[i] = (uint32_t)c;
-        c >>= 32;
+  for (int i = 0; i < 12; i++) {
+    const int64_t acc = c + (int64_t)u[i] * f + (int64_t)v[i] * g + (int64_t)((uint64_t)k * pm.w[i]);
+    r[i] = (uint32_t)acc;
+    c = acc >> 32;
+  }
+  r[12] = (uint32_t)c;
+#pragma unroll
+  for (int i = 0; i < 12; i++) out[i] = __funnelshift_r(r[i], r[i + 1], 30);
+  // out is in (-2p, 3p), as a 384-bit two's complement value: at most two
+  // additions or two subtractions of p bring it into [0, p)
+#pragma unroll 1
+  for (int rep = 0; rep < 2 && (int32_t)out[11] < 0; rep++) {
+    uint64_t t = 0;
+#pragma unroll
+    for (int i = 0; i < 12; i++) {
+      t += (uint64_t)out[i] + pm.w[i];
+      out[i] = (uint32_t)t;
+      t >>= 32;
+    }
+  }
+#pragma unroll 1
+  for (int rep = 0; rep < 2; rep++) {
+    uint32_t d[12];
+    int64_t t = 0;
+#pragma unroll
+    for (int i = 0; i < 12; i++) {
+      t += (int64_t)out[i] - pm.w[i];
+      d[i] = (uint32_t)t;
+      t >>= 32;
+    }
+    if (t < 0) break;
+#pragma unroll
+    for (int i = 0; i < 12; i++) out[i] = d[i];
+  }
+}
+}  // namespace inv_detail
+
+DEVNI fp fp_inv_vartime(fp y) {
+  if (fp_is_zero(y)) return y;
+  const fp pm = FP_MOD_INIT, r2 = FP_R2_INIT;
+  uint32_t a[12], b[12], u[12], v[12];
+#pragma unroll
+  for (int i = 0; i < 12; i++) {
+    a[i] = y.w[i];
+    b[i] = pm.w[i];
+    u[i] = r2.w[i];
+    v[i] = 0;
+  }
+#pragma unroll 1
+  for (int it = 0; it < 32; it++) {
+    uint32_t any = 0;
+#pragma unroll
+    for (int i = 0; i < 12; i++) any |= a[i];
+    if (any == 0) break;
+    // n = max(bit length of a, of b, 64); s = n - 33
+    int top = 1;
+    uint32_t mt = a[1] | b[1];
+#pragma unroll
+    for (int i = 2; i < 12; i++) {
+      const uint32_t m = a[i] | b[i];
+      if (m) {
+        top = i;
+        mt = m;
       }
     }
-  };
-  // the loop ends within 2 * 381 subtractions; the bound only guards the thread
-#pragma unroll 1
-  for (int guard = 0; guard < 4096; guard++) {
-    if (is_one(u) || is_one(v)) break;
-#pragma unroll 1
-    while (!(u[0] & 1) && !is_zero(u)) {
-      shr1(u);
-      half_mod(x1);
+    const int n = max(32 * top + 32 - __clz(mt), 64), s = n - 33, q = s >> 5, sh = s & 31;
+    uint32_t a0 = 0, a1 = 0, a2 = 0, b0 = 0, b1 = 0, b2 = 0;
+#pragma unroll
+    for (int i = 0; i < 12; i++) {
+      if (i == q) { a0 = a[i]; b0 = b[i]; }
+      if (i == q + 1) { a1 = a[i]; b1 = b[i]; }
+      if (i == q + 2) { a2 = a[i]; b2 = b[i]; }
     }
-#pragma unroll 1
-    while (!(v[0] & 1) && !is_zero(v)) {
-      shr1(v);
-      half_mod(x2);
+    // top 33 bits (bits s .. s+32) above the low 31 bits
+    const uint32_t ta = __funnelshift_r(a0, a1, sh), tb = __funnelshift_r(b0, b1, sh);
+    const uint32_t ha = __funnelshift_r(a1, a2, sh) & 1u, hb = __funnelshift_r(b1, b2, sh) & 1u;
+    uint64_t xa = ((uint64_t)((ta >> 1) | (ha << 31)) << 32) | ((ta << 31) | (a[0] & 0x7fffffffu));
+    uint64_t xb = ((uint64_t)((tb >> 1) | (hb << 31)) << 32) | ((tb << 31) | (b[0] & 0x7fffffffu));
+    int32_t f0 = 1, g0 = 0, f1 = 0, g1 = 1;
+#pragma unroll
+    for (int j = 0; j < 30; j++) {
+      if (xa & 1) {
+        if (xa < xb) {
+          const uint64_t tx = xa; xa = xb; xb = tx;
+          const int32_t tf = f0; f0 = f1; f1 = tf;
+          const int32_t tg = g0; g0 = g1; g1 = tg;
+        }
+        xa -= xb;
+        f0 -= f1;
+        g0 -= g1;
+      }
+      xa >>= 1;
+      f1 += f1;
+      g1 += g1;
     }
-    if (geq(u, v)) {
-      sub(u, v);
-      sub_mod(x1, x2);
-    } else {
-      sub(v, u);
-      sub_mod(x2, x1);
+    uint32_t na[12], nb[12];
+    if (inv_detail::lin_div30(a, b, f0, g0, na)) { f0 = -f0; g0 = -g0; }
+    if (inv_detail::lin_div30(a, b, f1, g1, nb)) { f1 = -f1; g1 = -g1; }
+    uint32_t nu[12], nv[12];
+    inv_detail::mod_div30(u, v, f0, g0, nu);
+    inv_detail::mod_div30(u, v, f1, g1, nv);
+#pragma unroll
+    for (int i = 0; i < 12; i++) {
+      a[i] = na[i];
+      b[i] = nb[i];
+      u[i] = nu[i];
+      v[i] = nv[i];
     }
   }
   fp r;
-  const bool use1 = is_one(u);
 #pragma unroll
-  for (int i = 0; i < 12; i++) r.w[i] = use1 ? x1[i] : x2[i];
-  const fp r3 = {{0xd94ca1e0u, 0xed48ac6bu, 0x03a7adf8u, 0x315f831eu, 0x615e29ddu, 0x9a53352au, 0x921e1761u,
-                  0x34c04e5eu, 0x65724728u, 0x2512d435u, 0x91755d4du, 0x0aa63460u}};  // R^3 mod p
-  return fp_mul(r, r3);
+  for (int i = 0; i < 12; i++) r.w[i] = v[i];
+  return r;
 }
 // sqrt for p = 3 mod 4: s = a^((p+1)/4); returns false if a is not a square.
 DEV bool fp_sqrt(fp a, fp &out) {

@@ -290,7 +290,7 @@ G1_DBL_WITH(g1_dbl_cios, fp_mul_cios)
 //   18/19 out-of-line fp_mul (1 / 3 chains)   20/21 rolled-loop fp_mul (1 / 3 chains)
 //   22 g1_dbl over out-of-line fp_mul   23 g1_dbl over rolled fp_mul
 //   24/25 CIOS fp_mul out of line (1 / 3 chains)   26 CIOS inlined
-//   27 g1_dbl over CIOS fp_mul
+//   27 g1_dbl over CIOS fp_mul   28 fp_inv_vartime
 __global__ void __launch_bounds__(32) k_latency_probe(double *cyc, fp *sink, uint32_t n) {
   fp a = fp_one(), b = fp_one(), c = fp_one(), k = fp_one();
   a.w[0] += threadIdx.x + 3;
@@ -308,7 +308,7 @@ __global__ void __launch_bounds__(32) k_latency_probe(double *cyc, fp *sink, uin
   fr s = fr_one(), sk = fr_one();
   sk.w[1] ^= 0x1234u;
   long long t0, t1;
-  const int R = 28;
+  const int R = 29;
   double res[R];
 #define LAT(IDX, ITERS, BODY)                          \
   t0 = clock64();                                      \
@@ -343,6 +343,7 @@ __global__ void __launch_bounds__(32) k_latency_probe(double *cyc, fp *sink, uin
   LAT(25, n, a = fp_mul_cios(a, k); b = fp_mul_cios(b, k); c = fp_mul_cios(c, k));
   LAT(26, n, a = fp_mul_cios_inl(a, k));
   LAT(27, n / 4, P = g1_dbl_cios(P));
+  LAT(28, n / 64, a = fp_inv_vartime(a));
 #undef LAT
   if (threadIdx.x == 0)
     for (int i = 0; i < R; i++) cyc[i] = res[i];
@@ -355,18 +356,18 @@ __global__ void __launch_bounds__(32) k_latency_probe(double *cyc, fp *sink, uin
 // Fills cycles[0..cap) with the per-operation latencies of k_latency_probe;
 // returns how many were written.
 extern "C" int32_t cubbs_bbs_gpu_latency_probe_for_test_v2(double *cycles, int32_t cap) {
-  if (!cycles || cap < 28) return -1;
+  if (!cycles || cap < 29) return -1;
   try {
     CallScope scope;
     Runtime &rt = scope.rt;
-    double *d = rt.arena.alloc<double>(28);
+    double *d = rt.arena.alloc<double>(29);
     fp *sink = rt.arena.alloc<fp>(32);
     k_latency_probe<<<1, 32, 0, rt.stream>>>(d, sink, 64);  // warm-up
     k_latency_probe<<<1, 32, 0, rt.stream>>>(d, sink, 512);
     CUBBS_CHECK(cudaGetLastError());
-    CUBBS_CHECK(cudaMemcpyAsync(cycles, d, 28 * sizeof(double), cudaMemcpyDeviceToHost, rt.stream));
+    CUBBS_CHECK(cudaMemcpyAsync(cycles, d, 29 * sizeof(double), cudaMemcpyDeviceToHost, rt.stream));
     CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
-    return 28;
+    return 29;
   } catch (const CudaError &) {
     return -2;
   }
