@@ -6,21 +6,29 @@ exponentiation) is a fixed sequence of Fp12 operations.  Each operation is
 compiled here into a *program* of phases that one warp (32 lanes) runs over a
 per-check array of Fp slots in shared memory:
 
-  MUL phase : lane l computes slot[out] = slot[a] * slot[b]   (one Fp product)
-  LIN phase : lane l computes slot[out] = sum_k +-slot[t_k]   (at most 6 terms)
+  MUL phase : lane l computes slot[out] = (sum_i k_i slot[a_i]) * (sum_j k_j slot[b_j])
+              (one Fp product of two short weighted sums, at most 7 terms each)
+  LIN phase : lane l computes slot[out] = sum_i k_i slot[t_i]   (at most 14 terms)
   INV phase : lane 0 computes slot[out] = slot[a]^-1
 
-Every lane runs the same instruction stream in a phase (only its table entry
-differs), so the assembly of Karatsuba products costs a few modular additions
-per lane instead of the divergent per-lane code of an Fp2-level team.
+The coefficients k are small signed integers (|k| < 64).  Every lane runs the
+same instruction stream in a phase (only its table entry differs), so the
+assembly of Karatsuba products costs a few multiply-adds per lane instead of
+the divergent per-lane code of an Fp2-level team.
 
 The Fp12 formulas are written once below over a symbolic Fp type whose
-products become MUL nodes and whose additions stay linear forms until a
-product or an output needs them.  The graph is scheduled greedily into
-alternating LIN / MUL phases (at most 32 nodes each, longest path first),
-temporaries get slots by liveness, and every program is checked numerically
-against an independent schoolbook Fp12 (tower Fp2 = Fp[u]/(u^2+1),
-Fp6 = Fp2[v]/(v^3 - (1+u)), Fp12 = Fp6[w]/(w^2 - v)) before it is emitted.
+products become MUL nodes and whose additions stay weighted linear forms until
+a product or an output needs them.  A form of at most KMUL terms is summed by
+the product's own lane; a longer one becomes a LIN node.  A LIN node whose
+only use is inside another sum is folded into it while the sum stays within
+its width.  The graph is scheduled greedily into LIN / MUL phases (at most 32
+nodes each, longest path first), temporaries get slots by liveness, and every
+program is checked numerically against an independent schoolbook Fp12 (tower
+Fp2 = Fp[u]/(u^2+1), Fp6 = Fp2[v]/(v^3 - (1+u)), Fp12 = Fp6[w]/(w^2 - v))
+before it is emitted.  Each program is compiled under a few settings (LIN
+width, product-operand width, whether Fp2 product results get slots of their
+own) and the one with the lowest modelled cycle count is kept; the model's
+per-phase costs were measured on the device for this kernel.
 
 Formulas: Fp2/Fp6/Fp12 Karatsuba and the complex Fp12 squaring; the sparse
 line value l(P) = A + (B xP) v + yP v w; Granger-Scott cyclotomic squaring
@@ -29,14 +37,24 @@ PKC 2010); Fp12 inverse through the Fp6 and Fp2 norms.
 
 Usage: python gen_pairing_program.py [--check-only]
 """
+import itertools
 import pathlib
 import random
 import sys
 
 P = 0x1A0111EA397FE69A4B1BA7B6434BACD764774B84F38512BF6730D2A0F6B0F6241EABFFFEB153FFFFB9FEFFFFFFFFAAAB
 LANES = 32
-TMAX = 6          # terms per LIN entry
 NONE = 0xFFFF
+SLOT_BITS = 9     # term = slot | (coefficient & 0x7f) << 9
+COEF_MAX = 63
+WLIN_MAX = 14     # terms per LIN entry
+KMUL_MAX = 7      # terms per product operand
+UNIT_MAX = 6      # LIN phases whose coefficients are all +-1 and at most this wide use the plain sum
+
+# settings of one compilation (set by compile_program); with "expand", a
+# coefficient k becomes |k| repeated terms of coefficient +-1, so the sums can
+# run as plain LIN phases
+CFG = {"wlin": 6, "kmul": 1, "mat": True, "expand": False}
 
 # ----------------------------------------------------------------------------- slot map
 # Six Fp12 registers of 12 slots each; register r, Fp2 coefficient k (0..5 =
@@ -56,10 +74,18 @@ def reg_slot(r, k, j):
 
 
 # ----------------------------------------------------------------------------- graph
+def _terms(form):
+    """Canonical term tuple ((coef, node), ...) of a form {node: coef}."""
+    t = sorted(((c, n) for n, c in form.items() if c), key=lambda t: (t[1], t[0]))
+    if CFG["expand"]:
+        t = [(1 if c > 0 else -1, n) for c, n in t for _ in range(abs(c))]
+    return tuple(t)
+
+
 class Graph:
     def __init__(self):
         self.kind = []      # 'in', 'mul', 'lin', 'inv'
-        self.args = []      # in: slot; mul: (a, b); lin: [(sign, node)]; inv: a
+        self.args = []      # in: slot; mul: (terms_a, terms_b); lin: terms; inv: node
         self.key = {}
 
     def _add(self, kind, args, key=None):
@@ -75,29 +101,34 @@ class Graph:
     def inp(self, slot):
         return self._add("in", slot, ("in", slot))
 
+    def lin(self, terms, width):
+        """LIN node of the weighted terms, split into a tree of at most `width` terms each."""
+        terms = list(terms)
+        while len(terms) > width:
+            head, terms = tuple(terms[:width]), terms[width:]
+            terms.append((1, self._add("lin", head, ("lin", head))))
+        terms = tuple(sorted(terms, key=lambda t: (t[1], t[0])))
+        return self._add("lin", terms, ("lin", terms))
+
     def materialize(self, form):
         """Node holding the linear form {node: coef}."""
-        form = {n: c for n, c in form.items() if c}
-        if not form:
+        t = _terms(form)
+        if not t:
             return self.inp(ZERO_SLOT)
-        if len(form) == 1:
-            (n, c), = form.items()
-            if c == 1:
-                return n
-        terms = []
-        for n, c in sorted(form.items(), key=lambda x: (x[1] < 0, x[0])):
-            terms += [(1 if c > 0 else -1, n)] * abs(c)
-        while len(terms) > TMAX:  # split into a tree of LIN nodes
-            head, terms = terms[:TMAX], terms[TMAX:]
-            terms.append((1, self._lin(head)))
-        return self._lin(terms)
+        if len(t) == 1 and t[0][0] == 1:
+            return t[0][1]
+        return self.lin(t, CFG["wlin"])
 
-    def _lin(self, terms):
-        terms = sorted(terms, key=lambda t: (t[0] < 0, t[1]))
-        return self._add("lin", terms, ("lin", tuple(terms)))
+    def operand(self, form):
+        t = _terms(form)
+        if not t:
+            return ((1, self.inp(ZERO_SLOT)),)
+        if len(t) <= CFG["kmul"]:
+            return t
+        return ((1, self.materialize(form)),)
 
     def mul(self, fa, fb):
-        a, b = self.materialize(fa), self.materialize(fb)
+        a, b = self.operand(fa), self.operand(fb)
         a, b = min(a, b), max(a, b)
         return self._add("mul", (a, b), ("mul", a, b))
 
@@ -176,8 +207,11 @@ def bmul(a, b):
 
 
 def mat(x):
-    """Results of Fp2 products are kept in slots of their own (as nodes): the
-    sums built on them stay short, which shortens the assembly phases."""
+    """With CFG["mat"], results of Fp2 products get slots of their own (as
+    nodes), so the sums built on them stay short; without it they stay forms
+    and fold into the sums and operands that use them."""
+    if not CFG["mat"]:
+        return x
     return S.of(x.g, x.g.materialize(x.f)) if isinstance(x, S) and x.f else x
 
 
@@ -401,29 +435,59 @@ PROGRAMS = {
 class Program:
     def __init__(self, name):
         self.name = name
-        self.phases = []   # (type, [entry per lane])  type 0 LIN, 1 MUL, 2 INV; entry (out, op, args)
+        # (type, [entry per lane]); type 0 LIN, 1 MUL, 2 INV
+        # entry: (out, 'lin', terms) | (out, 'mul', (terms_a, terms_b)) | (out, 'inv', terms)
+        # with terms ((coef, slot), ...)
+        self.phases = []
         self.ntmp = 0
         self.nmul = 0
+        self.cfg = None
 
 
-def compile_program(name, builder):
+def _fold(g, terms, width):
+    """Replaces LIN-node terms by their own terms while the sum stays within `width`."""
+    form = {}
+    for c, n in terms:
+        form[n] = form.get(n, 0) + c
+    changed = True
+    while changed:
+        changed = False
+        for n in sorted(form, reverse=True):
+            if g.kind[n] != "lin":
+                continue
+            cand = dict(form)
+            c = cand.pop(n)
+            for c2, m in g.args[n]:
+                cand[m] = cand.get(m, 0) + c * c2
+            cand = {m: v for m, v in cand.items() if v}
+            if 0 < len(_terms(cand)) <= width and all(abs(v) <= COEF_MAX for v in cand.values()):
+                form, changed = cand, True
+                break
+    return _terms(form)
+
+
+def compile_program(name, builder, cfg):
+    CFG.update(cfg)
     g = Graph()
     outs = builder(g)
-    # output nodes: one LIN per output slot, built from the form (unshared)
-    out_nodes = []
+    out_nodes = []  # one LIN per output slot (unshared)
     for slot, v in outs:
-        form = {n: c for n, c in v.f.items() if c}
-        terms = []
-        for n, c in sorted(form.items(), key=lambda x: (x[1] < 0, x[0])):
-            terms += [(1 if c > 0 else -1, n)] * abs(c)
-        if not terms:
-            terms = [(1, g.inp(ZERO_SLOT))]
-        while len(terms) > TMAX:
-            head, terms = terms[:TMAX], terms[TMAX:]
-            terms.append((1, g._lin(head)))
+        t = _terms(v.f) or ((1, g.inp(ZERO_SLOT)),)
+        if len(t) > CFG["wlin"]:
+            t = g.args[g.lin(t, CFG["wlin"])]
         g.kind.append("lin")
-        g.args.append(sorted(terms, key=lambda t: (t[0] < 0, t[1])))
+        g.args.append(t)
         out_nodes.append((len(g.kind) - 1, slot))
+    for n in range(len(g.kind)):  # nodes are in topological order
+        if g.kind[n] == "mul":
+            a, b = g.args[n]
+            g.args[n] = (_fold(g, a, CFG["kmul"]), _fold(g, b, CFG["kmul"]))
+        elif g.kind[n] == "lin":
+            g.args[n] = _fold(g, g.args[n], CFG["wlin"])
+    for n in range(len(g.kind)):
+        for c, _ in (g.args[n][0] + g.args[n][1] if g.kind[n] == "mul" else
+                     g.args[n] if g.kind[n] == "lin" else ()):
+            assert abs(c) <= COEF_MAX, (name, c)
     out_of = {n: s for n, s in out_nodes}
 
     def deps(n):
@@ -431,10 +495,10 @@ def compile_program(name, builder):
         if k == "in":
             return []
         if k == "mul":
-            return list(a)
+            return [m for _, m in a[0] + a[1]]
         if k == "inv":
             return [a]
-        return [t[1] for t in a]
+        return [m for _, m in a]
 
     # reachable set
     need, stack = set(), [n for n, _ in out_nodes]
@@ -459,7 +523,6 @@ def compile_program(name, builder):
     done = {n for n in need if g.kind[n] == "in"}
     todo = need - done
     phase_of = {}
-    prog = Program(name)
     plan = []
     while todo:
         ready = [n for n in todo if all(d in done for d in deps(n))]
@@ -510,20 +573,71 @@ def compile_program(name, builder):
                 ntmp += 1
             slot[n] = s
             busy.append((last_use[n], s))
+    prog = Program(name)
     prog.ntmp = ntmp
+    prog.cfg = dict(cfg)
+    st = lambda terms: tuple((c, slot[m]) for c, m in terms)
     for ptype, batch in plan:
         entries = []
         for n in batch:
             k, a = g.kind[n], g.args[n]
             if k == "mul":
-                entries.append((slot[n], "mul", (slot[a[0]], slot[a[1]])))
+                entries.append((slot[n], "mul", (st(a[0]), st(a[1]))))
                 prog.nmul += 1
             elif k == "inv":
-                entries.append((slot[n], "inv", (slot[a],)))
+                entries.append((slot[n], "inv", ((1, slot[a]),)))
             else:
-                entries.append((slot[n], "lin", tuple((sg, slot[t]) for sg, t in a)))
+                entries.append((slot[n], "lin", st(a)))
         prog.phases.append((ptype, entries))
     return prog
+
+
+# ----------------------------------------------------------------------------- cost model
+# Cycles of one warp, fitted to the measured cycles of every program on GB300
+# (within about 2 percent): an Fp product 2860; a weighted product operand
+# 403 + 191 per term; a LIN phase with coefficients +-1 452 + 189 per term, a
+# weighted one 814 + 192 per term; the inverse ~79k; 150 per program run.
+def _plain(terms):
+    return len(terms) == 1 and terms[0][0] == 1
+
+
+def _unit(entries):
+    return all(abs(c) == 1 for _, _, t in entries for c, _ in t) and max(len(t) for _, _, t in entries) <= UNIT_MAX
+
+
+def phase_cost(ptype, entries):
+    if ptype == 2:
+        return 79000
+    if ptype == 1:
+        c = 2860
+        for side in (0, 1):
+            if not all(_plain(e[2][side]) for e in entries):
+                c += 403 + 191 * max(len(e[2][side]) for e in entries)
+        return c
+    w = max(len(t) for _, _, t in entries)
+    return 452 + 189 * w if _unit(entries) else 814 + 192 * w
+
+
+def program_cost(prog):
+    return 150 + sum(phase_cost(t, e) for t, e in prog.phases)
+
+
+SETTINGS = [{"wlin": w, "kmul": k, "mat": m, "expand": x}
+            for w, k, m, x in itertools.product([4, 6, 8, 10, 12, 14], [1, 2, 3, 4, 6, 7], [True, False],
+                                                [False, True])]
+
+
+def best_program(name, rng):
+    best = None
+    for cfg in SETTINGS:
+        try:
+            p = compile_program(name, PROGRAMS[name], cfg)
+        except AssertionError:
+            continue
+        if best is None or program_cost(p) < program_cost(best):
+            best = p
+    check(best, rng)
+    return best
 
 
 # ----------------------------------------------------------------------------- independent check
@@ -589,22 +703,6 @@ def gammas():
     return out
 
 
-def simulate(prog, slots):
-    s = dict(slots)
-    for ptype, entries in prog.phases:
-        res = []
-        for out, op, args in entries:
-            if op == "mul":
-                res.append((out, s[args[0]] * s[args[1]] % P))
-            elif op == "inv":
-                res.append((out, pow(s[args[0]], P - 2, P)))
-            else:
-                res.append((out, sum(sg * s[t] for sg, t in args) % P))
-        for out, v in res:
-            s[out] = v
-    return s
-
-
 def random_slots(rng, cyclo_regs=()):
     s = {i: rng.randrange(P) for i in range(TMP_BASE)}
     s[ZERO_SLOT] = 0
@@ -657,6 +755,23 @@ def expected(name, s):
     return r, fn()
 
 
+def simulate(prog, slots):
+    s = dict(slots)
+    wsum = lambda terms: sum(c * s[t] for c, t in terms)
+    for ptype, entries in prog.phases:
+        res = []
+        for out, op, args in entries:
+            if op == "mul":
+                res.append((out, wsum(args[0]) * wsum(args[1]) % P))
+            elif op == "inv":
+                res.append((out, pow(wsum(args), P - 2, P)))
+            else:
+                res.append((out, wsum(args) % P))
+        for out, v in res:
+            s[out] = v
+    return s
+
+
 def check(prog, rng, trials=2):
     for _ in range(trials):
         s = random_slots(rng, cyclo_regs=(REG_R,) if prog.name == "CYCLO_R" else ())
@@ -671,10 +786,52 @@ def check(prog, rng, trials=2):
 
 # ----------------------------------------------------------------------------- emission
 ORDER = list(PROGRAMS)
+T_LIN, T_MUL, T_INV = 0, 1, 2
+F_UNIT_OR_PLAIN_A, F_PLAIN_B = 0x100, 0x200
+
+
+def _term(c, sl):
+    assert 0 <= sl < (1 << SLOT_BITS) and -64 <= c <= COEF_MAX
+    return sl | ((c & 0x7F) << SLOT_BITS)
+
+
+def phase_words(ptype, entries):
+    """16 u16 words per lane: out, type word, terms 0..6 (LIN terms / operand a),
+    terms 7..13 (LIN terms / operand b)."""
+    pad = lambda terms, n, unit: list(terms) + [(1 if unit else 0, ZERO_SLOT)] * (n - len(terms))
+    rows = []
+    if ptype == 1:
+        plain = [all(_plain(e[2][side]) for e in entries) for side in (0, 1)]
+        width = [1 if plain[side] else max(len(e[2][side]) for e in entries) for side in (0, 1)]
+        assert max(width) <= KMUL_MAX
+        tw = T_MUL << 12 | width[1] << 4 | width[0] | (F_UNIT_OR_PLAIN_A if plain[0] else 0) | \
+            (F_PLAIN_B if plain[1] else 0)
+    elif ptype == 2:
+        tw = T_INV << 12 | 1
+    else:
+        width = max(len(t) for _, _, t in entries)
+        assert width <= WLIN_MAX
+        unit = _unit(entries)
+        tw = T_LIN << 12 | width | (F_UNIT_OR_PLAIN_A if unit else 0)
+    for l in range(LANES):
+        u = [NONE, tw] + [_term(0, ZERO_SLOT)] * 14
+        if l < len(entries):
+            out, op, args = entries[l]
+            u[0] = out
+            if op == "mul":
+                for side in (0, 1):
+                    for t, (c, sl) in enumerate(pad(args[side], width[side], False)):
+                        u[2 + 7 * side + t] = _term(c, sl)
+            else:
+                for t, (c, sl) in enumerate(pad(args, width if op == "lin" else 1, op == "lin" and unit)):
+                    u[2 + t] = _term(c, sl)
+        rows.append(u)
+    return rows
 
 
 def emit(progs):
     nslot = TMP_BASE + max(p.ntmp for p in progs)
+    assert nslot <= 1 << SLOT_BITS
     lines = ["// GENERATED by gen_pairing_program.py -- do not edit by hand.",
              "// Phase tables of the warp-per-check pairing (see pairing_team.cuh).",
              "#pragma once", "#include <stdint.h>", "",
@@ -684,59 +841,56 @@ def emit(progs):
              "#define PP_ZERO_SLOT %d" % ZERO_SLOT,
              "#define PP_REG(r) (12 * (r))",
              "enum { PP_REG_F, PP_REG_T, PP_REG_A, PP_REG_X, PP_REG_R, PP_REG_U };",
-             "enum { PP_LIN = 0, PP_MUL = 1, PP_INV = 2 };", ""]
+             "enum { PP_LIN = %d, PP_MUL = %d, PP_INV = %d };" % (T_LIN, T_MUL, T_INV),
+             "#define PP_F_UNIT 0x%03x    // LIN: coefficients +-1, at most %d terms" % (F_UNIT_OR_PLAIN_A, UNIT_MAX),
+             "#define PP_F_PLAIN_A 0x%03x // MUL: operand a is one slot with coefficient 1" % F_UNIT_OR_PLAIN_A,
+             "#define PP_F_PLAIN_B 0x%03x // MUL: operand b likewise" % F_PLAIN_B, ""]
     lines.append("enum {" + ", ".join("PP_" + n for n in ORDER) + ", PP_NPROG };")
-    first, types, ents = [], [], []
+    first, ents, nph = [], [], 0
     for p in progs:
-        first.append(len(types))
+        first.append(nph)
         for ptype, entries in p.phases:
-            types.append(ptype)
+            nph += 1
             row = []
-            # every lane of a LIN phase runs the phase's largest term count;
-            # shorter sums are padded with the zero slot
-            width = max((len(a) for _, op, a in entries if op == "lin"), default=0)
-            for l in range(LANES):
-                u = [NONE, ptype << 8 | width, 0, 0, 0, 0, 0, 0]
-                if l < len(entries):
-                    out, op, args = entries[l]
-                    u[0] = out
-                    if op == "lin":
-                        padded = list(args) + [(1, ZERO_SLOT)] * (width - len(args))
-                        for t, (sg, sl) in enumerate(padded):
-                            assert sl < 0x8000
-                            u[2 + t] = sl | (0x8000 if sg < 0 else 0)
-                    else:
-                        for t, sl in enumerate(args):
-                            u[2 + t] = sl
-                row.append("{0x%08x, 0x%08x, 0x%08x, 0x%08x}" % tuple(u[2 * k] | (u[2 * k + 1] << 16)
-                                                                     for k in range(4)))
+            for u in phase_words(ptype, entries):
+                w = [u[2 * k] | (u[2 * k + 1] << 16) for k in range(8)]
+                row.append("{0x%08x, 0x%08x, 0x%08x, 0x%08x}, {0x%08x, 0x%08x, 0x%08x, 0x%08x}" % tuple(w))
             ents.append("  " + ", ".join(row) + ",")
-    first.append(len(types))
-    lines.append("#define PP_NPHASE %d" % len(types))
+    first.append(nph)
+    lines.append("#define PP_NPHASE %d" % nph)
     lines.append("__device__ const uint16_t PP_PROG_FIRST[PP_NPROG + 1] = {" + ", ".join(map(str, first)) + "};")
-    lines.append("// entry per (phase, lane): u16 out (PP_NONE: idle lane), u16 phase type << 8 | term count")
-    lines.append("// (LIN: the same count on every lane of the phase, short sums padded with the zero slot),")
-    lines.append("// then u16 x 6 terms (LIN; bit 15: subtract) or operand slots (MUL: a, b; INV: a)")
-    lines.append("__device__ const uint4 PP_ENTRY[PP_NPHASE * PP_LANES] = {")
+    lines.append("// Two uint4 per (phase, lane), as 16 u16: out slot (PP_NONE: idle lane); type << 12 |")
+    lines.append("// flags | nb << 4 | na (LIN: na = term count, the same on every lane of the phase);")
+    lines.append("// terms 0..6 (LIN terms, MUL operand a); terms 7..13 (LIN terms, MUL operand b).")
+    lines.append("// A term is slot | (signed 7-bit coefficient) << 9; short sums are padded with the zero slot.")
+    lines.append("__device__ const uint4 PP_ENTRY[PP_NPHASE * PP_LANES * 2] = {")
     lines += ents
     lines.append("};")
-    summary = ["// %-11s %3d phases (%s), %3d products, %3d temporaries" %
-               (p.name, len(p.phases), "".join("LMI"[t] for t, _ in p.phases), p.nmul, p.ntmp) for p in progs]
+    summary = []
+    for p in progs:
+        desc = ""
+        for t, e in p.phases:
+            if t == 1:
+                desc += "M"
+            elif t == 2:
+                desc += "I"
+            else:
+                desc += "L" if _unit(e) else "W"
+        summary.append("// %-11s %3d phases (%s), %3d products, %3d temporaries, ~%d cycles" %
+                       (p.name, len(p.phases), desc, p.nmul, p.ntmp, program_cost(p)))
     return "\n".join(lines[:4] + summary + lines[4:]) + "\n"
 
 
 def main():
     rng = random.Random(20240601)
-    progs = []
-    for name in ORDER:
-        p = compile_program(name, PROGRAMS[name])
-        check(p, rng)
-        progs.append(p)
+    progs = [best_program(name, rng) for name in ORDER]
     text = emit(progs)
     if "--check-only" not in sys.argv:
         out = pathlib.Path(__file__).resolve().parent / "pairing_program.cuh"
         out.write_text(text)
         print("wrote", out, "phases:", sum(len(p.phases) for p in progs))
+    for p in progs:
+        print("%-11s %3d phases ~%6d cycles  %s" % (p.name, len(p.phases), program_cost(p), p.cfg))
 
 
 if __name__ == "__main__":

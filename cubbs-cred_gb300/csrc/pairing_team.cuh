@@ -8,16 +8,17 @@
 // registers F, T, A, X, R, U (12 slots each), the current lines of both
 // pairs, the two points, the Frobenius constants, a zero slot and the
 // temporaries of the programs.  A program is a list of phases; in a phase
-// every lane reads its table entry and either computes one Fp product (MUL),
-// one signed sum of at most six slots (LIN), or, on lane 0, one Fp inverse
-// (INV).  All lanes run the same instruction stream, the products of an
-// Fp12 operation run side by side (up to 32 per phase), and results are
-// written only after every lane of the phase has read its operands, so a
-// program may overwrite its own input register.
+// every lane reads its table entry and either computes one Fp product of two
+// short weighted sums of slots (MUL), one weighted sum of at most 14 slots
+// (LIN), or, on lane 0, one Fp inverse (INV).  All lanes run the same
+// instruction stream, the products of an Fp12 operation run side by side (up
+// to 32 per phase), and results are written only after every lane of the
+// phase has read its operands, so a program may overwrite its own input
+// register.
 //
 // Compared with a 16-lane team working at Fp2 granularity, a phase costs one
 // Fp product instead of three in a row, and the assembly of Karatsuba terms
-// is a few modular additions per lane instead of divergent per-lane code.
+// is a few multiply-adds per lane instead of divergent per-lane code.
 #pragma once
 #include "pairing.cuh"
 #include "pairing_program.cuh"
@@ -40,23 +41,25 @@ DEV void st(fp *sl, uint32_t i, const fp &r) {
   p[2] = make_uint4(r.w[8], r.w[9], r.w[10], r.w[11]);
 }
 
+constexpr uint32_t PP_SLOT_MASK = 0x1ffu;  // term = slot | signed 7-bit coefficient << 9
+
 DEV uint32_t term(const uint4 &e, int t) {
   const uint32_t w = t < 2 ? e.y : t < 4 ? e.z : e.w;
   return (t & 1) ? w >> 16 : w & 0xffffu;
 }
 
-// Signed sum of N reduced slots (N is the same on every lane of a phase): a
-// subtracted term x enters as p - x, every term is loaded and prepared before
-// the sums, and the terms are added as a pairwise tree of plain 12-limb
-// additions (every partial sum stays below N p <= 6p < 2^384); conditional
-// subtractions of 4p, 2p and p, as many as N needs, reduce the result once.
-// No branch depends on the lane.
+// Signed sum of N reduced slots with coefficients +-1 (N is the same on every
+// lane of a phase): a subtracted term x enters as p - x, every term is loaded
+// and prepared before the sums, and the terms are added as a pairwise tree of
+// plain 12-limb additions (every partial sum stays below N p <= 6p < 2^384);
+// conditional subtractions of 4p, 2p and p, as many as N needs, reduce the
+// result once.  No branch depends on the lane.
 template <int N> DEV fp lin_n(const fp *sl, const uint4 &e) {
   fp v[N];
 #pragma unroll
   for (int t = 0; t < N; t++) {
     const uint32_t tv = term(e, t);
-    const fp x = ld(sl, tv & 0x7fffu);
+    const fp x = ld(sl, tv & PP_SLOT_MASK);
     fp y;
     fp_from_mod(y.w, x.w);
     const bool neg = (tv & 0x8000u) != 0;
@@ -84,26 +87,97 @@ DEV fp lin(const fp *sl, const uint4 &e, int n) {
   }
 }
 
+// Up to 14 terms of an entry as a shift register: term t in bits 16 t .. 16 t + 15.
+struct Terms {
+  uint32_t w[7];
+};
+DEV Terms terms_lo(const uint4 &e0, const uint4 &e1) {  // terms 0..13
+  return {{e0.y, e0.z, e0.w, e1.x, e1.y, e1.z, e1.w}};
+}
+DEV Terms terms_hi(const uint4 &e1) {  // terms 7..13
+  return {{__funnelshift_r(e1.x, e1.y, 16), __funnelshift_r(e1.y, e1.z, 16), __funnelshift_r(e1.z, e1.w, 16),
+           e1.w >> 16, 0u, 0u, 0u}};
+}
+
+// sum_t k_t slot[s_t] mod p over the first n terms of q (n is the same on
+// every lane of a phase; |k_t| <= 64, n <= 14).  A term with k < 0 enters as
+// |k| (p - x).  The products accumulate per limb in 64 bits (at most
+// 14 * 64 * 2^32 < 2^42 each), so S = sum_j acc_j 2^(32 j) < 896 p < 2^391.
+// Before any carry, q = floor(S / p) - (0..3) comes from the top of S,
+// acc_11 + floor(acc_10 / 2^32) (S / 2^352 less at most 1), times
+// 1 / (floor(p / 2^352) + 1) in single precision (relative error below 2^-22
+// on a quotient below 2^10), minus one; q p is taken off limb by limb and one
+// signed carry pass leaves S - q p in [0, 4p).  Two conditional subtractions
+// finish the reduction.
+DEVNI fp wsum(const fp *sl, Terms q, int n) {
+  const fp pm = FP_MOD_INIT;
+  uint64_t acc[12];
+#pragma unroll
+  for (int j = 0; j < 12; j++) acc[j] = 0;
+#pragma unroll 1
+  for (int t = 0; t < n; t++) {
+    const uint32_t v = q.w[0] & 0xffffu;
+#pragma unroll
+    for (int i = 0; i < 6; i++) q.w[i] = __funnelshift_r(q.w[i], q.w[i + 1], 16);
+    q.w[6] >>= 16;
+    const fp x = ld(sl, v & PP_SLOT_MASK);
+    fp y;
+    fp_from_mod(y.w, x.w);
+    const int k = (int32_t)(v << 16) >> 25;
+    const bool neg = k < 0;
+    const uint32_t m = (uint32_t)(neg ? -k : k);
+#pragma unroll
+    for (int j = 0; j < 12; j++) acc[j] += (uint64_t)(neg ? y.w[j] : x.w[j]) * m;
+  }
+  constexpr float INV_PTOP = 1.0f / 436277739.0f;  // 1 / (floor(p / 2^352) + 1)
+  const uint64_t top = acc[11] + (acc[10] >> 32);
+  uint32_t qq = (uint32_t)(__ull2float_rn(top) * INV_PTOP);
+  qq = qq ? qq - 1 : 0;
+  int64_t c = 0;
+  fp out;
+#pragma unroll
+  for (int j = 0; j < 12; j++) {
+    c += (int64_t)acc[j] - (int64_t)((uint64_t)qq * pm.w[j]);
+    out.w[j] = (uint32_t)c;
+    c >>= 32;
+  }
+  fp_csub2(out.w, out.w);
+  fp_csub1(out.w, out.w);
+  return out;
+}
+
 // Runs program `prog` on the slot array of this warp's check.  The table
 // entry of the next phase is fetched while the current one computes.
 DEVNI void run(fp *sl, int lane, int prog) {
   const int ph0 = PP_PROG_FIRST[prog], ph1 = PP_PROG_FIRST[prog + 1];
-  uint4 e = __ldg(&PP_ENTRY[ph0 * PP_LANES + lane]);
+  const uint4 *tab = PP_ENTRY + 2 * lane;
+  uint4 e0 = __ldg(&tab[2 * PP_LANES * ph0]), e1 = __ldg(&tab[2 * PP_LANES * ph0 + 1]);
 #pragma unroll 1
   for (int ph = ph0; ph < ph1; ph++) {
-    const uint4 next = __ldg(&PP_ENTRY[min(ph + 1, ph1 - 1) * PP_LANES + lane]);
-    const uint32_t out = e.x & 0xffffu, type = e.x >> 24, n = (e.x >> 16) & 0xffu;
+    const int nx = min(ph + 1, ph1 - 1);
+    const uint4 n0 = __ldg(&tab[2 * PP_LANES * nx]), n1 = __ldg(&tab[2 * PP_LANES * nx + 1]);
+    const uint32_t out = e0.x & 0xffffu, tw = e0.x >> 16, type = tw >> 12;
+    const int na = (int)(tw & 15u), nb = (int)((tw >> 4) & 15u);
     const bool act = out != PP_NONE;
     fp r = fp_zero();
     if (act) {
-      if (type == PP_MUL) r = fp_mul(ld(sl, e.y & 0xffffu), ld(sl, e.y >> 16));
-      else if (type == PP_LIN) r = lin(sl, e, (int)n);
-      else r = fp_inv_vartime(ld(sl, e.y & 0xffffu));  // PP_INV: public value, variable time
+      if (type == PP_MUL) {
+        const fp x = (tw & PP_F_PLAIN_A) ? ld(sl, e0.y & PP_SLOT_MASK) : wsum(sl, terms_lo(e0, e1), na);
+        const fp y = (tw & PP_F_PLAIN_B) ? ld(sl, (e1.x >> 16) & PP_SLOT_MASK) : wsum(sl, terms_hi(e1), nb);
+        // one warp, one dependent product per lane: the inlined CIOS product has
+        // the shortest single-warp latency of the Fp products here
+        r = fp_mul_cios_inl(x, y);
+      } else if (type == PP_LIN) {
+        r = (tw & PP_F_UNIT) ? lin(sl, e0, na) : wsum(sl, terms_lo(e0, e1), na);
+      } else {
+        r = fp_inv_vartime(ld(sl, e0.y & PP_SLOT_MASK));  // PP_INV: public value, variable time
+      }
     }
     __syncwarp();
     if (act) st(sl, out, r);
     __syncwarp();
-    e = next;
+    e0 = n0;
+    e1 = n1;
   }
 }
 
