@@ -400,6 +400,7 @@ def main():
 
     tera_imad, giga_fpmul = pkg.int_peaks()
     table_w = pkg.table_window()  # chosen for the 102 generators of L = 100
+    part_sms = pkg.sm_partition()
 
     # ---------------- timed: device-resident ProofVerify (headline) + ProofGen
     def barrier():
@@ -500,6 +501,8 @@ def main():
             "config": {"workload": "BBS ProofGen+ProofVerify, L=100 x 64 B, 50 disclosed, 1024 proofs per batch",
                        "batch": n, "L": L, "disclosed": R, "l2": "flushed (256 MiB write) between timed steps",
                        "fixed_base_window": table_w,
+                       "sm_partition": {"pairing_check": part_sms[0], "rest": part_sms[1],
+                                        "status": part_sms[2]},
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "per_op_ops_per_s": {
                 "proof_verify_L100": round(value / world, 2),

@@ -472,6 +472,20 @@ def msm_uneven_bench(n_msms=16384, k_min=2, k_max=257, seed=4, tune=True, warmup
             "checked": chk.value, "mismatch": mm.value}
 
 
+def sm_partition():
+    """(small, rest) SM counts of the ProofVerify SM partition: the aggregated
+    pairing check runs alone on `small` SMs, everything else on `rest`; (0, 0)
+    when the partition is off (driver without green contexts, or
+    CUBBS_BBS_SM_PARTITION=0), with the reason as a third value (0 when on)."""
+    a, b, st = ctypes.c_int32(0), ctypes.c_int32(0), ctypes.c_int32(0)
+    fn = lib().cubbs_bbs_gpu_sm_partition_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    if fn(*(ctypes.cast(ctypes.pointer(v), ctypes.c_void_p) for v in (a, b, st))):
+        raise RuntimeError("sm_partition failed")
+    return a.value, b.value, st.value
+
+
 def table_window():
     """Window width of the resident fixed-base table (0 before it is built)."""
     w = ctypes.c_int32(0)

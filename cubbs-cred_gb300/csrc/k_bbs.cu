@@ -1129,19 +1129,29 @@ void span_end(cudaStream_t s, int k, const char *name) {
 // need only the affine points, and the challenge kernel rejects every proof
 // with a point outside G1 before any result is read.  Each of these kernels
 // fills only part of the GPU, so running them side by side shortens the step.
+// With the SM partition, the four streams are those of the larger partition
+// and the aggregated pairing chain (random-coefficient scaling, group sums,
+// one check per key group: the step's critical path, made of kernels that
+// fill only a few SMs) runs alone on the smaller one, when its groups fit
+// there two to an SM.  Sharing SMs with the MSM kernels stretched that chain
+// from about 3.5 ms to 5 ms.
 void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
-  cudaStream_t s = rt.stream, s2 = rt.stream2, s3 = rt.stream3;
+  const bool part = rt.part[0] != nullptr;
+  cudaStream_t s0 = rt.stream;
+  cudaStream_t s = part ? rt.part[0] : rt.stream, s2 = part ? rt.part[1] : rt.stream2;
+  cudaStream_t s3 = part ? rt.part[2] : rt.stream3, s4 = part ? rt.part[3] : rt.stream4;
   size_t n = b.n, nm = b.ml.count(), npts = b.pts48.size() / 48;
   uint32_t N = (uint32_t)n, stride = (uint32_t)b.stride;
   PvItem *it = reinterpret_cast<PvItem *>(b.ditems);
   const PvItem *it0 = reinterpret_cast<const PvItem *>(b.ditems0);
-  CUBBS_CHECK(cudaEventRecord(rt.ev_fork, s));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_fork, s0));
+  if (part) CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_fork, 0));
   CUBBS_CHECK(cudaStreamWaitEvent(s2, rt.ev_fork, 0));
   SPAN(s2, "g1_decode", launch_g1_decode(s2, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, false));
   CUBBS_CHECK(cudaEventRecord(rt.ev_mid, s2));
-  CUBBS_CHECK(cudaStreamWaitEvent(rt.stream4, rt.ev_mid, 0));
-  SPAN(rt.stream4, "g1_subgroup", launch_g1_subgroup(rt.stream4, b.pts, b.dec, (uint32_t)npts, b.sub));
-  CUBBS_CHECK(cudaEventRecord(rt.ev_sub, rt.stream4));
+  CUBBS_CHECK(cudaStreamWaitEvent(s4, rt.ev_mid, 0));
+  SPAN(s4, "g1_subgroup", launch_g1_subgroup(s4, b.pts, b.dec, (uint32_t)npts, b.sub));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_sub, s4));
   CUBBS_CHECK(cudaStreamWaitEvent(s3, rt.ev_mid, 0));
   const uint32_t G = (uint32_t)b.h_gslot.size();
   if (G) {
@@ -1152,11 +1162,24 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
       if (r <= 0) throw CudaError(cudaErrorUnknown, "getrandom");
       got += (size_t)r;
     }
-    SPAN(s3, "pairing_aggregate",
-         k_agg_scale<<<blocks_for(4 * n, 32), 32, 0, s3>>>(it0, N, b.pts, b.dec, b.group_of, seed, b.scaled);
-         CUBBS_CHECK(cudaMemsetAsync(b.gjobs, 0, G * sizeof(PairJob), s3));
-         k_agg_sum<<<dim3(G, 2), 256, 0, s3>>>(b.scaled, b.perm, b.goff, b.gslot, b.gjobs);
-         launch_pairing_check_split(s3, b.gjobs, G, rt.d_lines, b.gok));
+    // the random-coefficient scaling, the group sums and the group checks
+    // run on the small partition when the groups fit there two to an SM
+    const bool alone = part && G <= 2 * (uint32_t)rt.sh.small_sms;
+    cudaStream_t sa = alone ? rt.part_check : s3;
+    if (alone) {
+      CUBBS_CHECK(cudaEventRecord(rt.ev_gc, s3));
+      CUBBS_CHECK(cudaStreamWaitEvent(sa, rt.ev_gc, 0));
+    }
+    SPAN(sa, "agg_scale",
+         k_agg_scale<<<blocks_for(4 * n, 32), 32, 0, sa>>>(it0, N, b.pts, b.dec, b.group_of, seed, b.scaled));
+    SPAN(sa, "agg_sum",
+         CUBBS_CHECK(cudaMemsetAsync(b.gjobs, 0, G * sizeof(PairJob), sa));
+         k_agg_sum<<<dim3(G, 2), 256, 0, sa>>>(b.scaled, b.perm, b.goff, b.gslot, b.gjobs));
+    SPAN(sa, "pairing_check", launch_pairing_check_split(sa, b.gjobs, G, rt.d_lines, b.gok));
+    if (alone) {
+      CUBBS_CHECK(cudaEventRecord(rt.ev_gc2, sa));
+      CUBBS_CHECK(cudaStreamWaitEvent(s3, rt.ev_gc2, 0));
+    }
     SPAN(s3, "pairing_kernel",
          k_pv_pairjobs_agg<<<blocks_for(n, 128), 128, 0, s3>>>(it0, N, b.pts, b.dec, b.group_of, b.gok, b.pj,
                                                                 b.ok);
@@ -1185,6 +1208,10 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   SPAN(s, "challenge",
        k_pv_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.sub, b.fixed, b.v));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_join, 0));
+  if (part) {
+    CUBBS_CHECK(cudaEventRecord(rt.ev_done, s));
+    CUBBS_CHECK(cudaStreamWaitEvent(s0, rt.ev_done, 0));
+  }
   b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 8 + (G ? 3 : 0);
 }
 

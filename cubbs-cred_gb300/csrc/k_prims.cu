@@ -1029,6 +1029,24 @@ extern "C" int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi, const uint8
   ABI_GUARD_END
 }
 
+// SM counts of the ProofVerify partition (small: the aggregated pairing
+// check; rest: every other kernel of the call); both 0 when it is off, and
+// *status tells why (0: on; 1: turned off; 200 + k: driver entry point k missing; else
+// 1000 * failed step + driver or runtime result).
+extern "C" int32_t cubbs_bbs_gpu_sm_partition_v2(int32_t *small_sms, int32_t *rest_sms, int32_t *status) {
+  if (!small_sms || !rest_sms || !status) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  try {
+    CallScope scope;
+    const bool on = scope.rt.part[0] != nullptr;
+    *small_sms = on ? scope.rt.sh.small_sms : 0;
+    *rest_sms = on ? scope.rt.sh.rest_sms : 0;
+    *status = on ? 0 : (scope.rt.sh.partition_status ? scope.rt.sh.partition_status : 99);
+    return CUBBS_BBS_GPU_SUCCESS;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}
+
 // Window width of the resident fixed-base table (0 before the first table is built).
 extern "C" int32_t cubbs_bbs_gpu_table_window_v2(int32_t *w) {
   if (!w) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;

@@ -69,7 +69,123 @@ void SharedState::init() {
   CUBBS_CHECK(cudaStreamSynchronize(prep));
   line_used = 2;
   slot_info.assign(2, PkSlot{DEC_OK});
+  init_partition();
   initialised = true;
+}
+
+namespace {
+__global__ void k_partition_probe(int *flag) {
+  if (threadIdx.x == 0) atomicAdd(flag, 1);
+}
+template <class F> F driver_fn(const char *name) {
+  void *fn = nullptr;
+  cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+  if (cudaGetDriverEntryPointByVersion(name, &fn, CUDART_VERSION, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess)
+    return nullptr;
+  return reinterpret_cast<F>(fn);
+}
+}  // namespace
+
+// Splits the device's SMs into a partition of CUBBS_BBS_SM_PARTITION SMs
+// (default 16, where ProofVerify at 1024 proofs ran fastest on GB300: 8 SMs
+// slow the scaling kernel, 24 gain nothing; the driver rounds to multiples of
+// 8; 0 turns the partition off) and the rest, as two green contexts (CUDA driver API,
+// entry points looked up through the runtime).  A self-test launches a kernel
+// on each and hands an event from one to the other; if any step fails the
+// partition stays off and ProofVerify runs on the plain streams.
+void SharedState::init_partition() {
+  const int want = env_int("CUBBS_BBS_SM_PARTITION", 16);
+  if (want <= 0 || want >= sm_count) {
+    partition_status = 1;
+    return;
+  }
+  using GetDevice = CUresult (*)(CUdevice *, int);
+  using GetRes = CUresult (*)(CUdevice, CUdevResource *, CUdevResourceType);
+  using Split = CUresult (*)(CUdevResource *, unsigned *, const CUdevResource *, CUdevResource *, unsigned, unsigned);
+  using GenDesc = CUresult (*)(CUdevResourceDesc *, CUdevResource *, unsigned);
+  using Create = CUresult (*)(CUgreenCtx *, CUdevResourceDesc, CUdevice, unsigned);
+  using Destroy = CUresult (*)(CUgreenCtx);
+  using StreamCreate = CUresult (*)(CUstream *, CUgreenCtx, unsigned, int);
+  auto get_device = driver_fn<GetDevice>("cuDeviceGet");
+  auto get_res = driver_fn<GetRes>("cuDeviceGetDevResource");
+  auto split = driver_fn<Split>("cuDevSmResourceSplitByCount");
+  auto gen_desc = driver_fn<GenDesc>("cuDevResourceGenerateDesc");
+  auto create = driver_fn<Create>("cuGreenCtxCreate");
+  auto destroy = driver_fn<Destroy>("cuGreenCtxDestroy");
+  auto stream_create = driver_fn<StreamCreate>("cuGreenCtxStreamCreate");
+  const void *fns[] = {(void *)get_device, (void *)get_res, (void *)split, (void *)gen_desc,
+                       (void *)create, (void *)destroy, (void *)stream_create};
+  for (int k = 0; k < 7; k++)
+    if (!fns[k]) {
+      partition_status = 200 + k;  // entry point k of the list above is missing
+      return;
+    }
+  // partition_status: 1000 * step + CUresult of the step that failed
+  auto fail = [this](int step, CUresult r) {
+    partition_status = 1000 * step + (int)r;
+    return false;
+  };
+  CUdevice dev;
+  CUdevResource all{}, small{}, rest{};
+  unsigned groups = 1;
+  CUresult r;
+  if ((r = get_device(&dev, device)) != CUDA_SUCCESS) return (void)fail(3, r);
+  if ((r = get_res(dev, &all, CU_DEV_RESOURCE_TYPE_SM)) != CUDA_SUCCESS) return (void)fail(4, r);
+  if ((r = split(&small, &groups, &all, &rest, 0, (unsigned)want)) != CUDA_SUCCESS) return (void)fail(5, r);
+  if (groups != 1 || small.sm.smCount == 0 || rest.sm.smCount == 0) return (void)fail(6, CUDA_SUCCESS);
+  CUdevResourceDesc dsmall, drest;
+  if ((r = gen_desc(&dsmall, &small, 1)) != CUDA_SUCCESS) return (void)fail(7, r);
+  if ((r = gen_desc(&drest, &rest, 1)) != CUDA_SUCCESS) return (void)fail(8, r);
+  CUgreenCtx gs = nullptr, gr = nullptr;
+  if ((r = create(&gs, dsmall, dev, CU_GREEN_CTX_DEFAULT_STREAM)) != CUDA_SUCCESS) return (void)fail(9, r);
+  if ((r = create(&gr, drest, dev, CU_GREEN_CTX_DEFAULT_STREAM)) != CUDA_SUCCESS) {
+    destroy(gs);
+    return (void)fail(10, r);
+  }
+  // self-test: a kernel on each partition, ordered by an event
+  CUstream a = nullptr, b = nullptr;
+  cudaEvent_t ev = nullptr;
+  int *flag = nullptr;
+  int step = 11;
+  bool ok = stream_create(&a, gs, CU_STREAM_NON_BLOCKING, 0) == CUDA_SUCCESS &&
+            stream_create(&b, gr, CU_STREAM_NON_BLOCKING, 0) == CUDA_SUCCESS;
+  if (ok) {
+    step = 12;
+    ok = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess &&
+         cudaMalloc(&flag, sizeof(int)) == cudaSuccess && cudaMemsetAsync(flag, 0, sizeof(int), b) == cudaSuccess;
+  }
+  int got = 0;
+  if (ok) {
+    step = 13;
+    k_partition_probe<<<1, 32, 0, b>>>(flag);
+    ok = cudaGetLastError() == cudaSuccess && cudaEventRecord(ev, b) == cudaSuccess &&
+         cudaStreamWaitEvent(a, ev, 0) == cudaSuccess;
+  }
+  if (ok) {
+    step = 14;
+    k_partition_probe<<<1, 32, 0, a>>>(flag);
+    ok = cudaGetLastError() == cudaSuccess &&
+         cudaMemcpyAsync(&got, flag, sizeof(int), cudaMemcpyDeviceToHost, a) == cudaSuccess &&
+         cudaStreamSynchronize(a) == cudaSuccess && got == 2;
+  }
+  const cudaError_t last = cudaGetLastError();  // a failed probe leaves no sticky error behind
+  if (a) cudaStreamDestroy(a);
+  if (b) cudaStreamDestroy(b);
+  if (ev) cudaEventDestroy(ev);
+  if (flag) cudaFree(flag);
+  if (!ok) {
+    destroy(gs);
+    destroy(gr);
+    partition_status = 1000 * step + (int)last;
+    return;
+  }
+  green_small = gs;
+  green_rest = gr;
+  small_sms = (int)small.sm.smCount;
+  rest_sms = (int)rest.sm.smCount;
+  green_stream_create = stream_create;
+  partition_status = 0;
 }
 
 // Build generators up to d_gens[count) on the device: P1 is decoded from its
@@ -235,6 +351,26 @@ Runtime::Runtime(SharedState &s)
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_side, cudaEventDisableTiming));
   CUBBS_CHECK(cudaStreamCreateWithFlags(&stream4, cudaStreamNonBlocking));
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_sub, cudaEventDisableTiming));
+  if (sh.green_rest) {
+    int lo = 0, hi = 0;
+    CUBBS_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+    bool ok = true;
+    for (int k = 0; k < 4 && ok; k++)
+      ok = sh.green_stream_create(&part[k], sh.green_rest, CU_STREAM_NON_BLOCKING, k == 2 ? hi : 0) == CUDA_SUCCESS;
+    ok = ok && sh.green_stream_create(&part_check, sh.green_small, CU_STREAM_NON_BLOCKING, hi) == CUDA_SUCCESS;
+    if (ok) {
+      CUBBS_CHECK(cudaEventCreateWithFlags(&ev_gc, cudaEventDisableTiming));
+      CUBBS_CHECK(cudaEventCreateWithFlags(&ev_gc2, cudaEventDisableTiming));
+      CUBBS_CHECK(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming));
+    } else {
+      for (auto &p : part) {
+        if (p) cudaStreamDestroy(p);
+        p = nullptr;
+      }
+      if (part_check) cudaStreamDestroy(part_check);
+      part_check = nullptr;
+    }
+  }
   arena.reserve((size_t)256 << 20);
   staging.reserve((size_t)64 << 20);
   pack.reserve((size_t)64 << 20);

@@ -2,6 +2,7 @@
 // device arena, pinned staging, the resident prepared state (generators,
 // fixed-base window tables, public-key Miller lines) and launch helpers.
 #pragma once
+#include <cuda.h>  // driver types of the SM partition (entry points come through the runtime)
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -123,9 +124,19 @@ struct SharedState {
   std::vector<PkSlot> slot_info;
   int workspaces = 4;           // concurrent calls (CUBBS_BBS_WORKSPACES)
   MsmTuning msm_tuning;         // uneven-MSM chunk length / window per size class
+  // SM partition of ProofVerify (green contexts): a few SMs for the
+  // aggregated pairing chain (scaling, group sums, single-block checks), the
+  // rest for every other kernel of the call, so that the chain's few warps do
+  // not share their SMs with the MSM kernels.  Null when the driver offers no
+  // partition or CUBBS_BBS_SM_PARTITION is 0.
+  CUgreenCtx green_small = nullptr, green_rest = nullptr;
+  int small_sms = 0, rest_sms = 0;
+  int partition_status = -1;  // 0: on; else why it is off (step * 1000 + driver result)
+  CUresult (*green_stream_create)(CUstream *, CUgreenCtx, unsigned, int) = nullptr;
 
   static SharedState &get();
   void init();                              // device, prep stream, -P2/P2 lines
+  void init_partition();                    // green_small / green_rest, when available
   // the following run with mu held exclusively
   void grow_generators(int count);
   void grow_table(int gens);
@@ -152,6 +163,11 @@ struct Runtime {
   // stream -> stream2 (ev_fork), stream2 -> stream3, stream4 (ev_mid), back to stream
   // (ev_side, ev_join, ev_sub)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_mid = nullptr, ev_side = nullptr, ev_sub = nullptr;
+  // ProofVerify on the SM partition: part[0..3] play stream..stream4 on the
+  // larger partition, part_check runs the aggregated pairing chain on the
+  // smaller one (all null without a partition)
+  cudaStream_t part[4] = {nullptr, nullptr, nullptr, nullptr}, part_check = nullptr;
+  cudaEvent_t ev_gc = nullptr, ev_gc2 = nullptr, ev_done = nullptr;
   DeviceArena arena;
   HostStaging staging;
   HostStaging pack;  // pinned: the packed batch bytes, copied to the device without a host copy
