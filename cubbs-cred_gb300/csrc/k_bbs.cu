@@ -1199,7 +1199,7 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
          launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
                          reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1,
                          b.msc));
-  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, b.domain));
+  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, rt.sh.d_dom_prefix, b.domain));
   SPAN(s, "scalar_prep",
        k_pv_rows<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms));
   SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
@@ -1241,7 +1241,7 @@ void run_pgen(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
          launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
                          reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1,
                          b.msc));
-  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, b.domain));
+  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, rt.sh.d_dom_prefix, b.domain));
   SPAN(s, "fixed_msm",
        k_pg_rows_b<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms);
        launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
@@ -1284,7 +1284,7 @@ void run_verify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
          launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
                          reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1,
                          b.msc));
-  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, b.domain));
+  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, rt.sh.d_dom_prefix, b.domain));
   SPAN(s, "scalar_prep",
        k_verify_rows<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms));
   SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
@@ -1323,7 +1323,7 @@ void run(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
     SPAN(s, "g1_decode", launch_g1_decode(s, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, true));
     launches++;
   }
-  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, b.domain));
+  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, rt.sh.d_dom_prefix, b.domain));
   launches++;
   switch (b.op) {
     case OP_PVERIFY:
@@ -1349,6 +1349,34 @@ void run(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
 
 uint8_t *upload_mapdst(Runtime &rt) {
   return upload(rt, reinterpret_cast<const uint8_t *>(MAP_DST_H), sizeof(MAP_DST_H) - 1);
+}
+
+// Points every item whose key resolved to a slot at the resident domain-hash
+// prefix of its (key slot, L), building the prefixes a batch meets for the
+// first time (under the exclusive lock, like the keys' Miller lines).  Items
+// keep the full hash when the generators do not cover their L yet.
+void attach_domain_prefixes(Runtime &rt, OpBatch &b, const std::vector<int> &slots) {
+  SharedState &sh = rt.sh;
+  std::vector<uint64_t> key(b.n, UINT64_MAX);
+  std::vector<std::pair<uint64_t, const uint8_t *>> fresh;
+  uint64_t last = UINT64_MAX;
+  for (size_t i = 0; i < b.n; i++) {
+    const uint32_t L = b.dj[i].L;
+    if (slots[i] < 0 || (int)L + 2 > sh.gen_count) continue;
+    key[i] = (uint64_t)(uint32_t)slots[i] << 32 | L;
+    if (key[i] != last && !sh.dom_prefix.count(key[i])) fresh.emplace_back(key[i], b.pks[i]);
+    last = key[i];
+  }
+  if (!fresh.empty()) {
+    rt.lock->unlock();
+    {
+      std::unique_lock<std::shared_mutex> ex(sh.mu);
+      sh.add_domain_prefixes(fresh);
+    }
+    rt.lock->lock();
+  }
+  for (size_t i = 0; i < b.n; i++)
+    if (key[i] != UINT64_MAX) b.dj[i].prefix = sh.dom_prefix.at(key[i]);
 }
 
 void finish_pks(Runtime &rt, OpBatch &b, bool need_table = true) {
@@ -1386,6 +1414,7 @@ void finish_pks(Runtime &rt, OpBatch &b, bool need_table = true) {
     }
   }
   if (need_table) rt.ensure_table((int)b.maxL + 2);
+  attach_domain_prefixes(rt, b, slots);
 }
 
 // --------------------------------------------------------------------------- planners (host packing)

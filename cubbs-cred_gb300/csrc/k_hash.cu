@@ -41,18 +41,27 @@ __global__ void k_h2s_flat(const uint8_t *msgs, const uint32_t *offs, const uint
   out[i] = h2s_finish(c, dst, dlen);
 }
 
-// calculate_domain (crates/cubbs-bbs-protocol/src/utils/util.rs:147-189)
+static_assert(sizeof(sha_ctx) == DOMAIN_PREFIX_BYTES, "domain prefix size");
+
+// calculate_domain (crates/cubbs-bbs-protocol/src/utils/util.rs:147-189).  The
+// input starts with Z_pad || PK || I2OSP(L, 8) || Q1 .. H_L (78 of its 80
+// SHA-256 blocks at L = 100), the same for every item of a key and message
+// count: an item whose (key, L) has a resident prefix starts from that state.
 __global__ void k_domain(const DomainJob *jobs, uint32_t n, const uint8_t *blob, const uint8_t *gens_c,
-                         fr *out) {
+                         const sha_ctx *prefixes, fr *out) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   DomainJob j = jobs[i];
   sha_ctx c;
-  xmd_begin(c);
-  sha_bytes(c, blob + j.pk_off, 96);
-  sha_u64be(c, j.L, 8);
-  // Q1, H1..H_L are d_gens_c[1 .. L+1]
-  sha_bytes(c, gens_c + 48, 48 * (j.L + 1));
+  if (prefixes && j.prefix != DOMAIN_NO_PREFIX) {
+    c = prefixes[j.prefix];
+  } else {
+    xmd_begin(c);
+    sha_bytes(c, blob + j.pk_off, 96);
+    sha_u64be(c, j.L, 8);
+    // Q1, H1..H_L are d_gens_c[1 .. L+1]
+    sha_bytes(c, gens_c + 48, 48 * (j.L + 1));
+  }
   sha_bytes(c, API_ID, API_ID_LEN);
   sha_u64be(c, j.hdr_len, 8);
   sha_bytes(c, blob + j.hdr_off, j.hdr_len);
@@ -144,8 +153,29 @@ void launch_h2s_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *offs, 
   if (n) k_h2s_flat<<<blocks_for(n, 128), 128, 0, s>>>(msgs, offs, lens, n, dst, dlen, out);
 }
 void launch_domain(cudaStream_t s, const DomainJob *jobs, uint32_t n, const uint8_t *blob,
-                   const uint8_t *gens_c, fr *out) {
-  if (n) k_domain<<<blocks_for(n, 64), 64, 0, s>>>(jobs, n, blob, gens_c, out);
+                   const uint8_t *gens_c, const uint8_t *prefixes, fr *out) {
+  if (n)
+    k_domain<<<blocks_for(n, 64), 64, 0, s>>>(jobs, n, blob, gens_c, reinterpret_cast<const sha_ctx *>(prefixes),
+                                              out);
+}
+
+// The domain-hash prefix of each job's (key, L): the SHA-256 state after
+// Z_pad || PK || I2OSP(L, 8) || Q1 .. H_L, stored at prefixes[index].
+__global__ void k_domain_prefix(const DomainPrefixJob *jobs, uint32_t n, const uint8_t *gens_c, sha_ctx *out) {
+  uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const DomainPrefixJob &j = jobs[i];
+  sha_ctx c;
+  xmd_begin(c);
+  sha_bytes(c, j.pk, 96);
+  sha_u64be(c, j.L, 8);
+  sha_bytes(c, gens_c + 48, 48 * (j.L + 1));
+  out[j.index] = c;
+}
+void launch_domain_prefix(cudaStream_t s, const DomainPrefixJob *jobs, uint32_t n, const uint8_t *gens_c,
+                          uint8_t *prefixes) {
+  if (n)
+    k_domain_prefix<<<blocks_for(n, 64), 64, 0, s>>>(jobs, n, gens_c, reinterpret_cast<sha_ctx *>(prefixes));
 }
 void launch_make_generator_seeds(cudaStream_t s, int first, int count, uint8_t *state, uint8_t *seeds) {
   k_generator_seeds<<<1, 1, 0, s>>>(first, count, state, seeds);

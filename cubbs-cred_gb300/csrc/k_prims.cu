@@ -694,7 +694,7 @@ extern "C" int32_t cubbs_bbs_gpu_prepare_b_batch_v2(uint32_t abi, CuBbsBbsGpuPre
   uint8_t *dblob = upload(rt, blob.data(), blob.size());
   DomainJob *ddj = upload(rt, dj.data(), n);
   fr *domain = rt.arena.alloc<fr>(n);
-  launch_domain(rt.stream, ddj, (uint32_t)n, dblob, rt.d_gens_c, domain);
+  launch_domain(rt.stream, ddj, (uint32_t)n, dblob, rt.d_gens_c, nullptr, domain);
   std::vector<uint32_t> raw(8 * n);
   CUBBS_CHECK(cudaMemcpyAsync(raw.data(), domain, 32 * n, cudaMemcpyDeviceToHost, rt.stream));
   CUBBS_CHECK(cudaStreamSynchronize(rt.stream));

@@ -442,6 +442,46 @@ void Runtime::resolve_pks(const std::vector<const uint8_t *> &pk_ptrs, std::vect
   }
 }
 
+// Builds the domain-hash prefixes of (key slot << 32 | L, key bytes) pairs not
+// resident yet (the generators already cover each L).  Growing the array
+// waits for the device first: no call may still read the old one.
+void SharedState::add_domain_prefixes(const std::vector<std::pair<uint64_t, const uint8_t *>> &fresh) {
+  std::vector<DomainPrefixJob> jobs;
+  for (const auto &f : fresh) {
+    if (dom_prefix.count(f.first)) continue;
+    const uint32_t index = (uint32_t)dom_prefix.size();
+    dom_prefix.emplace(f.first, index);
+    DomainPrefixJob j;
+    std::memcpy(j.pk, f.second, 96);
+    j.L = (uint32_t)(f.first & 0xffffffffu);
+    j.index = index;
+    jobs.push_back(j);
+  }
+  if (jobs.empty()) return;
+  const uint32_t need = (uint32_t)dom_prefix.size();
+  if (need > dom_prefix_cap) {
+    uint32_t ncap = dom_prefix_cap ? dom_prefix_cap : 64;
+    while (ncap < need) ncap *= 2;
+    uint8_t *np = nullptr;
+    CUBBS_CHECK(cudaMalloc(&np, (size_t)ncap * DOMAIN_PREFIX_BYTES));
+    if (d_dom_prefix) {
+      CUBBS_CHECK(cudaDeviceSynchronize());
+      CUBBS_CHECK(cudaMemcpy(np, d_dom_prefix, (size_t)dom_prefix_cap * DOMAIN_PREFIX_BYTES,
+                             cudaMemcpyDeviceToDevice));
+      cudaFree(d_dom_prefix);
+    }
+    d_dom_prefix = np;
+    dom_prefix_cap = ncap;
+  }
+  DomainPrefixJob *dj = nullptr;
+  CUBBS_CHECK(cudaMalloc(&dj, jobs.size() * sizeof(DomainPrefixJob)));
+  CUBBS_CHECK(cudaMemcpyAsync(dj, jobs.data(), jobs.size() * sizeof(DomainPrefixJob), cudaMemcpyHostToDevice, prep));
+  launch_domain_prefix(prep, dj, (uint32_t)jobs.size(), d_gens_c, d_dom_prefix);
+  CUBBS_CHECK(cudaGetLastError());
+  CUBBS_CHECK(cudaStreamSynchronize(prep));
+  cudaFree(dj);
+}
+
 // ---------------------------------------------------------------- workspace pool
 namespace {
 std::mutex g_pool_mu;

@@ -143,6 +143,12 @@ struct SharedState {
   int table_window_for(int gens) const;
   bool table_covers(int gens) const;
   void add_pks(const std::vector<std::string> &fresh);
+  // Resident domain-hash prefixes (DomainJob::prefix), one per (key slot, L):
+  // key slot << 32 | L -> index into d_dom_prefix (DOMAIN_PREFIX_BYTES each).
+  std::unordered_map<uint64_t, uint32_t> dom_prefix;
+  uint8_t *d_dom_prefix = nullptr;
+  uint32_t dom_prefix_cap = 0;
+  void add_domain_prefixes(const std::vector<std::pair<uint64_t, const uint8_t *>> &fresh);  // mu held exclusively
 };
 
 // One call's workspace: arena, pinned staging, two streams and the events
@@ -207,11 +213,22 @@ void launch_sha256_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *off
 void launch_xmd48_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens,
                        uint32_t n, const uint8_t *dst, uint32_t dlen, uint8_t *out);
 // domain = H2S(PK || I2OSP(L,8) || Q1..H_L || api_id || I2OSP(hlen,8) || header)
+// `prefix` indexes the resident SHA-256 state after Z_pad || PK || I2OSP(L,8) ||
+// Q1..H_L of the item's (key, L) (DOMAIN_NO_PREFIX: hash the whole input).
+constexpr uint32_t DOMAIN_NO_PREFIX = 0xffffffffu;
 struct DomainJob {
   uint32_t pk_off, hdr_off, hdr_len, L;
+  uint32_t prefix = DOMAIN_NO_PREFIX;
+};
+constexpr size_t DOMAIN_PREFIX_BYTES = 104;  // one SHA-256 context (sha_ctx)
+struct DomainPrefixJob {
+  uint8_t pk[96];
+  uint32_t L, index;  // index: the context's place in the resident array
 };
 void launch_domain(cudaStream_t s, const DomainJob *jobs, uint32_t n, const uint8_t *blob,
-                   const uint8_t *gens_c, fr *out_raw);
+                   const uint8_t *gens_c, const uint8_t *prefixes, fr *out_raw);
+void launch_domain_prefix(cudaStream_t s, const DomainPrefixJob *jobs, uint32_t n, const uint8_t *gens_c,
+                          uint8_t *prefixes);
 void launch_make_generator_seeds(cudaStream_t s, int first, int count, uint8_t *seeds_state,
                                  uint8_t *seeds_out);
 void launch_hash_generators(cudaStream_t s, int first, int count, const uint8_t *seeds, g1a *gens,
