@@ -55,7 +55,9 @@ MODEL_M = {
 # (dram__bytes_read.sum + dram__bytes_write.sum): k_fixed_msm read 12.77 MB for
 # 512 rows x 12 terms x 16 windows at L = 10; table reads scale with rows x terms,
 # so a 1024 x 102-term launch moves 12.82 MB x (1024 x 102) / (512 x 12) = 218 MB.
-TRAFFIC_BYTES = {"fixed_msm": 12.82e6 * (1024 * 102) / (512 * 12)}
+# k_var_mul_pair read 0.25 MB for 1024 terms (points, scalars, jobs); the bench's
+# launch has 4 terms per proof, 4096 terms: 0.25 MB x 4096 / 1024 = 1.0 MB.
+TRAFFIC_BYTES = {"fixed_msm": 12.82e6 * (1024 * 102) / (512 * 12), "var_mul": 0.25e6 * 4096 / 1024}
 
 
 def drbg(seed: bytes, label: bytes, i: int, n: int) -> bytes:
@@ -476,7 +478,7 @@ def main():
         roof = {"bound": "imad", "kernel": stage[0], "achieved": round(achieved, 3), "peak": round(tera_imad, 3),
                 "unit": "T IMAD/s (32-bit integer multiply-add)", "frac": round(achieved / tera_imad, 4),
                 "traffic": round(traffic) if traffic else None,
-                "traffic_unit": "bytes per launch (ncu capture, scaled by table reads)",
+                "traffic_unit": "bytes per launch (ncu capture of a smaller case, scaled to this launch)",
                 "peak_source": "measured in this run (k_imad_peak, 16 independent mad.lo chains)",
                 "model_m_per_op": model, "stage_ms": round(stage[1], 3)}
     whole = n * MODEL_M["proof_verify"]["total"] * IMAD_PER_M / (pv_step / 1e3) / 1e12
