@@ -472,6 +472,23 @@ def msm_uneven_bench(n_msms=16384, k_min=2, k_max=257, seed=4, tune=True, warmup
             "checked": chk.value, "mismatch": mm.value}
 
 
+def msm_tuning(chunk=None, window=None):
+    """Uneven-MSM engine settings per size class (K <= 8, <= 32, <= 96, larger):
+    with chunk and window (4 values each) they replace the process's settings.
+    Returns the (chunk, window) lists in force."""
+    fn = lib().cubbs_bbs_gpu_msm_tuning_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_void_p] * 4
+    cin = (ctypes.c_uint32 * 4)(*chunk) if chunk is not None else None
+    win = (ctypes.c_uint32 * 4)(*window) if window is not None else None
+    cout, wout = (ctypes.c_uint32 * 4)(), (ctypes.c_uint32 * 4)()
+    rc = fn(ctypes.cast(cin, ctypes.c_void_p) if cin else None, ctypes.cast(win, ctypes.c_void_p) if win else None,
+            ctypes.cast(cout, ctypes.c_void_p), ctypes.cast(wout, ctypes.c_void_p))
+    if rc:
+        raise ValueError(f"msm_tuning returned {rc}")
+    return list(cout), list(wout)
+
+
 def sm_partition():
     """(small, rest) SM counts of the ProofVerify SM partition: the aggregated
     pairing check runs alone on `small` SMs, everything else on `rest`; (0, 0)
@@ -497,22 +514,28 @@ def table_window():
     return w.value
 
 
-def fixed_msm_autotune(scalars_be, rows, terms, w_lo=4, w_hi=16, steps=3):
+def fixed_msm_autotune(scalars_be, rows, terms, w_lo=4, w_hi=16, steps=3, with_mismatches=False):
     """Times the fixed-base MSM kernel over rows x terms scalars (bases: the first
-    `terms` resident generators) for table window widths w_lo..w_hi; the fastest
-    width stays in use.  Returns ([ms per width], best width)."""
+    `terms` resident generators) for table window widths w_lo..w_hi, after
+    checking each width's first 64 rows against a table-free recomputation; the
+    fastest agreeing width stays in use.  Returns ([ms per width; -1 for a width
+    that disagreed], best width) and, with with_mismatches, the mismatch count."""
     nw = w_hi - w_lo + 1
     ms = (ctypes.c_float * nw)()
     best = ctypes.c_int32(0)
+    bad = ctypes.c_int32(0)
     sb = ctypes.create_string_buffer(scalars_be, len(scalars_be))
     fn = lib().cubbs_bbs_gpu_fixed_msm_autotune_v2
     fn.restype = ctypes.c_int32
     fn.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_int32,
-                   ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p]
+                   ctypes.c_int32, ctypes.c_int32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     rc = fn(ABI_VERSION, ctypes.cast(sb, ctypes.c_void_p), rows, terms, w_lo, w_hi, steps,
-            ctypes.cast(ms, ctypes.c_void_p), ctypes.cast(ctypes.pointer(best), ctypes.c_void_p))
+            ctypes.cast(ms, ctypes.c_void_p), ctypes.cast(ctypes.pointer(best), ctypes.c_void_p),
+            ctypes.cast(ctypes.pointer(bad), ctypes.c_void_p))
     if rc:
-        raise RuntimeError(f"fixed_msm_autotune returned {rc}")
+        raise RuntimeError(f"fixed_msm_autotune returned {rc} ({bad.value} widths disagreed)")
+    if with_mismatches:
+        return list(ms), best.value, bad.value
     return list(ms), best.value
 
 

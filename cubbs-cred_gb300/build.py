@@ -28,7 +28,7 @@ def _nvcc() -> str:
 
 
 def _headers_mtime() -> float:
-    hs = list(CSRC.glob("*.cuh")) + [ROOT.parent / "include" / "cubbs_bbs_gpu_abi.h"]
+    hs = list(CSRC.glob("*.cuh")) + list((ROOT.parent / "include").glob("*.h"))
     return max(h.stat().st_mtime for h in hs)
 
 

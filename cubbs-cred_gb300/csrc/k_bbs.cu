@@ -1136,7 +1136,7 @@ void span_end(cudaStream_t s, int k, const char *name) {
 // there two to an SM.  Sharing SMs with the MSM kernels stretched that chain
 // from about 3.5 ms to 5 ms.
 void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
-  const bool part = rt.part[0] != nullptr;
+  const bool part = !b.h_gslot.empty() && rt.use_partition();
   cudaStream_t s0 = rt.stream;
   cudaStream_t s = part ? rt.part[0] : rt.stream, s2 = part ? rt.part[1] : rt.stream2;
   cudaStream_t s3 = part ? rt.part[2] : rt.stream3, s4 = part ? rt.part[3] : rt.stream4;

@@ -541,3 +541,36 @@ extern "C" int32_t cubbs_bbs_gpu_msm_uneven_bench_v2(uint32_t abi, size_t n_msms
     return CUBBS_BBS_GPU_ERR_INTERNAL;
   }
 }
+
+// Uneven-MSM engine settings per size class of K (K <= 8, <= 32, <= 96,
+// larger): chunk length (terms per lane, 1..256) and window width
+// (4..MSM_C_MAX).  Non-null chunk_in / window_in replace the process's
+// settings (both or neither; out-of-range values are rejected), then the
+// settings in force are written to chunk_out / window_out when non-null.
+extern "C" int32_t cubbs_bbs_gpu_msm_tuning_v2(const uint32_t *chunk_in, const uint32_t *window_in,
+                                               uint32_t *chunk_out, uint32_t *window_out) {
+  if ((chunk_in == nullptr) != (window_in == nullptr)) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  if (chunk_in)
+    for (int c = 0; c < MSM_CLASSES; c++)
+      if (chunk_in[c] < 1 || chunk_in[c] > 256 || window_in[c] < 4 || window_in[c] > MSM_C_MAX)
+        return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  try {
+    CallScope scope;
+    Runtime &rt = scope.rt;
+    if (chunk_in) {
+      MsmTuning t;
+      for (int c = 0; c < MSM_CLASSES; c++) {
+        t.chunk[c] = chunk_in[c];
+        t.window[c] = window_in[c];
+      }
+      rt.set_msm_tuning(t);
+    }
+    for (int c = 0; c < MSM_CLASSES; c++) {
+      if (chunk_out) chunk_out[c] = rt.sh.msm_tuning.chunk[c];
+      if (window_out) window_out[c] = rt.sh.msm_tuning.window[c];
+    }
+    return CUBBS_BBS_GPU_SUCCESS;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}

@@ -969,14 +969,18 @@ extern "C" int32_t cubbs_bbs_gpu_pairing_eq_aggregate_v2(uint32_t abi, const CuB
 // [P1, Q1, H1, ...]: rows x terms canonical big-endian scalars.  For every
 // window width w in [w_lo, w_hi] the table is rebuilt with width w and the
 // MSM kernel is timed with CUDA events over `steps` launches (256 MiB L2
-// flush before each); ms_per_w[w - w_lo] gets the mean, and the width with
-// the lowest time stays as the process's table width (*best_w).  The
+// flush before each); ms_per_w[w - w_lo] gets the mean.  Each width's output
+// rows (the first 64, compressed) are compared with the same rows computed
+// without any table (GLV variable-base terms over the affine generators plus
+// a row sum); a width that disagrees gets ms_per_w = -1, counts in
+// *mismatched and is never chosen.  The fastest agreeing width stays as the
+// process's table width (*best_w; 0 and ERR_INTERNAL if none agreed).  The
 // reference sweeps its comb width by term count (prepare_b_msm.cu:315-329).
 extern "C" int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi, const uint8_t *scalars_be, size_t rows,
                                                        size_t terms, int32_t w_lo, int32_t w_hi, int32_t steps,
-                                                       float *ms_per_w, int32_t *best_w) {
+                                                       float *ms_per_w, int32_t *best_w, int32_t *mismatched) {
   if (!abi_ok(abi) || !scalars_be || rows == 0 || terms == 0 || terms > 1024 || w_lo < 4 || w_hi > 16 ||
-      w_lo > w_hi || steps <= 0 || !ms_per_w || !best_w)
+      w_lo > w_hi || steps <= 0 || !ms_per_w || !best_w || !mismatched)
     return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   ABI_GUARD_BEGIN
   CallScope scope;
@@ -992,17 +996,44 @@ extern "C" int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi, const uint8
   std::vector<uint32_t> nt(rows, (uint32_t)terms);
   uint32_t *dnt = upload(rt, nt.data(), rows);
   g1 *out = rt.arena.alloc<g1>(rows);
+  // check rows: the first min(rows, 64), recomputed without the table
+  const size_t RC = std::min<size_t>(rows, 64);
+  std::vector<VarJob> cj(RC * terms);
+  std::vector<uint32_t> cstart(RC + 1);
+  for (size_t r = 0; r <= RC; r++) cstart[r] = (uint32_t)(r * terms);
+  for (size_t j = 0; j < RC * terms; j++) cj[j] = {(uint32_t)(j % terms), 0u};
+  VarJob *dcj = upload(rt, cj.data(), cj.size());
+  uint32_t *dcs = upload(rt, cstart.data(), RC + 1);
+  g1 *cv = rt.arena.alloc<g1>(RC * terms);
+  g1 *cref = rt.arena.alloc<g1>(RC);
+  uint8_t *dref48 = rt.arena.alloc<uint8_t>(48 * RC), *dout48 = rt.arena.alloc<uint8_t>(48 * RC);
+  std::vector<uint8_t> href(48 * RC), hout(48 * RC);
+  static std::once_flag flush_once;
   static uint8_t *flush = nullptr;
+  static cudaError_t flush_err = cudaSuccess;
   const size_t FLUSH = (size_t)256 << 20;
-  if (!flush) CUBBS_CHECK(cudaMalloc(&flush, FLUSH));
+  std::call_once(flush_once, [&] { flush_err = cudaMalloc(&flush, FLUSH); });
+  CUBBS_CHECK(flush_err);
   cudaEvent_t e0, e1;
   CUBBS_CHECK(cudaEventCreate(&e0));
   CUBBS_CHECK(cudaEventCreate(&e1));
   float best = 0;
-  int bw = w_lo;
+  int bw = 0;
+  *mismatched = 0;
   for (int w = w_lo; w <= w_hi; w++) {
     rt.set_table_window(w, (int)terms);
-    launch_fixed_msm(s, rt.table, sc, (uint32_t)terms, dnt, (uint32_t)rows, out);  // warm-up
+    if (w == w_lo) {
+      // the generators now cover `terms` (the table build grew them) and stay put
+      launch_var_mul(s, rt.d_gens, dcj, sc, (uint32_t)(RC * terms), cv);
+      k_row_sum<<<blocks_for(RC * 32, 128), 128, 0, s>>>(nullptr, cv, dcs, (uint32_t)RC, cref);
+      launch_g1_compress(s, cref, (uint32_t)RC, dref48);
+      CUBBS_CHECK(cudaMemcpyAsync(href.data(), dref48, href.size(), cudaMemcpyDeviceToHost, s));
+    }
+    launch_fixed_msm(s, rt.table, sc, (uint32_t)terms, dnt, (uint32_t)rows, out);  // warm-up and check
+    launch_g1_compress(s, out, (uint32_t)RC, dout48);
+    CUBBS_CHECK(cudaMemcpyAsync(hout.data(), dout48, hout.size(), cudaMemcpyDeviceToHost, s));
+    CUBBS_CHECK(cudaStreamSynchronize(s));
+    const bool agree = std::memcmp(href.data(), hout.data(), href.size()) == 0;
     float total = 0;
     for (int k = 0; k < steps; k++) {
       CUBBS_CHECK(cudaMemsetAsync(flush, k & 0xff, FLUSH, s));
@@ -1014,8 +1045,12 @@ extern "C" int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi, const uint8
       CUBBS_CHECK(cudaEventElapsedTime(&ms, e0, e1));
       total += ms;
     }
-    ms_per_w[w - w_lo] = total / steps;
-    if (w == w_lo || ms_per_w[w - w_lo] < best) {
+    ms_per_w[w - w_lo] = agree ? total / steps : -1.0f;
+    if (!agree) {
+      ++*mismatched;
+      continue;
+    }
+    if (bw == 0 || ms_per_w[w - w_lo] < best) {
       best = ms_per_w[w - w_lo];
       bw = w;
     }
@@ -1023,21 +1058,27 @@ extern "C" int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi, const uint8
   CUBBS_CHECK(cudaGetLastError());
   cudaEventDestroy(e0);
   cudaEventDestroy(e1);
-  rt.set_table_window(bw, (int)terms);
   *best_w = bw;
+  if (bw == 0) {
+    rt.set_table_window(0, (int)terms);  // back to the automatic width
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+  rt.set_table_window(bw, (int)terms);
   return CUBBS_BBS_GPU_SUCCESS;
   ABI_GUARD_END
 }
 
 // SM counts of the ProofVerify partition (small: the aggregated pairing
 // check; rest: every other kernel of the call); both 0 when it is off, and
-// *status tells why (0: on; 1: turned off; 200 + k: driver entry point k missing; else
-// 1000 * failed step + driver or runtime result).
+// *status tells why (0: on; 1: turned off; 2: off under an injected profiler;
+// 200 + k: driver entry point k missing; else 1000 * failed step + driver or
+// runtime result).  The partition is made on first use: by this query or by
+// the first ProofVerify batch with a key group.
 extern "C" int32_t cubbs_bbs_gpu_sm_partition_v2(int32_t *small_sms, int32_t *rest_sms, int32_t *status) {
   if (!small_sms || !rest_sms || !status) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   try {
     CallScope scope;
-    const bool on = scope.rt.part[0] != nullptr;
+    const bool on = scope.rt.use_partition();
     *small_sms = on ? scope.rt.sh.small_sms : 0;
     *rest_sms = on ? scope.rt.sh.rest_sms : 0;
     *status = on ? 0 : (scope.rt.sh.partition_status ? scope.rt.sh.partition_status : 99);

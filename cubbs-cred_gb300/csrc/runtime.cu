@@ -69,8 +69,14 @@ void SharedState::init() {
   CUBBS_CHECK(cudaStreamSynchronize(prep));
   line_used = 2;
   slot_info.assign(2, PkSlot{DEC_OK});
-  init_partition();
   initialised = true;
+}
+
+void SharedState::ensure_partition() {
+  std::lock_guard<std::mutex> g(init_mu);
+  if (partition_tried) return;
+  partition_tried = true;
+  init_partition();
 }
 
 namespace {
@@ -94,7 +100,16 @@ template <class F> F driver_fn(const char *name) {
 // entry points looked up through the runtime).  A self-test launches a kernel
 // on each and hands an event from one to the other; if any step fails the
 // partition stays off and ProofVerify runs on the plain streams.
+// Under a profiler that injects itself (CUDA_INJECTION64_PATH set, as ncu and
+// nsys do) the partition stays off unless CUBBS_BBS_SM_PARTITION asks for it:
+// such tools may stop listing kernels at the first green-context launch.
 void SharedState::init_partition() {
+  const char *inj = std::getenv("CUDA_INJECTION64_PATH");
+  const char *setting = std::getenv("CUBBS_BBS_SM_PARTITION");
+  if (inj && *inj && !(setting && *setting)) {
+    partition_status = 2;
+    return;
+  }
   const int want = env_int("CUBBS_BBS_SM_PARTITION", 16);
   if (want <= 0 || want >= sm_count) {
     partition_status = 1;
@@ -351,29 +366,38 @@ Runtime::Runtime(SharedState &s)
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_side, cudaEventDisableTiming));
   CUBBS_CHECK(cudaStreamCreateWithFlags(&stream4, cudaStreamNonBlocking));
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_sub, cudaEventDisableTiming));
-  if (sh.green_rest) {
-    int lo = 0, hi = 0;
-    CUBBS_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
-    bool ok = true;
-    for (int k = 0; k < 4 && ok; k++)
-      ok = sh.green_stream_create(&part[k], sh.green_rest, CU_STREAM_NON_BLOCKING, k == 2 ? hi : 0) == CUDA_SUCCESS;
-    ok = ok && sh.green_stream_create(&part_check, sh.green_small, CU_STREAM_NON_BLOCKING, hi) == CUDA_SUCCESS;
-    if (ok) {
-      CUBBS_CHECK(cudaEventCreateWithFlags(&ev_gc, cudaEventDisableTiming));
-      CUBBS_CHECK(cudaEventCreateWithFlags(&ev_gc2, cudaEventDisableTiming));
-      CUBBS_CHECK(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming));
-    } else {
-      for (auto &p : part) {
-        if (p) cudaStreamDestroy(p);
-        p = nullptr;
-      }
-      if (part_check) cudaStreamDestroy(part_check);
-      part_check = nullptr;
-    }
-  }
   arena.reserve((size_t)256 << 20);
   staging.reserve((size_t)64 << 20);
   pack.reserve((size_t)64 << 20);
+}
+
+// The workspace's streams on the SM partition, made the first time a call on
+// this workspace can use them (the workspace belongs to one call at a time).
+bool Runtime::use_partition() {
+  if (part[0]) return true;
+  if (part_tried) return false;
+  part_tried = true;
+  sh.ensure_partition();
+  if (!sh.green_rest) return false;
+  int lo = 0, hi = 0;
+  CUBBS_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
+  cudaStream_t p[4] = {nullptr, nullptr, nullptr, nullptr}, pc = nullptr;
+  bool ok = true;
+  for (int k = 0; k < 4 && ok; k++)
+    ok = sh.green_stream_create(&p[k], sh.green_rest, CU_STREAM_NON_BLOCKING, k == 2 ? hi : 0) == CUDA_SUCCESS;
+  ok = ok && sh.green_stream_create(&pc, sh.green_small, CU_STREAM_NON_BLOCKING, hi) == CUDA_SUCCESS;
+  if (!ok) {
+    for (auto q : p)
+      if (q) cudaStreamDestroy(q);
+    if (pc) cudaStreamDestroy(pc);
+    return false;
+  }
+  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_gc, cudaEventDisableTiming));
+  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_gc2, cudaEventDisableTiming));
+  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_done, cudaEventDisableTiming));
+  for (int k = 0; k < 4; k++) part[k] = p[k];
+  part_check = pc;
+  return true;
 }
 
 // Growth from inside a call: drop the shared hold, grow under the exclusive

@@ -15,6 +15,7 @@
 #include <vector>
 
 #include "../../include/cubbs_bbs_gpu_abi.h"
+#include "../../include/cubbs_bbs_gpu_test.h"  // the definitions are checked against these declarations
 #include "pairing.cuh"
 
 namespace cubbs {
@@ -131,12 +132,17 @@ struct SharedState {
   // partition or CUBBS_BBS_SM_PARTITION is 0.
   CUgreenCtx green_small = nullptr, green_rest = nullptr;
   int small_sms = 0, rest_sms = 0;
-  int partition_status = -1;  // 0: on; else why it is off (step * 1000 + driver result)
+  int partition_status = -1;  // 0: on; -1: not tried yet; else why it is off (step * 1000 + driver result)
+  bool partition_tried = false;
   CUresult (*green_stream_create)(CUstream *, CUgreenCtx, unsigned, int) = nullptr;
 
   static SharedState &get();
   void init();                              // device, prep stream, -P2/P2 lines
-  void init_partition();                    // green_small / green_rest, when available
+  // green_small / green_rest, made on first use (the first ProofVerify batch
+  // with a key group, or a partition query), not at library start: small
+  // calls then never launch on a green context
+  void ensure_partition();
+  void init_partition();
   // the following run with mu held exclusively
   void grow_generators(int count);
   void grow_table(int gens);
@@ -174,12 +180,16 @@ struct Runtime {
   // smaller one (all null without a partition)
   cudaStream_t part[4] = {nullptr, nullptr, nullptr, nullptr}, part_check = nullptr;
   cudaEvent_t ev_gc = nullptr, ev_gc2 = nullptr, ev_done = nullptr;
+  bool part_tried = false;
   DeviceArena arena;
   HostStaging staging;
   HostStaging pack;  // pinned: the packed batch bytes, copied to the device without a host copy
   std::shared_lock<std::shared_mutex> *lock = nullptr;  // the running call's shared hold
 
   explicit Runtime(SharedState &s);
+  // true when part[] / part_check exist (makes the shared partition and this
+  // workspace's streams on it the first time)
+  bool use_partition();
   void ensure_generators(int count);  // d_gens[0..count) (P1 + count-1 generators)
   void ensure_table(int gens);        // fixed-base table covering d_gens[0..gens)
   void set_table_window(int w, int gens);  // rebuild the table with window width w (0: automatic)
@@ -253,6 +263,10 @@ void launch_var_mul(cudaStream_t s, const g1a *points, const VarJob *jobs, const
                     g1 *out,
                     bool pairs = true);
 void launch_g1_compress(cudaStream_t s, const g1 *pts, uint32_t n, uint8_t *out48);
+// Launches k_g1_decode and k_var_mul_pair over zero items on the legacy
+// default stream of the current device (module load and local-memory sizing
+// ahead of real work; nothing is read or written).
+cudaError_t warm_decode_and_var_mul_kernels(uint8_t *any_device_buffer);
 struct MsmDevice {
   uint32_t n = 0, nterms = 0, nchunks = 0, nunits = 0;
   uint8_t *term_c = nullptr, *unit_c = nullptr;
