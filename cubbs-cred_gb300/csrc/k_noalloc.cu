@@ -6,23 +6,27 @@
 // file-scope scratch array instead of the library's growable arena, and the
 // call makes no cudaMalloc / cudaFree / cudaHostAlloc and takes no library
 // runtime state.  It exists for callers that must not allocate device or
-// pinned memory while they run: callers that record the work into a stream
-// capture or a pre-planned command sequence, callers on a hard memory budget
-// that have reserved all free device memory up front, and callers inside a
-// custom allocator's own code path, where a nested allocation would re-enter
-// that allocator.
+// pinned memory while they run: callers on a hard memory budget that have
+// reserved all free device memory up front (a cudaMalloc would fail or evict
+// their reservation), and callers inside a custom allocator's own code path,
+// where a nested allocation would re-enter that allocator.
 //
 // Limits and rules (also stated beside the declaration in the header):
 //  * at most CUBBS_BBS_GPU_NOALLOC_MSM_MAX_TERMS terms per call; a larger
 //    term_count is rejected with CUBBS_BBS_GPU_ERR_NOALLOC_LIMIT before any
 //    CUDA call;
 //  * the first call on a device does set-up with that device current: it
-//    looks up the scratch array's device address (cudaGetSymbolAddress),
-//    which may load this library's module and let the driver size the
-//    per-thread stack.  Make that first call before any stream capture;
+//    looks up the scratch array's device address (cudaGetSymbolAddress) and
+//    launches every kernel the call uses once over zero terms, so that module
+//    loading, and the growth of the local memory the driver reserves for the
+//    kernels it launches, happen then and not in a later call;
+//  * the call is synchronous: it copies with cudaMemcpy on the legacy default
+//    stream and returns after the result is on the host.  It cannot be
+//    captured into a CUDA graph, and it must not be made while any stream
+//    capture is active in the process (a legacy-stream copy would invalidate
+//    a capture in global mode);
 //  * every call on a device shares the one scratch array.  Overlapping calls
-//    would race on it, so calls are serialised by a process-wide lock and
-//    are synchronous (they return after the result is on the host); work
+//    would race on it, so calls are serialised by a process-wide lock; work
 //    that the caller runs against the same library in other ways does not
 //    touch this array;
 //  * the status word that the kernels OR flags into is cleared on the device
@@ -126,8 +130,11 @@ __global__ void __launch_bounds__(kReduceThreads) k_na_sum_compress(uint8_t *scr
   for (int k = 0; k < 48; k++) res->point[k] = b[k];
 }
 
-// Device address of the scratch array for the current device (set-up on the
-// first call per device).  Caller holds g_mu.
+// Device address of the scratch array for the current device.  Set-up on the
+// first call per device: the address, then one launch over zero terms of every
+// kernel a call uses (whatever the first call's term count), which loads them
+// and lets the driver grow its local-memory reservation for them now rather
+// than in a later call.  Caller holds g_mu.
 cudaError_t scratch_for_current_device(uint8_t **out) {
   int dev = -1;
   cudaError_t e = cudaGetDevice(&dev);
@@ -137,7 +144,13 @@ cudaError_t scratch_for_current_device(uint8_t **out) {
     void *p = nullptr;
     e = cudaGetSymbolAddress(&p, g_msm_scratch);
     if (e != cudaSuccess) return e;
-    g_scratch_ptr[dev] = static_cast<uint8_t *>(p);
+    uint8_t *scratch = static_cast<uint8_t *>(p);
+    k_na_prepare<<<1, 128>>>(scratch, 0);
+    k_na_sum_compress<<<1, kReduceThreads>>>(scratch, 0);
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = warm_decode_and_var_mul_kernels(scratch)) != cudaSuccess) return e;
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
+    g_scratch_ptr[dev] = scratch;
   }
   *out = g_scratch_ptr[dev];
   return cudaSuccess;

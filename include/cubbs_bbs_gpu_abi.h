@@ -299,16 +299,19 @@ int32_t cubbs_bbs_gpu_g1_msm_batch_v2(uint32_t abi_version, CuBbsBbsGpuG1MsmItem
  * contiguous 48-byte compressed points and 32-byte big-endian scalars; same
  * result and per-item codes as one item of cubbs_bbs_gpu_g1_msm_batch_v2
  * (result.value = route 4).  Every device buffer is a slice of one fixed
- * scratch array in the library (under 2 MiB), so the call makes no device or
- * pinned allocation: for callers that must not allocate while they run (a
- * reserved-memory budget, code inside an allocator, work recorded ahead of
- * time).  Limits: term_count <= CUBBS_BBS_GPU_NOALLOC_MSM_MAX_TERMS, else
- * CUBBS_BBS_GPU_ERR_NOALLOC_LIMIT (returned and in result.code) with no CUDA
- * call made.  The first call on a device does one-time set-up with that
- * device current (looks up the scratch address; the driver may load the
- * module and size the thread stack): make it before any stream capture.
- * All calls share the scratch array, so overlapping calls would race; the
- * library serialises them with a lock and each call is synchronous. */
+ * scratch array in the library (under 2 MiB, held by every device that loads
+ * the library until exit), so the call makes no device or pinned allocation:
+ * for callers that must not allocate while they run (a process that has
+ * reserved all free device memory up front, code inside an allocator, where
+ * an allocation would re-enter it).  Limits: term_count <=
+ * CUBBS_BBS_GPU_NOALLOC_MSM_MAX_TERMS, else CUBBS_BBS_GPU_ERR_NOALLOC_LIMIT
+ * (returned and in result.code) with no CUDA call made.  The first call on a
+ * device does one-time set-up with that device current (looks up the scratch
+ * address and loads the kernels it launches).  The call is synchronous (it
+ * copies on the legacy default stream and returns with the result on the
+ * host): do not make it while any stream capture is active.  All calls share
+ * the scratch array, so overlapping calls would race; the library
+ * serialises them with a lock. */
 #define CUBBS_BBS_GPU_NOALLOC_MSM_MAX_TERMS 4096u
 #define CUBBS_BBS_GPU_ERR_NOALLOC_LIMIT 4
 int32_t cubbs_bbs_gpu_g1_msm_noalloc_v2(uint32_t abi_version, const uint8_t *points48,

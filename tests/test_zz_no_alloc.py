@@ -66,3 +66,49 @@ def test_empty_identity_and_bad_inputs_match_batch_entry(gpu, oracle):
             assert out == bout
     assert [c for c, _ in want] == [0, 0, 0, gpu.ERR_INVALID_INPUT, gpu.ERR_INVALID_INPUT, 0]
     assert want[0][1] == ident and want[2][1] == ident
+
+
+NO_ALLOC_CHILD = r"""
+import ctypes, json, sys
+sys.path.insert(0, sys.argv[1])
+sys.path.insert(0, sys.argv[1] + "/tests")
+from tests.conftest import load_package
+from oracle import oracle_ctypes as O
+from helpers import scalar
+pkg = load_package()
+pkg.build()
+pkg.lib()  # loads libcudart through the library's own dependency
+cudart = ctypes.CDLL("libcudart.so.13")
+free, total = ctypes.c_size_t(), ctypes.c_size_t()
+def free_bytes():
+    assert cudart.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+p1, _ = O.generators(1)
+pts = [O.g1_mul(p1, scalar(b"na-mem", b"pt", i)) for i in range(64)]
+scs = [scalar(b"na-mem", b"k", i) for i in range(64)]
+first = pkg.g1_msm_noalloc([], [])  # set-up call with zero terms
+before = free_bytes()
+outs = [pkg.g1_msm_noalloc(pts[:n], scs[:n]) for n in (1, 37, 64, 2, 64)]
+after = free_bytes()
+print(json.dumps({"first": list(first[:2]), "codes": [o[:2] for o in outs], "before": before, "after": after,
+                  "match": outs[2][2] == O.g1_msm(pts, scs)}))
+"""
+
+
+def test_no_device_allocation_after_set_up():
+    """In a fresh process: a set-up call with zero terms, then calls of 1 to 64
+    terms; the device's free memory (cudaMemGetInfo) does not move, so no call
+    after the set-up allocated device memory (or grew the driver's local-memory
+    reservation)."""
+    import json
+    import os
+    import pathlib
+    import subprocess
+    import sys
+    root = pathlib.Path(__file__).resolve().parents[1]
+    out = subprocess.run([sys.executable, "-c", NO_ALLOC_CHILD, str(root)], capture_output=True, text=True,
+                         timeout=600, env=dict(os.environ))
+    assert out.returncode == 0, out.stderr[-3000:]
+    res = json.loads(out.stdout.strip().splitlines()[-1])
+    assert res["first"] == [0, 0] and all(c == [0, 0] for c in res["codes"]) and res["match"]
+    assert res["after"] == res["before"], res
