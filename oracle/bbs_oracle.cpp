@@ -13,8 +13,12 @@
 //   crates/cubbs-bbs-protocol/src/bbsplus/signature.rs:544-728   (core_sign, core_verify)
 //   crates/cubbs-bbs-protocol/src/bbsplus/proof.rs:173-225,1568-1867,2155-2426,3015-3078
 // and the third-party arithmetic it calls (bls12_381_plus 0.8.18 field/curve/
-// pairing and point encodings; elliptic-curve 0.13.8 ExpandMsgXmd; RFC 9380
-// BLS12381G1_XMD:SHA-256_SSWU_RO_).  Parity is pinned by the CFRG fixtures.
+// pairing and point encodings; elliptic-curve 0.13.8 ExpandMsgXmd and
+// ExpandMsgXof; sha2 0.10.9; sha3 SHAKE-256; RFC 9380
+// BLS12381G1_XMD:SHA-256_SSWU_RO_ and BLS12381G1_XOF:SHAKE-256_SSWU_RO_).
+// Both ciphersuites of ciphersuites.rs:49-79 are restated: the suite of the
+// calling thread (oracle_set_suite) selects API_ID, P1 and the expander.
+// Parity is pinned by the CFRG fixtures of both suites.
 #include "bbs_oracle.h"
 
 #include <algorithm>
@@ -130,6 +134,116 @@ bool expand_xmd(const uint8_t *msg, size_t len, const uint8_t *dst, size_t dlen,
     std::memcpy(out + off, bi, std::min((size_t)32, n - off));
   }
   return true;
+}
+
+// ============================================================ SHAKE-256 (FIPS 202)
+// Keccak-f[1600] on 25 64-bit lanes (state index x + 5 y), 24 rounds; the
+// round constants are those of FIPS 202 section 3.2.5, computed here from its
+// rc(t) LFSR rather than tabulated.
+struct Keccak {
+  uint64_t a[25];
+  static uint64_t rol(uint64_t x, int n) { return n ? (x << n) | (x >> (64 - n)) : x; }
+  static bool rc_bit(int t) {  // FIPS 202 Algorithm 5
+    if (t % 255 == 0) return true;
+    uint32_t r = 0x80;  // bits R[0..7], R[0] the most significant of the byte
+    for (int i = 1; i <= t % 255; i++) {
+      uint32_t r8 = r & 1;  // R[7] before the shift
+      r >>= 1;
+      if (r8) r ^= 0x80 | 0x08 | 0x04 | 0x02;  // R[0], R[4], R[5], R[6] ^= R[8]
+    }
+    return (r & 0x80) != 0;
+  }
+  static uint64_t round_constant(int ir) {
+    uint64_t rc = 0;
+    for (int j = 0; j <= 6; j++)
+      if (rc_bit(j + 7 * ir)) rc |= 1ull << ((1 << j) - 1);
+    return rc;
+  }
+  void permute() {
+    static uint64_t RC[24];
+    static int ROT[25];
+    static std::once_flag once;
+    std::call_once(once, [] {
+      for (int i = 0; i < 24; i++) RC[i] = round_constant(i);
+      // rho offsets (FIPS 202 Algorithm 2): walk (x, y) -> (y, 2x + 3y)
+      ROT[0] = 0;
+      int x = 1, y = 0;
+      for (int t = 0; t < 24; t++) {
+        ROT[x + 5 * y] = ((t + 1) * (t + 2) / 2) % 64;
+        int nx = y, ny = (2 * x + 3 * y) % 5;
+        x = nx;
+        y = ny;
+      }
+    });
+    for (int ir = 0; ir < 24; ir++) {
+      uint64_t c[5], d[5], b[25];
+      for (int x = 0; x < 5; x++) c[x] = a[x] ^ a[x + 5] ^ a[x + 10] ^ a[x + 15] ^ a[x + 20];
+      for (int x = 0; x < 5; x++) d[x] = c[(x + 4) % 5] ^ rol(c[(x + 1) % 5], 1);
+      for (int i = 0; i < 25; i++) a[i] ^= d[i % 5];
+      // rho and pi: B[y, 2x + 3y] = rot(A[x, y])
+      for (int x = 0; x < 5; x++)
+        for (int y = 0; y < 5; y++) b[y + 5 * ((2 * x + 3 * y) % 5)] = rol(a[x + 5 * y], ROT[x + 5 * y]);
+      for (int x = 0; x < 5; x++)
+        for (int y = 0; y < 5; y++)
+          a[x + 5 * y] = b[x + 5 * y] ^ (~b[(x + 1) % 5 + 5 * y] & b[(x + 2) % 5 + 5 * y]);
+      a[0] ^= RC[ir];
+    }
+  }
+};
+
+// SHAKE-256: rate 136 bytes, domain padding 0x1F ... 0x80.
+struct Shake256 {
+  Keccak k;
+  size_t pos = 0;
+  Shake256() { std::memset(k.a, 0, sizeof k.a); }
+  void xor_byte(size_t i, uint8_t b) { k.a[i / 8] ^= (uint64_t)b << (8 * (i % 8)); }
+  void update(const uint8_t *p, size_t n) {
+    for (size_t i = 0; i < n; i++) {
+      xor_byte(pos++, p[i]);
+      if (pos == 136) {
+        k.permute();
+        pos = 0;
+      }
+    }
+  }
+  void squeeze(uint8_t *out, size_t n) {
+    xor_byte(pos, 0x1F);
+    xor_byte(135, 0x80);
+    k.permute();
+    size_t off = 0;
+    while (n) {
+      size_t take = std::min(n, (size_t)136 - off);
+      for (size_t i = 0; i < take; i++) *out++ = (uint8_t)(k.a[(off + i) / 8] >> (8 * ((off + i) % 8)));
+      n -= take;
+      off += take;
+      if (off == 136 && n) {
+        k.permute();
+        off = 0;
+      }
+    }
+  }
+};
+
+// RFC 9380 section 5.3.2 expand_message_xof with SHAKE-256 (k = 128):
+// SHAKE256(msg || I2OSP(n, 2) || DST || I2OSP(len(DST), 1), n).
+bool expand_xof(const uint8_t *msg, size_t len, const uint8_t *dst, size_t dlen, uint8_t *out, size_t n) {
+  if (dlen > 255 || n == 0 || n > 65535) return false;
+  Shake256 h;
+  if (len) h.update(msg, len);
+  uint8_t lib[2] = {(uint8_t)(n >> 8), (uint8_t)n};
+  h.update(lib, 2);
+  if (dlen) h.update(dst, dlen);
+  uint8_t dl = (uint8_t)dlen;
+  h.update(&dl, 1);
+  h.squeeze(out, n);
+  return true;
+}
+
+// Ciphersuite of the calling thread: 0 BLS12-381-SHA-256 (expand_message_xmd),
+// 1 BLS12-381-SHAKE-256 (expand_message_xof).
+thread_local int SUITE = 0;
+bool expand_message(const uint8_t *msg, size_t len, const uint8_t *dst, size_t dlen, uint8_t *out, size_t n) {
+  return SUITE == 1 ? expand_xof(msg, len, dst, dlen, out, n) : expand_xmd(msg, len, dst, dlen, out, n);
 }
 
 // ============================================================ Montgomery fields
@@ -583,7 +697,8 @@ typedef CurveOps<Fp2> G2;
 typedef Jac<Fp> G1P;
 typedef Jac<Fp2> G2P;
 
-G1P G1_GEN, P1_POINT;
+G1P G1_GEN, P1_POINTS[2];
+#define P1_POINT (P1_POINTS[SUITE])
 G2P G2_GEN;
 
 // --- encodings (bls12_381 zkcrypto format: flags in the top 3 bits of byte 0)
@@ -870,7 +985,7 @@ G1P iso_map(const Fp &x, const Fp &y) {
 
 G1P hash_to_curve(const uint8_t *msg, size_t len, const uint8_t *dst, size_t dlen) {
   uint8_t ub[128];
-  expand_xmd(msg, len, dst, dlen, ub, 128);
+  expand_message(msg, len, dst, dlen, ub, 128);
   Fp u0 = Fp::from_be64_mod(ub), u1 = Fp::from_be64_mod(ub + 64);
   Fp x, y;
   sswu(u0, x, y);
@@ -912,21 +1027,25 @@ void init_all() {
   FROB_GAMMA[0] = Fp2::one();
   for (int k = 1; k < 6; k++) FROB_GAMMA[k] = FROB_GAMMA[k - 1] * g;
   init_isogeny();
-  // P1 (ciphersuites.rs:78)
-  uint8_t p1[48];
-  const char *P1_HEX =
-      "a8ce256102840821a3e94ea9025e4662b205762f9776b3a766c872b948f1fd225e7c59698588e70d11406d161b4e28c9";
-  for (int i = 0; i < 48; i++) {
-    auto hv = [](char c) { return (c >= '0' && c <= '9') ? c - '0' : c - 'a' + 10; };
-    p1[i] = (uint8_t)(hv(P1_HEX[2 * i]) << 4 | hv(P1_HEX[2 * i + 1]));
+  // P1 of each suite (ciphersuites.rs:62 SHAKE-256, :78 SHA-256)
+  const char *P1_HEX[2] = {
+      "a8ce256102840821a3e94ea9025e4662b205762f9776b3a766c872b948f1fd225e7c59698588e70d11406d161b4e28c9",
+      "8929dfbc7e6642c4ed9cba0856e493f8b9d7d5fcb0c31ef8fdcd34d50648a56c795e106e9eada6e0bda386b414150755"};
+  for (int su = 0; su < 2; su++) {
+    uint8_t p1[48];
+    for (int i = 0; i < 48; i++) {
+      auto hv = [](char c) { return (c >= '0' && c <= '9') ? c - '0' : c - 'a' + 10; };
+      p1[i] = (uint8_t)(hv(P1_HEX[su][2 * i]) << 4 | hv(P1_HEX[su][2 * i + 1]));
+    }
+    g1_decompress(p1, P1_POINTS[su]);
   }
-  g1_decompress(p1, P1_POINT);
 }
 inline void ensure_init() { std::call_once(INIT_FLAG, init_all); }
 
 // ============================================================ BBS protocol
-const std::string API_ID = "BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_H2G_HM2S_";
-const std::string CS_ID = "BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_";
+const std::string API_IDS[2] = {"BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_H2G_HM2S_",
+                                "BBS_BLS12381G1_XOF:SHAKE-256_SSWU_RO_H2G_HM2S_"};
+#define API_ID (API_IDS[SUITE])
 
 Bytes str_bytes(const std::string &s) { return Bytes(s.begin(), s.end()); }
 void i2osp(Bytes &out, u64 x, int n) {
@@ -936,7 +1055,7 @@ void i2osp(Bytes &out, u64 x, int n) {
 bool hash_to_scalar(const uint8_t *msg, size_t len, const Bytes &dst, Fr &out) {
   if (dst.size() > 255) return false;
   uint8_t ub[48];
-  if (!expand_xmd(msg, len, dst.data(), dst.size(), ub, 48)) return false;
+  if (!expand_message(msg, len, dst.data(), dst.size(), ub, 48)) return false;
   out = Fr::from_okm(ub);
   return true;
 }
@@ -946,24 +1065,27 @@ bool hash_to_scalar(const Bytes &msg, const Bytes &dst, Fr &out) {
 
 // Generators cache: prefix-stable chain (generators.rs:119-146)
 std::mutex GEN_MU;
-std::vector<G1P> GEN_CACHE;        // Q1, H1, H2, ...
-std::vector<Bytes> GEN_CACHE_C;    // compressed
-Bytes GEN_V;                       // chain state after GEN_CACHE.size() steps
+std::vector<G1P> GEN_CACHES[2];    // Q1, H1, H2, ... per suite
+std::vector<Bytes> GEN_CACHES_C[2];  // compressed
+Bytes GEN_VS[2];                   // chain state after GEN_CACHE.size() steps
 
 void generators(size_t count, std::vector<G1P> &out, std::vector<Bytes> *comp = nullptr) {
   std::lock_guard<std::mutex> g(GEN_MU);
+  std::vector<G1P> &GEN_CACHE = GEN_CACHES[SUITE];
+  std::vector<Bytes> &GEN_CACHE_C = GEN_CACHES_C[SUITE];
+  Bytes &GEN_V = GEN_VS[SUITE];
   Bytes seed_dst = str_bytes(API_ID + "SIG_GENERATOR_SEED_");
   Bytes gen_dst = str_bytes(API_ID + "SIG_GENERATOR_DST_");
   if (GEN_CACHE.empty()) {
     Bytes seed = str_bytes(API_ID + "MESSAGE_GENERATOR_SEED");
     GEN_V.assign(48, 0);
-    expand_xmd(seed.data(), seed.size(), seed_dst.data(), seed_dst.size(), GEN_V.data(), 48);
+    expand_message(seed.data(), seed.size(), seed_dst.data(), seed_dst.size(), GEN_V.data(), 48);
   }
   while (GEN_CACHE.size() < count) {
     Bytes v = GEN_V;
     i2osp(v, GEN_CACHE.size() + 1, 8);
     Bytes nv(48);
-    expand_xmd(v.data(), v.size(), seed_dst.data(), seed_dst.size(), nv.data(), 48);
+    expand_message(v.data(), v.size(), seed_dst.data(), seed_dst.size(), nv.data(), 48);
     GEN_V = nv;
     G1P gpt = hash_to_curve(nv.data(), 48, gen_dst.data(), gen_dst.size());
     GEN_CACHE.push_back(gpt);
@@ -1005,16 +1127,17 @@ G1P compute_b(const std::vector<G1P> &gens, const std::vector<Fr> &m, const Fr &
   return B;
 }
 
-// seeded_random_scalars (util.rs:329-358).  A single expand_message call
-// covers at most 170 scalars (255*32 bytes); larger counts are derived in
-// chunks of 170 with seed || I2OSP(chunk, 2) (build-defined extension).
+// seeded_random_scalars (util.rs:329-358).  With expand_message_xmd a single
+// call covers at most 170 scalars (255*32 bytes); larger counts are derived in
+// chunks of 170 with seed || I2OSP(chunk, 2) (build-defined extension).  With
+// expand_message_xof one call covers up to 1365 scalars (65535 bytes).
 bool seeded_random_scalars(const uint8_t *seed, size_t slen, const uint8_t *dst, size_t dlen,
                            size_t count, std::vector<Fr> &out) {
   out.clear();
-  const size_t CHUNK = 170;
+  const size_t CHUNK = SUITE == 1 ? 1365 : 170;
   if (count <= CHUNK) {
     Bytes v(48 * count);
-    if (count && !expand_xmd(seed, slen, dst, dlen, v.data(), v.size())) return false;
+    if (count && !expand_message(seed, slen, dst, dlen, v.data(), v.size())) return false;
     for (size_t i = 0; i < count; i++) out.push_back(Fr::from_okm(v.data() + 48 * i));
     return true;
   }
@@ -1023,7 +1146,7 @@ bool seeded_random_scalars(const uint8_t *seed, size_t slen, const uint8_t *dst,
     Bytes s(seed, seed + slen);
     i2osp(s, c, 2);
     Bytes v(48 * n);
-    if (!expand_xmd(s.data(), s.size(), dst, dlen, v.data(), v.size())) return false;
+    if (!expand_message(s.data(), s.size(), dst, dlen, v.data(), v.size())) return false;
     for (size_t i = 0; i < n; i++) out.push_back(Fr::from_okm(v.data() + 48 * i));
   }
   return true;
@@ -1044,6 +1167,27 @@ int oracle_sha256(const uint8_t *msg, size_t len, uint8_t out[32]) {
 int oracle_expand_message_xmd(const uint8_t *msg, size_t len, const uint8_t *dst, size_t dst_len,
                               uint8_t *out, size_t out_len) {
   return expand_xmd(msg, len, dst, dst_len, out, out_len) ? 0 : 1;
+}
+
+int oracle_expand_message_xof(const uint8_t *msg, size_t len, const uint8_t *dst, size_t dst_len,
+                              uint8_t *out, size_t out_len) {
+  return expand_xof(msg, len, dst, dst_len, out, out_len) ? 0 : 1;
+}
+
+int oracle_shake256(const uint8_t *msg, size_t len, uint8_t *out, size_t out_len) {
+  Shake256 h;
+  if (len) h.update(msg, len);
+  h.squeeze(out, out_len);
+  return 0;
+}
+
+// Selects the calling thread's ciphersuite (0 SHA-256, 1 SHAKE-256) for every
+// later call on this thread; returns the previous one (-1 for an unknown suite).
+int oracle_set_suite(int suite) {
+  if (suite != 0 && suite != 1) return -1;
+  int prev = SUITE;
+  SUITE = suite;
+  return prev;
 }
 
 int oracle_hash_to_scalar(const uint8_t *msg, size_t len, const uint8_t *dst, size_t dst_len,

@@ -19,6 +19,15 @@ MAP_DST = API_ID + b"MAP_MSG_TO_SCALAR_AS_HASH_"
 H2S_DST = API_ID + b"H2S_"
 MOCKED_SCALAR_DST = API_ID + b"MOCK_RANDOM_SCALARS_DST_"
 SEED_MOCKED_SCALAR = b"3.141592653589793238462643383279"
+# ciphersuites (crates/cubbs-bbs-protocol/src/bbsplus/ciphersuites.rs:49-79)
+SUITE_SHA256, SUITE_SHAKE256 = 0, 1
+API_IDS = {SUITE_SHA256: API_ID, SUITE_SHAKE256: b"BBS_BLS12381G1_XOF:SHAKE-256_SSWU_RO_H2G_HM2S_"}
+
+
+def suite_dsts(suite: int):
+    """(map-to-scalar DST, hash-to-scalar DST, mocked-scalar DST) of a suite."""
+    a = API_IDS[suite]
+    return a + b"MAP_MSG_TO_SCALAR_AS_HASH_", a + b"H2S_", a + b"MOCK_RANDOM_SCALARS_DST_"
 
 _u8p = ctypes.POINTER(ctypes.c_uint8)
 _szp = ctypes.POINTER(ctypes.c_size_t)
@@ -46,6 +55,9 @@ def _declare(L):
     sigs = {
         "oracle_sha256": [P, S, P],
         "oracle_expand_message_xmd": [P, S, P, S, P, S],
+        "oracle_expand_message_xof": [P, S, P, S, P, S],
+        "oracle_shake256": [P, S, P, S],
+        "oracle_set_suite": [ctypes.c_int],
         "oracle_hash_to_scalar": [P, S, P, S, P],
         "oracle_keygen": [P, S, P, S, P, S, P],
         "oracle_sk_to_pk": [P, P],
@@ -73,6 +85,30 @@ def _declare(L):
         fn.restype = ctypes.c_int
 
 
+def _suited(fn):
+    """Adds a `suite` keyword (0 SHA-256, 1 SHAKE-256): the call runs with the
+    oracle's per-thread ciphersuite set to it."""
+    import functools
+
+    @functools.wraps(fn)
+    def run(*args, suite=SUITE_SHA256, **kw):
+        L = lib()
+        prev = L.oracle_set_suite(suite)
+        if prev < 0:
+            raise ValueError(f"unknown ciphersuite {suite}")
+        prev_py = getattr(_TLS, "suite", SUITE_SHA256)
+        _TLS.suite = suite
+        try:
+            return fn(*args, **kw)
+        finally:
+            _TLS.suite = prev_py
+            L.oracle_set_suite(prev)
+    return run
+
+
+_TLS = threading.local()
+
+
 def _buf(b: bytes):
     return ctypes.cast(ctypes.c_char_p(b), ctypes.c_void_p) if b else None
 
@@ -97,6 +133,21 @@ def expand_message_xmd(msg: bytes, dst: bytes, n: int) -> bytes:
     return out.raw
 
 
+def expand_message_xof(msg: bytes, dst: bytes, n: int) -> bytes:
+    out = ctypes.create_string_buffer(n)
+    rc = lib().oracle_expand_message_xof(_buf(msg), len(msg), _buf(dst), len(dst), out, n)
+    if rc:
+        raise ValueError("expand_message_xof rejected its input")
+    return out.raw
+
+
+def shake256(msg: bytes, n: int) -> bytes:
+    out = ctypes.create_string_buffer(n)
+    lib().oracle_shake256(_buf(msg), len(msg), out, n)
+    return out.raw
+
+
+@_suited
 def hash_to_scalar(msg: bytes, dst: bytes) -> bytes:
     out = ctypes.create_string_buffer(32)
     if lib().oracle_hash_to_scalar(_buf(msg), len(msg), _buf(dst), len(dst), out):
@@ -104,6 +155,7 @@ def hash_to_scalar(msg: bytes, dst: bytes) -> bytes:
     return out.raw
 
 
+@_suited
 def keygen(key_material: bytes, key_info: bytes = b"", key_dst: bytes = None) -> bytes:
     out = ctypes.create_string_buffer(32)
     kd = key_dst if key_dst is not None else None
@@ -121,6 +173,7 @@ def sk_to_pk(sk: bytes) -> bytes:
     return out.raw
 
 
+@_suited
 def generators(count: int):
     out = ctypes.create_string_buffer(48 * count)
     p1 = ctypes.create_string_buffer(48)
@@ -128,12 +181,14 @@ def generators(count: int):
     return p1.raw, [out.raw[48 * i:48 * (i + 1)] for i in range(count)]
 
 
+@_suited
 def hash_to_curve_g1(msg: bytes, dst: bytes) -> bytes:
     out = ctypes.create_string_buffer(48)
     lib().oracle_hash_to_curve_g1(_buf(msg), len(msg), _buf(dst), len(dst), out)
     return out.raw
 
 
+@_suited
 def seeded_random_scalars(seed: bytes, dst: bytes, count: int):
     out = ctypes.create_string_buffer(32 * max(1, count))
     if lib().oracle_seeded_random_scalars(_buf(seed), len(seed), _buf(dst), len(dst), count, out):
@@ -141,6 +196,7 @@ def seeded_random_scalars(seed: bytes, dst: bytes, count: int):
     return [out.raw[32 * i:32 * (i + 1)] for i in range(count)]
 
 
+@_suited
 def sign(sk: bytes, pk: bytes, header: bytes, msgs):
     data, lens = _pack(msgs)
     sig = ctypes.create_string_buffer(80)
@@ -153,6 +209,7 @@ def sign(sk: bytes, pk: bytes, header: bytes, msgs):
     return sig.raw, b.raw, dom.raw
 
 
+@_suited
 def verify(pk: bytes, sig: bytes, header: bytes, msgs) -> int:
     """0 valid, 2 invalid signature, 1 undecodable input."""
     data, lens = _pack(msgs)
@@ -160,8 +217,10 @@ def verify(pk: bytes, sig: bytes, header: bytes, msgs) -> int:
                                _buf(data), lens, len(msgs))
 
 
-def proof_gen(pk, sig, header, ph, msgs, disclosed, seed=SEED_MOCKED_SCALAR,
-              dst=MOCKED_SCALAR_DST):
+@_suited
+def proof_gen(pk, sig, header, ph, msgs, disclosed, seed=SEED_MOCKED_SCALAR, dst=None):
+    if dst is None:  # the mocked-scalar DST of the call's suite
+        dst = suite_dsts(_TLS.suite)[2]
     data, lens = _pack(msgs)
     idx = (ctypes.c_size_t * max(1, len(disclosed)))(*disclosed)
     cap = 512 + 48 * len(msgs) + 48 * len(disclosed) + 32 * len(msgs)
@@ -176,6 +235,7 @@ def proof_gen(pk, sig, header, ph, msgs, disclosed, seed=SEED_MOCKED_SCALAR,
     return out.raw[:n.value]
 
 
+@_suited
 def proof_verify(pk, proof, header, ph, disclosed_msgs, disclosed) -> int:
     """0 valid, 2 invalid proof, 1 undecodable public key."""
     data, lens = _pack(disclosed_msgs)
@@ -185,6 +245,7 @@ def proof_verify(pk, proof, header, ph, disclosed_msgs, disclosed) -> int:
                                      len(disclosed_msgs), idx)
 
 
+@_suited
 def calculate_domain(pk: bytes, header: bytes, L: int) -> bytes:
     out = ctypes.create_string_buffer(32)
     if lib().oracle_calculate_domain(_buf(pk), _buf(header), len(header), L, out):

@@ -1,7 +1,9 @@
-"""Regenerate tests/golden/cfrg_bls12381_sha256.json from the reference tree.
+"""Regenerate tests/golden/cfrg_bls12381_sha256.json and
+tests/golden/cfrg_bls12381_shake256.json from the reference tree.
 
 The reference's known-answer data for the BBS hot path lives in
   CFRG-IETF-BBS/fixture_data/bls12-381-sha-256/   (CFRG draft fixtures)
+  CFRG-IETF-BBS/fixture_data/bls12-381-shake-256/ (the same for the SHAKE-256 suite)
   native/cuda/tests/sha256_smoke.cpp:25-37          (SHA-256 strings)
   native/cuda/tests/prepare_b_smoke.cpp:58-86       (6-term B-MSM and its expected B)
 This script reads those files as data and writes one compact JSON fixture so
@@ -15,14 +17,18 @@ import re
 import sys
 
 
-def main(ref_root: str) -> None:
-    ref = pathlib.Path(ref_root)
-    fx = ref / "CFRG-IETF-BBS" / "fixture_data" / "bls12-381-sha-256"
+def fixtures(fx: pathlib.Path) -> dict:
     out = {}
     for name in ["h2s", "MapMessageToScalarAsHash", "generators", "mockedRng", "keypair"]:
         out[name] = json.loads((fx / f"{name}.json").read_text())
     out["signature"] = [json.loads(p.read_text()) for p in sorted((fx / "signature").glob("*.json"))]
     out["proof"] = [json.loads(p.read_text()) for p in sorted((fx / "proof").glob("*.json"))]
+    return out
+
+
+def main(ref_root: str) -> None:
+    ref = pathlib.Path(ref_root)
+    out = fixtures(ref / "CFRG-IETF-BBS" / "fixture_data" / "bls12-381-sha-256")
 
     sha_src = (ref / "native" / "cuda" / "tests" / "sha256_smoke.cpp").read_text()
     block = sha_src[sha_src.index("messages = {"):sha_src.index("std::vector<uint8_t> packed")]
@@ -48,6 +54,10 @@ def main(ref_root: str) -> None:
     }
     dst = pathlib.Path(__file__).with_name("cfrg_bls12381_sha256.json")
     dst.write_text(json.dumps(out, indent=1, sort_keys=True) + "\n")
+    print(f"wrote {dst} ({dst.stat().st_size} bytes)")
+    shake = fixtures(ref / "CFRG-IETF-BBS" / "fixture_data" / "bls12-381-shake-256")
+    dst = pathlib.Path(__file__).with_name("cfrg_bls12381_shake256.json")
+    dst.write_text(json.dumps(shake, indent=1, sort_keys=True) + "\n")
     print(f"wrote {dst} ({dst.stat().st_size} bytes)")
 
 
