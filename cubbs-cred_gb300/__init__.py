@@ -23,6 +23,9 @@ BACKEND_KIND_CUDA = 1
 API_ID = b"BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_H2G_HM2S_"
 MAP_DST = API_ID + b"MAP_MSG_TO_SCALAR_AS_HASH_"
 H2S_DST = API_ID + b"H2S_"
+# ciphersuites (CUBBS_BBS_CIPHERSUITE_*): 0 BLS12-381-SHA-256, 1 BLS12-381-SHAKE-256
+SUITE_SHA256, SUITE_SHAKE256 = 0, 1
+API_ID_SHAKE256 = b"BBS_BLS12381G1_XOF:SHAKE-256_SSWU_RO_H2G_HM2S_"
 
 
 class ByteSlice(ctypes.Structure):
@@ -165,6 +168,13 @@ def lib():
             "cubbs_bbs_gpu_expand_xmd_sha256_48_batch_for_test_v2": [U32, P, P, P, S, P, S, P],
             "cubbs_bbs_gpu_hash_to_scalar_sha256_batch_for_test_v2": [U32, P, P, P, S, P, S, P],
             "cubbs_bbs_gpu_g1_msm_noalloc_v2": [U32, P, P, S, P, P],
+            "cubbs_bbs_gpu_sign_batch_cs_v2": [U32, U32, P, S, P],
+            "cubbs_bbs_gpu_verify_batch_cs_v2": [U32, U32, P, S, P],
+            "cubbs_bbs_gpu_proof_gen_batch_cs_v2": [U32, U32, P, S, P],
+            "cubbs_bbs_gpu_proof_gen_seeded_batch_cs_v2": [U32, U32, P, S, P, P],
+            "cubbs_bbs_gpu_proof_verify_batch_cs_v2": [U32, U32, P, S, P],
+            "cubbs_bbs_gpu_expand_xof_shake256_48_batch_for_test_v2": [U32, P, P, P, S, P, S, P],
+            "cubbs_bbs_gpu_hash_to_scalar_shake256_batch_for_test_v2": [U32, P, P, P, S, P, S, P],
         }
         for name in _SYMBOLS:
             fn = getattr(_LIB, name)
@@ -187,6 +197,10 @@ _SYMBOLS = [
     "cubbs_bbs_gpu_proof_gen_t2_prepare_batch_v2", "cubbs_bbs_gpu_sha256_batch_for_test_v2",
     "cubbs_bbs_gpu_expand_xmd_sha256_48_batch_for_test_v2",
     "cubbs_bbs_gpu_hash_to_scalar_sha256_batch_for_test_v2", "cubbs_bbs_gpu_g1_msm_noalloc_v2",
+    "cubbs_bbs_gpu_sign_batch_cs_v2", "cubbs_bbs_gpu_verify_batch_cs_v2", "cubbs_bbs_gpu_proof_gen_batch_cs_v2",
+    "cubbs_bbs_gpu_proof_gen_seeded_batch_cs_v2", "cubbs_bbs_gpu_proof_verify_batch_cs_v2",
+    "cubbs_bbs_gpu_expand_xof_shake256_48_batch_for_test_v2",
+    "cubbs_bbs_gpu_hash_to_scalar_shake256_batch_for_test_v2",
 ]
 
 
@@ -244,7 +258,15 @@ def proof_capacity(message_count: int, disclosed_count: int) -> int:
     return 512 + message_count * 48 + disclosed_count * 48
 
 
-def sign_batch(reqs):
+def _op_call(name, suite, *args):
+    """The *_batch_v2 entry for the SHA-256 suite, its *_batch_cs_v2 twin otherwise."""
+    if suite == SUITE_SHA256:
+        _call(name, ABI_VERSION, *args)
+    else:
+        _call(name.replace("_batch_v2", "_batch_cs_v2"), ABI_VERSION, suite, *args)
+
+
+def sign_batch(reqs, suite=SUITE_SHA256):
     """reqs: list of (sk, pk, header, [messages]) -> list of (code, signature bytes)."""
     k = _Keep()
     items = (SignItem * len(reqs))()
@@ -254,18 +276,18 @@ def sign_batch(reqs):
         outs.append(buf)
         items[i] = SignItem(k.bytes(sk), k.bytes(pk), k.bytes(hdr), k.slices(msgs), len(msgs), ob)
     res = (Result * len(reqs))()
-    _call("cubbs_bbs_gpu_sign_batch_v2", ABI_VERSION, items, len(reqs), res)
+    _op_call("cubbs_bbs_gpu_sign_batch_v2", suite, items, len(reqs), res)
     return [(res[i].code, outs[i].raw[:items[i].signature_out.len]) for i in range(len(reqs))]
 
 
-def verify_batch(reqs):
+def verify_batch(reqs, suite=SUITE_SHA256):
     """reqs: list of (pk, signature, header, [messages]) -> list of (code, valid)."""
     k = _Keep()
     items = (VerifyItem * len(reqs))()
     for i, (pk, sig, hdr, msgs) in enumerate(reqs):
         items[i] = VerifyItem(k.bytes(pk), k.bytes(sig), k.bytes(hdr), k.slices(msgs), len(msgs))
     res = (Result * len(reqs))()
-    _call("cubbs_bbs_gpu_verify_batch_v2", ABI_VERSION, items, len(reqs), res)
+    _op_call("cubbs_bbs_gpu_verify_batch_v2", suite, items, len(reqs), res)
     return [(res[i].code, bool(res[i].value)) for i in range(len(reqs))]
 
 
@@ -280,21 +302,21 @@ def _proof_gen_items(k, reqs):
     return items, outs
 
 
-def proof_gen_batch(reqs, seeds=None):
+def proof_gen_batch(reqs, seeds=None, suite=SUITE_SHA256):
     """reqs: list of (pk, signature, header, ph, [messages], [disclosed]).  With seeds
     (one 32-byte seed per item) the blinding is deterministic; otherwise OS randomness."""
     k = _Keep()
     items, outs = _proof_gen_items(k, reqs)
     res = (Result * len(reqs))()
     if seeds is None:
-        _call("cubbs_bbs_gpu_proof_gen_batch_v2", ABI_VERSION, items, len(reqs), res)
+        _op_call("cubbs_bbs_gpu_proof_gen_batch_v2", suite, items, len(reqs), res)
     else:
         sb = ctypes.create_string_buffer(b"".join(seeds), 32 * len(seeds))
-        _call("cubbs_bbs_gpu_proof_gen_seeded_batch_v2", ABI_VERSION, items, len(reqs), sb, res)
+        _op_call("cubbs_bbs_gpu_proof_gen_seeded_batch_v2", suite, items, len(reqs), sb, res)
     return [(res[i].code, outs[i].raw[:items[i].proof_out.len]) for i in range(len(reqs))]
 
 
-def proof_verify_batch(reqs):
+def proof_verify_batch(reqs, suite=SUITE_SHA256):
     """reqs: list of (pk, proof, header, ph, [disclosed messages], [disclosed indexes], L)."""
     k = _Keep()
     items = (ProofVerifyItem * len(reqs))()
@@ -302,7 +324,7 @@ def proof_verify_batch(reqs):
         items[i] = ProofVerifyItem(k.bytes(pk), k.bytes(proof), k.bytes(hdr), k.bytes(ph), k.slices(dmsgs),
                                    len(dmsgs), k.index(didx), L)
     res = (Result * len(reqs))()
-    _call("cubbs_bbs_gpu_proof_verify_batch_v2", ABI_VERSION, items, len(reqs), res)
+    _op_call("cubbs_bbs_gpu_proof_verify_batch_v2", suite, items, len(reqs), res)
     return [(res[i].code, bool(res[i].value)) for i in range(len(reqs))]
 
 
@@ -337,19 +359,22 @@ def sha256_batch(msgs):
     return [out.raw[32 * i:32 * i + 32] for i in range(len(msgs))]
 
 
-def expand_xmd48_batch(msgs, dst):
+def expand_xmd48_batch(msgs, dst, suite=SUITE_SHA256):
+    """48 bytes of the suite's expand_message (xmd over SHA-256 / xof over SHAKE-256) per message."""
     d, o, l = _flat(msgs)
     out = ctypes.create_string_buffer(48 * max(1, len(msgs)))
-    _call("cubbs_bbs_gpu_expand_xmd_sha256_48_batch_for_test_v2", ABI_VERSION, d, o, l,
-          ctypes.c_size_t(len(msgs)), dst, ctypes.c_size_t(len(dst)), out)
+    name = ("cubbs_bbs_gpu_expand_xmd_sha256_48_batch_for_test_v2" if suite == SUITE_SHA256 else
+            "cubbs_bbs_gpu_expand_xof_shake256_48_batch_for_test_v2")
+    _call(name, ABI_VERSION, d, o, l, ctypes.c_size_t(len(msgs)), dst, ctypes.c_size_t(len(dst)), out)
     return [out.raw[48 * i:48 * i + 48] for i in range(len(msgs))]
 
 
-def hash_to_scalar_batch(msgs, dst):
+def hash_to_scalar_batch(msgs, dst, suite=SUITE_SHA256):
     d, o, l = _flat(msgs)
     out = ctypes.create_string_buffer(32 * max(1, len(msgs)))
-    _call("cubbs_bbs_gpu_hash_to_scalar_sha256_batch_for_test_v2", ABI_VERSION, d, o, l,
-          ctypes.c_size_t(len(msgs)), dst, ctypes.c_size_t(len(dst)), out)
+    name = ("cubbs_bbs_gpu_hash_to_scalar_sha256_batch_for_test_v2" if suite == SUITE_SHA256 else
+            "cubbs_bbs_gpu_hash_to_scalar_shake256_batch_for_test_v2")
+    _call(name, ABI_VERSION, d, o, l, ctypes.c_size_t(len(msgs)), dst, ctypes.c_size_t(len(dst)), out)
     return [out.raw[32 * i:32 * i + 32] for i in range(len(msgs))]
 
 

@@ -5,7 +5,7 @@
 // them from the curve (Velu on the rational 11-torsion kernel of E').
 #pragma once
 #include "curve.cuh"
-#include "sha256.cuh"
+#include "suite.cuh"
 
 DEV fp poly_eval(const fp *c, int n, const fp &x) {
   fp r = c[n - 1];
@@ -46,13 +46,16 @@ DEV g1a map_to_curve_g1(fp u) {
   return r;
 }
 
-// hash_to_curve(msg, dst): returns an XYZZ point (cofactor cleared with h_eff = |z| + 1).
+// hash_to_curve(msg, dst) with the expander of suite S (expand_message_xmd /
+// expand_message_xof, 128 bytes): returns an XYZZ point (cofactor cleared with
+// h_eff = |z| + 1).
+template <int S = SUITE_SHA256>
 DEV g1 hash_to_curve_g1(const uint8_t *msg, uint32_t len, const uint8_t *dst, uint32_t dlen) {
-  sha_ctx c;
-  xmd_begin(c);
-  sha_bytes(c, msg, len);
+  hash_ctx<S> c;
+  msg_begin(c);
+  msg_bytes(c, msg, len);
   uint8_t ub[128];
-  xmd_finish(c, dst, dlen, 128, ub);
+  msg_finish(c, dst, dlen, 128, ub);
   g1a q0 = map_to_curve_g1(fp_from_be64_mod(ub));
   g1a q1 = map_to_curve_g1(fp_from_be64_mod(ub + 64));
   g1 r = g1_add_aff(g1_from_aff(q0), q1);

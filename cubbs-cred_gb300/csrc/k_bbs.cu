@@ -25,7 +25,7 @@
 
 #include "bbs_dst.cuh"
 #include "runtime.cuh"
-#include "sha256.cuh"
+#include "suite.cuh"
 
 namespace cubbs {
 
@@ -331,6 +331,7 @@ __global__ void __launch_bounds__(128) k_pv_pairjobs_agg(const PvItem *items0, u
 }
 
 // T1, T2 -> compressed; recompute the challenge (a mismatch marks the item invalid).
+template <int S>
 __global__ void __launch_bounds__(64) k_pv_finish(PvItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
                                                   const fr *domain, const int32_t *dec_status,
                                                   const int32_t *outside_g1, const g1 *t2fix, const g1 *v) {
@@ -363,21 +364,21 @@ __global__ void __launch_bounds__(64) k_pv_finish(PvItem *items, uint32_t n, con
   g1_compress_aff_or_inf(aff[1], fin[1], t2c);
   const uint8_t *pr = blob + it.proof_off;
   const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
-  sha_ctx c;
-  xmd_begin(c);
-  sha_u64be(c, it.R, 8);
+  hash_ctx<S> c;
+  msg_begin(c);
+  msg_u64be(c, it.R, 8);
   #pragma unroll 1
   for (uint32_t k = 0; k < it.R; k++) {
-    sha_u64be(c, idx[k], 8);
-    sha_fr_be(c, msc[it.msg_base + k]);
+    msg_u64be(c, idx[k], 8);
+    msg_fr_be(c, msc[it.msg_base + k]);
   }
-  sha_bytes(c, pr, 144);
-  sha_bytes(c, t1c, 48);
-  sha_bytes(c, t2c, 48);
-  sha_fr_be(c, domain[i]);
-  sha_u64be(c, it.ph_len, 8);
-  sha_bytes(c, blob + it.ph_off, it.ph_len);
-  fr ch = h2s_finish(c, DST_H2S, DST_H2S_LEN);
+  msg_bytes(c, pr, 144);
+  msg_bytes(c, t1c, 48);
+  msg_bytes(c, t2c, 48);
+  msg_fr_be(c, domain[i]);
+  msg_u64be(c, it.ph_len, 8);
+  msg_bytes(c, blob + it.ph_off, it.ph_len);
+  fr ch = h2s_api<S>(c);
   if (i == 0) debug_record(t1c, t2c, domain[i], ch, it.R, idx, it.R ? &msc[it.msg_base] : nullptr);
   fr cp;
   fr_raw_from_be32(pr + 240 + 32 * it.U, cp);
@@ -391,6 +392,7 @@ struct SignItem {
   int32_t status;
 };
 
+template <int S>
 __global__ void __launch_bounds__(64) k_sign_prep(SignItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
                                                   const fr *domain, fr *rows, uint32_t stride, uint32_t *nterms,
                                                   fr *e_out) {
@@ -405,13 +407,13 @@ __global__ void __launch_bounds__(64) k_sign_prep(SignItem *items, uint32_t n, c
     return;
   }
   // e = hash_to_scalar(sk || m_1..m_L || domain, api_id || "H2S_")  (signature.rs:564-577)
-  sha_ctx c;
-  xmd_begin(c);
-  sha_fr_be(c, sk);
+  hash_ctx<S> c;
+  msg_begin(c);
+  msg_fr_be(c, sk);
   #pragma unroll 1
-  for (uint32_t k = 0; k < it.L; k++) sha_fr_be(c, msc[it.msg_base + k]);
-  sha_fr_be(c, domain[i]);
-  fr e = h2s_finish(c, DST_H2S, DST_H2S_LEN);
+  for (uint32_t k = 0; k < it.L; k++) msg_fr_be(c, msc[it.msg_base + k]);
+  msg_fr_be(c, domain[i]);
+  fr e = h2s_api<S>(c);
   e_out[i] = e;
   fr ske = fr_add(sk, e);
   if (fr_is_zero(ske)) {
@@ -537,13 +539,39 @@ struct PgItem {
 };
 
 // seeded_random_scalars(5+U, seed, api_id || "MOCK_RANDOM_SCALARS_DST_") (util.rs:329-358);
-// more than 170 scalars are drawn in chunks keyed by seed || I2OSP(chunk, 2).
+// with expand_message_xmd more than 170 scalars are drawn in chunks keyed by
+// seed || I2OSP(chunk, 2); with expand_message_xof one call covers up to 1365
+// (65535 bytes) and larger counts are chunked the same way.
+template <int S>
 __global__ void __launch_bounds__(64) k_pg_random(const PgItem *items, uint32_t n, const uint8_t *blob,
                                                   fr *rs, uint32_t rs_stride) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   PgItem it = items[i];
   if (it.status != ST_OK) return;
+  if constexpr (S == SUITE_SHAKE256) {
+    const uint32_t count = 5 + it.U, CH = 1365;
+    fr *out = rs + (size_t)i * rs_stride;
+#pragma unroll 1
+    for (uint32_t c0 = 0; c0 < count; c0 += CH) {
+      const uint32_t m = min(CH, count - c0);
+      shake_ctx c;
+      xof_begin(c);
+      shake_bytes(c, blob + it.seed_off, 32);
+      if (count > CH) {
+        shake_byte(c, (uint8_t)((c0 / CH) >> 8));
+        shake_byte(c, (uint8_t)(c0 / CH));
+      }
+      xof_start_output(c, SuiteDst<S>::dst_mock(), SuiteDst<S>::dst_mock_len, 48 * m);
+#pragma unroll 1
+      for (uint32_t k = 0; k < m; k++) {
+        uint8_t okm[48];
+        shake_squeeze(c, okm, 48);
+        out[c0 + k] = fr_raw_from_okm(okm);
+      }
+    }
+    return;
+  }
   const uint8_t *dst = DST_MOCK;
   uint32_t count = 5 + it.U;
   const uint32_t CH = 170;
@@ -706,6 +734,7 @@ __global__ void __launch_bounds__(64) k_pg_vars(PgItem *items, uint32_t n, const
   jobs[7 * i + 6] = {2 * i + 1, fb}; jscal[7 * i + 6] = frr_mul(r3t, r2);
 }
 
+template <int S>
 __global__ void __launch_bounds__(64) k_pg_finish(PgItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
                                                   const fr *domain, const fr *rs, uint32_t rs_stride,
                                                   const g1 *t2fix, const g1 *v, uint8_t *out) {
@@ -734,21 +763,21 @@ __global__ void __launch_bounds__(64) k_pg_finish(PgItem *items, uint32_t n, con
   g1_compress_aff_or_inf(aff[3], fin[3], t1c);
   g1_compress_aff_or_inf(aff[4], fin[4], t2c);
   const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
-  sha_ctx c;
-  xmd_begin(c);
-  sha_u64be(c, it.R, 8);
+  hash_ctx<S> c;
+  msg_begin(c);
+  msg_u64be(c, it.R, 8);
   #pragma unroll 1
   for (uint32_t k = 0; k < it.R; k++) {
-    sha_u64be(c, idx[k], 8);
-    sha_fr_be(c, msc[it.msg_base + idx[k]]);
+    msg_u64be(c, idx[k], 8);
+    msg_fr_be(c, msc[it.msg_base + idx[k]]);
   }
-  sha_bytes(c, o, 144);
-  sha_bytes(c, t1c, 48);
-  sha_bytes(c, t2c, 48);
-  sha_fr_be(c, domain[i]);
-  sha_u64be(c, it.ph_len, 8);
-  sha_bytes(c, blob + it.ph_off, it.ph_len);
-  fr ch = h2s_finish(c, DST_H2S, DST_H2S_LEN);
+  msg_bytes(c, o, 144);
+  msg_bytes(c, t1c, 48);
+  msg_bytes(c, t2c, 48);
+  msg_fr_be(c, domain[i]);
+  msg_u64be(c, it.ph_len, 8);
+  msg_bytes(c, blob + it.ph_off, it.ph_len);
+  fr ch = h2s_api<S>(c);
   if (i == 0) debug_record(t1c, t2c, domain[i], ch, it.R, idx, it.R ? &msc[it.msg_base + idx[0]] : nullptr);
   const fr *r = rs + (size_t)i * rs_stride;
   fr r1 = r[0], r2 = r[1], et = r[2], r1t = r[3], r3t = r[4];
@@ -1093,7 +1122,11 @@ void upload(Runtime &rt, OpBatch &b) {
   b.out = rt.arena.alloc<uint8_t>(b.out_total + 1);
 }
 
-static const char MAP_DST_H[] = "BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_H2G_HM2S_MAP_MSG_TO_SCALAR_AS_HASH_";
+// api_id || "MAP_MSG_TO_SCALAR_AS_HASH_" of each suite (ciphersuites.rs:21-79)
+static const char *const MAP_DST_H[SUITE_COUNT] = {
+    "BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_H2G_HM2S_MAP_MSG_TO_SCALAR_AS_HASH_",
+    "BBS_BLS12381G1_XOF:SHAKE-256_SSWU_RO_H2G_HM2S_MAP_MSG_TO_SCALAR_AS_HASH_"};
+uint32_t map_dst_len(const Runtime &rt) { return (uint32_t)std::strlen(MAP_DST_H[rt.suite]); }
 
 // Optional per-kernel spans (benchmark breakdown): span k runs from a[k] to
 // b[k], both recorded on the stream the kernel is launched on, so kernels that
@@ -1197,16 +1230,15 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   if (nm)
     SPAN(s, "hash_messages",
          launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
-                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1,
-                         b.msc));
-  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, rt.sh.d_dom_prefix, b.domain));
+                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, map_dst_len(rt), b.msc, rt.suite));
+  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c(), rt.ss().d_dom_prefix, b.domain, rt.suite));
   SPAN(s, "scalar_prep",
        k_pv_rows<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms));
-  SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
+  SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table(), b.rows, stride, b.nterms, N, b.fixed));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_side, 0));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_sub, 0));
   SPAN(s, "challenge",
-       k_pv_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.sub, b.fixed, b.v));
+       CUBBS_SUITE_DISPATCH(rt.suite, k_pv_finish<S><<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.sub, b.fixed, b.v)));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_join, 0));
   if (part) {
     CUBBS_CHECK(cudaEventRecord(rt.ev_done, s));
@@ -1231,20 +1263,19 @@ void run_pgen(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   SPAN(s3, "g1_decode", launch_g1_decode(s3, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, false));
   SPAN(s3, "g1_subgroup", launch_g1_subgroup(s3, b.pts, b.dec, (uint32_t)npts, b.sub));
   CUBBS_CHECK(cudaEventRecord(rt.ev_join, s3));
-  SPAN(s2, "random_scalars", k_pg_random<<<blocks_for(n, 64), 64, 0, s2>>>(it0, N, b.dblob, b.rs, rss));
+  SPAN(s2, "random_scalars", CUBBS_SUITE_DISPATCH(rt.suite, k_pg_random<S><<<blocks_for(n, 64), 64, 0, s2>>>(it0, N, b.dblob, b.rs, rss)));
   SPAN(s2, "fixed_msm_t2",
        k_pg_rows_t2<<<blocks_for(n, 128), 128, 0, s2>>>(it0, N, b.dblob, b.rs, rss, b.rows, stride, b.nterms);
-       launch_fixed_msm(s2, rt.table, b.rows + (size_t)n * stride, stride, b.nterms + n, N, b.fixed + n));
+       launch_fixed_msm(s2, rt.table(), b.rows + (size_t)n * stride, stride, b.nterms + n, N, b.fixed + n));
   CUBBS_CHECK(cudaEventRecord(rt.ev_side, s2));
   if (nm)
     SPAN(s, "hash_messages",
          launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
-                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1,
-                         b.msc));
-  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, rt.sh.d_dom_prefix, b.domain));
+                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, map_dst_len(rt), b.msc, rt.suite));
+  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c(), rt.ss().d_dom_prefix, b.domain, rt.suite));
   SPAN(s, "fixed_msm",
        k_pg_rows_b<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms);
-       launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
+       launch_fixed_msm(s, rt.table(), b.rows, stride, b.nterms, N, b.fixed));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_side, 0));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_join, 0));
   SPAN(s, "var_prep",
@@ -1252,8 +1283,8 @@ void run_pgen(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
                                                   b.jobs, b.jscal));
   SPAN(s, "var_mul", launch_var_mul(s, b.vpts, b.jobs, b.jscal, 7 * N, b.v));
   SPAN(s, "finish",
-       k_pg_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rs, rss, b.fixed + n, b.v,
-                                                    b.out));
+       CUBBS_SUITE_DISPATCH(rt.suite, k_pg_finish<S><<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rs, rss, b.fixed + n, b.v,
+                                                    b.out)));
   b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 9;
 }
 
@@ -1282,12 +1313,11 @@ void run_verify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   if (nm)
     SPAN(s, "hash_messages",
          launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
-                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1,
-                         b.msc));
-  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, rt.sh.d_dom_prefix, b.domain));
+                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, map_dst_len(rt), b.msc, rt.suite));
+  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c(), rt.ss().d_dom_prefix, b.domain, rt.suite));
   SPAN(s, "scalar_prep",
        k_verify_rows<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms));
-  SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
+  SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table(), b.rows, stride, b.nterms, N, b.fixed));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_side, 0));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_sub, 0));
   SPAN(s, "finish",
@@ -1314,8 +1344,7 @@ void run(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   if (nm) {
     SPAN(s, "hash_messages",
          launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
-                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, sizeof(MAP_DST_H) - 1,
-                         b.msc));
+                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, map_dst_len(rt), b.msc, rt.suite));
     launches++;
   }
   size_t npts = b.pts48.size() / 48;
@@ -1323,7 +1352,7 @@ void run(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
     SPAN(s, "g1_decode", launch_g1_decode(s, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, true));
     launches++;
   }
-  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c, rt.sh.d_dom_prefix, b.domain));
+  SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c(), rt.ss().d_dom_prefix, b.domain, rt.suite));
   launches++;
   switch (b.op) {
     case OP_PVERIFY:
@@ -1331,9 +1360,9 @@ void run(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
     case OP_SIGN: {
       SignItem *it = reinterpret_cast<SignItem *>(b.ditems);
       SPAN(s, "scalar_prep",
-           k_sign_prep<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms,
-                                                        b.e));
-      SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table, b.rows, stride, b.nterms, N, b.fixed));
+           CUBBS_SUITE_DISPATCH(rt.suite, k_sign_prep<S><<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms,
+                                                        b.e)));
+      SPAN(s, "fixed_msm", launch_fixed_msm(s, rt.table(), b.rows, stride, b.nterms, N, b.fixed));
       SPAN(s, "finish", k_sign_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.fixed, b.e, b.out));
       launches += 3;
       break;
@@ -1348,7 +1377,7 @@ void run(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
 }
 
 uint8_t *upload_mapdst(Runtime &rt) {
-  return upload(rt, reinterpret_cast<const uint8_t *>(MAP_DST_H), sizeof(MAP_DST_H) - 1);
+  return upload(rt, reinterpret_cast<const uint8_t *>(MAP_DST_H[rt.suite]), map_dst_len(rt));
 }
 
 // Points every item whose key resolved to a slot at the resident domain-hash
@@ -1356,27 +1385,29 @@ uint8_t *upload_mapdst(Runtime &rt) {
 // first time (under the exclusive lock, like the keys' Miller lines).  Items
 // keep the full hash when the generators do not cover their L yet.
 void attach_domain_prefixes(Runtime &rt, OpBatch &b, const std::vector<int> &slots) {
+  if (rt.suite != SUITE_SHA256) return;  // the SHAKE-256 domain hashes its whole input
   SharedState &sh = rt.sh;
+  SuiteState &ss = rt.ss();
   std::vector<uint64_t> key(b.n, UINT64_MAX);
   std::vector<std::pair<uint64_t, const uint8_t *>> fresh;
   uint64_t last = UINT64_MAX;
   for (size_t i = 0; i < b.n; i++) {
     const uint32_t L = b.dj[i].L;
-    if (slots[i] < 0 || (int)L + 2 > sh.gen_count) continue;
+    if (slots[i] < 0 || (int)L + 2 > ss.gen_count) continue;
     key[i] = (uint64_t)(uint32_t)slots[i] << 32 | L;
-    if (key[i] != last && !sh.dom_prefix.count(key[i])) fresh.emplace_back(key[i], b.pks[i]);
+    if (key[i] != last && !ss.dom_prefix.count(key[i])) fresh.emplace_back(key[i], b.pks[i]);
     last = key[i];
   }
   if (!fresh.empty()) {
     rt.lock->unlock();
     {
       std::unique_lock<std::shared_mutex> ex(sh.mu);
-      sh.add_domain_prefixes(fresh);
+      sh.add_domain_prefixes(rt.suite, fresh);
     }
     rt.lock->lock();
   }
   for (size_t i = 0; i < b.n; i++)
-    if (key[i] != UINT64_MAX) b.dj[i].prefix = sh.dom_prefix.at(key[i]);
+    if (key[i] != UINT64_MAX) b.dj[i].prefix = ss.dom_prefix.at(key[i]);
 }
 
 void finish_pks(Runtime &rt, OpBatch &b, bool need_table = true) {
@@ -1760,14 +1791,16 @@ static void execute(Runtime &rt, OpBatch &b) {
 
 using namespace cubbs;
 
+static bool suite_ok(uint32_t suite) { return suite == CUBBS_BBS_CIPHERSUITE_SHA256 || suite == CUBBS_BBS_CIPHERSUITE_SHAKE256; }
+
 // ----------------------------------------------------------------------------- ProofVerify
-extern "C" int32_t cubbs_bbs_gpu_proof_verify_batch_v2(uint32_t abi, const CuBbsBbsGpuProofVerifyItem *items,
-                                                       size_t n, CuBbsBbsGpuResult *results) {
-  if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+static int32_t proof_verify_impl(int suite, const CuBbsBbsGpuProofVerifyItem *items, size_t n,
+                                 CuBbsBbsGpuResult *results) {
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   try {
     CallScope scope;
     Runtime &rt = scope.rt;
+    rt.suite = suite;
     OpBatch b(rt);
     int32_t st = plan_pverify(items, n, b);
     if (st != CUBBS_BBS_GPU_SUCCESS) return st;
@@ -1778,6 +1811,20 @@ extern "C" int32_t cubbs_bbs_gpu_proof_verify_batch_v2(uint32_t abi, const CuBbs
   } catch (const CudaError &) {
     return CUBBS_BBS_GPU_ERR_INTERNAL;
   }
+}
+
+extern "C" int32_t cubbs_bbs_gpu_proof_verify_batch_v2(uint32_t abi, const CuBbsBbsGpuProofVerifyItem *items,
+                                                       size_t n, CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  return proof_verify_impl(CUBBS_BBS_CIPHERSUITE_SHA256, items, n, results);
+}
+
+extern "C" int32_t cubbs_bbs_gpu_proof_verify_batch_cs_v2(uint32_t abi, uint32_t suite,
+                                                          const CuBbsBbsGpuProofVerifyItem *items, size_t n,
+                                                          CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || !suite_ok(suite) || (n > 0 && (items == nullptr || results == nullptr)))
+    return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  return proof_verify_impl((int)suite, items, n, results);
 }
 
 // Test export: host-side phase times (ms) of one ProofVerify call, in order:
@@ -1816,13 +1863,12 @@ extern "C" int32_t cubbs_bbs_gpu_proof_verify_phases_for_test_v2(const CuBbsBbsG
 }
 
 // ----------------------------------------------------------------------------- Verify
-extern "C" int32_t cubbs_bbs_gpu_verify_batch_v2(uint32_t abi, const CuBbsBbsGpuVerifyItem *items, size_t n,
-                                                 CuBbsBbsGpuResult *results) {
-  if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+static int32_t verify_impl(int suite, const CuBbsBbsGpuVerifyItem *items, size_t n, CuBbsBbsGpuResult *results) {
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   try {
     CallScope scope;
     Runtime &rt = scope.rt;
+    rt.suite = suite;
     OpBatch b(rt);
     int32_t st = plan_verify(items, n, b);
     if (st != CUBBS_BBS_GPU_SUCCESS) return st;
@@ -1835,14 +1881,26 @@ extern "C" int32_t cubbs_bbs_gpu_verify_batch_v2(uint32_t abi, const CuBbsBbsGpu
   }
 }
 
-// ----------------------------------------------------------------------------- Sign
-extern "C" int32_t cubbs_bbs_gpu_sign_batch_v2(uint32_t abi, CuBbsBbsGpuSignItem *items, size_t n,
-                                               CuBbsBbsGpuResult *results) {
+extern "C" int32_t cubbs_bbs_gpu_verify_batch_v2(uint32_t abi, const CuBbsBbsGpuVerifyItem *items, size_t n,
+                                                 CuBbsBbsGpuResult *results) {
   if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  return verify_impl(CUBBS_BBS_CIPHERSUITE_SHA256, items, n, results);
+}
+
+extern "C" int32_t cubbs_bbs_gpu_verify_batch_cs_v2(uint32_t abi, uint32_t suite, const CuBbsBbsGpuVerifyItem *items,
+                                                    size_t n, CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || !suite_ok(suite) || (n > 0 && (items == nullptr || results == nullptr)))
+    return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  return verify_impl((int)suite, items, n, results);
+}
+
+// ----------------------------------------------------------------------------- Sign
+static int32_t sign_impl(int suite, CuBbsBbsGpuSignItem *items, size_t n, CuBbsBbsGpuResult *results) {
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   try {
     CallScope scope;
     Runtime &rt = scope.rt;
+    rt.suite = suite;
     OpBatch b(rt);
     int32_t st = plan_sign(items, n, b);
     if (st != CUBBS_BBS_GPU_SUCCESS) return st;
@@ -1871,12 +1929,26 @@ extern "C" int32_t cubbs_bbs_gpu_sign_batch_v2(uint32_t abi, CuBbsBbsGpuSignItem
   }
 }
 
+extern "C" int32_t cubbs_bbs_gpu_sign_batch_v2(uint32_t abi, CuBbsBbsGpuSignItem *items, size_t n,
+                                               CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  return sign_impl(CUBBS_BBS_CIPHERSUITE_SHA256, items, n, results);
+}
+
+extern "C" int32_t cubbs_bbs_gpu_sign_batch_cs_v2(uint32_t abi, uint32_t suite, CuBbsBbsGpuSignItem *items, size_t n,
+                                                  CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || !suite_ok(suite) || (n > 0 && (items == nullptr || results == nullptr)))
+    return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  return sign_impl((int)suite, items, n, results);
+}
+
 // ----------------------------------------------------------------------------- ProofGen
-static int32_t proof_gen_impl(CuBbsBbsGpuProofGenItem *items, size_t n, const uint8_t (*seeds)[32],
+static int32_t proof_gen_impl(int suite, CuBbsBbsGpuProofGenItem *items, size_t n, const uint8_t (*seeds)[32],
                               CuBbsBbsGpuResult *results) {
   try {
     CallScope scope;
     Runtime &rt = scope.rt;
+    rt.suite = suite;
     OpBatch b(rt);
     std::vector<uint8_t> os_seeds;
     int32_t st = plan_pgen(items, n, seeds, b, os_seeds);
@@ -1912,7 +1984,15 @@ extern "C" int32_t cubbs_bbs_gpu_proof_gen_batch_v2(uint32_t abi, CuBbsBbsGpuPro
                                                     CuBbsBbsGpuResult *results) {
   if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
-  return proof_gen_impl(items, n, nullptr, results);
+  return proof_gen_impl(CUBBS_BBS_CIPHERSUITE_SHA256, items, n, nullptr, results);
+}
+
+extern "C" int32_t cubbs_bbs_gpu_proof_gen_batch_cs_v2(uint32_t abi, uint32_t suite, CuBbsBbsGpuProofGenItem *items,
+                                                       size_t n, CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || !suite_ok(suite) || (n > 0 && (items == nullptr || results == nullptr)))
+    return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
+  return proof_gen_impl((int)suite, items, n, nullptr, results);
 }
 
 extern "C" int32_t cubbs_bbs_gpu_proof_gen_seeded_batch_v2(uint32_t abi, CuBbsBbsGpuProofGenItem *items, size_t n,
@@ -1920,7 +2000,16 @@ extern "C" int32_t cubbs_bbs_gpu_proof_gen_seeded_batch_v2(uint32_t abi, CuBbsBb
   if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr || seeds == nullptr)))
     return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
-  return proof_gen_impl(items, n, seeds, results);
+  return proof_gen_impl(CUBBS_BBS_CIPHERSUITE_SHA256, items, n, seeds, results);
+}
+
+extern "C" int32_t cubbs_bbs_gpu_proof_gen_seeded_batch_cs_v2(uint32_t abi, uint32_t suite,
+                                                              CuBbsBbsGpuProofGenItem *items, size_t n,
+                                                              const uint8_t (*seeds)[32], CuBbsBbsGpuResult *results) {
+  if (!abi_ok(abi) || !suite_ok(suite) || (n > 0 && (items == nullptr || results == nullptr || seeds == nullptr)))
+    return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
+  return proof_gen_impl((int)suite, items, n, seeds, results);
 }
 
 // ----------------------------------------------------------------------------- device-resident timing

@@ -21,23 +21,25 @@ __global__ void k_sha256_flat(const uint8_t *msgs, const uint32_t *offs, const u
   sha_final(c, digests + 32 * (size_t)i);
 }
 
-__global__ void k_xmd48_flat(const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens, uint32_t n,
-                             const uint8_t *dst, uint32_t dlen, uint8_t *out) {
+template <int S>
+__global__ void k_expand48_flat(const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens, uint32_t n,
+                                const uint8_t *dst, uint32_t dlen, uint8_t *out) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  sha_ctx c;
-  xmd_begin(c);
-  sha_bytes(c, msgs + offs[i], lens[i]);
-  xmd_finish(c, dst, dlen, 48, out + 48 * (size_t)i);
+  hash_ctx<S> c;
+  msg_begin(c);
+  msg_bytes(c, msgs + offs[i], lens[i]);
+  msg_finish(c, dst, dlen, 48, out + 48 * (size_t)i);
 }
 
+template <int S>
 __global__ void k_h2s_flat(const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens, uint32_t n,
                            const uint8_t *dst, uint32_t dlen, fr *out) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  sha_ctx c;
-  xmd_begin(c);
-  sha_bytes(c, msgs + offs[i], lens[i]);
+  hash_ctx<S> c;
+  msg_begin(c);
+  msg_bytes(c, msgs + offs[i], lens[i]);
   out[i] = h2s_finish(c, dst, dlen);
 }
 
@@ -46,60 +48,69 @@ static_assert(sizeof(sha_ctx) == DOMAIN_PREFIX_BYTES, "domain prefix size");
 // calculate_domain (crates/cubbs-bbs-protocol/src/utils/util.rs:147-189).  The
 // input starts with Z_pad || PK || I2OSP(L, 8) || Q1 .. H_L (78 of its 80
 // SHA-256 blocks at L = 100), the same for every item of a key and message
-// count: an item whose (key, L) has a resident prefix starts from that state.
+// count: an item whose (key, L) has a resident prefix starts from that state
+// (suite 0 only; the SHAKE-256 suite hashes the whole input).
+template <int S>
 __global__ void k_domain(const DomainJob *jobs, uint32_t n, const uint8_t *blob, const uint8_t *gens_c,
                          const sha_ctx *prefixes, fr *out) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   DomainJob j = jobs[i];
-  sha_ctx c;
-  if (prefixes && j.prefix != DOMAIN_NO_PREFIX) {
-    c = prefixes[j.prefix];
-  } else {
-    xmd_begin(c);
-    sha_bytes(c, blob + j.pk_off, 96);
-    sha_u64be(c, j.L, 8);
-    // Q1, H1..H_L are d_gens_c[1 .. L+1]
-    sha_bytes(c, gens_c + 48, 48 * (j.L + 1));
+  hash_ctx<S> c;
+  bool resumed = false;
+  if constexpr (S == SUITE_SHA256) {
+    if (prefixes && j.prefix != DOMAIN_NO_PREFIX) {
+      c = prefixes[j.prefix];
+      resumed = true;
+    }
   }
-  sha_bytes(c, API_ID, API_ID_LEN);
-  sha_u64be(c, j.hdr_len, 8);
-  sha_bytes(c, blob + j.hdr_off, j.hdr_len);
-  out[i] = h2s_finish(c, DST_H2S, DST_H2S_LEN);
+  if (!resumed) {
+    msg_begin(c);
+    msg_bytes(c, blob + j.pk_off, 96);
+    msg_u64be(c, j.L, 8);
+    // Q1, H1..H_L are d_gens_c[1 .. L+1]
+    msg_bytes(c, gens_c + 48, 48 * (j.L + 1));
+  }
+  msg_bytes(c, SuiteDst<S>::api_id(), SuiteDst<S>::api_id_len);
+  msg_u64be(c, j.hdr_len, 8);
+  msg_bytes(c, blob + j.hdr_off, j.hdr_len);
+  out[i] = h2s_api<S>(c);
 }
 
 // Generator seed chain (generators.rs:131-144): v_0 = expand(seed, seed_dst),
 // v_i = expand(v_{i-1} || I2OSP(i, 8), seed_dst).  Sequential, one thread.
 // state holds v_{first-1} (48 bytes) on entry and v_{first+count-1} on exit.
-__global__ void k_generator_seeds(int first, int count, uint8_t *state, uint8_t *seeds) {
+template <int S> __global__ void k_generator_seeds(int first, int count, uint8_t *state, uint8_t *seeds) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  const uint8_t *dst = DST_GEN_SEED;
+  const uint8_t *dst = SuiteDst<S>::dst_gen_seed();
+  constexpr uint32_t dlen = SuiteDst<S>::dst_gen_seed_len;
   uint8_t v[48];
   if (first == 1) {
-    sha_ctx c;
-    xmd_begin(c);
-    sha_bytes(c, GEN_SEED, GEN_SEED_LEN);
-    xmd_finish(c, dst, DST_GEN_SEED_LEN, 48, v);
+    hash_ctx<S> c;
+    msg_begin(c);
+    msg_bytes(c, SuiteDst<S>::gen_seed(), SuiteDst<S>::gen_seed_len);
+    msg_finish(c, dst, dlen, 48, v);
   } else {
     for (int k = 0; k < 48; k++) v[k] = state[k];
   }
   #pragma unroll 1
   for (int i = first; i < first + count; i++) {
-    sha_ctx c;
-    xmd_begin(c);
-    sha_bytes(c, v, 48);
-    sha_u64be(c, (uint64_t)i, 8);
-    xmd_finish(c, dst, DST_GEN_SEED_LEN, 48, v);
+    hash_ctx<S> c;
+    msg_begin(c);
+    msg_bytes(c, v, 48);
+    msg_u64be(c, (uint64_t)i, 8);
+    msg_finish(c, dst, dlen, 48, v);
     for (int k = 0; k < 48; k++) seeds[48 * (size_t)(i - first) + k] = v[k];
   }
   for (int k = 0; k < 48; k++) state[k] = v[k];
 }
 
 // generator i (1-based: Q1 = 1, H_j = j + 1) = hash_to_curve(v_i, api_id || "SIG_GENERATOR_DST_")
+template <int S>
 __global__ void k_hash_generators(int first, int count, const uint8_t *seeds, g1a *gens, uint8_t *gens_c) {
   int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= count) return;
-  g1 p = hash_to_curve_g1(seeds + 48 * (size_t)t, 48, DST_GEN, DST_GEN_LEN);
+  g1 p = hash_to_curve_g1<S>(seeds + 48 * (size_t)t, 48, SuiteDst<S>::dst_gen(), SuiteDst<S>::dst_gen_len);
   g1a a;
   g1_to_aff(p, a);
   int idx = first + t;  // d_gens index: P1 at 0, Q1 at 1
@@ -131,9 +142,10 @@ __global__ void k_sign_e(const SignEJob *jobs, uint32_t n, const uint8_t *blob, 
   out[i] = h2s_finish(c, dst, dlen);
 }
 
-__global__ void k_decode_p1(g1a *gens, uint8_t *gens_c) {
+template <int S> __global__ void k_decode_p1(g1a *gens, uint8_t *gens_c) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
-  const uint8_t p1[48] = C_P1_COMPRESSED;
+  uint8_t p1[48];
+  for (int k = 0; k < 48; k++) p1[k] = SuiteDst<S>::p1_compressed()[k];
   g1a a;
   g1_decompress(p1, a, false);
   gens[0] = a;
@@ -144,19 +156,23 @@ void launch_sha256_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *off
                         uint32_t n, uint8_t *digests) {
   if (n) k_sha256_flat<<<blocks_for(n, 128), 128, 0, s>>>(msgs, offs, lens, n, digests);
 }
-void launch_xmd48_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens,
-                       uint32_t n, const uint8_t *dst, uint32_t dlen, uint8_t *out) {
-  if (n) k_xmd48_flat<<<blocks_for(n, 128), 128, 0, s>>>(msgs, offs, lens, n, dst, dlen, out);
+void launch_expand48_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens,
+                          uint32_t n, const uint8_t *dst, uint32_t dlen, uint8_t *out, int suite) {
+  if (n)
+    CUBBS_SUITE_DISPATCH(suite, k_expand48_flat<S><<<blocks_for(n, 128), 128, 0, s>>>(msgs, offs, lens, n, dst,
+                                                                                       dlen, out));
 }
 void launch_h2s_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens,
-                     uint32_t n, const uint8_t *dst, uint32_t dlen, fr *out) {
-  if (n) k_h2s_flat<<<blocks_for(n, 128), 128, 0, s>>>(msgs, offs, lens, n, dst, dlen, out);
+                     uint32_t n, const uint8_t *dst, uint32_t dlen, fr *out, int suite) {
+  if (n)
+    CUBBS_SUITE_DISPATCH(suite, k_h2s_flat<S><<<blocks_for(n, 128), 128, 0, s>>>(msgs, offs, lens, n, dst, dlen,
+                                                                                  out));
 }
 void launch_domain(cudaStream_t s, const DomainJob *jobs, uint32_t n, const uint8_t *blob,
-                   const uint8_t *gens_c, const uint8_t *prefixes, fr *out) {
+                   const uint8_t *gens_c, const uint8_t *prefixes, fr *out, int suite) {
   if (n)
-    k_domain<<<blocks_for(n, 64), 64, 0, s>>>(jobs, n, blob, gens_c, reinterpret_cast<const sha_ctx *>(prefixes),
-                                              out);
+    CUBBS_SUITE_DISPATCH(suite, k_domain<S><<<blocks_for(n, 64), 64, 0, s>>>(
+                                    jobs, n, blob, gens_c, reinterpret_cast<const sha_ctx *>(prefixes), out));
 }
 
 // The domain-hash prefix of each job's (key, L): the SHA-256 state after
@@ -177,14 +193,18 @@ void launch_domain_prefix(cudaStream_t s, const DomainPrefixJob *jobs, uint32_t 
   if (n)
     k_domain_prefix<<<blocks_for(n, 64), 64, 0, s>>>(jobs, n, gens_c, reinterpret_cast<sha_ctx *>(prefixes));
 }
-void launch_make_generator_seeds(cudaStream_t s, int first, int count, uint8_t *state, uint8_t *seeds) {
-  k_generator_seeds<<<1, 1, 0, s>>>(first, count, state, seeds);
+void launch_make_generator_seeds(cudaStream_t s, int first, int count, uint8_t *state, uint8_t *seeds, int suite) {
+  CUBBS_SUITE_DISPATCH(suite, k_generator_seeds<S><<<1, 1, 0, s>>>(first, count, state, seeds));
 }
 void launch_hash_generators(cudaStream_t s, int first, int count, const uint8_t *seeds, g1a *gens,
-                            uint8_t *gens_c) {
-  if (count) k_hash_generators<<<blocks_for(count, 32), 32, 0, s>>>(first, count, seeds, gens, gens_c);
+                            uint8_t *gens_c, int suite) {
+  if (count)
+    CUBBS_SUITE_DISPATCH(suite, k_hash_generators<S><<<blocks_for(count, 32), 32, 0, s>>>(first, count, seeds,
+                                                                                           gens, gens_c));
 }
-void launch_decode_p1(cudaStream_t s, g1a *gens, uint8_t *gens_c) { k_decode_p1<<<1, 1, 0, s>>>(gens, gens_c); }
+void launch_decode_p1(cudaStream_t s, g1a *gens, uint8_t *gens_c, int suite) {
+  CUBBS_SUITE_DISPATCH(suite, k_decode_p1<S><<<1, 1, 0, s>>>(gens, gens_c));
+}
 
 // ----------------------------------------------------------------------------- ABI: hashing
 namespace {
@@ -246,18 +266,22 @@ static int32_t flat_test_call(uint32_t abi, const uint8_t *messages, const size_
     rt.arena.reserve(total + 16 * n + 64 * n + 4096);
     FlatMsgs f = stage_flat(rt, ptrs.data(), lengths, n);
     uint8_t *ddst = stage_bytes(rt, dst, dst_len);
-    size_t out_sz = mode == 0 ? 32 : (mode == 1 ? 48 : 32);
+    // mode: 0 SHA-256, 1 expand_message_xmd (48 B), 2 hash_to_scalar over xmd,
+    // 3 expand_message_xof (48 B), 4 hash_to_scalar over xof
+    const bool expand = mode == 1 || mode == 3, h2s = mode == 2 || mode == 4;
+    const int suite = mode >= 3 ? SUITE_SHAKE256 : SUITE_SHA256;
+    size_t out_sz = expand ? 48 : 32;
     uint8_t *dout = rt.arena.alloc<uint8_t>(n * 48);
     if (mode == 0) {
       launch_sha256_flat(rt.stream, f.bytes, f.offs, f.lens, (uint32_t)n, dout);
-    } else if (mode == 1) {
-      launch_xmd48_flat(rt.stream, f.bytes, f.offs, f.lens, (uint32_t)n, ddst, (uint32_t)dst_len, dout);
+    } else if (expand) {
+      launch_expand48_flat(rt.stream, f.bytes, f.offs, f.lens, (uint32_t)n, ddst, (uint32_t)dst_len, dout, suite);
     } else {
       launch_h2s_flat(rt.stream, f.bytes, f.offs, f.lens, (uint32_t)n, ddst, (uint32_t)dst_len,
-                      reinterpret_cast<fr *>(dout));
+                      reinterpret_cast<fr *>(dout), suite);
     }
     CUBBS_CHECK(cudaGetLastError());
-    if (mode == 2) {
+    if (h2s) {
       std::vector<uint32_t> raw(8 * n);
       CUBBS_CHECK(cudaMemcpyAsync(raw.data(), dout, 32 * n, cudaMemcpyDeviceToHost, rt.stream));
       CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
@@ -286,6 +310,16 @@ extern "C" int32_t cubbs_bbs_gpu_expand_xmd_sha256_48_batch_for_test_v2(
     uint32_t abi, const uint8_t *messages, const size_t *offsets, const size_t *lengths, size_t n,
     const uint8_t *dst, size_t dst_len, uint8_t *outputs) {
   return flat_test_call(abi, messages, offsets, lengths, n, dst, dst_len, outputs, 1);
+}
+extern "C" int32_t cubbs_bbs_gpu_expand_xof_shake256_48_batch_for_test_v2(
+    uint32_t abi, const uint8_t *messages, const size_t *offsets, const size_t *lengths, size_t n,
+    const uint8_t *dst, size_t dst_len, uint8_t *outputs) {
+  return flat_test_call(abi, messages, offsets, lengths, n, dst, dst_len, outputs, 3);
+}
+extern "C" int32_t cubbs_bbs_gpu_hash_to_scalar_shake256_batch_for_test_v2(
+    uint32_t abi, const uint8_t *messages, const size_t *offsets, const size_t *lengths, size_t n,
+    const uint8_t *dst, size_t dst_len, uint8_t *scalars) {
+  return flat_test_call(abi, messages, offsets, lengths, n, dst, dst_len, scalars, 4);
 }
 extern "C" int32_t cubbs_bbs_gpu_hash_to_scalar_sha256_batch_for_test_v2(
     uint32_t abi, const uint8_t *messages, const size_t *offsets, const size_t *lengths, size_t n,

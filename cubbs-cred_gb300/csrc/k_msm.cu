@@ -369,7 +369,7 @@ MsmWork make_work(Runtime &rt, cudaStream_t s, uint64_t seed, const std::vector<
   w.sc = rt.arena.alloc<fr>(w.terms);
   w.pts = rt.arena.alloc<g1a>(w.terms);
   w.jobs = rt.arena.alloc<VarJob>(w.terms);
-  if (w.terms) k_msm_gen<<<blocks_for(w.terms, 128), 128, 0, s>>>(seed, w.terms, rt.table, w.sc, w.pts, w.jobs);
+  if (w.terms) k_msm_gen<<<blocks_for(w.terms, 128), 128, 0, s>>>(seed, w.terms, rt.table(), w.sc, w.pts, w.jobs);
   CUBBS_CHECK(cudaGetLastError());
   return w;
 }

@@ -195,7 +195,7 @@ void run_plan(Runtime &rt, Plan &pl, std::vector<uint8_t> &out48, std::vector<ui
         if (hs[r]) hfst[r * pl.fixed_stride] |= 1;
     }
     fixed = rt.arena.alloc<g1>(R);
-    launch_fixed_msm(s, rt.table, fsc, pl.fixed_stride, dnt, (uint32_t)R, fixed);
+    launch_fixed_msm(s, rt.table(), fsc, pl.fixed_stride, dnt, (uint32_t)R, fixed);
   }
   CUBBS_CHECK(cudaStreamSynchronize(s));
   std::vector<VarJob> jobs(nvar);
@@ -694,7 +694,7 @@ extern "C" int32_t cubbs_bbs_gpu_prepare_b_batch_v2(uint32_t abi, CuBbsBbsGpuPre
   uint8_t *dblob = upload(rt, blob.data(), blob.size());
   DomainJob *ddj = upload(rt, dj.data(), n);
   fr *domain = rt.arena.alloc<fr>(n);
-  launch_domain(rt.stream, ddj, (uint32_t)n, dblob, rt.d_gens_c, nullptr, domain);
+  launch_domain(rt.stream, ddj, (uint32_t)n, dblob, rt.d_gens_c(), nullptr, domain);
   std::vector<uint32_t> raw(8 * n);
   CUBBS_CHECK(cudaMemcpyAsync(raw.data(), domain, 32 * n, cudaMemcpyDeviceToHost, rt.stream));
   CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
@@ -1024,12 +1024,12 @@ extern "C" int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi, const uint8
     rt.set_table_window(w, (int)terms);
     if (w == w_lo) {
       // the generators now cover `terms` (the table build grew them) and stay put
-      launch_var_mul(s, rt.d_gens, dcj, sc, (uint32_t)(RC * terms), cv);
+      launch_var_mul(s, rt.d_gens(), dcj, sc, (uint32_t)(RC * terms), cv);
       k_row_sum<<<blocks_for(RC * 32, 128), 128, 0, s>>>(nullptr, cv, dcs, (uint32_t)RC, cref);
       launch_g1_compress(s, cref, (uint32_t)RC, dref48);
       CUBBS_CHECK(cudaMemcpyAsync(href.data(), dref48, href.size(), cudaMemcpyDeviceToHost, s));
     }
-    launch_fixed_msm(s, rt.table, sc, (uint32_t)terms, dnt, (uint32_t)rows, out);  // warm-up and check
+    launch_fixed_msm(s, rt.table(), sc, (uint32_t)terms, dnt, (uint32_t)rows, out);  // warm-up and check
     launch_g1_compress(s, out, (uint32_t)RC, dout48);
     CUBBS_CHECK(cudaMemcpyAsync(hout.data(), dout48, hout.size(), cudaMemcpyDeviceToHost, s));
     CUBBS_CHECK(cudaStreamSynchronize(s));
@@ -1038,7 +1038,7 @@ extern "C" int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi, const uint8
     for (int k = 0; k < steps; k++) {
       CUBBS_CHECK(cudaMemsetAsync(flush, k & 0xff, FLUSH, s));
       CUBBS_CHECK(cudaEventRecord(e0, s));
-      launch_fixed_msm(s, rt.table, sc, (uint32_t)terms, dnt, (uint32_t)rows, out);
+      launch_fixed_msm(s, rt.table(), sc, (uint32_t)terms, dnt, (uint32_t)rows, out);
       CUBBS_CHECK(cudaEventRecord(e1, s));
       CUBBS_CHECK(cudaEventSynchronize(e1));
       float ms = 0;
@@ -1093,7 +1093,7 @@ extern "C" int32_t cubbs_bbs_gpu_table_window_v2(int32_t *w) {
   if (!w) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   try {
     CallScope scope;
-    *w = scope.rt.table.entries ? scope.rt.table.w : 0;
+    *w = scope.rt.table().entries ? scope.rt.table().w : 0;
     return CUBBS_BBS_GPU_SUCCESS;
   } catch (const CudaError &) {
     return CUBBS_BBS_GPU_ERR_INTERNAL;

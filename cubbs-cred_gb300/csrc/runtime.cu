@@ -203,50 +203,51 @@ void SharedState::init_partition() {
   partition_status = 0;
 }
 
-// Build generators up to d_gens[count) on the device: P1 is decoded from its
-// published encoding; Q1, H1, ... come from the seed chain + hash_to_curve.
-void SharedState::grow_generators(int count) {
-  if (count <= gen_count) return;
-  int ncap = gen_capacity ? gen_capacity : 256;
+// Build generators of `suite` up to d_gens[count) on the device: P1 is decoded
+// from its published encoding; Q1, H1, ... come from the seed chain +
+// hash_to_curve with the suite's expander.
+void SharedState::grow_generators(int suite, int count) {
+  SuiteState &g = suites[suite];
+  if (count <= g.gen_count) return;
+  int ncap = g.gen_capacity ? g.gen_capacity : 256;
   while (ncap < count) ncap *= 2;
-  if (ncap != gen_capacity) {
+  if (ncap != g.gen_capacity) {
     g1a *ng = nullptr;
     uint8_t *nc = nullptr;
     CUBBS_CHECK(cudaMalloc(&ng, (size_t)ncap * sizeof(g1a)));
     CUBBS_CHECK(cudaMalloc(&nc, (size_t)ncap * 48 + 48));
-    if (gen_count) {
+    if (g.gen_count) {
       CUBBS_CHECK(cudaDeviceSynchronize());  // no call may still read the old arrays
-      CUBBS_CHECK(cudaMemcpy(ng, d_gens, (size_t)gen_count * sizeof(g1a), cudaMemcpyDeviceToDevice));
-      CUBBS_CHECK(cudaMemcpy(nc, d_gens_c, (size_t)gen_count * 48 + 48, cudaMemcpyDeviceToDevice));
-      cudaFree(d_gens);
-      cudaFree(d_gens_c);
+      CUBBS_CHECK(cudaMemcpy(ng, g.d_gens, (size_t)g.gen_count * sizeof(g1a), cudaMemcpyDeviceToDevice));
+      CUBBS_CHECK(cudaMemcpy(nc, g.d_gens_c, (size_t)g.gen_count * 48 + 48, cudaMemcpyDeviceToDevice));
+      cudaFree(g.d_gens);
+      cudaFree(g.d_gens_c);
     }
-    d_gens = ng;
-    d_gens_c = nc;
-    gen_capacity = ncap;
+    g.d_gens = ng;
+    g.d_gens_c = nc;
+    g.gen_capacity = ncap;
   }
-  static uint8_t *d_seed_state = nullptr;
-  if (!d_seed_state) CUBBS_CHECK(cudaMalloc(&d_seed_state, 64));
-  if (gen_count == 0) {
-    launch_decode_p1(prep, d_gens, d_gens_c);
-    gen_count = 1;
+  if (!g.d_seed_state) CUBBS_CHECK(cudaMalloc(&g.d_seed_state, 64));
+  if (g.gen_count == 0) {
+    launch_decode_p1(prep, g.d_gens, g.d_gens_c, suite);
+    g.gen_count = 1;
   }
-  int first = gen_count;  // 1-based generator number == d_gens index
-  int n = count - gen_count;
+  int first = g.gen_count;  // 1-based generator number == d_gens index
+  int n = count - g.gen_count;
   uint8_t *seeds = nullptr;
   CUBBS_CHECK(cudaMalloc(&seeds, (size_t)n * 48));
-  launch_make_generator_seeds(prep, first, n, d_seed_state, seeds);
-  launch_hash_generators(prep, first, n, seeds, d_gens, d_gens_c);
+  launch_make_generator_seeds(prep, first, n, g.d_seed_state, seeds, suite);
+  launch_hash_generators(prep, first, n, seeds, g.d_gens, g.d_gens_c, suite);
   CUBBS_CHECK(cudaGetLastError());
   CUBBS_CHECK(cudaStreamSynchronize(prep));
   cudaFree(seeds);
-  gen_count = count;
-  h_gens_c.resize((size_t)gen_count * 48);
-  CUBBS_CHECK(cudaMemcpy(h_gens_c.data(), d_gens_c, h_gens_c.size(), cudaMemcpyDeviceToHost));
+  g.gen_count = count;
+  g.h_gens_c.resize((size_t)g.gen_count * 48);
+  CUBBS_CHECK(cudaMemcpy(g.h_gens_c.data(), g.d_gens_c, g.h_gens_c.size(), cudaMemcpyDeviceToHost));
 }
 
-// Fixed-base window table over d_gens[0..gens).  Rebuilt (all generators)
-// when it must grow; built in generator chunks to bound the scratch.
+// Fixed-base window table over d_gens[0..gens) of a suite.  Rebuilt (all
+// generators) when it must grow; built in generator chunks to bound the scratch.
 // Window width of a table over `gens` generators: the explicit setting, else
 // the widest w in 8..16 whose table (gens * ceil(256/w) * 2^(w-1) affine
 // points) fits in TABLE_BUDGET.  A wider window costs fewer mixed additions
@@ -262,16 +263,18 @@ int SharedState::table_window_for(int gens) const {
   return 8;
 }
 
-bool SharedState::table_covers(int gens) const {
-  return table.entries && table.gens >= gens && (table_w == 0 || table.w == table_w);
+bool SharedState::table_covers(int suite, int gens) const {
+  const FixedTable &t = suites[suite].table;
+  return t.entries && t.gens >= gens && (table_w == 0 || t.w == table_w);
 }
 
-void SharedState::grow_table(int gens) {
-  if (table_covers(gens)) return;
+void SharedState::grow_table(int suite, int gens) {
+  if (table_covers(suite, gens)) return;
+  SuiteState &g = suites[suite];
   int want = 1;
   while (want < gens) want *= 2;
   if (want < 64) want = 64;
-  grow_generators(want);
+  grow_generators(suite, want);
   FixedTable t;
   t.w = table_window_for(want);
   t.nwin = 255 / t.w + 1;
@@ -292,17 +295,17 @@ void SharedState::grow_table(int gens) {
   for (int g0 = 0; g0 < want; g0 += chunk) {
     int g1n = std::min(want, g0 + chunk);
     // the kernel indexes scratch by (g - g0) * nwin + k
-    launch_build_table(prep, d_gens, g0, g1n, t, scratch, prod);
+    launch_build_table(prep, g.d_gens, g0, g1n, t, scratch, prod);
     CUBBS_CHECK(cudaGetLastError());
     CUBBS_CHECK(cudaStreamSynchronize(prep));
   }
   cudaFree(scratch);
   cudaFree(prod);
-  if (table.entries) {
+  if (g.table.entries) {
     CUBBS_CHECK(cudaDeviceSynchronize());
-    cudaFree(table.entries);
+    cudaFree(g.table.entries);
   }
-  table = t;
+  g.table = t;
 }
 
 // Decode, check and line-precompute public keys not seen before.
@@ -349,8 +352,7 @@ void SharedState::add_pks(const std::vector<std::string> &keys) {
 }
 
 Runtime::Runtime(SharedState &s)
-    : sh(s), device(s.device), sm_count(s.sm_count), gen_count(s.gen_count), d_gens(s.d_gens),
-      d_gens_c(s.d_gens_c), table(s.table), table_w(s.table_w), d_lines(s.d_lines) {
+    : sh(s), device(s.device), sm_count(s.sm_count), table_w(s.table_w), d_lines(s.d_lines) {
   CUBBS_CHECK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
   CUBBS_CHECK(cudaStreamCreateWithFlags(&stream2, cudaStreamNonBlocking));
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_fork, cudaEventDisableTiming));
@@ -403,21 +405,21 @@ bool Runtime::use_partition() {
 // Growth from inside a call: drop the shared hold, grow under the exclusive
 // lock (the grow functions re-check), take the shared hold again.
 void Runtime::ensure_generators(int count) {
-  if (count <= sh.gen_count) return;
+  if (count <= ss().gen_count) return;
   lock->unlock();
   {
     std::unique_lock<std::shared_mutex> ex(sh.mu);
-    sh.grow_generators(count);
+    sh.grow_generators(suite, count);
   }
   lock->lock();
 }
 
 void Runtime::ensure_table(int gens) {
-  if (sh.table_covers(gens)) return;
+  if (sh.table_covers(suite, gens)) return;
   lock->unlock();
   {
     std::unique_lock<std::shared_mutex> ex(sh.mu);
-    sh.grow_table(gens);
+    sh.grow_table(suite, gens);
   }
   lock->lock();
 }
@@ -427,7 +429,7 @@ void Runtime::set_table_window(int w, int gens) {
   {
     std::unique_lock<std::shared_mutex> ex(sh.mu);
     sh.table_w = w;
-    sh.grow_table(std::max(gens, sh.table.gens));
+    sh.grow_table(suite, std::max(gens, ss().table.gens));
   }
   lock->lock();
 }
@@ -469,7 +471,11 @@ void Runtime::resolve_pks(const std::vector<const uint8_t *> &pk_ptrs, std::vect
 // Builds the domain-hash prefixes of (key slot << 32 | L, key bytes) pairs not
 // resident yet (the generators already cover each L).  Growing the array
 // waits for the device first: no call may still read the old one.
-void SharedState::add_domain_prefixes(const std::vector<std::pair<uint64_t, const uint8_t *>> &fresh) {
+void SharedState::add_domain_prefixes(int suite, const std::vector<std::pair<uint64_t, const uint8_t *>> &fresh) {
+  SuiteState &g = suites[suite];
+  auto &dom_prefix = g.dom_prefix;
+  auto &d_dom_prefix = g.d_dom_prefix;
+  auto &dom_prefix_cap = g.dom_prefix_cap;
   std::vector<DomainPrefixJob> jobs;
   for (const auto &f : fresh) {
     if (dom_prefix.count(f.first)) continue;
@@ -500,7 +506,7 @@ void SharedState::add_domain_prefixes(const std::vector<std::pair<uint64_t, cons
   DomainPrefixJob *dj = nullptr;
   CUBBS_CHECK(cudaMalloc(&dj, jobs.size() * sizeof(DomainPrefixJob)));
   CUBBS_CHECK(cudaMemcpyAsync(dj, jobs.data(), jobs.size() * sizeof(DomainPrefixJob), cudaMemcpyHostToDevice, prep));
-  launch_domain_prefix(prep, dj, (uint32_t)jobs.size(), d_gens_c, d_dom_prefix);
+  launch_domain_prefix(prep, dj, (uint32_t)jobs.size(), g.d_gens_c, d_dom_prefix);
   CUBBS_CHECK(cudaGetLastError());
   CUBBS_CHECK(cudaStreamSynchronize(prep));
   cudaFree(dj);
@@ -545,6 +551,7 @@ void release_workspace(Runtime &rt) {
 
 CallScope::CallScope() : rt(acquire_workspace()), lock(rt.sh.mu) {
   rt.lock = &lock;
+  rt.suite = SUITE_SHA256;
   rt.arena.reset();
   rt.staging.reset();
   rt.pack.reset();

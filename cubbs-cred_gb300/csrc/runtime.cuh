@@ -17,6 +17,7 @@
 #include "../../include/cubbs_bbs_gpu_abi.h"
 #include "../../include/cubbs_bbs_gpu_test.h"  // the definitions are checked against these declarations
 #include "pairing.cuh"
+#include "suite.cuh"
 
 namespace cubbs {
 
@@ -97,11 +98,30 @@ struct MsmPlan {
   uint32_t nparts = 0;
   void build(const std::vector<uint32_t> &K, const MsmTuning &tune);
 };
+// Prepared state of one ciphersuite (the generators and everything built on
+// them differ between BLS12-381-SHA-256 and BLS12-381-SHAKE-256).
+struct SuiteState {
+  // generators: d_gens[0] = P1, d_gens[1] = Q1, d_gens[1 + i] = H_i
+  int gen_count = 0;            // entries of d_gens built (P1 included)
+  int gen_capacity = 0;
+  g1a *d_gens = nullptr;
+  uint8_t *d_gens_c = nullptr;  // compressed, same indexing as d_gens
+  std::vector<uint8_t> h_gens_c;  // host copy of d_gens_c[0..gen_count)
+  uint8_t *d_seed_state = nullptr;  // generator seed chain after gen_count - 1 steps
+  FixedTable table;
+  // Resident domain-hash prefixes (DomainJob::prefix), one per (key slot, L):
+  // key slot << 32 | L -> index into d_dom_prefix (DOMAIN_PREFIX_BYTES each).
+  // SHA-256 suite only.
+  std::unordered_map<uint64_t, uint32_t> dom_prefix;
+  uint8_t *d_dom_prefix = nullptr;
+  uint32_t dom_prefix_cap = 0;
+};
+
 // Process-wide prepared state shared by every call: generators, the
-// fixed-base window table and the Miller lines of -P2, P2 and every public
-// key seen.  Calls hold `mu` shared while their kernels may read the state;
-// growing it (more generators, a wider table, new keys) takes `mu` exclusive,
-// so nothing is reallocated under a running call.
+// fixed-base window table (per ciphersuite) and the Miller lines of -P2, P2
+// and every public key seen.  Calls hold `mu` shared while their kernels may
+// read the state; growing it (more generators, a wider table, new keys) takes
+// `mu` exclusive, so nothing is reallocated under a running call.
 struct SharedState {
   std::shared_mutex mu;
   std::mutex init_mu;
@@ -109,13 +129,7 @@ struct SharedState {
   int device = 0;
   int sm_count = 0;
   cudaStream_t prep = nullptr;  // stream that builds prepared state
-  // generators: d_gens[0] = P1, d_gens[1] = Q1, d_gens[1 + i] = H_i
-  int gen_count = 0;            // entries of d_gens built (P1 included)
-  int gen_capacity = 0;
-  g1a *d_gens = nullptr;
-  uint8_t *d_gens_c = nullptr;  // compressed, same indexing as d_gens
-  std::vector<uint8_t> h_gens_c;  // host copy of d_gens_c[0..gen_count)
-  FixedTable table;
+  SuiteState suites[SUITE_COUNT];
   int table_w = 0;              // fixed-base window width; 0 = widest that fits the table budget
   // Miller lines: slot 0 = -P2, slot 1 = P2, slots >= 2 = public keys
   line2 *d_lines = nullptr;
@@ -144,17 +158,12 @@ struct SharedState {
   void ensure_partition();
   void init_partition();
   // the following run with mu held exclusively
-  void grow_generators(int count);
-  void grow_table(int gens);
+  void grow_generators(int suite, int count);
+  void grow_table(int suite, int gens);
   int table_window_for(int gens) const;
-  bool table_covers(int gens) const;
+  bool table_covers(int suite, int gens) const;
   void add_pks(const std::vector<std::string> &fresh);
-  // Resident domain-hash prefixes (DomainJob::prefix), one per (key slot, L):
-  // key slot << 32 | L -> index into d_dom_prefix (DOMAIN_PREFIX_BYTES each).
-  std::unordered_map<uint64_t, uint32_t> dom_prefix;
-  uint8_t *d_dom_prefix = nullptr;
-  uint32_t dom_prefix_cap = 0;
-  void add_domain_prefixes(const std::vector<std::pair<uint64_t, const uint8_t *>> &fresh);  // mu held exclusively
+  void add_domain_prefixes(int suite, const std::vector<std::pair<uint64_t, const uint8_t *>> &fresh);
 };
 
 // One call's workspace: arena, pinned staging, two streams and the events
@@ -165,12 +174,13 @@ struct Runtime {
   SharedState &sh;
   int &device;
   int &sm_count;
-  int &gen_count;
-  g1a *&d_gens;
-  uint8_t *&d_gens_c;
-  FixedTable &table;
   int &table_w;
   line2 *&d_lines;
+  int suite = SUITE_SHA256;  // ciphersuite of the running call (set by the entry point)
+  SuiteState &ss() const { return sh.suites[suite]; }
+  const FixedTable &table() const { return ss().table; }
+  g1a *d_gens() const { return ss().d_gens; }
+  uint8_t *d_gens_c() const { return ss().d_gens_c; }
   cudaStream_t stream = nullptr, stream2 = nullptr, stream3 = nullptr, stream4 = nullptr;
   // stream -> stream2 (ev_fork), stream2 -> stream3, stream4 (ev_mid), back to stream
   // (ev_side, ev_join, ev_sub)
@@ -198,7 +208,7 @@ struct Runtime {
   // device for new keys).  pk_ptrs[i] -> slot index; status per key.
   void resolve_pks(const std::vector<const uint8_t *> &pk_ptrs, std::vector<int> &slots,
                    std::vector<int> &status);
-  const std::vector<uint8_t> &host_gens_c() const { return sh.h_gens_c; }
+  const std::vector<uint8_t> &host_gens_c() const { return ss().h_gens_c; }
 };
 
 // Takes a free workspace from the pool (waiting while all are busy), makes the
@@ -217,11 +227,11 @@ inline unsigned blocks_for(size_t n, unsigned tpb) { return (unsigned)((n + tpb 
 
 // Launchers implemented in the kernel translation units.
 void launch_h2s_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens,
-                     uint32_t n, const uint8_t *dst, uint32_t dlen, fr *out_raw);
+                     uint32_t n, const uint8_t *dst, uint32_t dlen, fr *out_raw, int suite = SUITE_SHA256);
 void launch_sha256_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens,
                         uint32_t n, uint8_t *digests);
-void launch_xmd48_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens,
-                       uint32_t n, const uint8_t *dst, uint32_t dlen, uint8_t *out);
+void launch_expand48_flat(cudaStream_t s, const uint8_t *msgs, const uint32_t *offs, const uint32_t *lens,
+                          uint32_t n, const uint8_t *dst, uint32_t dlen, uint8_t *out, int suite);
 // domain = H2S(PK || I2OSP(L,8) || Q1..H_L || api_id || I2OSP(hlen,8) || header)
 // `prefix` indexes the resident SHA-256 state after Z_pad || PK || I2OSP(L,8) ||
 // Q1..H_L of the item's (key, L) (DOMAIN_NO_PREFIX: hash the whole input).
@@ -236,14 +246,14 @@ struct DomainPrefixJob {
   uint32_t L, index;  // index: the context's place in the resident array
 };
 void launch_domain(cudaStream_t s, const DomainJob *jobs, uint32_t n, const uint8_t *blob,
-                   const uint8_t *gens_c, const uint8_t *prefixes, fr *out_raw);
+                   const uint8_t *gens_c, const uint8_t *prefixes, fr *out_raw, int suite = SUITE_SHA256);
 void launch_domain_prefix(cudaStream_t s, const DomainPrefixJob *jobs, uint32_t n, const uint8_t *gens_c,
                           uint8_t *prefixes);
 void launch_make_generator_seeds(cudaStream_t s, int first, int count, uint8_t *seeds_state,
-                                 uint8_t *seeds_out);
+                                 uint8_t *seeds_out, int suite);
 void launch_hash_generators(cudaStream_t s, int first, int count, const uint8_t *seeds, g1a *gens,
-                            uint8_t *gens_c);
-void launch_decode_p1(cudaStream_t s, g1a *gens, uint8_t *gens_c);
+                            uint8_t *gens_c, int suite);
+void launch_decode_p1(cudaStream_t s, g1a *gens, uint8_t *gens_c, int suite);
 void launch_build_table(cudaStream_t s, const g1a *gens, int g0, int g1n, FixedTable t, g1 *scratch_xyzz,
                         fp *scratch_prod);
 // decode N compressed G1 points: status DEC_*; affine out

@@ -146,3 +146,12 @@ DEV fr h2s_finish(sha_ctx &c, const uint8_t *dst, uint32_t dlen) {
   xmd_finish(c, dst, dlen, 48, okm);
   return fr_raw_from_okm(okm);
 }
+
+// The suite-generic names used by the kernels (the SHAKE-256 forms are in keccak.cuh).
+DEV void msg_begin(sha_ctx &c) { xmd_begin(c); }
+DEV void msg_byte(sha_ctx &c, uint8_t b) { sha_byte(c, b); }
+DEV void msg_bytes(sha_ctx &c, const uint8_t *p, uint32_t n) { sha_bytes(c, p, n); }
+DEV void msg_u64be(sha_ctx &c, uint64_t x, int nbytes) { sha_u64be(c, x, nbytes); }
+DEV void msg_finish(sha_ctx &c, const uint8_t *dst, uint32_t dlen, uint32_t n, uint8_t *out) {
+  xmd_finish(c, dst, dlen, n, out);
+}

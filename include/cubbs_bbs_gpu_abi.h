@@ -278,6 +278,34 @@ int32_t cubbs_bbs_gpu_proof_gen_seeded_batch_v2(uint32_t abi_version,
                                                 const uint8_t (*seeds)[32],
                                                 CuBbsBbsGpuResult *results);
 
+/* ABI-compatible addition: the four operations under a chosen ciphersuite.
+ * The reference protocol crate defines two (crates/cubbs-bbs-protocol/src/
+ * bbsplus/ciphersuites.rs:49-79): Bls12381Sha256 (API_ID
+ * "BBS_BLS12381G1_XMD:SHA-256_SSWU_RO_H2G_HM2S_", expand_message_xmd over
+ * SHA-256) and Bls12381Shake256 (API_ID
+ * "BBS_BLS12381G1_XOF:SHAKE-256_SSWU_RO_H2G_HM2S_", expand_message_xof over
+ * SHAKE-256); its C ABI exposes only the first, which the *_batch_v2 entries
+ * above keep.  These take the suite as a second argument and the same item
+ * structs; an unknown suite is a call-level CUBBS_BBS_GPU_ERR_INVALID_INPUT.
+ * Each suite has its own generators (and P1), so keys, signatures and proofs
+ * of one suite do not verify under the other.  The seeded ProofGen of the
+ * SHAKE-256 suite draws up to 1365 scalars in one expansion (65535 bytes)
+ * and chunks past that as above. */
+#define CUBBS_BBS_CIPHERSUITE_SHA256 0u
+#define CUBBS_BBS_CIPHERSUITE_SHAKE256 1u
+int32_t cubbs_bbs_gpu_sign_batch_cs_v2(uint32_t abi_version, uint32_t suite, CuBbsBbsGpuSignItem *items,
+                                       size_t item_count, CuBbsBbsGpuResult *results);
+int32_t cubbs_bbs_gpu_verify_batch_cs_v2(uint32_t abi_version, uint32_t suite, const CuBbsBbsGpuVerifyItem *items,
+                                         size_t item_count, CuBbsBbsGpuResult *results);
+int32_t cubbs_bbs_gpu_proof_gen_batch_cs_v2(uint32_t abi_version, uint32_t suite, CuBbsBbsGpuProofGenItem *items,
+                                            size_t item_count, CuBbsBbsGpuResult *results);
+int32_t cubbs_bbs_gpu_proof_gen_seeded_batch_cs_v2(uint32_t abi_version, uint32_t suite,
+                                                   CuBbsBbsGpuProofGenItem *items, size_t item_count,
+                                                   const uint8_t (*seeds)[32], CuBbsBbsGpuResult *results);
+int32_t cubbs_bbs_gpu_proof_verify_batch_cs_v2(uint32_t abi_version, uint32_t suite,
+                                               const CuBbsBbsGpuProofVerifyItem *items, size_t item_count,
+                                               CuBbsBbsGpuResult *results);
+
 /* reference :249-251 */
 int32_t cubbs_bbs_gpu_messages_to_scalar_batch_v2(uint32_t abi_version,
                                                   CuBbsBbsGpuMessagesToScalarItem *items,

@@ -86,6 +86,16 @@ int32_t cubbs_bbs_gpu_pairs_h2s_for_test_v2(uint32_t abi_version, const uint8_t 
                                             uint32_t idx_off, uint32_t R, const uint8_t *mbe, uint8_t *out32,
                                             uint32_t *echo);
 int32_t cubbs_bbs_gpu_last_debug_record_for_test_v2(uint8_t *out256);
+/* expand_message_xof over SHAKE-256 (48 bytes per message) and hash_to_scalar
+ * over it (the SHAKE-256 suite's expander), one message per thread. */
+int32_t cubbs_bbs_gpu_expand_xof_shake256_48_batch_for_test_v2(uint32_t abi_version, const uint8_t *messages,
+                                                               const size_t *offsets, const size_t *lengths,
+                                                               size_t count, const uint8_t *dst, size_t dst_len,
+                                                               uint8_t *outputs);
+int32_t cubbs_bbs_gpu_hash_to_scalar_shake256_batch_for_test_v2(uint32_t abi_version, const uint8_t *messages,
+                                                                const size_t *offsets, const size_t *lengths,
+                                                                size_t count, const uint8_t *dst, size_t dst_len,
+                                                                uint8_t *scalars);
 /* Host phase times (ms6: workspace, plan, public keys, upload, device pipeline, results) of one
  * ProofVerify call. */
 int32_t cubbs_bbs_gpu_proof_verify_phases_for_test_v2(const CuBbsBbsGpuProofVerifyItem *items, size_t n,
