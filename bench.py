@@ -285,32 +285,80 @@ def serving_pv_section(pkg, rank, pv_reqs):
     and for each mode the highest rate whose p99 stays within P99_BOUND_MS."""
     import random
     P99_BOUND_MS = 50.0
+    REPEATS = 3
     rng = random.Random(2000 + rank)
     pool = [(pkg.OP_PROOF_VERIFY, r, None) for r in pv_reqs]
     res, _, _ = pkg.serve_replay(pool, [(i, 0) for i in range(len(pool))], mode=pkg.SERVE_QUEUE)  # warm
     assert all(c == 0 and v == 1 for c, v, _ in res)
     rows, best = [], {"served": None, "plain": None}
-    for rate in (25000, 50000, 100000, 150000, 200000, 250000, 300000):
+    for rate in (25000, 50000, 100000, 150000, 175000, 200000, 225000, 250000, 275000, 300000):
         count = max(4096, min(60000, int(rate * 0.2)))
-        t, schedule = 0.0, []
-        for _ in range(count):
-            t += rng.expovariate(rate)
-            schedule.append((rng.randrange(len(pool)), int(t * 1e9)))
-        row = {"rate_req_s": rate, "requests": count}
-        for name, mode in (("served", pkg.SERVE_QUEUE), ("plain", pkg.SERVE_PLAIN)):
-            res, lat, wall = pkg.serve_replay(pool, schedule, mode=mode, plain_batch=1024, plain_timeout_us=2000)
-            assert all(c == 0 and v == 1 for c, v, _ in res)
-            lat_ms = sorted(x / 1e6 for x in lat)
-            p99 = lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))]
-            row[name] = {"p50_ms": round(lat_ms[len(lat_ms) // 2], 3), "p99_ms": round(p99, 3),
-                         "ops_per_s": round(count / wall, 1)}
-            if p99 <= P99_BOUND_MS and (best[name] is None or row[name]["ops_per_s"] > best[name]["ops_per_s"]):
+        row = {"rate_req_s": rate, "requests": count, "repeats": REPEATS}
+        runs = {"served": [], "plain": []}
+        for rep in range(REPEATS):
+            t, schedule = 0.0, []
+            for _ in range(count):
+                t += rng.expovariate(rate)
+                schedule.append((rng.randrange(len(pool)), int(t * 1e9)))
+            for name, mode in (("served", pkg.SERVE_QUEUE), ("plain", pkg.SERVE_PLAIN)):
+                res, lat, wall = pkg.serve_replay(pool, schedule, mode=mode, plain_batch=1024,
+                                                  plain_timeout_us=2000)
+                assert all(c == 0 and v == 1 for c, v, _ in res)
+                lat_ms = sorted(x / 1e6 for x in lat)
+                runs[name].append((lat_ms[len(lat_ms) // 2], lat_ms[min(len(lat_ms) - 1, int(0.99 * len(lat_ms)))],
+                                   count / wall))
+        for name in ("served", "plain"):
+            p50s, p99s, opss = zip(*runs[name])
+            med = lambda v: statistics.median(v)
+            row[name] = {"p50_ms": round(med(p50s), 3), "p99_ms": round(med(p99s), 3),
+                         "ops_per_s": round(med(opss), 1),
+                         "p99_ms_min_max": [round(min(p99s), 3), round(max(p99s), 3)],
+                         "ops_per_s_min_max": [round(min(opss), 1), round(max(opss), 1)]}
+            if row[name]["p99_ms"] <= P99_BOUND_MS and (best[name] is None or
+                                                        row[name]["ops_per_s"] > best[name]["ops_per_s"]):
                 best[name] = {"rate_req_s": rate, **row[name]}
         rows.append(row)
+    # matched p99: the served rate with the most ops/s whose median p99 is no
+    # larger than the plain path's at its best rate within the bound
+    matched = None
+    if best["plain"] is not None:
+        cap = best["plain"]["p99_ms"]
+        cands = [r for r in rows if r["served"]["p99_ms"] <= cap]
+        if cands:
+            top = max(cands, key=lambda r: r["served"]["ops_per_s"])
+            matched = {"plain_p99_ms": cap, "plain_ops_per_s": best["plain"]["ops_per_s"],
+                       "served_rate_req_s": top["rate_req_s"], "served_p99_ms": top["served"]["p99_ms"],
+                       "served_ops_per_s": top["served"]["ops_per_s"],
+                       "served_over_plain": round(top["served"]["ops_per_s"] / best["plain"]["ops_per_s"], 3)}
     return {"workload": "ProofVerify L=100 x 64 B, 50 disclosed, Poisson arrivals of single requests; "
                         "served = continuous batching (4 slots, up to 1024 per batch), plain = batches of "
-                        "1024 or 2 ms, one at a time (the headline batched launch)",
-            "p99_bound_ms": P99_BOUND_MS, "best_within_p99_bound": best, "rates": rows}
+                        "1024 or 2 ms, one at a time (the headline batched launch); medians of %d runs per "
+                        "rate" % REPEATS,
+            "p99_bound_ms": P99_BOUND_MS, "best_within_p99_bound": best, "matched_p99": matched, "rates": rows}
+
+
+def multi_key_pv_section(pkg, rank, L, R, args):
+    """The headline ProofVerify batch spread over 64 keys (16 proofs per key, so
+    every key is one aggregated group of 16): device-resident ops/s beside the
+    single-key headline."""
+    keys = json.loads((ROOT / "tests" / "golden" / "keypairs256.json").read_text())[:64]
+    keys = [(bytes.fromhex(k["sk"]), bytes.fromhex(k["pk"])) for k in keys]
+    n = args.batch
+    reqs = make_requests(n, L, R, 64, b"cubbs-bench-mk-%d" % rank)
+    sigs = pkg.sign_batch([(keys[i % 64][0], keys[i % 64][1], r["hdr"], r["msgs"]) for i, r in enumerate(reqs)])
+    assert all(c == 0 for c, _ in sigs)
+    proofs = pkg.proof_gen_batch([(keys[i % 64][1], s, r["hdr"], r["ph"], r["msgs"], r["di"])
+                                  for i, (r, (_, s)) in enumerate(zip(reqs, sigs))], seeds=[r["seed"] for r in reqs])
+    assert all(c == 0 for c, _ in proofs)
+    pv = [(keys[i % 64][1], p, r["hdr"], r["ph"], [r["msgs"][j] for j in r["di"]], r["di"], L)
+          for i, (r, (_, p)) in enumerate(zip(reqs, proofs))]
+    ms, _, res, stages = pkg.bench_device_steps(pkg.OP_PROOF_VERIFY, pv, args.warmup, args.steps)
+    assert all(c == 0 and v == 1 for c, v in res)
+    step = statistics.mean(ms)
+    return {"workload": "the headline batch (%d proofs, L=%d, %d disclosed) over 64 keys, 16 proofs per key" %
+                        (n, L, R),
+            "ops_per_s": round(n / (step / 1e3), 2), "ms_per_step": round(step, 3),
+            "stages_ms": {k: round(v, 3) for k, v in stages}}
 
 
 def reference_arm(args):
@@ -452,6 +500,7 @@ def main():
     # ---------------- C5: serving queue vs plain batches under Poisson arrivals
     c5 = serving_section(pkg, rank) if not args.quick else None
     c5_pv = serving_pv_section(pkg, rank, pv_reqs) if not args.quick else None
+    c3_mk = multi_key_pv_section(pkg, rank, L, R, args) if not args.quick else None
 
     pv_step = statistics.mean(pv_ms)
     e2e_step = statistics.mean(e2e) * 1e3
@@ -526,6 +575,7 @@ def main():
             "uneven_msm_c4": c4,
             "serving_c5": c5,
             "serving_pv_L100": c5_pv,
+            "proof_verify_L100_64_keys": c3_mk,
         }
         print(json.dumps(line), flush=True)
     if dist is not None:

@@ -367,6 +367,125 @@ DEV bool g1_in_subgroup_pair(const LanePair &lp, g1a a) {
   fp ny = fp_neg(a.y);
   return fp_eq(t.X, fp_mul(bx, t.ZZ)) && fp_eq(t.Y, fp_mul(ny, t.ZZZ));
 }
+// ---- point arithmetic on a lane quad
+// Lanes 4k .. 4k+3 hold the same operands and split each formula's
+// independent products four ways: a doubling takes 3 product latencies
+// (instead of 5 on a pair, 9 on one lane), a mixed or an XYZZ addition 4
+// (5 / 7 on a pair).  In each round lane k of the quad computes product k and
+// every lane receives all of them by quad-masked shuffles; the four lanes take
+// the same branches, quads may diverge from one another.  Results equal the
+// one-lane formulas exactly (same products, same order of the sums).
+struct LaneQuad {
+  unsigned mask;  // the four lanes of the quad
+  int role;       // 0..3
+  int base;       // lane of role 0
+  DEV static LaneQuad here() {
+    const int lane = threadIdx.x & 31;
+    LaneQuad q;
+    q.base = lane & ~3;
+    q.mask = 0xFu << q.base;
+    q.role = lane & 3;
+    return q;
+  }
+};
+DEV fp quad_from(const LaneQuad &q, const fp &a, int src) {
+  fp r;
+#pragma unroll
+  for (int i = 0; i < 12; i++) r.w[i] = __shfl_sync(q.mask, a.w[i], q.base + src);
+  return r;
+}
+DEV fp quad_pick(const LaneQuad &q, const fp &a0, const fp &a1, const fp &a2, const fp &a3) {
+  fp r;
+#pragma unroll
+  for (int i = 0; i < 12; i++) r.w[i] = q.role == 0 ? a0.w[i] : q.role == 1 ? a1.w[i] : q.role == 2 ? a2.w[i] : a3.w[i];
+  return r;
+}
+// r_k = a_k b_k for k < N (2..4), product k computed by role k (a role >= N
+// repeats product 0); every lane gets every r_k.
+template <int N>
+DEV void quad_mul(const LaneQuad &q, const fp &a0, const fp &b0, const fp &a1, const fp &b1, const fp &a2,
+                  const fp &b2, const fp &a3, const fp &b3, fp &r0, fp &r1, fp &r2, fp &r3) {
+  const fp mine = fp_mul(quad_pick(q, a0, a1, N > 2 ? a2 : a0, N > 3 ? a3 : a0),
+                         quad_pick(q, b0, b1, N > 2 ? b2 : b0, N > 3 ? b3 : b0));
+  r0 = quad_from(q, mine, 0);
+  r1 = quad_from(q, mine, 1);
+  if (N > 2) r2 = quad_from(q, mine, 2);
+  if (N > 3) r3 = quad_from(q, mine, 3);
+}
+DEV g1 g1_dbl_quad(const LaneQuad &q, const g1 &p) {
+  if (g1_is_inf(p)) return p;
+  const fp U = fp_dbl(p.Y);
+  fp V, X2, W, S, ZZ3, M2, T, WY, ZZZ3, unused;
+  quad_mul<2>(q, U, U, p.X, p.X, U, U, U, U, V, X2, unused, unused);
+  const fp M = fp_add(fp_dbl(X2), X2);
+  quad_mul<4>(q, U, V, p.X, V, V, p.ZZ, M, M, W, S, ZZ3, M2);
+  g1 r;
+  r.X = fp_sub(fp_sub(M2, S), S);
+  quad_mul<3>(q, M, fp_sub(S, r.X), W, p.Y, W, p.ZZZ, M, M, T, WY, ZZZ3, unused);
+  r.Y = fp_sub(T, WY);
+  r.ZZ = ZZ3;
+  r.ZZZ = ZZZ3;
+  return r;
+}
+// p + q with q affine
+DEV g1 g1_add_aff_quad(const LaneQuad &lq, const g1 &p, const g1a &q) {
+  if (g1_is_inf(p)) return g1_from_aff(q);
+  fp U2, S2, PP, RR, PPP, Q, ZZ3, T, YP, ZZZ3, unused;
+  quad_mul<2>(lq, q.x, p.ZZ, q.y, p.ZZZ, q.x, q.x, q.x, q.x, U2, S2, unused, unused);
+  const fp P = fp_sub(U2, p.X), R = fp_sub(S2, p.Y);
+  if (fp_is_zero(P)) {
+    if (fp_is_zero(R)) return g1_dbl_quad(lq, g1_from_aff(q));
+    return g1_inf();
+  }
+  quad_mul<2>(lq, P, P, R, R, P, P, P, P, PP, RR, unused, unused);
+  quad_mul<3>(lq, P, PP, p.X, PP, p.ZZ, PP, P, P, PPP, Q, ZZ3, unused);
+  g1 r;
+  r.X = fp_sub(fp_sub(RR, PPP), fp_dbl(Q));
+  quad_mul<3>(lq, R, fp_sub(Q, r.X), p.Y, PPP, p.ZZZ, PPP, P, P, T, YP, ZZZ3, unused);
+  r.Y = fp_sub(T, YP);
+  r.ZZ = ZZ3;
+  r.ZZZ = ZZZ3;
+  return r;
+}
+DEV g1 g1_add_quad(const LaneQuad &lq, const g1 &p, const g1 &q) {
+  if (g1_is_inf(p)) return q;
+  if (g1_is_inf(q)) return p;
+  fp U1, U2, S1, S2, PP, RR, Z1, Z2, PPP, Q, ZZ3, T, SP, ZZZ3, unused;
+  quad_mul<4>(lq, p.X, q.ZZ, q.X, p.ZZ, p.Y, q.ZZZ, q.Y, p.ZZZ, U1, U2, S1, S2);
+  const fp P = fp_sub(U2, U1), R = fp_sub(S2, S1);
+  if (fp_is_zero(P)) {
+    if (fp_is_zero(R)) return g1_dbl_quad(lq, p);
+    return g1_inf();
+  }
+  quad_mul<4>(lq, P, P, R, R, p.ZZ, q.ZZ, p.ZZZ, q.ZZZ, PP, RR, Z1, Z2);
+  quad_mul<3>(lq, P, PP, U1, PP, Z1, PP, P, P, PPP, Q, ZZ3, unused);
+  g1 r;
+  r.X = fp_sub(fp_sub(RR, PPP), fp_dbl(Q));
+  quad_mul<3>(lq, R, fp_sub(Q, r.X), S1, PPP, Z2, PPP, P, P, T, SP, ZZZ3, unused);
+  r.Y = fp_sub(T, SP);
+  r.ZZ = ZZ3;
+  r.ZZZ = ZZZ3;
+  return r;
+}
+// [|z|]P and the G1 membership test on a lane quad.
+DEV g1 g1_mul_zabs_quad(const LaneQuad &q, const g1 &p) {
+  g1 acc = p;
+  #pragma unroll 1
+  for (int i = 62; i >= 0; i--) {
+    acc = g1_dbl_quad(q, acc);
+    if (zabs_bit(i)) acc = g1_add_quad(q, acc, p);
+  }
+  return acc;
+}
+DEV bool g1_in_subgroup_quad(const LaneQuad &q, g1a a) {
+  g1 t = g1_mul_zabs_quad(q, g1_mul_zabs_quad(q, g1_from_aff(a)));
+  if (g1_is_inf(t)) return false;
+  const fp beta = C_GLV_BETA;
+  fp bx = fp_mul(a.x, beta);
+  fp ny = fp_neg(a.y);
+  return fp_eq(t.X, fp_mul(bx, t.ZZ)) && fp_eq(t.Y, fp_mul(ny, t.ZZZ));
+}
+
 // Warp-wide sum of one XYZZ point per lane (the result is valid on lane 0).
 DEV g1 shfl_down_g1(const g1 &p, int delta) {
   g1 r;
@@ -517,6 +636,85 @@ DEV g1 g1_mul_glv_pair(const LanePair &lp, g1a p, fr k) {
     }
   }
   return acc;
+}
+
+// g1_mul_glv on a lane quad (all four lanes return k * P).
+DEV g1 g1_mul_glv_quad(const LaneQuad &lq, g1a p, fr k) {
+  uint32_t s[4], q[4];
+  glv_split(k, s, q);
+  int8_t ds[33], dq[33];
+  recode_w4(s, ds);
+  recode_w4(q, dq);
+  g1 tab[8];
+  tab[0] = g1_from_aff(p);
+  tab[1] = g1_dbl_quad(lq, g1_from_aff(p));
+  #pragma unroll 1
+  for (int i = 2; i < 8; i++) tab[i] = g1_add_aff_quad(lq, tab[i - 1], p);
+  g1 acc = g1_inf();
+  #pragma unroll 1
+  for (int i = 32; i >= 0; i--) {
+    if (i != 32) {
+      acc = g1_dbl_quad(lq, acc); acc = g1_dbl_quad(lq, acc); acc = g1_dbl_quad(lq, acc); acc = g1_dbl_quad(lq, acc);
+    }
+    int a = ds[i];
+    if (a) {
+      g1 t = tab[(a > 0 ? a : -a) - 1];
+      acc = g1_add_quad(lq, acc, a > 0 ? t : g1_neg(t));
+    }
+    int b = dq[i];
+    if (b) {
+      g1 t = g1_endo(tab[(b > 0 ? b : -b) - 1]);
+      acc = g1_add_quad(lq, acc, b > 0 ? t : g1_neg(t));
+    }
+  }
+  return acc;
+}
+
+// k * P on eight lanes: the quad of lanes 8j .. 8j+3 computes s P and the quad
+// of lanes 8j+4 .. 8j+7 computes q [lambda]P = q phi(P) (k = q lambda + s),
+// each with its own doubling chain (half the additions of the shared chain
+// each); the first quad adds the second quad's sum.  Lanes of the first quad
+// return k * P.  All eight lanes must call it.
+DEV g1 g1_mul_glv_octet(const LaneQuad &lq, g1a p, fr k) {
+  uint32_t s[4], q[4];
+  glv_split(k, s, q);
+  const int half = (threadIdx.x >> 2) & 1;
+  int8_t d[33];
+  recode_w4(half ? q : s, d);
+  if (half) {
+    const fp beta = C_GLV_BETA;
+    p.x = fp_mul(p.x, beta);  // phi(P) = (beta x, -y) = [lambda]P
+    p.y = fp_neg(p.y);
+  }
+  g1 tab[8];
+  tab[0] = g1_from_aff(p);
+  tab[1] = g1_dbl_quad(lq, g1_from_aff(p));
+  #pragma unroll 1
+  for (int i = 2; i < 8; i++) tab[i] = g1_add_aff_quad(lq, tab[i - 1], p);
+  g1 acc = g1_inf();
+  #pragma unroll 1
+  for (int i = 32; i >= 0; i--) {
+    if (i != 32) {
+      acc = g1_dbl_quad(lq, acc); acc = g1_dbl_quad(lq, acc); acc = g1_dbl_quad(lq, acc); acc = g1_dbl_quad(lq, acc);
+    }
+    const int a = d[i];
+    if (a) {
+      g1 t = tab[(a > 0 ? a : -a) - 1];
+      acc = g1_add_quad(lq, acc, a > 0 ? t : g1_neg(t));
+    }
+  }
+  // both quads meet here: the first takes the second's sum
+  const unsigned oct = 0xFFu << (threadIdx.x & 24);
+  g1 other;
+#pragma unroll
+  for (int i = 0; i < 12; i++) {
+    other.X.w[i] = __shfl_xor_sync(oct, acc.X.w[i], 4);
+    other.Y.w[i] = __shfl_xor_sync(oct, acc.Y.w[i], 4);
+    other.ZZ.w[i] = __shfl_xor_sync(oct, acc.ZZ.w[i], 4);
+    other.ZZZ.w[i] = __shfl_xor_sync(oct, acc.ZZZ.w[i], 4);
+  }
+  if (half) return acc;
+  return g1_add_quad(lq, acc, other);
 }
 
 // ------------------------------------------------------------------ G2 (Jacobian over Fp2)

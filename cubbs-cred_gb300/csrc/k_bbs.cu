@@ -330,6 +330,35 @@ __global__ void __launch_bounds__(128) k_pv_pairjobs_agg(const PvItem *items0, u
   pj[i] = job;
 }
 
+// Verify: one lane pair per (item, point) of an aggregated group:
+// scaled[2i] = rho_i A_i, scaled[2i+1] = rho_i (B_i - e_i A_i), from the
+// item's own pairing job (its two G1 points); an item whose job is not
+// evaluated, or a point the job skips (the identity), contributes nothing.
+__global__ void __launch_bounds__(32) k_vf_agg_scale(const PairJob *pj, uint32_t n, const int32_t *group_of,
+                                                     AggSeed seed, g1 *scaled) {
+  const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 1;
+  if (t >= 2 * n) return;  // both lanes of a pair leave together
+  const LanePair lp = LanePair::here();
+  const uint32_t i = t >> 1, which = t & 1;
+  const PairJob j = pj[i];
+  const bool use = group_of[i] >= 0 && j.active == 1 && !(j.flags & (which ? 2u : 1u));
+  uint32_t ra, rb;
+  agg_rho(seed, i, ra, rb);
+  const g1 r = use ? g1_mul_rho(lp, which ? j.pb : j.pa, ra, rb) : g1_inf();
+  if (lp.role == 0) scaled[t] = r;
+}
+// Verify: items of groups whose check passed are settled (ok = 1, job
+// skipped); the others keep their own job.
+__global__ void __launch_bounds__(128) k_vf_pairjobs_agg(uint32_t n, const int32_t *group_of,
+                                                         const uint8_t *group_ok, PairJob *pj, uint8_t *ok) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  if (pj[i].active == 1 && group_of[i] >= 0 && group_ok[group_of[i]]) {
+    pj[i].active = 2;
+    ok[i] = 1;
+  }
+}
+
 // T1, T2 -> compressed; recompute the challenge (a mismatch marks the item invalid).
 template <int S>
 __global__ void __launch_bounds__(64) k_pv_finish(PvItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
@@ -1029,7 +1058,10 @@ size_t fixed_rows_per_item(Op op) { return op == OP_PGEN ? 2 : 1; }
 // least 16 items as one group (the reference aggregates batches of 128 or more:
 // crates/cubbs-bbs/src/execution.rs:3797-3801).  Other items are checked alone.
 const size_t AGG_MIN_BATCH = 128, AGG_MIN_GROUP = 16;
-void plan_groups(Runtime &rt, OpBatch &b) {
+// Verify batches group the same way (the reference's GPU engine aggregates
+// Verify pairings of 128 or more items too: crates/cubbs-bbs/src/execution.rs:
+// 3797-3801, gpu_engine.rs:1756-1781).
+template <typename ItemT> void plan_groups_of(Runtime &rt, OpBatch &b) {
   const size_t n = b.n;
   b.h_group_of.assign(n, -1);
   b.h_perm.clear();
@@ -1039,7 +1071,7 @@ void plan_groups(Runtime &rt, OpBatch &b) {
     std::unordered_map<int32_t, std::vector<uint32_t>> by_slot;
     std::vector<int32_t> order;
     for (size_t i = 0; i < n; i++) {
-      const PvItem &p = reinterpret_cast<const PvItem *>(b.items.data())[i];
+      const ItemT &p = reinterpret_cast<const ItemT *>(b.items.data())[i];
       if (p.status != ST_OK || p.pk_status != DEC_OK) continue;
       auto &v = by_slot[p.pk_slot];
       if (v.empty()) order.push_back(p.pk_slot);
@@ -1118,7 +1150,8 @@ void upload(Runtime &rt, OpBatch &b) {
   b.e = rt.arena.alloc<fr>(n);
   b.vpts = rt.arena.alloc<g1a>(2 * n);
   if (b.op == OP_PGEN) b.rs = rt.arena.alloc<fr>(n * b.rs_stride);
-  if (b.op == OP_PVERIFY) plan_groups(rt, b);
+  if (b.op == OP_PVERIFY) plan_groups_of<PvItem>(rt, b);
+  if (b.op == OP_VERIFY) plan_groups_of<VerifyItem>(rt, b);
   b.out = rt.arena.alloc<uint8_t>(b.out_total + 1);
 }
 
@@ -1322,9 +1355,31 @@ void run_verify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_sub, 0));
   SPAN(s, "finish",
        k_verify_finish<<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.fixed, b.v, b.pts, b.dec, b.sub, b.pj));
-  if (n <= 256) SPAN(s, "pairing", launch_pairing_check_split(s, b.pj, N, rt.d_lines, b.ok));
-  else SPAN(s, "pairing", launch_pairing_check(s, b.pj, N, rt.d_lines, b.ok));
-  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 7;
+  const uint32_t G = (uint32_t)b.h_gslot.size();
+  if (G) {
+    // random-coefficient group checks per key, then the per-item checks of the
+    // items outside passing groups (as ProofVerify does; see k_agg_scale)
+    AggSeed seed;
+    size_t got = 0;
+    while (got < sizeof(seed)) {
+      ssize_t r = getrandom(reinterpret_cast<uint8_t *>(&seed) + got, sizeof(seed) - got, 0);
+      if (r <= 0) throw CudaError(cudaErrorUnknown, "getrandom");
+      got += (size_t)r;
+    }
+    SPAN(s, "agg_scale", k_vf_agg_scale<<<blocks_for(4 * n, 32), 32, 0, s>>>(b.pj, N, b.group_of, seed, b.scaled));
+    SPAN(s, "agg_sum",
+         CUBBS_CHECK(cudaMemsetAsync(b.gjobs, 0, G * sizeof(PairJob), s));
+         k_agg_sum<<<dim3(G, 2), 256, 0, s>>>(b.scaled, b.perm, b.goff, b.gslot, b.gjobs));
+    SPAN(s, "pairing_check", launch_pairing_check_split(s, b.gjobs, G, rt.d_lines, b.gok));
+    SPAN(s, "pairing",
+         k_vf_pairjobs_agg<<<blocks_for(n, 128), 128, 0, s>>>(N, b.group_of, b.gok, b.pj, b.ok);
+         launch_pairing_check_split(s, b.pj, N, rt.d_lines, b.ok));
+  } else if (n <= 256) {
+    SPAN(s, "pairing", launch_pairing_check_split(s, b.pj, N, rt.d_lines, b.ok));
+  } else {
+    SPAN(s, "pairing", launch_pairing_check(s, b.pj, N, rt.d_lines, b.ok));
+  }
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 7 + (G ? 4 : 0);
 }
 
 // The whole device pipeline of one batch (no host work, no transfers).

@@ -8,6 +8,8 @@
 // GLV variable base (kernels/variable_base_universal.cuh:25-331), BLST decode
 // and compress on the host (native/cuda/src/g1_msm_blst.cpp:614-732).  Here
 // decode and compress run on the device.
+#include <cstdlib>
+
 #include "runtime.cuh"
 
 namespace cubbs {
@@ -139,6 +141,36 @@ __global__ void __launch_bounds__(128) k_var_mul_pair(const g1a *points, const V
   const g1 r = g1_mul_glv_pair(lp, points[j.point], scalars[i]);
   if (lp.role == 0) out[i] = r;
 }
+// One lane quad per job (g1_mul_glv_quad).
+__global__ void __launch_bounds__(128) k_var_mul_quad(const g1a *points, const VarJob *jobs, const fr *scalars,
+                                                      uint32_t n, g1 *out) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t >> 2;
+  if (i >= n) return;  // the four lanes of a quad leave together
+  const LaneQuad lq = LaneQuad::here();
+  const VarJob j = jobs[i];
+  if (j.flags & 1) {
+    if (lq.role == 0) out[i] = g1_inf();
+    return;
+  }
+  const g1 r = g1_mul_glv_quad(lq, points[j.point], scalars[i]);
+  if (lq.role == 0) out[i] = r;
+}
+// Eight lanes per job (g1_mul_glv_octet): one quad per GLV half.
+__global__ void __launch_bounds__(128) k_var_mul_octet(const g1a *points, const VarJob *jobs, const fr *scalars,
+                                                       uint32_t n, g1 *out) {
+  const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t i = t >> 3;
+  if (i >= n) return;  // the eight lanes of a job leave together
+  const LaneQuad lq = LaneQuad::here();
+  const VarJob j = jobs[i];
+  if (j.flags & 1) {
+    if ((t & 7) == 0) out[i] = g1_inf();
+    return;
+  }
+  const g1 r = g1_mul_glv_octet(lq, points[j.point], scalars[i]);
+  if ((t & 7) == 0) out[i] = r;
+}
 __global__ void __launch_bounds__(128) k_var_mul(const g1a *points, const VarJob *jobs, const fr *scalars,
                                                  uint32_t n, g1 *out) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -175,10 +207,43 @@ __global__ void __launch_bounds__(32) k_g1_subgroup(const g1a *pts, const int32_
   const bool outside = status[i] == DEC_OK && !g1_in_subgroup_pair(lp, pts[i]);
   if (lp.role == 0) bad[i] = outside ? 1 : 0;
 }
-void launch_g1_subgroup(cudaStream_t s, const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad,
-                        bool pairs) {
+// One lane quad per point.
+__global__ void __launch_bounds__(64) k_g1_subgroup_quad(const g1a *pts, const int32_t *status, uint32_t n,
+                                                         int32_t *bad) {
+  const uint32_t i = (blockIdx.x * blockDim.x + threadIdx.x) >> 2;
+  if (i >= n) return;  // the four lanes of a quad leave together
+  const LaneQuad lq = LaneQuad::here();
+  const bool outside = status[i] == DEC_OK && !g1_in_subgroup_quad(lq, pts[i]);
+  if (lq.role == 0) bad[i] = outside ? 1 : 0;
+}
+
+// CUBBS_BBS_VAR_LANES (1, 2, 4 or 8; else 0: chosen by launch size).
+int var_lanes_setting() {
+  static const int v = [] {
+    const char *e = std::getenv("CUBBS_BBS_VAR_LANES");
+    const int x = e && *e ? std::atoi(e) : 0;
+    return (x == 1 || x == 2 || x == 4 || x == 8) ? x : 0;
+  }();
+  return v;
+}
+// Lanes per job for a launch of n jobs: the CUBBS_BBS_VAR_LANES setting, else
+// by size.  A few jobs leave the GPU idle, so each job's chain of products is
+// spread over more lanes (8: the two GLV halves on a quad each); thousands of
+// jobs fill the GPU, where lane pairs spend the fewest instructions per job.
+// Measured on GB300: in the 1024-proof ProofVerify step (4096 jobs) 2 lanes
+// 4.47 ms, 4 lanes 5.08, 8 lanes 5.40; Verify of 64 signatures (64 jobs) 8
+// lanes 12 % faster than 2.
+static int lanes_for(uint32_t n, int max_lanes) {
+  int l = var_lanes_setting();
+  if (l == 0) l = n <= 1024 ? 8 : n <= 2048 ? 4 : 2;
+  return l > max_lanes ? max_lanes : l;
+}
+
+void launch_g1_subgroup(cudaStream_t s, const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad, int lanes) {
   if (!n) return;
-  if (pairs) k_g1_subgroup<<<blocks_for(2 * (size_t)n, 32), 32, 0, s>>>(pts, status, n, bad);
+  if (lanes == 0) lanes = lanes_for(n, 4);
+  if (lanes >= 4) k_g1_subgroup_quad<<<blocks_for(4 * (size_t)n, 64), 64, 0, s>>>(pts, status, n, bad);
+  else if (lanes == 2) k_g1_subgroup<<<blocks_for(2 * (size_t)n, 32), 32, 0, s>>>(pts, status, n, bad);
   else k_g1_subgroup_lane<<<blocks_for(n, 32), 32, 0, s>>>(pts, status, n, bad);
 }
 void launch_g1_decode(cudaStream_t s, const uint8_t *pts48, uint32_t stride, uint32_t n, g1a *out, int32_t *status,
@@ -196,15 +261,21 @@ void launch_fixed_msm(cudaStream_t s, const FixedTable &t, const fr *scalars, ui
   if (rows) k_fixed_msm<<<blocks_for((size_t)rows * 32, 128), 128, 0, s>>>(t, scalars, stride, nterms, rows, out);
 }
 void launch_var_mul(cudaStream_t s, const g1a *points, const VarJob *jobs, const fr *scalars, uint32_t n, g1 *out,
-                    bool pairs) {
+                    int lanes) {
   if (!n) return;
-  if (pairs) k_var_mul_pair<<<blocks_for(2 * (size_t)n, 128), 128, 0, s>>>(points, jobs, scalars, n, out);
+  if (lanes == 0) lanes = lanes_for(n, 8);
+  if (lanes == 8) k_var_mul_octet<<<blocks_for(8 * (size_t)n, 128), 128, 0, s>>>(points, jobs, scalars, n, out);
+  else if (lanes == 4) k_var_mul_quad<<<blocks_for(4 * (size_t)n, 128), 128, 0, s>>>(points, jobs, scalars, n, out);
+  else if (lanes == 2) k_var_mul_pair<<<blocks_for(2 * (size_t)n, 128), 128, 0, s>>>(points, jobs, scalars, n, out);
   else k_var_mul<<<blocks_for(n, 128), 128, 0, s>>>(points, jobs, scalars, n, out);
 }
 cudaError_t warm_decode_and_var_mul_kernels(uint8_t *any_device_buffer) {
   // n = 0: every thread returns before touching memory
   k_g1_decode<<<1, 128>>>(any_device_buffer, 48, 0, nullptr, nullptr, true);
+  k_var_mul<<<1, 128>>>(nullptr, nullptr, nullptr, 0, nullptr);
   k_var_mul_pair<<<1, 128>>>(nullptr, nullptr, nullptr, 0, nullptr);
+  k_var_mul_quad<<<1, 128>>>(nullptr, nullptr, nullptr, 0, nullptr);
+  k_var_mul_octet<<<1, 128>>>(nullptr, nullptr, nullptr, 0, nullptr);
   return cudaGetLastError();
 }
 void launch_g1_compress(cudaStream_t s, const g1 *pts, uint32_t n, uint8_t *out48) {

@@ -257,8 +257,10 @@ void launch_decode_p1(cudaStream_t s, g1a *gens, uint8_t *gens_c, int suite);
 void launch_build_table(cudaStream_t s, const g1a *gens, int g0, int g1n, FixedTable t, g1 *scratch_xyzz,
                         fp *scratch_prod);
 // decode N compressed G1 points: status DEC_*; affine out
+// lanes per point: 1, 2 or 4 (0: chosen by the point count or CUBBS_BBS_VAR_LANES)
 void launch_g1_subgroup(cudaStream_t s, const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad,
-                        bool pairs = true);
+                        int lanes = 0);
+int var_lanes_setting();
 void launch_g1_decode(cudaStream_t s, const uint8_t *pts48, uint32_t stride, uint32_t n, g1a *out,
                       int32_t *status, bool check_subgroup);
 // fixed-base MSM rows: scalars raw Fr [row * stride + g] for g < nterms[row]
@@ -269,13 +271,13 @@ struct VarJob {
   uint32_t point;  // index into the point array
   uint32_t flags;  // bit0: point is infinity (result infinity)
 };
+// lanes per job: 1, 2, 4 or 8 (0: chosen by the job count or CUBBS_BBS_VAR_LANES)
 void launch_var_mul(cudaStream_t s, const g1a *points, const VarJob *jobs, const fr *scalars, uint32_t n,
-                    g1 *out,
-                    bool pairs = true);
+                    g1 *out, int lanes = 0);
 void launch_g1_compress(cudaStream_t s, const g1 *pts, uint32_t n, uint8_t *out48);
-// Launches k_g1_decode and k_var_mul_pair over zero items on the legacy
-// default stream of the current device (module load and local-memory sizing
-// ahead of real work; nothing is read or written).
+// Launches k_g1_decode and every variable-base kernel over zero items on the
+// legacy default stream of the current device (module load and local-memory
+// sizing ahead of real work; nothing is read or written).
 cudaError_t warm_decode_and_var_mul_kernels(uint8_t *any_device_buffer);
 struct MsmDevice {
   uint32_t n = 0, nterms = 0, nchunks = 0, nunits = 0;

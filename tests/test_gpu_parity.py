@@ -334,3 +334,39 @@ def test_sign_parts(gpu, oracle, golden):
     want = h(c["signature"])
     assert (code, sig[48:].hex()) == (0, want[48:].hex()), "e differs"
     assert sig[:48].hex() == want[:48].hex(), "A differs"
+
+
+def test_verify_aggregated_groups(gpu, oracle):
+    """Verify batches of 128 or more check each key's signatures (16 or more) as
+    one random-coefficient group and fall back to per-item checks when a group
+    fails.  Groups with failing items (signatures over other messages, a changed
+    header, a changed e, A outside G1, the identity A) and a passing group: every
+    verdict equals the oracle's and the verdict of the same item in a batch too
+    small to group."""
+    seed = b"verify-agg"
+    items = []
+    for key in range(3):
+        sk, pk = keypair(oracle, seed, key)
+        for i in range(60 if key < 2 else 20):
+            msgs = messages(seed, 100 * key + i, 8, 32)
+            sig = oracle.sign(sk, pk, b"hdr", msgs)[0]
+            items.append((pk, sig, b"hdr", msgs))
+    pk0 = items[0][0]
+    bad_msgs = messages(seed + b"-o", 0, 8, 32)
+    items[3] = (pk0, items[3][1], b"hdr", bad_msgs)                       # other messages
+    items[17] = (pk0, items[17][1], b"hdx", items[17][3])                 # changed header
+    e = (int.from_bytes(items[29][1][48:], "big") + 1).to_bytes(32, "big")
+    items[29] = (pk0, items[29][1][:48] + e, b"hdr", items[29][3])        # changed e
+    items[41] = (pk0, _on_curve_outside_g1(oracle, b"vagg") + items[41][1][48:], b"hdr", items[41][3])
+    items[77] = (items[77][0], bytes([0xC0]) + bytes(47) + items[77][1][48:], b"hdr", items[77][3])
+    items[130] = (items[0][0], items[130][1], b"hdr", items[130][3])      # verified under another key
+    want = [oracle.verify(*it) == 0 for it in items]
+    assert want.count(False) == 6 and len(items) == 140
+    got = gpu.verify_batch(items)
+    assert [v for _, v in got] == want
+    alone = []
+    for k in range(0, len(items), 50):
+        alone += [v for _, v in gpu.verify_batch(items[k:k + 50])]
+    assert alone == want
+    ok_items = [it for it, w in zip(items, want) if w]
+    assert all(v for _, v in gpu.verify_batch(ok_items))
