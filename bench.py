@@ -191,8 +191,9 @@ def fixed_msm_section(pkg, rank):
 
 def uneven_msm_section(pkg, rank):
     """C4: 16384 variable-base MSMs with K ~ U{2..257} (points u*P1, scalars uniform
-    mod r, one seed); chunk length and window per size class autotuned; the engine
-    replayed as one CUDA graph (prep + persistent launch + reduction)."""
+    mod r, one seed); thread-versus-warp mode, chunk length and window (4..12) per
+    size class autotuned; the engine replayed as one CUDA graph (prep +
+    persistent launch + reduction)."""
     n = 16384
     r = pkg.msm_uneven_bench(n_msms=n, k_min=2, k_max=257, seed=4 + rank, tune=True, warmup=3, steps=5)
     assert r["mismatch"] == 0, "uneven MSM engine disagrees with the per-term path"
@@ -202,7 +203,8 @@ def uneven_msm_section(pkg, rank):
             "decode_ms_all_points": round(r["decode_ms"], 3),
             "msms_per_s_with_decode": round(n / ((ms + r["decode_ms"]) / 1e3), 1),
             "autotuned": {"size_classes": ["K<=8", "K<=32", "K<=96", "K<=257"], "chunk_terms": r["chunk"],
-                          "window_bits": r["window"]},
+                          "window_bits": r["window"],
+                          "mode": ["warp" if m else "thread" for m in r["mode"]]},
             "checked_vs_per_term_glv": r["checked"], "l2": "flushed (256 MiB write) before each replay"}
 
 

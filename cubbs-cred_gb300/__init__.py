@@ -482,7 +482,7 @@ def msm_uneven_bench(n_msms=16384, k_min=2, k_max=257, seed=4, tune=True, warmup
     class], window=[per size class], checked, mismatch)."""
     ms = (ctypes.c_float * steps)()
     dec = ctypes.c_float(0)
-    tun = (ctypes.c_uint32 * 8)()
+    tun = (ctypes.c_uint32 * 12)()
     chk, mm = ctypes.c_uint32(0), ctypes.c_uint32(0)
     fn = lib().cubbs_bbs_gpu_msm_uneven_bench_v2
     fn.restype = ctypes.c_int32
@@ -493,25 +493,29 @@ def msm_uneven_bench(n_msms=16384, k_min=2, k_max=257, seed=4, tune=True, warmup
             ctypes.cast(ctypes.pointer(chk), ctypes.c_void_p), ctypes.cast(ctypes.pointer(mm), ctypes.c_void_p))
     if rc:
         raise RuntimeError(f"msm_uneven_bench returned {rc}")
-    return {"ms": list(ms), "decode_ms": dec.value, "chunk": list(tun[:4]), "window": list(tun[4:]),
+    return {"ms": list(ms), "decode_ms": dec.value, "chunk": list(tun[:4]), "window": list(tun[4:8]),
+            "mode": list(tun[8:]),
             "checked": chk.value, "mismatch": mm.value}
 
 
-def msm_tuning(chunk=None, window=None):
+def msm_tuning(chunk=None, window=None, mode=None):
     """Uneven-MSM engine settings per size class (K <= 8, <= 32, <= 96, larger):
-    with chunk and window (4 values each) they replace the process's settings.
-    Returns the (chunk, window) lists in force."""
+    with chunk, window and mode (4 values each; mode 0 thread, 1 warp; mode
+    defaults to thread) they replace the process's settings.  Returns the
+    (chunk, window, mode) lists in force."""
     fn = lib().cubbs_bbs_gpu_msm_tuning_v2
     fn.restype = ctypes.c_int32
-    fn.argtypes = [ctypes.c_void_p] * 4
-    cin = (ctypes.c_uint32 * 4)(*chunk) if chunk is not None else None
-    win = (ctypes.c_uint32 * 4)(*window) if window is not None else None
-    cout, wout = (ctypes.c_uint32 * 4)(), (ctypes.c_uint32 * 4)()
-    rc = fn(ctypes.cast(cin, ctypes.c_void_p) if cin else None, ctypes.cast(win, ctypes.c_void_p) if win else None,
-            ctypes.cast(cout, ctypes.c_void_p), ctypes.cast(wout, ctypes.c_void_p))
+    fn.argtypes = [ctypes.c_void_p] * 6
+    if chunk is not None and mode is None:
+        mode = [0] * 4
+    arrs = [(ctypes.c_uint32 * 4)(*v) if v is not None else None for v in (chunk, window, mode)]
+    outs = [(ctypes.c_uint32 * 4)() for _ in range(3)]
+    args = [ctypes.cast(a, ctypes.c_void_p) if a is not None else None for a in arrs]
+    args += [ctypes.cast(o, ctypes.c_void_p) for o in outs]
+    rc = fn(*args)
     if rc:
         raise ValueError(f"msm_tuning returned {rc}")
-    return list(cout), list(wout)
+    return tuple(list(o) for o in outs)
 
 
 def sm_partition():
@@ -681,6 +685,33 @@ def pairing_eq_batch(reqs):
     res = (Result * len(reqs))()
     _call("cubbs_bbs_gpu_pairing_eq_batch_v2", ABI_VERSION, items, len(reqs), res)
     return [(res[i].code, bool(res[i].value)) for i in range(len(reqs))]
+
+
+def g1_msm_pairing_batch(msms, pairs):
+    """Uneven MSMs ([points48], [scalars32]) and pairing checks (a48, b96, c48,
+    d96) in one persistent launch -> ([(code, point48)], [(code, e(a,b) == e(c,d))])."""
+    k = _Keep()
+    mitems = (G1MsmItem * max(1, len(msms)))()
+    outs = []
+    for i, (pts, scs) in enumerate(msms):
+        ob, buf = k.out(48)
+        outs.append(buf)
+        mitems[i] = G1MsmItem(k.slices(pts), k.slices(scs), len(pts), ob)
+    pitems = (PairingEqItem * max(1, len(pairs)))()
+    for i, (a, b, c, d) in enumerate(pairs):
+        pitems[i] = PairingEqItem(k.bytes(a), k.bytes(b), k.bytes(c), k.bytes(d))
+    mres = (Result * max(1, len(msms)))()
+    pres = (Result * max(1, len(pairs)))()
+    fn = lib().cubbs_bbs_gpu_g1_msm_pairing_batch_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                   ctypes.c_void_p, ctypes.c_void_p]
+    rc = fn(ABI_VERSION, ctypes.cast(mitems, ctypes.c_void_p), len(msms), ctypes.cast(pitems, ctypes.c_void_p),
+            len(pairs), ctypes.cast(mres, ctypes.c_void_p), ctypes.cast(pres, ctypes.c_void_p))
+    if rc:
+        raise RuntimeError(f"g1_msm_pairing_batch returned {rc}")
+    return ([(mres[i].code, outs[i].raw[:48]) for i in range(len(msms))],
+            [(pres[i].code, bool(pres[i].value)) for i in range(len(pairs))])
 
 
 def pairing_eq_aggregate(reqs):

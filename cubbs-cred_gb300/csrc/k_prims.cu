@@ -136,25 +136,142 @@ struct Plan {
   }
 };
 
+// Pairing checks that share the engine's persistent launch with the plan's
+// MSMs: the items in, per-item verdicts and decode failures out.
+struct PairRequest {
+  const CuBbsBbsGpuPairingEqItem *items = nullptr;
+  size_t n = 0;
+  std::vector<int> bad;
+  std::vector<uint8_t> ok;
+};
+bool pairing_items_ok(const CuBbsBbsGpuPairingEqItem *items, size_t n) {
+  for (size_t i = 0; i < n; i++) {
+    const auto &it = items[i];
+    if (it.lhs_g1.len != 48 || !it.lhs_g1.data || it.rhs_g1.len != 48 || !it.rhs_g1.data || it.lhs_g2.len != 96 ||
+        !it.lhs_g2.data || it.rhs_g2.len != 96 || !it.rhs_g2.data)
+      return false;
+  }
+  return true;
+}
+
+// Device pairing jobs e(lhs_g1, lhs_g2) * e(-rhs_g1, rhs_g2) == 1 of the items
+// (G2 points resolved to resident line slots, G1 points decoded with the
+// subgroup check); bad[i] = 1 for an item with an undecodable point.
+PairJob *prepare_pair_jobs(Runtime &rt, const CuBbsBbsGpuPairingEqItem *items, size_t n,
+                                  std::vector<int> &bad) {
+  std::vector<const uint8_t *> g2(2 * n);
+  for (size_t i = 0; i < n; i++) {
+    g2[2 * i] = items[i].lhs_g2.data;
+    g2[2 * i + 1] = items[i].rhs_g2.data;
+  }
+  std::vector<int> slots, st;
+  rt.resolve_pks(g2, slots, st);
+  std::vector<uint8_t> g1b(96 * n);
+  for (size_t i = 0; i < n; i++) {
+    std::memcpy(&g1b[96 * i], items[i].lhs_g1.data, 48);
+    std::memcpy(&g1b[96 * i + 48], items[i].rhs_g1.data, 48);
+  }
+  uint8_t *d = upload(rt, g1b.data(), g1b.size());
+  g1a *pts = rt.arena.alloc<g1a>(2 * n);
+  int32_t *pst = rt.arena.alloc<int32_t>(2 * n);
+  launch_g1_decode(rt.stream, d, 48, (uint32_t)(2 * n), pts, pst, true);
+  std::vector<g1a> hp(2 * n);
+  std::vector<int32_t> hst(2 * n);
+  CUBBS_CHECK(cudaMemcpyAsync(hp.data(), pts, sizeof(g1a) * 2 * n, cudaMemcpyDeviceToHost, rt.stream));
+  CUBBS_CHECK(cudaMemcpyAsync(hst.data(), pst, 8 * n, cudaMemcpyDeviceToHost, rt.stream));
+  CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+  std::vector<PairJob> jobs(n);
+  bad.assign(n, 0);
+  for (size_t i = 0; i < n; i++) {
+    PairJob &j = jobs[i];
+    j.pa = hp[2 * i];
+    j.pb = hp[2 * i + 1];
+    j.slot_a = slots[2 * i];
+    j.slot_b = slots[2 * i + 1];
+    j.flags = 0;
+    j.active = 1;
+    if (hst[2 * i] == DEC_BAD || hst[2 * i + 1] == DEC_BAD || st[2 * i] == DEC_BAD || st[2 * i + 1] == DEC_BAD) {
+      bad[i] = 1;
+      j.active = 0;
+    }
+    if (hst[2 * i] == DEC_INF || st[2 * i] == DEC_INF) j.flags |= 1;
+    if (hst[2 * i + 1] == DEC_INF || st[2 * i + 1] == DEC_INF) j.flags |= 2;
+  }
+  PairJob *dj = upload(rt, jobs.data(), n);
+  k_negate_pb<<<blocks_for(n, 128), 128, 0, rt.stream>>>(dj, (uint32_t)n);
+  return dj;
+}
+
+// The engine's kernels (prep, persistent launch, reduction) for a plan, from a
+// CUDA graph: one is captured the first time a workspace meets the plan's
+// shape and device buffers (the arena hands out the same addresses to the same
+// sequence of allocations) and replayed afterwards.  At most 32 graphs per
+// workspace are kept.
+void run_engine_graph(Runtime &rt, cudaStream_t s, const MsmPlan &mp, MsmDevice &md, const g1a *pts,
+                      const VarJob *djobs, const fr *vsc, uint8_t *dout) {
+  uint64_t key = 1469598103934665603ull;
+  auto mix = [&key](uint64_t v) { key = (key ^ v) * 1099511628211ull; };
+  for (const MsmUnit &u : mp.units) {
+    mix(u.kind_c);
+    mix(u.index);
+  }
+  for (const MsmChunk &c : mp.chunks) mix((uint64_t)c.first << 32 | c.count);
+  for (uint32_t v : mp.start) mix(v);
+  for (uint32_t v : mp.pstart) mix(v);
+  const void *ptrs[] = {pts, djobs, vsc, dout, md.term_c, md.chunks, md.units, md.pstart, md.start, md.koff,
+                        md.counter, md.phi, md.partials, md.gbuckets, md.pjobs, md.lines, md.pok};
+  for (const void *q : ptrs) mix((uint64_t)(uintptr_t)q);
+  mix((uint64_t)md.grid << 32 | md.warps_per_block);
+  mix(md.smem_per_warp);
+  auto it = rt.msm_graphs.find(key);
+  if (it == rt.msm_graphs.end()) {
+    if (rt.msm_graphs.size() >= 32) {
+      for (auto &g : rt.msm_graphs) cudaGraphExecDestroy(g.second);
+      rt.msm_graphs.clear();
+    }
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+    CUBBS_CHECK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    launch_msm_prep(s, md, pts, djobs, vsc);
+    launch_msm_main(s, md, pts, djobs, rt.sm_count, nullptr, dout);
+    CUBBS_CHECK(cudaStreamEndCapture(s, &graph));
+    const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CUBBS_CHECK(e);
+    it = rt.msm_graphs.emplace(key, exec).first;
+  }
+  CUBBS_CHECK(cudaGraphLaunch(it->second, s));
+}
+
 // Runs the plan; returns per-row compressed outputs and per-row ok flags.
-void run_plan(Runtime &rt, Plan &pl, std::vector<uint8_t> &out48, std::vector<uint8_t> &row_ok) {
+// With pairs (or force_engine) the MSMs take the persistent engine, and the
+// pairing checks run as units of the same launch.
+void run_plan(Runtime &rt, Plan &pl, std::vector<uint8_t> &out48, std::vector<uint8_t> &row_ok,
+              PairRequest *pairs = nullptr) {
   cudaStream_t s = rt.stream;
   size_t R = pl.rows, npts = pl.points_be.size() / 48, nvar = pl.var_point.size();
   size_t nfix = pl.has_fixed ? R * pl.fixed_stride : 0;
   // Many variable-only rows: the persistent bucket-method engine (k_msm.cu)
   // instead of one GLV multiplication per term plus a row sum.
-  const bool engine = !pl.has_fixed && R >= 32 && nvar >= 8 * R;
+  const bool engine = (pairs && pairs->n && !pl.has_fixed) || (!pl.has_fixed && R >= 32 && nvar >= 8 * R);
   MsmPlan mp;
   if (engine) {
     std::vector<uint32_t> K(R);
     for (size_t r = 0; r < R; r++) K[r] = pl.var_start[r + 1] - pl.var_start[r];
-    mp.build(K, rt.sh.msm_tuning);
+    mp.build(K, rt.sh.msm_tuning, pairs ? pairs->n : 0);
   }
-  const size_t eng_bytes = engine ? MsmDevice::arena_bytes(mp) : 0;
+  const size_t eng_bytes = engine ? MsmDevice::arena_bytes(mp, rt.sm_count) : 0;
+  const size_t np = pairs ? pairs->n : 0;
   rt.arena.reserve(8192 + npts * (sizeof(g1a) + 64) + nvar * (sizeof(g1) + sizeof(fr) + 48) +
-                   nfix * (sizeof(fr) + 40) + R * (2 * sizeof(g1) + 128) + eng_bytes);
+                   nfix * (sizeof(fr) + 40) + R * (2 * sizeof(g1) + 128) + eng_bytes + 65536 + np * 512);
   rt.staging.reserve(65536 + pl.points_be.size() + pl.var_scalars_be.size() + pl.fixed_scalars_be.size() +
-                     R * 128 + nvar * 16 + eng_bytes);
+                     R * 128 + nvar * 16 + eng_bytes + 65536 + np * 256);
+  const PairJob *pjobs = nullptr;
+  uint8_t *pok = nullptr;
+  if (np) {
+    pjobs = prepare_pair_jobs(rt, pairs->items, np, pairs->bad);
+    pok = rt.arena.alloc<uint8_t>(np);
+  }
   if (pl.has_fixed) rt.ensure_table((int)pl.fixed_stride);
   // decode points
   uint8_t *dpb = upload(rt, pl.points_be.data(), pl.points_be.size());
@@ -205,11 +322,17 @@ void run_plan(Runtime &rt, Plan &pl, std::vector<uint8_t> &out48, std::vector<ui
   }
   VarJob *djobs = upload(rt, jobs.data(), nvar);
   uint8_t *dout = rt.arena.alloc<uint8_t>(48 * R);
+  uint32_t *engine_err = nullptr, herr = 0;
   if (engine) {
     MsmDevice md;
     md.upload(rt, mp, s);
-    launch_msm_prep(s, md, pts, djobs, vsc);
-    launch_msm_main(s, md, pts, djobs, rt.sm_count, nullptr, dout);
+    if (np) {
+      md.pjobs = pjobs;
+      md.lines = rt.d_lines;
+      md.pok = pok;
+    }
+    run_engine_graph(rt, s, mp, md, pts, djobs, vsc, dout);
+    engine_err = md.counter + 1;
   } else {
     g1 *v = rt.arena.alloc<g1>(nvar);
     launch_var_mul(s, pts, djobs, vsc, (uint32_t)nvar, v);
@@ -221,7 +344,13 @@ void run_plan(Runtime &rt, Plan &pl, std::vector<uint8_t> &out48, std::vector<ui
   CUBBS_CHECK(cudaGetLastError());
   out48.resize(48 * R);
   if (R) CUBBS_CHECK(cudaMemcpyAsync(out48.data(), dout, 48 * R, cudaMemcpyDeviceToHost, s));
+  if (np) {
+    pairs->ok.resize(np);
+    CUBBS_CHECK(cudaMemcpyAsync(pairs->ok.data(), pok, np, cudaMemcpyDeviceToHost, s));
+  }
+  if (engine_err) CUBBS_CHECK(cudaMemcpyAsync(&herr, engine_err, 4, cudaMemcpyDeviceToHost, s));
   CUBBS_CHECK(cudaStreamSynchronize(s));
+  if (herr) throw CudaError(cudaErrorInvalidValue, "uneven-MSM engine: a unit had no room in its launch");
   row_ok.assign(R, 1);
   for (size_t r = 0; r < R; r++) {
     for (uint32_t j = pl.var_start[r]; j < pl.var_start[r + 1]; j++)
@@ -341,6 +470,57 @@ extern "C" int32_t cubbs_bbs_gpu_g1_msm_batch_v2(uint32_t abi, CuBbsBbsGpuG1MsmI
   for (size_t i = 0; i < n; i++) outs[i] = items[i].point_out;
   finish_rows(out, ok, outs.data(), results, n, CUBBS_BBS_MSM_ROUTE_CUBBS_UNIVERSAL);
   for (size_t i = 0; i < n; i++) items[i].point_out.len = outs[i].len;
+  return CUBBS_BBS_GPU_SUCCESS;
+  ABI_GUARD_END
+}
+
+// ----------------------------------------------------------------------------- MSMs and pairings in one launch
+// An uneven batch of G1 MSMs (the items of g1_msm_batch_v2) and of pairing
+// equality checks (the items of pairing_eq_batch_v2) evaluated by one
+// persistent engine launch: its warps take MSM units and pairing units from
+// one queue, pairing units first.  Results as the two separate entry points
+// give them.
+extern "C" int32_t cubbs_bbs_gpu_g1_msm_pairing_batch_v2(uint32_t abi, CuBbsBbsGpuG1MsmItem *msm_items,
+                                                         size_t msm_count,
+                                                         const CuBbsBbsGpuPairingEqItem *pairing_items,
+                                                         size_t pairing_count, CuBbsBbsGpuResult *msm_results,
+                                                         CuBbsBbsGpuResult *pairing_results) {
+  if (!abi_ok(abi) || (msm_count > 0 && (msm_items == nullptr || msm_results == nullptr)) ||
+      (pairing_count > 0 && (pairing_items == nullptr || pairing_results == nullptr)))
+    return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  for (size_t i = 0; i < msm_count; i++) {
+    const auto &it = msm_items[i];
+    if ((it.term_count > 0 && (!it.points || !it.scalars)) || !it.point_out.data || it.point_out.capacity < 48)
+      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+    for (size_t k = 0; k < it.term_count; k++)
+      if (it.points[k].len != 48 || !it.points[k].data || it.scalars[k].len != 32 || !it.scalars[k].data)
+        return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  }
+  if (!pairing_items_ok(pairing_items, pairing_count)) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  if (msm_count == 0 && pairing_count == 0) return CUBBS_BBS_GPU_SUCCESS;
+  ABI_GUARD_BEGIN
+  CallScope scope;
+  Runtime &rt = scope.rt;
+  Plan pl;
+  pl.rows = msm_count;
+  for (size_t i = 0; i < msm_count; i++) {
+    pl.var_start.push_back((uint32_t)pl.var_point.size());
+    for (size_t k = 0; k < msm_items[i].term_count; k++)
+      pl.add_var(pl.add_point(msm_items[i].points[k].data), msm_items[i].scalars[k].data);
+  }
+  pl.var_start.push_back((uint32_t)pl.var_point.size());
+  PairRequest pr;
+  pr.items = pairing_items;
+  pr.n = pairing_count;
+  std::vector<uint8_t> out, ok;
+  run_plan(rt, pl, out, ok, &pr);
+  std::vector<CuBbsBbsGpuByteBuffer> outs(msm_count);
+  for (size_t i = 0; i < msm_count; i++) outs[i] = msm_items[i].point_out;
+  finish_rows(out, ok, outs.data(), msm_results, msm_count, CUBBS_BBS_MSM_ROUTE_CUBBS_UNIVERSAL);
+  for (size_t i = 0; i < msm_count; i++) msm_items[i].point_out.len = outs[i].len;
+  for (size_t i = 0; i < pairing_count; i++)
+    pairing_results[i] = pr.bad[i] ? CuBbsBbsGpuResult{CUBBS_BBS_GPU_ERR_INVALID_INPUT, 0, 0}
+                                   : CuBbsBbsGpuResult{CUBBS_BBS_GPU_SUCCESS, pr.ok[i], 0};
   return CUBBS_BBS_GPU_SUCCESS;
   ABI_GUARD_END
 }
@@ -793,61 +973,19 @@ extern "C" int32_t cubbs_bbs_gpu_proof_gen_t2_prepare_batch_v2(uint32_t abi, CuB
 
 // ----------------------------------------------------------------------------- pairing equality
 // value = e(lhs_g1, lhs_g2) == e(rhs_g1, rhs_g2), via e(lhs, lhs2) * e(-rhs, rhs2) == 1
+
 extern "C" int32_t cubbs_bbs_gpu_pairing_eq_batch_v2(uint32_t abi, const CuBbsBbsGpuPairingEqItem *items, size_t n,
                                                      CuBbsBbsGpuResult *results) {
   if (!abi_ok(abi) || (n > 0 && (items == nullptr || results == nullptr))) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-  for (size_t i = 0; i < n; i++) {
-    const auto &it = items[i];
-    if (it.lhs_g1.len != 48 || !it.lhs_g1.data || it.rhs_g1.len != 48 || !it.rhs_g1.data || it.lhs_g2.len != 96 ||
-        !it.lhs_g2.data || it.rhs_g2.len != 96 || !it.rhs_g2.data)
-      return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
-  }
+  if (!pairing_items_ok(items, n)) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   if (n == 0) return CUBBS_BBS_GPU_SUCCESS;
   ABI_GUARD_BEGIN
   CallScope scope;
   Runtime &rt = scope.rt;
-  std::vector<const uint8_t *> g2(2 * n);
-  for (size_t i = 0; i < n; i++) {
-    g2[2 * i] = items[i].lhs_g2.data;
-    g2[2 * i + 1] = items[i].rhs_g2.data;
-  }
-  std::vector<int> slots, st;
-  rt.resolve_pks(g2, slots, st);
   rt.arena.reserve(65536 + n * 512);
   rt.staging.reserve(65536 + n * 256);
-  std::vector<uint8_t> g1b(96 * n);
-  for (size_t i = 0; i < n; i++) {
-    std::memcpy(&g1b[96 * i], items[i].lhs_g1.data, 48);
-    std::memcpy(&g1b[96 * i + 48], items[i].rhs_g1.data, 48);
-  }
-  uint8_t *d = upload(rt, g1b.data(), g1b.size());
-  g1a *pts = rt.arena.alloc<g1a>(2 * n);
-  int32_t *pst = rt.arena.alloc<int32_t>(2 * n);
-  launch_g1_decode(rt.stream, d, 48, (uint32_t)(2 * n), pts, pst, true);
-  std::vector<g1a> hp(2 * n);
-  std::vector<int32_t> hst(2 * n);
-  CUBBS_CHECK(cudaMemcpyAsync(hp.data(), pts, sizeof(g1a) * 2 * n, cudaMemcpyDeviceToHost, rt.stream));
-  CUBBS_CHECK(cudaMemcpyAsync(hst.data(), pst, 8 * n, cudaMemcpyDeviceToHost, rt.stream));
-  CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
-  std::vector<PairJob> jobs(n);
-  std::vector<int> bad(n, 0);
-  for (size_t i = 0; i < n; i++) {
-    PairJob &j = jobs[i];
-    j.pa = hp[2 * i];
-    j.pb = hp[2 * i + 1];
-    j.slot_a = slots[2 * i];
-    j.slot_b = slots[2 * i + 1];
-    j.flags = 0;
-    j.active = 1;
-    if (hst[2 * i] == DEC_BAD || hst[2 * i + 1] == DEC_BAD || st[2 * i] == DEC_BAD || st[2 * i + 1] == DEC_BAD) {
-      bad[i] = 1;
-      j.active = 0;
-    }
-    if (hst[2 * i] == DEC_INF || st[2 * i] == DEC_INF) j.flags |= 1;
-    if (hst[2 * i + 1] == DEC_INF || st[2 * i + 1] == DEC_INF) j.flags |= 2;
-  }
-  PairJob *dj = upload(rt, jobs.data(), n);
-  k_negate_pb<<<blocks_for(n, 128), 128, 0, rt.stream>>>(dj, (uint32_t)n);
+  std::vector<int> bad;
+  PairJob *dj = prepare_pair_jobs(rt, items, n, bad);
   uint8_t *ok = rt.arena.alloc<uint8_t>(n);
   launch_pairing_check(rt.stream, dj, (uint32_t)n, rt.d_lines, ok);
   CUBBS_CHECK(cudaGetLastError());

@@ -75,28 +75,47 @@ struct PkSlot {
   int status = DEC_BAD;  // DEC_OK / DEC_INF / DEC_BAD
 };
 
-// Uneven variable-base MSMs (k_msm.cu): chunks of t terms per lane, bucket
-// method of window c; t and c per size class of the term count K.
+// Uneven variable-base MSMs (k_msm.cu), per size class of the term count K:
+// thread mode (chunks of t terms per lane, each lane a bucket method of window
+// c <= 7 with its own buckets) or warp mode (one warp per MSM, window c in
+// 4..12, buckets shared by the warp's lanes).
 #define MSM_CLASSES 4  // K <= 8, <= 32, <= 96, larger
+#define MSM_MODE_THREAD 0u
+#define MSM_MODE_WARP 1u
+#define MSM_THREAD_C_MAX 7
+#define MSM_WARP_C_MAX 12
+#define MSM_WARP_SMEM_C_MAX 10  // warp-mode buckets in shared memory up to this window, global memory beyond
 struct MsmTuning {
-  uint32_t chunk[MSM_CLASSES] = {8, 16, 32, 48};
-  uint32_t window[MSM_CLASSES] = {4, 4, 5, 5};
+  // measured on GB300 over 16384 MSMs with K ~ U{2..257}: 120.7k MSMs/s
+  uint32_t chunk[MSM_CLASSES] = {8, 16, 32, 32};
+  uint32_t window[MSM_CLASSES] = {4, 4, 4, 4};
+  uint32_t mode[MSM_CLASSES] = {MSM_MODE_THREAD, MSM_MODE_THREAD, MSM_MODE_THREAD, MSM_MODE_THREAD};
 };
 struct MsmChunk {
   uint32_t first, count;  // term range
   uint32_t slot;          // partial index (0xffffffff: padding)
   uint32_t pad;
 };
+// Work unit of the persistent engine (one warp): kind << 8 | window, and the
+// first of 32 chunks (thread mode), the MSM (warp mode) or the pairing job.
+enum : uint32_t { MSM_UNIT_THREAD = 0, MSM_UNIT_WARP = 1, MSM_UNIT_PAIR = 2 };
+struct MsmUnit {
+  uint32_t kind_c;
+  uint32_t index;
+};
 int msm_size_class(uint32_t K);
 struct MsmPlan {
   std::vector<uint32_t> start;    // term offsets of the MSMs (n + 1)
   uint32_t terms = 0;
   std::vector<uint8_t> term_c;    // window width per term
-  std::vector<MsmChunk> chunks;   // units of 32, grouped by window width
-  std::vector<uint8_t> unit_c;
+  std::vector<MsmChunk> chunks;   // thread-mode chunks, 32 per unit
+  std::vector<MsmUnit> units;     // pairing units first, then the largest MSMs first
   std::vector<uint32_t> pstart;   // partial offsets of the MSMs (n + 1)
   uint32_t nparts = 0;
-  void build(const std::vector<uint32_t> &K, const MsmTuning &tune);
+  uint32_t max_warp_c = 0;        // widest warp-mode window (0: no warp units)
+  uint32_t max_warp_smem_c = 0;   // widest warp-mode window with buckets in shared memory (0: none)
+  uint32_t pair_units = 0;
+  void build(const std::vector<uint32_t> &K, const MsmTuning &tune, uint32_t pairings = 0);
 };
 // Prepared state of one ciphersuite (the generators and everything built on
 // them differ between BLS12-381-SHA-256 and BLS12-381-SHAKE-256).
@@ -191,6 +210,8 @@ struct Runtime {
   cudaStream_t part[4] = {nullptr, nullptr, nullptr, nullptr}, part_check = nullptr;
   cudaEvent_t ev_gc = nullptr, ev_gc2 = nullptr, ev_done = nullptr;
   bool part_tried = false;
+  // CUDA graphs of the uneven-MSM engine, keyed by plan shape and buffers (k_prims.cu)
+  std::unordered_map<uint64_t, cudaGraphExec_t> msm_graphs;
   DeviceArena arena;
   HostStaging staging;
   HostStaging pack;  // pinned: the packed batch bytes, copied to the device without a host copy
@@ -279,19 +300,29 @@ void launch_g1_compress(cudaStream_t s, const g1 *pts, uint32_t n, uint8_t *out4
 // legacy default stream of the current device (module load and local-memory
 // sizing ahead of real work; nothing is read or written).
 cudaError_t warm_decode_and_var_mul_kernels(uint8_t *any_device_buffer);
+struct PairJob;
 struct MsmDevice {
   uint32_t n = 0, nterms = 0, nchunks = 0, nunits = 0;
-  uint8_t *term_c = nullptr, *unit_c = nullptr;
+  uint8_t *term_c = nullptr;
   MsmChunk *chunks = nullptr;
-  uint32_t *pstart = nullptr, *koff = nullptr, *counter = nullptr;
+  MsmUnit *units = nullptr;
+  uint32_t *pstart = nullptr, *start = nullptr, *koff = nullptr, *counter = nullptr;
   g1a *phi = nullptr;
   g1 *partials = nullptr;
+  g1 *gbuckets = nullptr;  // global buckets of warp units whose window exceeds MSM_WARP_SMEM_C_MAX
+  uint32_t warps_per_block = 4, smem_per_warp = 0, grid = 0, gbucket_stride = 0;
+  // pairing units: e(pa, Q_slot_a) e(pb, Q_slot_b) == 1 for pjobs[0 .. pair_units)
+  const PairJob *pjobs = nullptr;
+  const line2 *lines = nullptr;
+  uint8_t *pok = nullptr;
   void upload(Runtime &rt, const MsmPlan &p, cudaStream_t s);
-  static size_t arena_bytes(const MsmPlan &p);
+  static size_t arena_bytes(const MsmPlan &p, int sm_count);
 };
 // term j of the flat term list uses point jobs[j].point (skipped when flags & 1)
 // and scalar scalars[j]; MSM i owns terms [start[i], start[i+1]).
 void launch_msm_prep(cudaStream_t s, const MsmDevice &d, const g1a *pts, const VarJob *jobs, const fr *scalars);
+// One persistent launch over all units (thread chunks, warp MSMs, pairing
+// checks), then the per-MSM reduction of the partials.
 void launch_msm_main(cudaStream_t s, const MsmDevice &d, const g1a *pts, const VarJob *jobs, int sm_count, g1 *out,
                      uint8_t *out48);
 void launch_pk_prepare(cudaStream_t s, const uint8_t *pks96, uint32_t n, int slot0, g2a *pk_aff,

@@ -345,6 +345,15 @@ int32_t cubbs_bbs_gpu_g1_msm_batch_v2(uint32_t abi_version, CuBbsBbsGpuG1MsmItem
 int32_t cubbs_bbs_gpu_g1_msm_noalloc_v2(uint32_t abi_version, const uint8_t *points48,
                                         const uint8_t *scalars32, size_t term_count,
                                         uint8_t *point_out48, CuBbsBbsGpuResult *result);
+/* Addition with no counterpart in the reference: an uneven batch of G1 MSMs
+ * (items as in cubbs_bbs_gpu_g1_msm_batch_v2) and of pairing equality checks
+ * (items as in cubbs_bbs_gpu_pairing_eq_batch_v2) evaluated by one persistent
+ * launch whose warps take MSM and pairing work from one queue.  Each result
+ * array gets what the separate entry point would return. */
+int32_t cubbs_bbs_gpu_g1_msm_pairing_batch_v2(uint32_t abi_version, CuBbsBbsGpuG1MsmItem *msm_items,
+                                              size_t msm_count, const CuBbsBbsGpuPairingEqItem *pairing_items,
+                                              size_t pairing_count, CuBbsBbsGpuResult *msm_results,
+                                              CuBbsBbsGpuResult *pairing_results);
 /* reference :268-271 */
 int32_t cubbs_bbs_gpu_g1_msm_common_points_batch_v2(uint32_t abi_version,
                                                     CuBbsBbsGpuG1MsmCommonPointsBatchItem *items,

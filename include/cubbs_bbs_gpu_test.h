@@ -38,16 +38,18 @@ int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi_version, const uint8_t 
                                             float *ms_per_w, int32_t *best_w, int32_t *mismatched);
 
 /* Uneven-MSM engine settings per size class (K <= 8, <= 32, <= 96, larger):
- * chunk length and window width; non-null inputs replace them, non-null
- * outputs receive the settings in force. */
-int32_t cubbs_bbs_gpu_msm_tuning_v2(const uint32_t *chunk_in, const uint32_t *window_in, uint32_t *chunk_out,
-                                    uint32_t *window_out);
+ * mode (0: thread per chunk of `chunk` terms, window 4..7; 1: warp per MSM,
+ * window 4..12), chunk length and window width; non-null inputs replace them,
+ * non-null outputs receive the settings in force. */
+int32_t cubbs_bbs_gpu_msm_tuning_v2(const uint32_t *chunk_in, const uint32_t *window_in, const uint32_t *mode_in,
+                                    uint32_t *chunk_out, uint32_t *window_out, uint32_t *mode_out);
 
 /* ---- benchmarks */
 
 /* Uneven variable-base MSM benchmark: n_msms MSMs with K ~ U{k_min..k_max}
- * generated on the device from `seed`; optional autotuning; CUDA-graph
- * replays (ms_out[steps]); decode cost; the first 64 MSMs rechecked. */
+ * generated on the device from `seed`; optional autotuning (tuning_out: 12
+ * values, chunk / window / mode per size class); CUDA-graph replays
+ * (ms_out[steps]); decode cost; the first 64 MSMs rechecked. */
 int32_t cubbs_bbs_gpu_msm_uneven_bench_v2(uint32_t abi_version, size_t n_msms, uint32_t k_min, uint32_t k_max,
                                          uint64_t seed, int32_t tune, int32_t warmup, int32_t steps, float *ms_out,
                                          float *decode_ms, uint32_t *tuning_out, uint32_t *checked,

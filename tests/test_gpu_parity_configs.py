@@ -56,24 +56,32 @@ def _uneven_msms(oracle, seed, n=64):
 
 def test_uneven_msm_engine_every_setting(gpu, oracle):
     """The engine (taken by g1_msm_batch_v2 for 32+ MSMs of 8+ terms each) under
-    the autotuned settings and under every window 4..7 with chunk lengths from
-    one term per lane to whole MSMs: every output equals the oracle's."""
+    the autotuned settings, in thread mode under every window 4..7 with chunk
+    lengths from one term per lane to whole MSMs, in warp mode (one warp per
+    MSM, shared buckets) under every window 4..12, and with the modes mixed per
+    size class: every output equals the oracle's."""
     msms, want = _uneven_msms(oracle, 21)
     saved = gpu.msm_tuning()
     try:
         r = gpu.msm_uneven_bench(n_msms=2048, k_min=2, k_max=257, seed=5, tune=True, warmup=0, steps=1)
         assert r["mismatch"] == 0
         tuned = gpu.msm_tuning()
-        assert tuned == (r["chunk"], r["window"])
+        assert tuned == (r["chunk"], r["window"], r["mode"])
         got = gpu.g1_msm_batch(msms)
         assert got == [(0, w) for w in want], "autotuned %s" % (tuned,)
         for c in (4, 5, 6, 7):
             for t in (1, 3, 16, 64, 256):
-                gpu.msm_tuning([t] * 4, [c] * 4)
+                gpu.msm_tuning([t] * 4, [c] * 4, [0] * 4)
                 got = gpu.g1_msm_batch(msms)
-                assert got == [(0, w) for w in want], "chunk %d window %d" % (t, c)
+                assert got == [(0, w) for w in want], "thread mode, chunk %d window %d" % (t, c)
+        for c in range(4, 13):
+            gpu.msm_tuning([8] * 4, [c] * 4, [1] * 4)
+            got = gpu.g1_msm_batch(msms)
+            assert got == [(0, w) for w in want], "warp mode, window %d" % c
         # mixed settings per size class
-        gpu.msm_tuning([2, 8, 24, 40], [7, 4, 6, 5])
+        gpu.msm_tuning([2, 8, 24, 40], [7, 4, 6, 5], [0, 0, 0, 0])
+        assert gpu.g1_msm_batch(msms) == [(0, w) for w in want]
+        gpu.msm_tuning([2, 8, 24, 40], [5, 9, 6, 11], [0, 1, 0, 1])
         assert gpu.g1_msm_batch(msms) == [(0, w) for w in want]
     finally:
         gpu.msm_tuning(*saved)
@@ -84,6 +92,10 @@ def test_msm_tuning_rejects_out_of_range(gpu):
         gpu.msm_tuning([8, 8, 8, 8], [3, 4, 4, 4])
     with pytest.raises(ValueError):
         gpu.msm_tuning([0, 8, 8, 8], [4, 4, 4, 4])
+    with pytest.raises(ValueError):  # thread mode stops at window 7
+        gpu.msm_tuning([8, 8, 8, 8], [8, 4, 4, 4], [0, 0, 0, 0])
+    with pytest.raises(ValueError):  # warp mode stops at window 12
+        gpu.msm_tuning([8, 8, 8, 8], [13, 4, 4, 4], [1, 0, 0, 0])
 
 
 # ----------------------------------------------------------------------------- fixed-base MSM widths
@@ -240,3 +252,31 @@ def test_proof_verify_identity_points(gpu, oracle):
     want2 = want + [oracle.proof_verify(pk, bad, b"h", b"p", [ms[0]], [0]) == 0]
     assert want2[-1] is False
     assert [v for _, v in gpu.proof_verify_batch(batch2)] == want2
+
+
+def test_msms_and_pairings_in_one_launch(gpu, oracle):
+    """An uneven batch of MSMs (sizes across every class, thread and warp units)
+    and pairing checks (true, false, identity and undecodable inputs) through
+    one persistent launch: every result equals the oracle's and the separate
+    entry points'; the same call again replays the engine's captured graph."""
+    msms, want = _uneven_msms(oracle, 33, n=40)
+    _, pk = keypair(oracle, b"mixed")
+    _, pk2 = keypair(oracle, b"mixed", 1)
+    p1, _ = oracle.generators(1)
+    a = oracle.g1_mul(p1, scalar(b"mixed", b"a", 0))
+    bad_g1 = bytes([a[0] ^ 0x01]) + a[1:]
+    pairs = [(a, pk, a, pk), (a, pk, a, pk2), (a, pk, p1, pk), (IDENT, pk, IDENT, pk2), (bad_g1, pk, a, pk)]
+    want_p = [(0, True), (0, False), (0, False), (0, True), (1, False)]
+    assert [oracle.pairing_eq(*r) == 0 for r in pairs[:4]] == [True, False, False, True]
+    saved = gpu.msm_tuning()
+    try:
+        for mode in ([0, 0, 0, 0], [1, 1, 1, 1], [0, 1, 0, 1]):
+            gpu.msm_tuning([8, 16, 32, 48], [5, 6, 6, 7], mode)
+            for _ in range(2):
+                got_m, got_p = gpu.g1_msm_pairing_batch(msms, pairs)
+                assert got_m == [(0, w) for w in want], mode
+                assert [(c, v if c == 0 else False) for c, v in got_p] == want_p
+        assert gpu.g1_msm_pairing_batch([], pairs)[1] == gpu.pairing_eq_batch(pairs)
+        assert gpu.g1_msm_pairing_batch(msms[:3], [])[0] == gpu.g1_msm_batch(msms[:3])
+    finally:
+        gpu.msm_tuning(*saved)
