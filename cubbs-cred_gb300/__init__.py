@@ -140,6 +140,19 @@ class ProofGenT2PrepareItem(ctypes.Structure):
                 ("t1_out", ByteBuffer)]
 
 
+class ProofValueBase(ctypes.Structure):
+    _fields_ = [("bbs_signature", ByteSlice), ("bbs_header", ByteSlice), ("public_key", ByteSlice),
+                ("hmac_key", ByteSlice), ("mandatory_pointers", ctypes.c_void_p),
+                ("mandatory_pointer_count", ctypes.c_size_t)]
+
+
+class ProofValueDerived(ctypes.Structure):
+    _fields_ = [("bbs_proof", ByteSlice), ("label_keys", ctypes.c_void_p), ("label_values", ctypes.c_void_p),
+                ("label_count", ctypes.c_size_t), ("mandatory_indexes", ctypes.c_void_p),
+                ("mandatory_count", ctypes.c_size_t), ("selective_indexes", ctypes.c_void_p),
+                ("selective_count", ctypes.c_size_t), ("presentation_header", ByteSlice)]
+
+
 _LIB = None
 
 
@@ -957,3 +970,126 @@ def prepared_call(op, reqs):
         _ = k  # keep the buffers alive with the closure
         return list(zip(view["code"].tolist(), view["value"].tolist()))
     return call
+
+
+# ----------------------------------------------------------------------------- bbs-2023 proofValue codec
+# Mirrors crates/cubbs-bbs-proofvalue/src/lib.rs (serialize_base / parse_base /
+# serialize_derived / parse_derived) over the library's C codec.
+PROOFVALUE_ERRORS = {10: "InvalidMultibasePrefix", 11: "InvalidCborPrefix", 12: "InvalidBaseProof",
+                     13: "InvalidDerivedProof", 14: "Base64", 15: "Cbor"}
+
+
+class ProofValueError(ValueError):
+    def __init__(self, code):
+        super().__init__(PROOFVALUE_ERRORS.get(code, f"code {code}"))
+        self.code = code
+        self.kind = PROOFVALUE_ERRORS.get(code)
+
+
+def _pv_text_out(fn, item):
+    """Runs a serialize entry point, growing the text buffer once if needed."""
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    need = ctypes.c_size_t(0)
+    cap = 4096
+    while True:
+        buf = ctypes.create_string_buffer(cap)
+        rc = fn(ABI_VERSION, ctypes.cast(ctypes.pointer(item), ctypes.c_void_p), ctypes.cast(buf, ctypes.c_void_p),
+                cap, ctypes.cast(ctypes.pointer(need), ctypes.c_void_p))
+        if rc == ERR_INSUFFICIENT_OUTPUT and need.value > cap:
+            cap = need.value
+            continue
+        if rc:
+            raise ProofValueError(rc)
+        return buf.raw[:need.value].decode("ascii")
+
+
+def _parse_u64_like_rust(text):
+    body = text[1:] if text.startswith("+") else text
+    if not body or not all("0" <= ch <= "9" for ch in body) or int(body) >= 1 << 64:
+        raise ProofValueError(13)
+    return int(body)
+
+
+def proofvalue_serialize_base(bbs_signature, bbs_header, public_key, hmac_key, mandatory_pointers):
+    """Base proof -> 'u2V0C...' (lib.rs:76-87)."""
+    k = _Keep()
+    ptrs = [p.encode("utf-8") for p in mandatory_pointers]
+    item = ProofValueBase(k.bytes(bbs_signature), k.bytes(bbs_header), k.bytes(public_key), k.bytes(hmac_key),
+                          k.slices(ptrs) if ptrs else None, len(ptrs))
+    return _pv_text_out(lib().cubbs_bbs_proofvalue_serialize_base_v2, item)
+
+
+def proofvalue_serialize_derived(bbs_proof, label_map, mandatory_indexes, selective_indexes, presentation_header):
+    """Derived proof -> 'u2V0D...' (lib.rs:103-114).  label_map: {'c14n<k>': 'b<v>'};
+    keys parsed as the reference does (a later key naming the same number wins)."""
+    nums = {}
+    for key in sorted(label_map):
+        val = label_map[key]
+        if not key.startswith("c14n") or not val.startswith("b"):
+            raise ProofValueError(13)
+        nums[_parse_u64_like_rust(key[4:])] = _parse_u64_like_rust(val[1:])
+    k = _Keep()
+    keys = sorted(nums)
+    U64 = ctypes.c_uint64
+
+    def arr(vals):
+        a = (U64 * max(1, len(vals)))(*vals)
+        k.refs.append(a)
+        return ctypes.cast(a, ctypes.c_void_p)
+    item = ProofValueDerived(k.bytes(bbs_proof), arr(keys), arr([nums[x] for x in keys]), len(keys),
+                             arr(mandatory_indexes), len(mandatory_indexes), arr(selective_indexes),
+                             len(selective_indexes), k.bytes(presentation_header))
+    return _pv_text_out(lib().cubbs_bbs_proofvalue_serialize_derived_v2, item)
+
+
+def _pv_parse(name, text, out):
+    raw = text.encode("utf-8") if isinstance(text, str) else text
+    cap = 4 * len(raw) + 4096
+    arena = ctypes.create_string_buffer(cap)
+    used = ctypes.c_size_t(0)
+    fn = getattr(lib(), name)
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t,
+                   ctypes.c_void_p, ctypes.c_void_p]
+    rc = fn(ABI_VERSION, raw, len(raw), ctypes.cast(arena, ctypes.c_void_p), cap,
+            ctypes.cast(ctypes.pointer(out), ctypes.c_void_p), ctypes.cast(ctypes.pointer(used), ctypes.c_void_p))
+    if rc:
+        raise ProofValueError(rc)
+    return arena
+
+
+def _slice_bytes(s):
+    return ctypes.string_at(s.data, s.len) if s.len else b""
+
+
+def _u64s(ptr, n):
+    return list((ctypes.c_uint64 * n).from_address(ptr)) if n else []
+
+
+def proofvalue_parse_base(text):
+    """'u2V0C...' -> dict of the base proof fields (lib.rs:89-101)."""
+    out = ProofValueBase()
+    keep = _pv_parse("cubbs_bbs_proofvalue_parse_base_v2", text, out)
+    ptrs = (ByteSlice * max(1, out.mandatory_pointer_count)).from_address(out.mandatory_pointers)
+    value = {"bbs_signature": _slice_bytes(out.bbs_signature), "bbs_header": _slice_bytes(out.bbs_header),
+             "public_key": _slice_bytes(out.public_key), "hmac_key": _slice_bytes(out.hmac_key),
+             "mandatory_pointers": [_slice_bytes(ptrs[i]).decode("utf-8")
+                                    for i in range(out.mandatory_pointer_count)]}
+    del keep
+    return value
+
+
+def proofvalue_parse_derived(text):
+    """'u2V0D...' -> dict of the derived proof fields (lib.rs:116-128)."""
+    out = ProofValueDerived()
+    keep = _pv_parse("cubbs_bbs_proofvalue_parse_derived_v2", text, out)
+    keys = _u64s(out.label_keys, out.label_count)
+    vals = _u64s(out.label_values, out.label_count)
+    value = {"bbs_proof": _slice_bytes(out.bbs_proof),
+             "label_map": {"c14n%d" % a: "b%d" % b for a, b in zip(keys, vals)},
+             "mandatory_indexes": _u64s(out.mandatory_indexes, out.mandatory_count),
+             "selective_indexes": _u64s(out.selective_indexes, out.selective_count),
+             "presentation_header": _slice_bytes(out.presentation_header)}
+    del keep
+    return value

@@ -354,6 +354,57 @@ int32_t cubbs_bbs_gpu_g1_msm_pairing_batch_v2(uint32_t abi_version, CuBbsBbsGpuG
                                               size_t msm_count, const CuBbsBbsGpuPairingEqItem *pairing_items,
                                               size_t pairing_count, CuBbsBbsGpuResult *msm_results,
                                               CuBbsBbsGpuResult *pairing_results);
+/* Addition with no counterpart in the reference C ABI: the W3C bbs-2023
+ * proofValue codec of the reference's crates/cubbs-bbs-protocol callers
+ * (crates/cubbs-bbs-proofvalue/src/lib.rs:1-220), host code, no GPU work.
+ * A proofValue is 'u' || base64url-no-pad(prefix || CBOR payload): prefix
+ * d9 5d 02 and [bstr signature(80), bstr header(64), bstr public key(96),
+ * bstr hmac key(32), [tstr mandatory pointer...]] for a base proof; prefix
+ * d9 5d 03 and [bstr proof, {uint: uint} label map, [uint mandatory index],
+ * [uint selective index], bstr presentation header] for a derived proof.  The
+ * label map is given in numeric form: label_keys[k] = n of "c14n<n>",
+ * label_values[k] = m of "b<m>".  Serialize writes the text to out (cap
+ * bytes; *len_out is the length needed); parse copies every field into the
+ * caller's arena and points the output struct into it (*arena_used bytes).
+ * Returns 0, CUBBS_BBS_GPU_ERR_INVALID_INPUT for malformed arguments,
+ * CUBBS_BBS_GPU_ERR_INSUFFICIENT_OUTPUT when out or the arena is too small,
+ * or one of the CUBBS_BBS_PROOFVALUE_ERR_* codes (the reference's error
+ * kinds, lib.rs:17-36). */
+#define CUBBS_BBS_PROOFVALUE_ERR_MULTIBASE_PREFIX 10
+#define CUBBS_BBS_PROOFVALUE_ERR_CBOR_PREFIX 11
+#define CUBBS_BBS_PROOFVALUE_ERR_INVALID_BASE 12
+#define CUBBS_BBS_PROOFVALUE_ERR_INVALID_DERIVED 13
+#define CUBBS_BBS_PROOFVALUE_ERR_BASE64 14
+#define CUBBS_BBS_PROOFVALUE_ERR_CBOR 15
+typedef struct CuBbsBbsProofValueBase {
+  CuBbsBbsGpuByteSlice bbs_signature;
+  CuBbsBbsGpuByteSlice bbs_header;
+  CuBbsBbsGpuByteSlice public_key;
+  CuBbsBbsGpuByteSlice hmac_key;
+  const CuBbsBbsGpuByteSlice *mandatory_pointers;
+  size_t mandatory_pointer_count;
+} CuBbsBbsProofValueBase;
+typedef struct CuBbsBbsProofValueDerived {
+  CuBbsBbsGpuByteSlice bbs_proof;
+  const uint64_t *label_keys;
+  const uint64_t *label_values;
+  size_t label_count;
+  const uint64_t *mandatory_indexes;
+  size_t mandatory_count;
+  const uint64_t *selective_indexes;
+  size_t selective_count;
+  CuBbsBbsGpuByteSlice presentation_header;
+} CuBbsBbsProofValueDerived;
+int32_t cubbs_bbs_proofvalue_serialize_base_v2(uint32_t abi_version, const CuBbsBbsProofValueBase *value,
+                                               char *out, size_t cap, size_t *len_out);
+int32_t cubbs_bbs_proofvalue_parse_base_v2(uint32_t abi_version, const char *text, size_t len, uint8_t *arena,
+                                           size_t arena_cap, CuBbsBbsProofValueBase *out, size_t *arena_used);
+int32_t cubbs_bbs_proofvalue_serialize_derived_v2(uint32_t abi_version, const CuBbsBbsProofValueDerived *value,
+                                                  char *out, size_t cap, size_t *len_out);
+int32_t cubbs_bbs_proofvalue_parse_derived_v2(uint32_t abi_version, const char *text, size_t len, uint8_t *arena,
+                                              size_t arena_cap, CuBbsBbsProofValueDerived *out,
+                                              size_t *arena_used);
+
 /* reference :268-271 */
 int32_t cubbs_bbs_gpu_g1_msm_common_points_batch_v2(uint32_t abi_version,
                                                     CuBbsBbsGpuG1MsmCommonPointsBatchItem *items,
