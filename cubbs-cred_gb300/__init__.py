@@ -11,6 +11,7 @@ There is no CPU path: loading fails loudly when the library is missing.
 import ctypes
 import os
 import pathlib
+import threading
 
 _HERE = pathlib.Path(__file__).resolve().parent
 LIB_PATH = _HERE / "lib" / "libcubbs_bbs_cuda.so"
@@ -895,6 +896,230 @@ def serve_replay(pool, schedule, mode=SERVE_QUEUE, max_inflight=0, max_batch_ite
         results.append((res[s].code, res[s].value, out))
     del arrays
     return results, [lat[s] for s in range(n)], wall.value
+
+
+class ServeQueueConfig(ctypes.Structure):
+    _fields_ = [("max_batch_items", ctypes.c_uint32), ("max_inflight", ctypes.c_uint32),
+                ("coalesce_us", ctypes.c_uint32), ("queue_capacity", ctypes.c_uint32)]
+
+
+class ServeSnapshot(ctypes.Structure):
+    _fields_ = [("queued", ctypes.c_uint64), ("dispatches", ctypes.c_uint64), ("dispatched_items", ctypes.c_uint64),
+                ("max_observed_batch", ctypes.c_uint64), ("last_batch_size", ctypes.c_uint64),
+                ("inflight_batches", ctypes.c_uint64), ("total_queue_wait_ms", ctypes.c_double),
+                ("average_queue_wait_ms", ctypes.c_double)]
+
+
+SERVE_MAX_QUEUES = 8
+
+
+def serve_queue(op, suite=0):
+    """Device serving queue of operation op (OP_*) under a ciphersuite (SUITE_*)."""
+    return op + 4 * suite
+
+_SERVE_DONE = ctypes.CFUNCTYPE(None, ctypes.c_void_p, ctypes.c_uint64, ctypes.POINTER(Result))
+_SERVE_PROCESSOR = ctypes.CFUNCTYPE(ctypes.c_int32, ctypes.c_void_p, ctypes.c_int32,
+                                    ctypes.POINTER(ctypes.c_void_p), ctypes.c_size_t, ctypes.POINTER(Result))
+
+
+class ServeReceiver:
+    """The reply to one enqueued request (BatchReceiver, batcher.rs:107-115)."""
+
+    def __init__(self, callback=None):
+        self._event = threading.Event()
+        self._value = None
+        self._callback = callback
+        self.ticket = 0
+
+    def _set(self, value):
+        self._value = value
+        self._event.set()
+        if self._callback is not None:
+            self._callback(value)
+
+    def done(self):
+        return self._event.is_set()
+
+    def _attach(self, keep, items, buf, op):
+        self._keep, self._items, self._buf, self._op = keep, items, buf, op
+
+    def output(self):
+        """Signature or proof bytes of a device Sign / ProofGen request."""
+        buf = getattr(self, "_buf", None)
+        if buf is None or not self._event.is_set():
+            return None
+        item = self._items[0]
+        n = item.signature_out.len if self._op == OP_SIGN else item.proof_out.len
+        return buf.raw[:n]
+
+    def receive(self, timeout=None):
+        """(code, value, bytes_written) of the request; raises TimeoutError."""
+        if not self._event.wait(timeout):
+            raise TimeoutError("serving queue did not reply in time")
+        return self._value
+
+
+class ServeQueue:
+    """Client of the native serving queue in the shape of the reference W3C
+    service's BatchQueue (crates/cubbs-w3c-service/src/batcher.rs:118-221):
+    per-queue batcher settings (configure / configure_batcher / config),
+    enqueue -> ServeReceiver, submit, snapshot.
+
+    processor=None: the queues are the four BBS operations on the device (queue
+    = OP_*, items are ABI item structs that stay alive until their reply).
+    Otherwise processor(queue, items) -> [(code, value, bytes_written)] is
+    called on a dispatch thread with a batch of the caller's objects, the
+    batcher's generic processor; it raising fails the batch with ERR_INTERNAL."""
+
+    def __init__(self, processor=None, max_inflight=0, max_batch_items=0, hbm_budget_bytes=0):
+        self._lib = lib()
+        self._handle = ctypes.c_void_p()
+        self._mu = threading.Lock()
+        self._pending = {}
+        self._objects = {}
+        self._next = 1
+        self._processor = processor
+        self._done_cb = _SERVE_DONE(self._on_done)
+        self._submit = self._lib.cubbs_bbs_gpu_serve_submit_notify
+        self._submit.restype = ctypes.c_int32
+        self._submit.argtypes = [ctypes.c_void_p, ctypes.c_int32, ctypes.c_void_p, ctypes.c_char_p, _SERVE_DONE,
+                                 ctypes.c_void_p, ctypes.c_void_p]
+        cfg = ServeConfig(max_inflight, max_batch_items, hbm_budget_bytes)
+        if processor is None:
+            self._proc_cb = None
+            rc = self._lib.cubbs_bbs_gpu_serve_create(ABI_VERSION, ctypes.byref(cfg), ctypes.byref(self._handle))
+        else:
+            self._proc_cb = _SERVE_PROCESSOR(self._on_batch)
+            fn = self._lib.cubbs_bbs_gpu_serve_create_with_processor
+            fn.argtypes = [ctypes.c_uint32, ctypes.c_void_p, _SERVE_PROCESSOR, ctypes.c_void_p, ctypes.c_void_p]
+            rc = fn(ABI_VERSION, ctypes.addressof(cfg), self._proc_cb, None, ctypes.addressof(self._handle))
+        if rc:
+            raise RuntimeError(f"serve_create returned {rc}")
+
+    def _on_batch(self, _ctx, queue, items, n, results):
+        try:
+            with self._mu:
+                objs = [self._objects[items[i]][0] for i in range(n)]
+            outs = list(self._processor(queue, objs))
+            for i in range(n):
+                code, value, written = outs[i] if i < len(outs) else (ERR_INTERNAL, 0, 0)
+                results[i].code, results[i].value, results[i].bytes_written = code, value, written
+            return SUCCESS
+        except Exception:  # noqa: BLE001 - a failing processor fails its batch
+            return ERR_INTERNAL
+
+    def _on_done(self, ctx, _ticket, result):
+        r = result.contents
+        with self._mu:
+            rec = self._pending.pop(ctx)
+            self._objects.pop(ctx, None)
+        rec._set((r.code, r.value, r.bytes_written))
+
+    def configure(self, queue, max_batch_items=0, max_inflight=0, coalesce_us=0, queue_capacity=0):
+        """Sets one queue's settings; returns those in force (config())."""
+        cfg = ServeQueueConfig(max_batch_items, max_inflight, coalesce_us, queue_capacity)
+        eff = ServeQueueConfig()
+        rc = self._lib.cubbs_bbs_gpu_serve_configure_queue(self._handle, queue, ctypes.byref(cfg), ctypes.byref(eff))
+        if rc:
+            raise ValueError(f"serve_configure_queue returned {rc}")
+        return {f: getattr(eff, f) for f, _ in ServeQueueConfig._fields_}
+
+    def configure_batcher(self, queue, interval_ms, max_batch_size, queue_capacity, pipelines):
+        """configure() from the reference's BatcherConfig fields (batcher.rs:21-27)."""
+        return self.configure(queue, max_batch_size, pipelines, interval_ms * 1000, queue_capacity)
+
+    def config(self, queue):
+        eff = ServeQueueConfig()
+        rc = self._lib.cubbs_bbs_gpu_serve_configure_queue(self._handle, queue, None, ctypes.byref(eff))
+        if rc:
+            raise ValueError(f"serve_configure_queue returned {rc}")
+        return {f: getattr(eff, f) for f, _ in ServeQueueConfig._fields_}
+
+    def enqueue(self, queue, item, seed=None, callback=None):
+        """Queues one request and returns its ServeReceiver; waits while the
+        queue is at its capacity (BatchQueue::enqueue, batcher.rs:171-190).
+        callback(reply), if given, runs on the dispatch thread when the reply
+        arrives (for event-loop clients); it may enqueue again."""
+        rec = ServeReceiver(callback)
+        with self._mu:
+            key = self._next
+            self._next += 1
+            self._pending[key] = rec
+            if self._processor is not None:
+                self._objects[key] = (item,)
+        ptr = key if self._processor is not None else ctypes.addressof(item)
+        ticket = ctypes.c_uint64()
+        rc = self._submit(self._handle, queue, ptr, seed, self._done_cb, key, ctypes.addressof(ticket))
+        if rc:
+            with self._mu:
+                self._pending.pop(key, None)
+                self._objects.pop(key, None)
+            raise ValueError(f"serve_submit_notify returned {rc}")
+        rec.ticket = ticket.value
+        return rec
+
+    def submit(self, queue, item, seed=None, timeout=None):
+        return self.enqueue(queue, item, seed).receive(timeout)
+
+    def enqueue_request(self, op, req, seed=None, callback=None, suite=SUITE_SHA256):
+        """Device queues: builds the ABI item of one request, shaped as for the
+        batch helpers (sign_batch ... proof_verify_batch), and queues it on the
+        queue of operation op (OP_*) under `suite`; the receiver's output() is
+        the signature or proof once replied."""
+        if self._processor is not None:
+            raise ValueError("enqueue_request needs a device queue")
+        if suite not in (SUITE_SHA256, SUITE_SHAKE256) or not 0 <= op < 4:
+            raise ValueError("unknown operation or ciphersuite")
+        k = _Keep()
+        buf = None
+        if op == OP_SIGN:
+            sk, pk, hdr, msgs = req
+            ob, buf = k.out(80)
+            items = (SignItem * 1)()
+            items[0] = SignItem(k.bytes(sk), k.bytes(pk), k.bytes(hdr), k.slices(msgs), len(msgs), ob)
+        elif op == OP_PROOF_GEN:
+            items, bufs = _proof_gen_items(k, [req])
+            buf = bufs[0]
+        else:
+            items = _op_items(op, [req], k)
+        rec = self.enqueue(serve_queue(op, suite), items[0], seed, callback)
+        rec._attach(k, items, buf, op)
+        return rec
+
+    def snapshot(self, queue=-1, counts_len=None):
+        """The batcher's metrics (BatcherSnapshot, batcher.rs:86-97) of one queue,
+        or of all with queue -1; batch_size_counts has counts_len entries
+        (default: the largest max_batch_items + 1)."""
+        if counts_len is None:
+            qs = [queue] if queue >= 0 else range(SERVE_MAX_QUEUES)
+            counts_len = max(self.config(q)["max_batch_items"] for q in qs) + 1
+        snap = ServeSnapshot()
+        counts = (ctypes.c_uint64 * max(1, counts_len))()
+        rc = self._lib.cubbs_bbs_gpu_serve_snapshot(self._handle, queue, ctypes.byref(snap), counts,
+                                                    ctypes.c_size_t(counts_len))
+        if rc:
+            raise ValueError(f"serve_snapshot returned {rc}")
+        out = {f: getattr(snap, f) for f, _ in ServeSnapshot._fields_}
+        out["batch_size_counts"] = list(counts)[:counts_len]
+        return out
+
+    def close(self):
+        """Serves what is queued, then frees the native queue."""
+        if self._handle:
+            self._lib.cubbs_bbs_gpu_serve_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # noqa: BLE001 - interpreter shutdown
+            pass
 
 
 def bench_device_steps(op, reqs, warmup, steps, seeds=None):

@@ -456,8 +456,10 @@ int32_t cubbs_bbs_gpu_proof_gen_t2_prepare_batch_v2(uint32_t abi_version,
  * oldest request waited longest, as many of its requests as fit in
  * max_batch_items and in the device-memory budget left by the running batches.
  * Items and their buffers are caller-owned and must stay alive until the
- * request's wait returns.  op: 0 Sign, 1 Verify, 2 ProofGen, 3 ProofVerify;
- * seed32 (ProofGen only, nullable) selects seeded blinding as in
+ * request's wait returns.  op: 0 Sign, 1 Verify, 2 ProofGen, 3 ProofVerify
+ * under BLS12-381-SHA-256, 4..7 the same under BLS12-381-SHAKE-256 (op & 3 is
+ * the operation, op >> 2 the CUBBS_BBS_CIPHERSUITE_* value), each its own
+ * queue; seed32 (ProofGen only, nullable) selects seeded blinding as in
  * cubbs_bbs_gpu_proof_gen_seeded_batch_v2, else OS randomness.  The result of
  * a request equals the result of the same request in a batch of its own. */
 typedef struct CuBbsBbsGpuServeConfig {
@@ -471,7 +473,80 @@ int32_t cubbs_bbs_gpu_serve_create(uint32_t abi_version, const CuBbsBbsGpuServeC
 int32_t cubbs_bbs_gpu_serve_submit(void *server, int32_t op, void *item, const uint8_t *seed32,
                                    uint64_t *ticket);
 int32_t cubbs_bbs_gpu_serve_wait(void *server, uint64_t ticket, CuBbsBbsGpuResult *result);
+/* Stops taking requests, serves every request still queued (their waits and
+ * callbacks complete), then frees the server. */
 int32_t cubbs_bbs_gpu_serve_destroy(void *server);
+
+/* Batcher settings of one queue, the per-operation BatcherConfig of the
+ * reference W3C service (crates/cubbs-w3c-service/src/batcher.rs:21-60):
+ *   max_batch_items <- max_batch_size (0: the server's max_batch_items);
+ *   max_inflight    <- pipelines, running batches of this queue, under the
+ *                      server's max_inflight slots shared by all queues
+ *                      (spawn_with_slots, batcher.rs:142-167) (0: no limit);
+ *   coalesce_us     <- interval_ms * 1000: a free slot that finds a partial
+ *                      batch waits up to this long for it to fill; a full
+ *                      batch leaves at once (batcher.rs:254-268) (0: none);
+ *   queue_capacity  <- queue_capacity: submit waits while the queue holds
+ *                      this many requests, like the batcher's bounded channel
+ *                      (0: unbounded).
+ * A new server's queues have {server max_batch_items, 0, 0, 0}. */
+#define CUBBS_BBS_GPU_SERVE_MAX_QUEUES 8
+typedef struct CuBbsBbsGpuServeQueueConfig {
+  uint32_t max_batch_items;
+  uint32_t max_inflight;
+  uint32_t coalesce_us;
+  uint32_t queue_capacity;
+} CuBbsBbsGpuServeQueueConfig;
+
+/* BatcherSnapshot (batcher.rs:86-97) of one queue, or of all with queue -1:
+ * queued = submitted and not yet dispatched; last_batch_size of all queues is
+ * the most recent dispatch of any queue; queue wait = submit to dispatch. */
+typedef struct CuBbsBbsGpuServeSnapshot {
+  uint64_t queued;
+  uint64_t dispatches;
+  uint64_t dispatched_items;
+  uint64_t max_observed_batch;
+  uint64_t last_batch_size;
+  uint64_t inflight_batches;
+  double total_queue_wait_ms;
+  double average_queue_wait_ms;
+} CuBbsBbsGpuServeSnapshot;
+
+/* Completion callback of cubbs_bbs_gpu_serve_submit_notify, called once per
+ * request on a dispatch thread, outside the server's lock (it may submit
+ * again); *result is valid only during the call. */
+typedef void (*CuBbsBbsGpuServeDone)(void *ctx, uint64_t ticket, const CuBbsBbsGpuResult *result);
+/* Batch processor of a server made by cubbs_bbs_gpu_serve_create_with_processor:
+ * processes items[0..count) of one queue and fills results[0..count); a
+ * nonzero return fails every request of the batch with that code. */
+typedef int32_t (*CuBbsBbsGpuServeProcessor)(void *ctx, int32_t queue, void *const *items, size_t count,
+                                             CuBbsBbsGpuResult *results);
+
+/* queue selects the operation queue (as op above); config NULL only reads the
+ * settings in force into *effective (nullable), which mirrors
+ * BatchQueue::config (batcher.rs:196-198). */
+int32_t cubbs_bbs_gpu_serve_configure_queue(void *server, int32_t queue,
+                                            const CuBbsBbsGpuServeQueueConfig *config,
+                                            CuBbsBbsGpuServeQueueConfig *effective);
+/* Like cubbs_bbs_gpu_serve_submit, but the result is delivered to done(ctx,
+ * ticket, result) instead of a wait (BatchQueue::enqueue and its oneshot
+ * reply, batcher.rs:171-190).  *ticket (nullable) is set before return; the
+ * ticket is not waitable. */
+int32_t cubbs_bbs_gpu_serve_submit_notify(void *server, int32_t op, void *item, const uint8_t *seed32,
+                                          CuBbsBbsGpuServeDone done, void *ctx, uint64_t *ticket);
+/* batch_size_counts[k] (k < counts_len; nullable when counts_len is 0) =
+ * batches of k requests dispatched, as BatcherSnapshot::batch_size_counts. */
+int32_t cubbs_bbs_gpu_serve_snapshot(void *server, int32_t queue, CuBbsBbsGpuServeSnapshot *out,
+                                     uint64_t *batch_size_counts, size_t counts_len);
+/* A server whose batches go to `processor` instead of the device: the
+ * reference's BatchQueue::spawn(config, processor) (batcher.rs:130-140) for
+ * callers that batch their own items (the service's JSON-LD stages).  Queues
+ * 0..CUBBS_BBS_GPU_SERVE_MAX_QUEUES-1; no device-memory admission; max_inflight
+ * 0 means 1.  No CUDA call is made on this server's behalf. */
+int32_t cubbs_bbs_gpu_serve_create_with_processor(uint32_t abi_version,
+                                                  const CuBbsBbsGpuServeConfig *config,
+                                                  CuBbsBbsGpuServeProcessor processor, void *ctx,
+                                                  void **server);
 /* Load replay for benchmarks and tests: request i arrives arrival_ns[i] after
  * the start (non-decreasing); mode 0 serves through the queue, mode 1 through
  * plain fixed-size batches (plain_batch requests, flushed after

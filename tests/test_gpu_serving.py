@@ -101,3 +101,62 @@ def test_mixed_results_equal_alone(gpu, pool_and_alone, mode, batch, budget, arr
     want = [alone[i] for i, _ in schedule]
     assert got == want
     assert all(x > 0 for x in lat) and wall > 0
+
+
+@pytest.mark.parametrize("coalesce_us,batch", [(2000, 128), (0, 4)])
+def test_batcher_client_results_equal_alone(gpu, pool_and_alone, coalesce_us, batch):
+    """The queue as the W3C batcher's replacement: per-operation batcher
+    settings (window, batch size, capacity, pipelines under the shared slots),
+    one request per enqueue with a reply callback or a receive, results equal
+    to each request alone, and the snapshot counting every dispatch."""
+    pool, alone = pool_and_alone
+    rng = random.Random(11)
+    order = list(range(len(pool)))
+    rng.shuffle(order)
+    with gpu.ServeQueue(max_inflight=4) as q:
+        for op in (gpu.OP_SIGN, gpu.OP_VERIFY, gpu.OP_PROOF_GEN, gpu.OP_PROOF_VERIFY):
+            q.configure(op, max_batch_items=batch, max_inflight=2, coalesce_us=coalesce_us, queue_capacity=64)
+        replies = {}
+        recs = []
+        for i in order:
+            op, req, sd = pool[i]
+            recs.append((i, q.enqueue_request(op, req, seed=sd,
+                                              callback=lambda reply, i=i: replies.__setitem__(i, reply))))
+        for i, rec in recs:
+            code, value, _ = rec.receive(60)
+            op = pool[i][0]
+            got = (code, rec.output()) if op in (gpu.OP_SIGN, gpu.OP_PROOF_GEN) else (code, bool(value))
+            assert got == alone[i], (i, op)
+            assert replies[i][0] == code
+        total = q.snapshot(-1)
+        assert total["dispatched_items"] == len(pool) and total["queued"] == 0
+        for op in range(4):
+            s = q.snapshot(op)
+            n = sum(1 for o, _, _ in pool if o == op)
+            assert s["dispatched_items"] == n
+            assert sum(k * c for k, c in enumerate(s["batch_size_counts"])) == n
+            assert s["max_observed_batch"] <= batch
+
+
+def test_batcher_client_shake256_queues(gpu, pool_and_alone):
+    """Queues 4..7 serve the same operations under BLS12-381-SHAKE-256: each
+    reply equals the SHAKE-256 batch entry on the same request alone."""
+    pool, _ = pool_and_alone
+    sub = pool[:16]
+    with gpu.ServeQueue(max_inflight=2) as q:
+        for op in range(4):
+            q.configure(gpu.serve_queue(op, gpu.SUITE_SHAKE256), max_batch_items=8, coalesce_us=500)
+        recs = [q.enqueue_request(op, req, seed=sd, suite=gpu.SUITE_SHAKE256) for op, req, sd in sub]
+        for (op, req, sd), rec in zip(sub, recs):
+            code, value, _ = rec.receive(60)
+            if op == gpu.OP_SIGN:
+                assert (code, rec.output()) == tuple(gpu.sign_batch([req], suite=gpu.SUITE_SHAKE256)[0])
+            elif op == gpu.OP_PROOF_GEN:
+                want = gpu.proof_gen_batch([req], seeds=[sd], suite=gpu.SUITE_SHAKE256)[0]
+                assert (code, rec.output()) == tuple(want)
+            elif op == gpu.OP_VERIFY:
+                assert (code, bool(value)) == tuple(gpu.verify_batch([req], suite=gpu.SUITE_SHAKE256)[0])
+            else:
+                assert (code, bool(value)) == tuple(gpu.proof_verify_batch([req], suite=gpu.SUITE_SHAKE256)[0])
+        assert q.snapshot(-1)["dispatched_items"] == len(sub)
+        assert sum(q.snapshot(op)["dispatched_items"] for op in range(4)) == 0
