@@ -557,7 +557,7 @@ def table_window():
     return w.value
 
 
-def fixed_msm_autotune(scalars_be, rows, terms, w_lo=4, w_hi=16, steps=3, with_mismatches=False):
+def fixed_msm_autotune(scalars_be, rows, terms, w_lo=4, w_hi=20, steps=3, with_mismatches=False):
     """Times the fixed-base MSM kernel over rows x terms scalars (bases: the first
     `terms` resident generators) for table window widths w_lo..w_hi, after
     checking each width's first 64 rows against a table-free recomputation; the
@@ -1170,6 +1170,25 @@ def int_peaks():
     if fn(ctypes.cast(ctypes.pointer(a), ctypes.c_void_p), ctypes.cast(ctypes.pointer(b), ctypes.c_void_p)):
         raise RuntimeError("int_peaks failed")
     return a.value, b.value
+
+
+PAIRING_PROGRAMS = ["DBL", "ADD", "DBL1", "ADD1", "MUL_F_F_X", "CONJ_F", "INV_U_F", "EASY1_T", "EASY2_T",
+                    "COPY_R_T", "COPY_R_A", "COPY_R_X", "CYCLO_R", "MUL_R_R_T", "MUL_R_R_A", "MUL_R_R_X", "S1_A",
+                    "S2_A", "S3_A", "S4_X", "S5_R", "MUL_R_R_CA"]
+
+
+def pairing_probe(wide=False):
+    """SM cycles of one run of each pairing program on a lone team (one warp, or
+    two with wide=True): {program name: cycles}."""
+    buf = (ctypes.c_double * 64)()
+    name = "cubbs_bbs_gpu_pairing_probe_wide_for_test_v2" if wide else "cubbs_bbs_gpu_pairing_probe_for_test_v2"
+    fn = getattr(lib(), name)
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_int32]
+    n = fn(ctypes.cast(buf, ctypes.c_void_p), 64)
+    if n != len(PAIRING_PROGRAMS):
+        raise RuntimeError(f"{name} returned {n}")
+    return {k: buf[i] for i, k in enumerate(PAIRING_PROGRAMS)}
 
 
 def prepared_call(op, reqs):

@@ -3,8 +3,8 @@
 
 A 2-pair pairing check (Miller loop over precomputed lines, final
 exponentiation) is a fixed sequence of Fp12 operations.  Each operation is
-compiled here into a *program* of phases that one warp (32 lanes) runs over a
-per-check array of Fp slots in shared memory:
+compiled here into a *program* of phases that a team of lanes (one warp of 32,
+or two warps of 64) runs over a per-check array of Fp slots in shared memory:
 
   MUL phase : lane l computes slot[out] = (sum_i k_i slot[a_i]) * (sum_j k_j slot[b_j])
               (one Fp product of two short weighted sums, at most 7 terms each)
@@ -21,8 +21,8 @@ products become MUL nodes and whose additions stay weighted linear forms until
 a product or an output needs them.  A form of at most KMUL terms is summed by
 the product's own lane; a longer one becomes a LIN node.  A LIN node whose
 only use is inside another sum is folded into it while the sum stays within
-its width.  The graph is scheduled greedily into LIN / MUL phases (at most 32
-nodes each, longest path first), temporaries get slots by liveness, and every
+its width.  The graph is scheduled greedily into LIN / MUL phases (at most one
+node per lane of the team, longest path first), temporaries get slots by liveness, and every
 program is checked numerically against an independent schoolbook Fp12 (tower
 Fp2 = Fp[u]/(u^2+1), Fp6 = Fp2[v]/(v^3 - (1+u)), Fp12 = Fp6[w]/(w^2 - v))
 before it is emitted.  Each program is compiled under a few settings (LIN
@@ -795,7 +795,7 @@ def _term(c, sl):
     return sl | ((c & 0x7F) << SLOT_BITS)
 
 
-def phase_words(ptype, entries):
+def phase_words(ptype, entries, lanes):
     """16 u16 words per lane: out, type word, terms 0..6 (LIN terms / operand a),
     terms 7..13 (LIN terms / operand b)."""
     pad = lambda terms, n, unit: list(terms) + [(1 if unit else 0, ZERO_SLOT)] * (n - len(terms))
@@ -813,7 +813,7 @@ def phase_words(ptype, entries):
         assert width <= WLIN_MAX
         unit = _unit(entries)
         tw = T_LIN << 12 | width | (F_UNIT_OR_PLAIN_A if unit else 0)
-    for l in range(LANES):
+    for l in range(lanes):
         u = [NONE, tw] + [_term(0, ZERO_SLOT)] * 14
         if l < len(entries):
             out, op, args = entries[l]
@@ -829,13 +829,51 @@ def phase_words(ptype, entries):
     return rows
 
 
-def emit(progs):
-    nslot = TMP_BASE + max(p.ntmp for p in progs)
+def _table_lines(progs, lanes, sfx):
+    """PP_PROG_FIRST<sfx> and PP_ENTRY<sfx> for one team width."""
+    first, ents, nph = [], [], 0
+    for p in progs:
+        first.append(nph)
+        for ptype, entries in p.phases:
+            assert len(entries) <= lanes
+            nph += 1
+            row = []
+            for u in phase_words(ptype, entries, lanes):
+                w = [u[2 * k] | (u[2 * k + 1] << 16) for k in range(8)]
+                row.append("{0x%08x, 0x%08x, 0x%08x, 0x%08x}, {0x%08x, 0x%08x, 0x%08x, 0x%08x}" % tuple(w))
+            ents.append("  " + ", ".join(row) + ",")
+    first.append(nph)
+    lines = ["#define PP_NPHASE%s %d" % (sfx, nph),
+             "__device__ const uint16_t PP_PROG_FIRST%s[PP_NPROG + 1] = {%s};" % (sfx, ", ".join(map(str, first))),
+             "__device__ const uint4 PP_ENTRY%s[PP_NPHASE%s * PP_LANES%s * 2] = {" % (sfx, sfx, sfx)]
+    return lines + ents + ["};"]
+
+
+def _summary(progs, lanes):
+    out = ["// %d lanes:" % lanes]
+    for p in progs:
+        desc = ""
+        for t, e in p.phases:
+            if t == 1:
+                desc += "M"
+            elif t == 2:
+                desc += "I"
+            else:
+                desc += "L" if _unit(e) else "W"
+        out.append("// %-11s %3d phases (%s), %3d products, %3d temporaries, ~%d cycles" %
+                   (p.name, len(p.phases), desc, p.nmul, p.ntmp, program_cost(p)))
+    return out
+
+
+def emit(sets):
+    """sets: [(lanes, programs)], the one-warp team first."""
+    nslot = TMP_BASE + max(p.ntmp for _, progs in sets for p in progs)
     assert nslot <= 1 << SLOT_BITS
     lines = ["// GENERATED by gen_pairing_program.py -- do not edit by hand.",
              "// Phase tables of the warp-per-check pairing (see pairing_team.cuh).",
              "#pragma once", "#include <stdint.h>", "",
-             "#define PP_LANES %d" % LANES, "#define PP_NONE 0x%04x" % NONE,
+             "#define PP_LANES %d" % sets[0][0], "#define PP_LANES_W %d" % sets[1][0],
+             "#define PP_NONE 0x%04x" % NONE,
              "#define PP_SLOTS %d" % nslot, "#define PP_LINE_BASE %d" % LINE_BASE,
              "#define PP_PT_BASE %d" % PT_BASE, "#define PP_GAMMA_BASE %d" % GAMMA_BASE,
              "#define PP_ZERO_SLOT %d" % ZERO_SLOT,
@@ -846,51 +884,37 @@ def emit(progs):
              "#define PP_F_PLAIN_A 0x%03x // MUL: operand a is one slot with coefficient 1" % F_UNIT_OR_PLAIN_A,
              "#define PP_F_PLAIN_B 0x%03x // MUL: operand b likewise" % F_PLAIN_B, ""]
     lines.append("enum {" + ", ".join("PP_" + n for n in ORDER) + ", PP_NPROG };")
-    first, ents, nph = [], [], 0
-    for p in progs:
-        first.append(nph)
-        for ptype, entries in p.phases:
-            nph += 1
-            row = []
-            for u in phase_words(ptype, entries):
-                w = [u[2 * k] | (u[2 * k + 1] << 16) for k in range(8)]
-                row.append("{0x%08x, 0x%08x, 0x%08x, 0x%08x}, {0x%08x, 0x%08x, 0x%08x, 0x%08x}" % tuple(w))
-            ents.append("  " + ", ".join(row) + ",")
-    first.append(nph)
-    lines.append("#define PP_NPHASE %d" % nph)
-    lines.append("__device__ const uint16_t PP_PROG_FIRST[PP_NPROG + 1] = {" + ", ".join(map(str, first)) + "};")
     lines.append("// Two uint4 per (phase, lane), as 16 u16: out slot (PP_NONE: idle lane); type << 12 |")
     lines.append("// flags | nb << 4 | na (LIN: na = term count, the same on every lane of the phase);")
     lines.append("// terms 0..6 (LIN terms, MUL operand a); terms 7..13 (LIN terms, MUL operand b).")
     lines.append("// A term is slot | (signed 7-bit coefficient) << 9; short sums are padded with the zero slot.")
-    lines.append("__device__ const uint4 PP_ENTRY[PP_NPHASE * PP_LANES * 2] = {")
-    lines += ents
-    lines.append("};")
+    lines.append("// PP_*: one-warp teams (PP_LANES lanes); PP_*_W: two-warp teams (PP_LANES_W lanes).")
+    lines += _table_lines(sets[0][1], sets[0][0], "")
+    lines += _table_lines(sets[1][1], sets[1][0], "_W")
     summary = []
-    for p in progs:
-        desc = ""
-        for t, e in p.phases:
-            if t == 1:
-                desc += "M"
-            elif t == 2:
-                desc += "I"
-            else:
-                desc += "L" if _unit(e) else "W"
-        summary.append("// %-11s %3d phases (%s), %3d products, %3d temporaries, ~%d cycles" %
-                       (p.name, len(p.phases), desc, p.nmul, p.ntmp, program_cost(p)))
+    for lanes, progs in sets:
+        summary += _summary(progs, lanes)
     return "\n".join(lines[:4] + summary + lines[4:]) + "\n"
+
+
+def compile_all(lanes, rng):
+    """Every program for a team of `lanes` lanes (phases of at most that many entries)."""
+    global LANES
+    LANES = lanes
+    return [best_program(name, rng) for name in ORDER]
 
 
 def main():
     rng = random.Random(20240601)
-    progs = [best_program(name, rng) for name in ORDER]
-    text = emit(progs)
+    sets = [(32, compile_all(32, rng)), (64, compile_all(64, rng))]
+    text = emit(sets)
     if "--check-only" not in sys.argv:
         out = pathlib.Path(__file__).resolve().parent / "pairing_program.cuh"
         out.write_text(text)
-        print("wrote", out, "phases:", sum(len(p.phases) for p in progs))
-    for p in progs:
-        print("%-11s %3d phases ~%6d cycles  %s" % (p.name, len(p.phases), program_cost(p), p.cfg))
+        print("wrote", out, "phases:", [sum(len(p.phases) for p in progs) for _, progs in sets])
+    for lanes, progs in sets:
+        for p in progs:
+            print("%2d lanes %-11s %3d phases ~%6d cycles  %s" % (lanes, p.name, len(p.phases), program_cost(p), p.cfg))
 
 
 if __name__ == "__main__":

@@ -112,10 +112,10 @@ __global__ void __launch_bounds__(128) k_pv_rows(PvItem *items, uint32_t n, cons
   }
 }
 
-// The four variable-base jobs of each proof (Bbar*c, Abar*e^, D*r1^, D*r3^),
-// from the untouched input items and the decoded points; a proof whose points
-// or scalars do not decode gets jobs at infinity (k_pv_rows and k_pv_finish
-// mark it invalid).
+// The four variable-base jobs of each proof, from the untouched input items
+// and the decoded points: the terms of T1 (Bbar*c, Abar*e^, D*r1^) as jobs
+// 3i .. 3i+2 and D*r3^ as job 3n + i; a proof whose points or scalars do not
+// decode gets jobs at infinity (k_pv_rows and k_pv_finish mark it invalid).
 __global__ void __launch_bounds__(128) k_pv_jobs(const PvItem *items0, uint32_t n, const uint8_t *blob,
                                                  const int32_t *dec_status, VarJob *jobs, fr *jscal) {
   uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -129,19 +129,20 @@ __global__ void __launch_bounds__(128) k_pv_jobs(const PvItem *items0, uint32_t 
   if (ok) ok = fr_raw_from_be32(pr + 144, ecap) && fr_raw_from_be32(pr + 176, r1cap) &&
                fr_raw_from_be32(pr + 208, r3cap) && fr_raw_from_be32(pr + 240 + 32 * it.U, c);
   if (!ok) {
-    for (int k = 0; k < 4; k++) jobs[4 * i + k] = {0, 1};
+    for (int k = 0; k < 3; k++) jobs[3 * i + k] = {0, 1};
+    jobs[3 * n + i] = {0, 1};
     return;
   }
   // points: 3i+0 Abar, 3i+1 Bbar, 3i+2 D
   uint32_t fa = dec_status[3 * i] == DEC_INF, fb = dec_status[3 * i + 1] == DEC_INF, fd = dec_status[3 * i + 2] == DEC_INF;
-  jobs[4 * i + 0] = {3 * i + 1, fb};
-  jscal[4 * i + 0] = c;
-  jobs[4 * i + 1] = {3 * i + 0, fa};
-  jscal[4 * i + 1] = ecap;
-  jobs[4 * i + 2] = {3 * i + 2, fd};
-  jscal[4 * i + 2] = r1cap;
-  jobs[4 * i + 3] = {3 * i + 2, fd};
-  jscal[4 * i + 3] = r3cap;
+  jobs[3 * i + 0] = {3 * i + 1, fb};
+  jscal[3 * i + 0] = c;
+  jobs[3 * i + 1] = {3 * i + 0, fa};
+  jscal[3 * i + 1] = ecap;
+  jobs[3 * i + 2] = {3 * i + 2, fd};
+  jscal[3 * i + 2] = r1cap;
+  jobs[3 * n + i] = {3 * i + 2, fd};
+  jscal[3 * n + i] = r3cap;
 }
 
 // Pairing job of each proof, built from the untouched input items and the
@@ -380,8 +381,8 @@ __global__ void __launch_bounds__(64) k_pv_finish(PvItem *items, uint32_t n, con
   }
   g1 T1 = g1_inf(), T2 = g1_inf();
   if (act) {
-    T1 = g1_add(g1_add(v[4 * i], v[4 * i + 1]), v[4 * i + 2]);
-    T2 = g1_add(t2fix[i], v[4 * i + 3]);
+    T1 = g1_add(g1_add(v[3 * i], v[3 * i + 1]), v[3 * i + 2]);
+    T2 = g1_add(t2fix[i], v[3 * n + i]);
   }
   const g1 T[2] = {T1, T2};
   g1a aff[2];

@@ -30,34 +30,52 @@ __global__ void __launch_bounds__(128) k_g1_decode(const uint8_t *pts, uint32_t 
   status[i] = st;
 }
 
-// One thread per (generator, window): entries d * 2^(w k) G_g for d = 1..half,
-// normalised to affine with one batched inversion.
-__global__ void __launch_bounds__(64) k_table_build(const g1a *gens, int g0, int g1n, FixedTable t, g1 *scratch,
-                                                    fp *prod) {
-  int tid = blockIdx.x * blockDim.x + threadIdx.x;
-  int total = (g1n - g0) * t.nwin;
-  if (tid >= total) return;
-  int g = g0 + tid / t.nwin, k = tid % t.nwin;
+// Window bases of a table chunk: bases[(g - g0) * nwin + k] = 2^(w k) G_g in
+// affine form, one thread per (generator, window).
+__global__ void __launch_bounds__(64) k_table_bases(const g1a *gens, int g0, int g1n, FixedTable t, g1a *bases) {
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tid >= (g1n - g0) * t.nwin) return;
+  const int g = g0 + tid / t.nwin, k = tid % t.nwin;
   g1 B = g1_from_aff(gens[g]);
   #pragma unroll 1
   for (int i = 0; i < t.w * k; i++) B = g1_dbl(B);
-  g1a Ba;
-  g1_to_aff(B, Ba);
-  g1 *E = scratch + (size_t)tid * t.half;
-  fp *Pp = prod + (size_t)tid * t.half;
+  g1_to_aff(B, bases[tid]);
+}
+
+// Table entries d * B for d = 1..half of every window base B, one thread per
+// run of `run` consecutive entries: the thread reaches (d0 + 1) B by double-
+// and-add from B, adds B for each further entry and normalises its run to
+// affine with one batched inversion.  The runs keep the build parallel at
+// wide windows (2^19 entries per window at w = 20).
+__global__ void __launch_bounds__(64) k_table_build(const g1a *bases, int g0, int g1n, FixedTable t, int run,
+                                                    g1 *scratch, fp *prod) {
+  const size_t tid = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int runs = t.half / run;
+  if (tid >= (size_t)(g1n - g0) * t.nwin * runs) return;
+  const size_t base_i = tid / runs;
+  const int d0 = (int)(tid % runs) * run;
+  const g1a Ba = bases[base_i];
   g1 e = g1_from_aff(Ba);
+  const uint32_t m = (uint32_t)d0 + 1;  // e = m * B
+  #pragma unroll 1
+  for (int b = 30 - __clz(m); b >= 0; b--) {
+    e = g1_dbl(e);
+    if ((m >> b) & 1) e = g1_add_aff(e, Ba);
+  }
+  g1 *E = scratch + tid * run;
+  fp *Pp = prod + tid * run;
   fp acc = fp_one();
   #pragma unroll 1
-  for (int j = 0; j < t.half; j++) {
+  for (int j = 0; j < run; j++) {
     if (j > 0) e = g1_add_aff(e, Ba);
     E[j] = e;
     acc = fp_mul(acc, fp_mul(e.ZZ, e.ZZZ));
     Pp[j] = acc;
   }
   fp inv = fp_inv(acc);  // inverse of prod_j ZZ_j ZZZ_j
-  g1a *dst = t.entries + ((size_t)g * t.nwin + k) * t.half;
+  g1a *dst = t.entries + ((size_t)g0 * t.nwin + base_i) * t.half + d0;
   #pragma unroll 1
-  for (int j = t.half - 1; j >= 0; j--) {
+  for (int j = run - 1; j >= 0; j--) {
     fp zinv = j > 0 ? fp_mul(inv, Pp[j - 1]) : inv;  // 1 / (ZZ_j ZZZ_j)
     g1 ej = E[j];
     inv = fp_mul(inv, fp_mul(ej.ZZ, ej.ZZZ));
@@ -250,9 +268,13 @@ void launch_g1_decode(cudaStream_t s, const uint8_t *pts48, uint32_t stride, uin
                       bool check_subgroup) {
   if (n) k_g1_decode<<<blocks_for(n, 128), 128, 0, s>>>(pts48, stride, n, out, status, check_subgroup);
 }
-void launch_build_table(cudaStream_t s, const g1a *gens, int g0, int g1n, FixedTable t, g1 *scratch, fp *prod) {
-  int total = (g1n - g0) * t.nwin;
-  if (total > 0) k_table_build<<<blocks_for(total, 64), 64, 0, s>>>(gens, g0, g1n, t, scratch, prod);
+void launch_build_table(cudaStream_t s, const g1a *gens, int g0, int g1n, FixedTable t, g1a *bases, g1 *scratch,
+                        fp *prod) {
+  const int nb = (g1n - g0) * t.nwin;
+  if (nb <= 0) return;
+  k_table_bases<<<blocks_for(nb, 64), 64, 0, s>>>(gens, g0, g1n, t, bases);
+  const int run = std::min(t.half, 256);
+  k_table_build<<<blocks_for((size_t)nb * (t.half / run), 64), 64, 0, s>>>(bases, g0, g1n, t, run, scratch, prod);
 }
 void launch_fixed_msm(cudaStream_t s, const FixedTable &t, const fr *scalars, uint32_t stride,
                       const uint32_t *nterms, uint32_t rows, g1 *out) {

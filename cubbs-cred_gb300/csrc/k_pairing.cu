@@ -6,6 +6,8 @@
 // Reference: G2 line precompute by BLST on the host (g1_msm_blst.cpp:441-486),
 // Miller loop over precomputed lines and final-verify kernels
 // (native/cuda/src/kernels/pairing.cuh:376-478, host :579-737).
+#include <cstdlib>
+
 #include "pairing_team.cuh"
 #include "runtime.cuh"
 
@@ -88,14 +90,56 @@ __global__ void __launch_bounds__(64) k_pairing_check_split(const PairJob *jobs,
   if (lane == 0) ok[item] = one ? 1 : 0;
 }
 
+// The same with a two-warp team per pair (four warps per check): team t runs
+// the Miller loop of pair t on named barrier 1 + t, then team 0 multiplies
+// the two values and runs the final exponentiation.  Phases of up to 64
+// products take one round (pairing_team.cuh).
+__global__ void __launch_bounds__(128) k_pairing_check_split_wide(const PairJob *jobs, uint32_t n,
+                                                                  const line2 *lines, uint8_t *ok) {
+  extern __shared__ __align__(16) uint8_t pp_smem[];
+  const int team = threadIdx.x >> 6, lane = threadIdx.x & 63, bar = 1 + team;
+  fp *sl = reinterpret_cast<fp *>(pp_smem) + team * PP_SLOTS;
+  const uint32_t item = blockIdx.x;
+  if (item >= n) return;
+  const PairJob &j = jobs[item];
+  if (j.active != 1) {  // 0: not evaluated (result 0); 2: settled before the launch (ok[item] kept)
+    if (threadIdx.x == 0 && j.active == 0) ok[item] = 0;
+    return;
+  }
+  const bool skip = (j.flags >> team) & 1;
+  const line2 *L = lines + (size_t)(team ? j.slot_b : j.slot_a) * MILLER_LINES;
+  pp::miller_one<64>(sl, lane, team ? j.pb : j.pa, L, skip, bar);
+  __syncthreads();
+  if (team != 0) return;
+  if (lane < 12) pp::st(sl, PP_REG(PP_REG_X) + lane, pp::ld(sl + PP_SLOTS, PP_REG(PP_REG_F) + lane));
+  pp::team_sync<64>(bar);
+  pp::run<64>(sl, lane, PP_MUL_F_F_X, bar);
+  pp::run<64>(sl, lane, PP_CONJ_F, bar);  // z < 0
+  const bool one = pp::final_exp_is_one<64>(sl, lane, bar);
+  if (lane == 0) ok[item] = one ? 1 : 0;
+}
+
+// Two-warp teams unless CUBBS_BBS_PAIR_TEAM=32 (one warp per pair).
+static bool wide_pair_teams() {
+  static const bool v = [] {
+    const char *e = std::getenv("CUBBS_BBS_PAIR_TEAM");
+    return !(e && std::atoi(e) == 32);
+  }();
+  return v;
+}
+
 void launch_pairing_check_split(cudaStream_t s, const PairJob *jobs, uint32_t n, const line2 *lines, uint8_t *ok) {
   const size_t smem = 2 * (size_t)PP_SLOTS * sizeof(fp);
   static const bool attr = [smem] {
     CUBBS_CHECK(cudaFuncSetAttribute(k_pairing_check_split, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    CUBBS_CHECK(
+        cudaFuncSetAttribute(k_pairing_check_split_wide, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
     return true;
   }();
   (void)attr;
-  if (n) k_pairing_check_split<<<n, 64, smem, s>>>(jobs, n, lines, ok);
+  if (!n) return;
+  if (wide_pair_teams()) k_pairing_check_split_wide<<<n, 128, smem, s>>>(jobs, n, lines, ok);
+  else k_pairing_check_split<<<n, 64, smem, s>>>(jobs, n, lines, ok);
 }
 
 // Latency probe: SM cycles of one run of each pairing program on a lone warp
@@ -112,6 +156,40 @@ __global__ void __launch_bounds__(32) k_pp_probe(double *cycles, int reps) {
     for (int r = 0; r < reps; r++) pp::run(sl, lane, prog);
     const long long t1 = clock64();
     if (lane == 0) cycles[prog] = (double)(t1 - t0) / reps;
+  }
+}
+
+// The same for two-warp teams (one block of 64 threads, the PP_ENTRY_W tables).
+__global__ void __launch_bounds__(64) k_pp_probe_wide(double *cycles, int reps) {
+  extern __shared__ __align__(16) uint8_t pp_smem[];
+  fp *sl = reinterpret_cast<fp *>(pp_smem);
+  const int lane = threadIdx.x;
+  for (int i = lane; i < PP_SLOTS; i += 64) pp::st(sl, i, fp_one());
+  __syncthreads();
+  for (int prog = 0; prog < PP_NPROG; prog++) {
+    const long long t0 = clock64();
+#pragma unroll 1
+    for (int r = 0; r < reps; r++) pp::run<64>(sl, lane, prog, 1);
+    const long long t1 = clock64();
+    if (lane == 0) cycles[prog] = (double)(t1 - t0) / reps;
+  }
+}
+
+extern "C" int32_t cubbs_bbs_gpu_pairing_probe_wide_for_test_v2(double *cycles, int32_t cap) {
+  if (!cycles || cap < PP_NPROG) return -1;
+  try {
+    CallScope scope;
+    Runtime &rt = scope.rt;
+    double *d = rt.arena.alloc<double>(PP_NPROG);
+    const size_t smem = (size_t)PP_SLOTS * sizeof(fp);
+    k_pp_probe_wide<<<1, 64, smem, rt.stream>>>(d, 2);  // warm-up
+    k_pp_probe_wide<<<1, 64, smem, rt.stream>>>(d, 16);
+    CUBBS_CHECK(cudaGetLastError());
+    CUBBS_CHECK(cudaMemcpyAsync(cycles, d, PP_NPROG * sizeof(double), cudaMemcpyDeviceToHost, rt.stream));
+    CUBBS_CHECK(cudaStreamSynchronize(rt.stream));
+    return PP_NPROG;
+  } catch (const CudaError &) {
+    return -2;
   }
 }
 

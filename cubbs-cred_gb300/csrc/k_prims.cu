@@ -1117,7 +1117,7 @@ extern "C" int32_t cubbs_bbs_gpu_pairing_eq_aggregate_v2(uint32_t abi, const CuB
 extern "C" int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi, const uint8_t *scalars_be, size_t rows,
                                                        size_t terms, int32_t w_lo, int32_t w_hi, int32_t steps,
                                                        float *ms_per_w, int32_t *best_w, int32_t *mismatched) {
-  if (!abi_ok(abi) || !scalars_be || rows == 0 || terms == 0 || terms > 1024 || w_lo < 4 || w_hi > 16 ||
+  if (!abi_ok(abi) || !scalars_be || rows == 0 || terms == 0 || terms > 1024 || w_lo < 4 || w_hi > MAX_TABLE_WINDOW ||
       w_lo > w_hi || steps <= 0 || !ms_per_w || !best_w || !mismatched)
     return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
   ABI_GUARD_BEGIN

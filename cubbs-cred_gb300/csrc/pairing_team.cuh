@@ -19,6 +19,12 @@
 // Compared with a 16-lane team working at Fp2 granularity, a phase costs one
 // Fp product instead of three in a row, and the assembly of Karatsuba terms
 // is a few multiply-adds per lane instead of divergent per-lane code.
+//
+// A team is one warp or two: the programs are compiled for both widths, and a
+// two-warp team runs phases of up to 64 entries between named barriers, so an
+// Fp12 product or a Miller step's squaring (36..54 products) takes one round of
+// products instead of two.  Latency-bound checks (the group checks of an
+// aggregated batch, small batches) use two-warp teams.
 #pragma once
 #include "pairing.cuh"
 #include "pairing_program.cuh"
@@ -146,16 +152,32 @@ DEVNI fp wsum(const fp *sl, Terms q, int n) {
   return out;
 }
 
-// Runs program `prog` on the slot array of this warp's check.  The table
-// entry of the next phase is fetched while the current one computes.
-DEVNI void run(fp *sl, int lane, int prog) {
-  const int ph0 = PP_PROG_FIRST[prog], ph1 = PP_PROG_FIRST[prog + 1];
-  const uint4 *tab = PP_ENTRY + 2 * lane;
-  uint4 e0 = __ldg(&tab[2 * PP_LANES * ph0]), e1 = __ldg(&tab[2 * PP_LANES * ph0 + 1]);
+// Synchronisation of a team of W lanes: one warp (W = 32), or two consecutive
+// warps (W = 64) on named barrier `bar` (1..15; barrier 0 is __syncthreads),
+// which also orders their shared-memory accesses.
+template <int W> DEV void team_sync(int bar) {
+  if constexpr (W == 32) {
+    __syncwarp();
+  } else {
+    static_assert(W == 64, "teams are one or two warps");
+    asm volatile("bar.sync %0, 64;" ::"r"(bar) : "memory");
+  }
+}
+
+// Runs program `prog` on the slot array of this team's check, from the phase
+// tables of its width (PP_ENTRY: one warp; PP_ENTRY_W: two warps, whose
+// phases hold up to 64 entries, so an Fp12 product takes one round of
+// products instead of two).  The table entry of the next phase is fetched
+// while the current one computes.
+template <int W = 32> DEVNI void run(fp *sl, int lane, int prog, int bar = 0) {
+  const uint16_t *first = W == 32 ? PP_PROG_FIRST : PP_PROG_FIRST_W;
+  const int ph0 = first[prog], ph1 = first[prog + 1];
+  const uint4 *tab = (W == 32 ? PP_ENTRY : PP_ENTRY_W) + 2 * lane;
+  uint4 e0 = __ldg(&tab[2 * W * ph0]), e1 = __ldg(&tab[2 * W * ph0 + 1]);
 #pragma unroll 1
   for (int ph = ph0; ph < ph1; ph++) {
     const int nx = min(ph + 1, ph1 - 1);
-    const uint4 n0 = __ldg(&tab[2 * PP_LANES * nx]), n1 = __ldg(&tab[2 * PP_LANES * nx + 1]);
+    const uint4 n0 = __ldg(&tab[2 * W * nx]), n1 = __ldg(&tab[2 * W * nx + 1]);
     const uint32_t out = e0.x & 0xffffu, tw = e0.x >> 16, type = tw >> 12;
     const int na = (int)(tw & 15u), nb = (int)((tw >> 4) & 15u);
     const bool act = out != PP_NONE;
@@ -173,21 +195,21 @@ DEVNI void run(fp *sl, int lane, int prog) {
         r = fp_inv_vartime(ld(sl, e0.y & PP_SLOT_MASK));  // PP_INV: public value, variable time
       }
     }
-    __syncwarp();
+    team_sync<W>(bar);
     if (act) st(sl, out, r);
-    __syncwarp();
+    team_sync<W>(bar);
     e0 = n0;
     e1 = n1;
   }
 }
 
 // dst = base^|z| for base in the cyclotomic subgroup (dst register R).
-DEV void exp_by_zabs(fp *sl, int lane, int copy_prog, int mul_prog) {
-  run(sl, lane, copy_prog);
+template <int W = 32> DEV void exp_by_zabs(fp *sl, int lane, int copy_prog, int mul_prog, int bar = 0) {
+  run<W>(sl, lane, copy_prog, bar);
 #pragma unroll 1
   for (int i = 62; i >= 0; i--) {
-    run(sl, lane, PP_CYCLO_R);
-    if (zabs_bit(i)) run(sl, lane, mul_prog);
+    run<W>(sl, lane, PP_CYCLO_R, bar);
+    if (zabs_bit(i)) run<W>(sl, lane, mul_prog, bar);
   }
 }
 
@@ -195,30 +217,38 @@ DEV void exp_by_zabs(fp *sl, int lane, int copy_prog, int mul_prog) {
 // Same steps as final_exponentiation of pairing.cuh:
 //   t = conj(f) f^-1, t = t^(p^2) t;  a = t^z conj(t);  a = a^z conj(a);
 //   b = a^z a^p;  c = (b^z)^z b^(p^2) conj(b);  result c t^3.
-DEV bool final_exp_is_one(fp *sl, int lane) {
-  run(sl, lane, PP_INV_U_F);
-  run(sl, lane, PP_EASY1_T);
-  run(sl, lane, PP_EASY2_T);
-  exp_by_zabs(sl, lane, PP_COPY_R_T, PP_MUL_R_R_T);
-  run(sl, lane, PP_S1_A);  // a = conj(t^|z|) conj(t)
-  exp_by_zabs(sl, lane, PP_COPY_R_A, PP_MUL_R_R_A);
-  run(sl, lane, PP_S2_A);  // a = conj(a^|z|) conj(a)
-  exp_by_zabs(sl, lane, PP_COPY_R_A, PP_MUL_R_R_A);
-  run(sl, lane, PP_S3_A);  // b = conj(a^|z|) a^p
-  exp_by_zabs(sl, lane, PP_COPY_R_A, PP_MUL_R_R_A);
-  run(sl, lane, PP_S4_X);  // x = b^z
-  exp_by_zabs(sl, lane, PP_COPY_R_X, PP_MUL_R_R_X);
-  run(sl, lane, PP_S5_R);  // r = (b^z)^z b^(p^2)
-  run(sl, lane, PP_MUL_R_R_CA);  // r = r conj(b)
-  run(sl, lane, PP_MUL_R_R_T);
-  run(sl, lane, PP_MUL_R_R_T);
-  run(sl, lane, PP_MUL_R_R_T);
-  bool mine = true;
-  if (lane < 12) {
-    const fp v = ld(sl, PP_REG(PP_REG_R) + lane);
-    mine = lane == 0 ? fp_eq(v, fp_one()) : fp_is_zero(v);
+template <int W = 32> DEV bool final_exp_is_one(fp *sl, int lane, int bar = 0) {
+  run<W>(sl, lane, PP_INV_U_F, bar);
+  run<W>(sl, lane, PP_EASY1_T, bar);
+  run<W>(sl, lane, PP_EASY2_T, bar);
+  exp_by_zabs<W>(sl, lane, PP_COPY_R_T, PP_MUL_R_R_T, bar);
+  run<W>(sl, lane, PP_S1_A, bar);  // a = conj(t^|z|) conj(t)
+  exp_by_zabs<W>(sl, lane, PP_COPY_R_A, PP_MUL_R_R_A, bar);
+  run<W>(sl, lane, PP_S2_A, bar);  // a = conj(a^|z|) conj(a)
+  exp_by_zabs<W>(sl, lane, PP_COPY_R_A, PP_MUL_R_R_A, bar);
+  run<W>(sl, lane, PP_S3_A, bar);  // b = conj(a^|z|) a^p
+  exp_by_zabs<W>(sl, lane, PP_COPY_R_A, PP_MUL_R_R_A, bar);
+  run<W>(sl, lane, PP_S4_X, bar);  // x = b^z
+  exp_by_zabs<W>(sl, lane, PP_COPY_R_X, PP_MUL_R_R_X, bar);
+  run<W>(sl, lane, PP_S5_R, bar);  // r = (b^z)^z b^(p^2)
+  run<W>(sl, lane, PP_MUL_R_R_CA, bar);  // r = r conj(b)
+  run<W>(sl, lane, PP_MUL_R_R_T, bar);
+  run<W>(sl, lane, PP_MUL_R_R_T, bar);
+  run<W>(sl, lane, PP_MUL_R_R_T, bar);
+  if constexpr (W == 32) {
+    bool mine = true;
+    if (lane < 12) {
+      const fp v = ld(sl, PP_REG(PP_REG_R) + lane);
+      mine = lane == 0 ? fp_eq(v, fp_one()) : fp_is_zero(v);
+    }
+    return __ballot_sync(0xffffffffu, !mine) == 0;
+  } else {
+    // every lane reads the result register (written before the last team_sync)
+    bool one = fp_eq(ld(sl, PP_REG(PP_REG_R)), fp_one());
+#pragma unroll 1
+    for (int k = 1; k < 12; k++) one = one && fp_is_zero(ld(sl, PP_REG(PP_REG_R) + k));
+    return one;
   }
-  return __ballot_sync(0xffffffffu, !mine) == 0;
 }
 
 // Lines idx of both pairs into the line slots (lanes 0..7); a skipped pair
@@ -271,7 +301,7 @@ DEV bool pairing_check(fp *sl, int lane, const g1a *P, const line2 *const *L, co
 // The Miller loop of a single pair (P, lines L) into register F of this warp's
 // slot array; a skipped pair leaves F = 1.  Also loads the Frobenius constants
 // and the zero slot, so the warp can run the final exponentiation after.
-DEV void miller_one(fp *sl, int lane, const g1a &P, const line2 *L, bool skip) {
+template <int W = 32> DEV void miller_one(fp *sl, int lane, const g1a &P, const line2 *L, bool skip, int bar = 0) {
   if (lane < 10) {
     const fp2 g[6] = C_FROB_GAMMA;
     const fp2 &ge = g[1 + (lane >> 1)];
@@ -283,7 +313,7 @@ DEV void miller_one(fp *sl, int lane, const g1a &P, const line2 *L, bool skip) {
   } else if (lane >= 16 && lane < 28) {
     st(sl, PP_REG(PP_REG_F) + lane - 16, lane == 16 ? fp_one() : fp_zero());
   }
-  __syncwarp();
+  team_sync<W>(bar);
   int idx = 0;
 #pragma unroll 1
   for (int i = 62; i >= 0; i--) {
@@ -296,9 +326,9 @@ DEV void miller_one(fp *sl, int lane, const g1a &P, const line2 *L, bool skip) {
       }
       st(sl, PP_LINE_BASE + lane, v);
     }
-    __syncwarp();
+    team_sync<W>(bar);
     idx++;
-    run(sl, lane, PP_DBL1);
+    run<W>(sl, lane, PP_DBL1, bar);
     if (zabs_bit(i)) {
       if (lane < 4) {
         fp v;
@@ -309,9 +339,9 @@ DEV void miller_one(fp *sl, int lane, const g1a &P, const line2 *L, bool skip) {
         }
         st(sl, PP_LINE_BASE + lane, v);
       }
-      __syncwarp();
+      team_sync<W>(bar);
       idx++;
-      run(sl, lane, PP_ADD1);
+      run<W>(sl, lane, PP_ADD1, bar);
     }
   }
 }

@@ -58,7 +58,13 @@ void SharedState::init() {
   // The kernels are register heavy; give them room for local-memory spills.
   CUBBS_CHECK(cudaDeviceSetLimit(cudaLimitStackSize, 16384));
   table_w = env_int("CUBBS_BBS_TABLE_WINDOW", 0);  // 0: chosen by table_window_for
-  if (table_w != 0 && (table_w < 4 || table_w > 16)) table_w = 0;
+  if (table_w != 0 && (table_w < 4 || table_w > MAX_TABLE_WINDOW)) table_w = 0;
+  {
+    size_t free_b = 0, total_b = 0;
+    CUBBS_CHECK(cudaMemGetInfo(&free_b, &total_b));
+    const int gib = env_int("CUBBS_BBS_TABLE_BUDGET_GIB", 0);
+    table_budget = gib > 0 ? (size_t)gib << 30 : total_b / 100 * 35;
+  }
   workspaces = env_int("CUBBS_BBS_WORKSPACES", 4);
   if (workspaces < 1 || workspaces > 64) workspaces = 4;
   line_capacity = 2 + 1024;
@@ -248,24 +254,34 @@ void SharedState::grow_generators(int suite, int count) {
 
 // Fixed-base window table over d_gens[0..gens) of a suite.  Rebuilt (all
 // generators) when it must grow; built in generator chunks to bound the scratch.
-// Window width of a table over `gens` generators: the explicit setting, else
-// the widest w in 8..16 whose table (gens * ceil(256/w) * 2^(w-1) affine
-// points) fits in TABLE_BUDGET.  A wider window costs fewer mixed additions
-// per term (16 at w = 16, 32 at w = 8); the entries are read at random, one
-// 96-byte point per addition, from HBM.
-static const size_t TABLE_BUDGET = (size_t)16 << 30;
-int SharedState::table_window_for(int gens) const {
-  if (table_w) return table_w;
-  for (int w = 16; w > 8; w--) {
-    const size_t bytes = (size_t)gens * (255 / w + 1) * ((size_t)1 << (w - 1)) * sizeof(g1a);
-    if (bytes <= TABLE_BUDGET) return w;
+// Window width of a suite's table over `gens` generators.  The tables of all
+// suites share the table budget (CUBBS_BBS_TABLE_BUDGET_GIB, default 35 % of
+// the device memory: 91 GiB on GB300).  Automatic: the width in
+// 8..MAX_TABLE_WINDOW with the fewest windows (ceil(256 / w), the mixed
+// additions per term) whose table fits what the other suites leave, the
+// narrowest of equals (w = 20 up to 128 generators on GB300: 13 additions per
+// term instead of 16 at w = 16).  An explicit width (CUBBS_BBS_TABLE_WINDOW,
+// the fixed-base autotuner) is narrowed until the table fits.  The entries are
+// read at random, one 96-byte point per addition, from HBM.
+int SharedState::table_window_for(int suite, int gens) const {
+  size_t others = 0;
+  for (int s = 0; s < SUITE_COUNT; s++)
+    if (s != suite && suites[s].table.entries) others += table_bytes(suites[s].table.gens, suites[s].table.w);
+  const size_t budget = table_budget > others ? table_budget - others : 0;
+  if (table_w) {
+    for (int w = table_w; w > 4; w--)
+      if (table_bytes(gens, w) <= budget) return w;
+    return 4;
   }
-  return 8;
+  int best = 8;
+  for (int w = 8; w <= MAX_TABLE_WINDOW; w++)
+    if (table_bytes(gens, w) <= budget && 255 / w < 255 / best) best = w;
+  return best;
 }
 
 bool SharedState::table_covers(int suite, int gens) const {
   const FixedTable &t = suites[suite].table;
-  return t.entries && t.gens >= gens && (table_w == 0 || t.w == table_w);
+  return t.entries && t.gens >= gens && t.req_w == table_w;
 }
 
 void SharedState::grow_table(int suite, int gens) {
@@ -275,8 +291,16 @@ void SharedState::grow_table(int suite, int gens) {
   while (want < gens) want *= 2;
   if (want < 64) want = 64;
   grow_generators(suite, want);
+  // the caller holds the prepared state exclusively (no call is in flight), so
+  // the old table goes first and the two never occupy the device together
+  if (g.table.entries) {
+    CUBBS_CHECK(cudaDeviceSynchronize());
+    cudaFree(g.table.entries);
+    g.table = FixedTable{};
+  }
   FixedTable t;
-  t.w = table_window_for(want);
+  t.req_w = table_w;
+  t.w = table_window_for(suite, want);
   t.nwin = 255 / t.w + 1;
   t.half = 1 << (t.w - 1);
   t.gens = want;
@@ -290,21 +314,28 @@ void SharedState::grow_table(int suite, int gens) {
   if (chunk > want) chunk = want;
   g1 *scratch = nullptr;
   fp *prod = nullptr;
-  CUBBS_CHECK(cudaMalloc(&scratch, (size_t)chunk * per_gen * sizeof(g1)));
-  CUBBS_CHECK(cudaMalloc(&prod, (size_t)chunk * per_gen * sizeof(fp)));
-  for (int g0 = 0; g0 < want; g0 += chunk) {
-    int g1n = std::min(want, g0 + chunk);
-    // the kernel indexes scratch by (g - g0) * nwin + k
-    launch_build_table(prep, g.d_gens, g0, g1n, t, scratch, prod);
-    CUBBS_CHECK(cudaGetLastError());
-    CUBBS_CHECK(cudaStreamSynchronize(prep));
+  g1a *bases = nullptr;
+  try {
+    CUBBS_CHECK(cudaMalloc(&scratch, (size_t)chunk * per_gen * sizeof(g1)));
+    CUBBS_CHECK(cudaMalloc(&prod, (size_t)chunk * per_gen * sizeof(fp)));
+    CUBBS_CHECK(cudaMalloc(&bases, (size_t)chunk * t.nwin * sizeof(g1a)));
+    for (int g0 = 0; g0 < want; g0 += chunk) {
+      int g1n = std::min(want, g0 + chunk);
+      // the kernels index bases and scratch from generator g0
+      launch_build_table(prep, g.d_gens, g0, g1n, t, bases, scratch, prod);
+      CUBBS_CHECK(cudaGetLastError());
+      CUBBS_CHECK(cudaStreamSynchronize(prep));
+    }
+  } catch (const CudaError &) {
+    cudaFree(scratch);
+    cudaFree(prod);
+    cudaFree(bases);
+    cudaFree(entries);
+    throw;
   }
   cudaFree(scratch);
   cudaFree(prod);
-  if (g.table.entries) {
-    CUBBS_CHECK(cudaDeviceSynchronize());
-    cudaFree(g.table.entries);
-  }
+  cudaFree(bases);
   g.table = t;
 }
 

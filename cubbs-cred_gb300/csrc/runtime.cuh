@@ -66,10 +66,17 @@ struct HostStaging {
 
 // Fixed-base window table over the generator list [P1, Q1, H1, ...]:
 // entry (g, k, d-1) = d * 2^(w k) * G_g (affine), d = 1..2^(w-1).
+constexpr int MAX_TABLE_WINDOW = 20;  // widest fixed-base window (13 windows, 654 MB per generator)
+
 struct FixedTable {
   int w = 0, nwin = 0, half = 0, gens = 0;
+  int req_w = 0;  // the width setting it was built under (0: automatic)
   g1a *entries = nullptr;
 };
+// Bytes of a fixed-base table over `gens` generators at window width w.
+inline size_t table_bytes(int gens, int w) {
+  return (size_t)gens * (size_t)(255 / w + 1) * ((size_t)1 << (w - 1)) * sizeof(g1a);
+}
 
 struct PkSlot {
   int status = DEC_BAD;  // DEC_OK / DEC_INF / DEC_BAD
@@ -149,7 +156,7 @@ struct SharedState {
   int sm_count = 0;
   cudaStream_t prep = nullptr;  // stream that builds prepared state
   SuiteState suites[SUITE_COUNT];
-  int table_w = 0;              // fixed-base window width; 0 = widest that fits the table budget
+  int table_w = 0;              // fixed-base window width; 0 = fewest windows within the table budget
   // Miller lines: slot 0 = -P2, slot 1 = P2, slots >= 2 = public keys
   line2 *d_lines = nullptr;
   g2a *d_pk_aff = nullptr;
@@ -179,7 +186,8 @@ struct SharedState {
   // the following run with mu held exclusively
   void grow_generators(int suite, int count);
   void grow_table(int suite, int gens);
-  int table_window_for(int gens) const;
+  int table_window_for(int suite, int gens) const;
+  size_t table_budget = 0;  // device bytes for the tables of all suites
   bool table_covers(int suite, int gens) const;
   void add_pks(const std::vector<std::string> &fresh);
   void add_domain_prefixes(int suite, const std::vector<std::pair<uint64_t, const uint8_t *>> &fresh);
@@ -275,8 +283,8 @@ void launch_make_generator_seeds(cudaStream_t s, int first, int count, uint8_t *
 void launch_hash_generators(cudaStream_t s, int first, int count, const uint8_t *seeds, g1a *gens,
                             uint8_t *gens_c, int suite);
 void launch_decode_p1(cudaStream_t s, g1a *gens, uint8_t *gens_c, int suite);
-void launch_build_table(cudaStream_t s, const g1a *gens, int g0, int g1n, FixedTable t, g1 *scratch_xyzz,
-                        fp *scratch_prod);
+void launch_build_table(cudaStream_t s, const g1a *gens, int g0, int g1n, FixedTable t, g1a *bases,
+                        g1 *scratch_xyzz, fp *scratch_prod);
 // decode N compressed G1 points: status DEC_*; affine out
 // lanes per point: 1, 2 or 4 (0: chosen by the point count or CUBBS_BBS_VAR_LANES)
 void launch_g1_subgroup(cudaStream_t s, const g1a *pts, const int32_t *status, uint32_t n, int32_t *bad,

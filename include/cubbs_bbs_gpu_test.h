@@ -28,11 +28,12 @@ int32_t cubbs_bbs_gpu_table_window_v2(int32_t *w);
  * partition on first use. */
 int32_t cubbs_bbs_gpu_sm_partition_v2(int32_t *small_sms, int32_t *rest_sms, int32_t *status);
 
-/* Fixed-base table width sweep w_lo..w_hi (4..16) over rows x terms scalars
+/* Fixed-base table width sweep w_lo..w_hi (4..20) over rows x terms scalars
  * against the first `terms` generators [P1, Q1, H1, ...]: each width's first
  * 64 rows are compared with a table-free recomputation (ms_per_w = -1 and
  * *mismatched counts the width when they differ); the fastest agreeing width
- * stays in use (*best_w). */
+ * stays in use (*best_w).  A width whose table does not fit the table budget
+ * is narrowed to one that does (the table in use then reports the width). */
 int32_t cubbs_bbs_gpu_fixed_msm_autotune_v2(uint32_t abi_version, const uint8_t *scalars_be, size_t rows,
                                             size_t terms, int32_t w_lo, int32_t w_hi, int32_t steps,
                                             float *ms_per_w, int32_t *best_w, int32_t *mismatched);
@@ -74,6 +75,8 @@ int32_t cubbs_bbs_gpu_int_peaks_v2(double *tera_imad, double *giga_fpmul);
 /* ---- probes (SM cycles of single programs) */
 int32_t cubbs_bbs_gpu_latency_probe_for_test_v2(double *cycles, int32_t cap);
 int32_t cubbs_bbs_gpu_pairing_probe_for_test_v2(double *cycles, int32_t cap);
+/* the same for two-warp teams (the 64-lane phase tables) */
+int32_t cubbs_bbs_gpu_pairing_probe_wide_for_test_v2(double *cycles, int32_t cap);
 int32_t cubbs_bbs_gpu_fpmul_rates_for_test_v2(const int32_t *warps_per_sm, int32_t n, double *rates);
 
 /* ---- arithmetic test exports (compared with the oracle by the tests) */

@@ -4,7 +4,7 @@ through the C ABI against the oracle (bit-exact):
 * the uneven variable-base MSM engine (16384-MSM workload's K ~ U{2..257})
   on MSMs from every size class, under the autotuned settings and under every
   forced (chunk, window) setting the engine accepts;
-* the fixed-base MSM (4096 x 12-term workload) at every table width 4..16;
+* the fixed-base MSM (4096 x 12-term workload) at every table width 4..20;
 * ProofVerify at the headline shape (1024 proofs, L = 100, 50 disclosed) over
   several keys, with about 2 % invalid items of several kinds;
 * proofs whose Abar, Bbar or D is the identity encoding, which the reference
@@ -101,7 +101,7 @@ def test_msm_tuning_rejects_out_of_range(gpu):
 # ----------------------------------------------------------------------------- fixed-base MSM widths
 def test_fixed_msm_every_table_width(gpu, oracle):
     """The 12-term fixed-base MSM over [P1, Q1, H1..H10] at every table width
-    4..16 (the autotuner's sweep with one width selects it): each width's
+    4..20 (the autotuner's sweep with one width selects it): each width's
     output equals the oracle's, and the autotuner's own check finds no width
     that disagrees."""
     p1, gens = oracle.generators(11)
@@ -112,15 +112,20 @@ def test_fixed_msm_every_table_width(gpu, oracle):
     want = pmap(oracle.g1_msm, [(pts, row) for row in rows])
     flat = b"".join(b"".join(row) for row in rows)
     before = gpu.table_window()
+    seen = set()
     try:
-        for w in range(4, 17):
+        for w in range(4, 21):
             ms, best, bad = gpu.fixed_msm_autotune(flat, len(rows), 12, w, w, steps=1, with_mismatches=True)
             assert bad == 0 and best == w and ms[0] > 0
-            assert gpu.table_window() == w
+            # a table too large for the budget is narrowed (only possible at the widest widths)
+            got_w = gpu.table_window()
+            assert got_w == w or (w > 16 and 16 <= got_w < w)
+            seen.add(got_w)
             got = gpu.g1_msm_common_points(pts, rows)
             assert [(c, route, out) for c, route, out in got] == [(0, 2, x) for x in want], "width %d" % w
-        ms, best, bad = gpu.fixed_msm_autotune(flat, len(rows), 12, 4, 16, steps=1, with_mismatches=True)
-        assert bad == 0 and 4 <= best <= 16 and all(m > 0 for m in ms)
+        assert set(range(4, 17)) <= seen
+        ms, best, bad = gpu.fixed_msm_autotune(flat, len(rows), 12, 4, 20, steps=1, with_mismatches=True)
+        assert bad == 0 and 4 <= best <= 20 and all(m > 0 for m in ms)
     finally:
         restore = before if before else 16
         gpu.fixed_msm_autotune(flat, len(rows), 12, restore, restore, steps=1)

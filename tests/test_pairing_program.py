@@ -1,6 +1,6 @@
-"""The phase tables of the warp-per-check pairing (pairing_program.cuh), decoded
-the way pp::run in pairing_team.cuh decodes them, against the independent
-schoolbook Fp12 of gen_pairing_program.py.
+"""The phase tables of the warp-per-check pairing (pairing_program.cuh), for
+one-warp and two-warp teams, decoded the way pp::run in pairing_team.cuh
+decodes them, against the independent schoolbook Fp12 of gen_pairing_program.py.
 
 The weighted sums are emulated limb for limb: 64-bit accumulators per limb,
 the single-precision quotient estimate taken from the top two accumulators
@@ -26,15 +26,20 @@ def gen():
     return mod
 
 
-@pytest.fixture(scope="module")
-def table():
+@pytest.fixture(scope="module", params=[("", 32), ("_W", 64)], ids=["one-warp", "two-warp"])
+def table(request):
+    """The phase table of one team width: (first phase per program, words, slots, lanes)."""
+    sfx, lanes = request.param
     txt = (CSRC / "pairing_program.cuh").read_text()
-    first = [int(x) for x in re.search(r"PP_PROG_FIRST\[PP_NPROG \+ 1\] = \{([^}]*)\}", txt).group(1).split(",")]
-    body = txt[txt.index("PP_ENTRY[PP_NPHASE * PP_LANES * 2] = {"):]
+    assert int(re.search(r"#define PP_LANES%s (\d+)" % sfx, txt).group(1)) == lanes
+    first = [int(x) for x in re.search(r"PP_PROG_FIRST%s\[PP_NPROG \+ 1\] = \{([^}]*)\}" % re.escape(sfx),
+                                       txt).group(1).split(",")]
+    start = txt.index("PP_ENTRY%s[PP_NPHASE%s * PP_LANES%s * 2] = {" % (sfx, sfx, sfx))
+    body = txt[start:txt.index("};", start)]
     words = [int(x, 16) for x in re.findall(r"0x([0-9a-f]{8})", body)]
     nslot = int(re.search(r"#define PP_SLOTS (\d+)", txt).group(1))
-    assert len(words) == first[-1] * 32 * 8
-    return first, words, nslot
+    assert len(words) == first[-1] * lanes * 8
+    return first, words, nslot, lanes
 
 
 P = 0x1A0111EA397FE69A4B1BA7B6434BACD764774B84F38512BF6730D2A0F6B0F6241EABFFFEB153FFFFB9FEFFFFFFFFAAAB
@@ -73,13 +78,13 @@ def _coef(v):
 
 
 def run_program(table, s, prog):
-    first, words, _ = table
+    first, words, _, lanes = table
     s = dict(s)
     for ph in range(first[prog], first[prog + 1]):
         res = []
         types = set()
-        for lane in range(32):
-            w = words[(ph * 32 + lane) * 8:(ph * 32 + lane) * 8 + 8]
+        for lane in range(lanes):
+            w = words[(ph * lanes + lane) * 8:(ph * lanes + lane) * 8 + 8]
             u = [(w[i // 2] >> (16 * (i % 2))) & 0xFFFF for i in range(16)]
             out, tw = u[0], u[1]
             types.add(tw)
