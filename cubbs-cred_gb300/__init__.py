@@ -1337,3 +1337,219 @@ def proofvalue_parse_derived(text):
              "presentation_header": _slice_bytes(out.presentation_header)}
     del keep
     return value
+
+
+# ----------------------------------------------------------------------------- bbs-2023 input producers
+# Mirrors crates/cubbs-vc-di-bbs/src/{hashing,hmac_label,canonical,key,prepared}.rs
+# through the library's cubbs_bbs2023_* entry points (host code, plus Sign /
+# Verify on the device for the batch issue and verify).  N-Quads are str lines
+# ending in "\n" (RDFC output), passed as UTF-8.
+
+BBS2023_ERRORS = {20: "InvalidHmacKeyLength", 21: "InvalidPublicKeyLength", 22: "InvalidMultibasePrefix",
+                  23: "InvalidMulticodecHeader", 24: "Base58", 25: "InvalidVerificationMethod"}
+BBS2023_HMAC_KEY_LEN = 32
+
+
+class Bbs2023Error(ValueError):
+    def __init__(self, code):
+        kind = BBS2023_ERRORS.get(code) or PROOFVALUE_ERRORS.get(code) or f"code {code}"
+        super().__init__(kind)
+        self.code = code
+        self.kind = kind
+
+
+class LabelEntry(ctypes.Structure):
+    _fields_ = [("input", ByteSlice), ("canonical", ByteSlice)]
+
+
+class Bbs2023IssueItem(ctypes.Structure):
+    _fields_ = [("secret_key", ByteSlice), ("public_key", ByteSlice), ("proof_hash", ByteSlice),
+                ("mandatory", ctypes.c_void_p), ("mandatory_count", ctypes.c_size_t),
+                ("non_mandatory", ctypes.c_void_p), ("non_mandatory_count", ctypes.c_size_t),
+                ("hmac_key", ByteSlice), ("mandatory_pointers", ctypes.c_void_p),
+                ("mandatory_pointer_count", ctypes.c_size_t), ("proof_value_out", ByteBuffer)]
+
+
+class Bbs2023VerifyBaseItem(ctypes.Structure):
+    _fields_ = [("public_key", ByteSlice), ("proof_hash", ByteSlice), ("mandatory", ctypes.c_void_p),
+                ("mandatory_count", ctypes.c_size_t), ("non_mandatory", ctypes.c_void_p),
+                ("non_mandatory_count", ctypes.c_size_t), ("proof_value", ByteSlice)]
+
+
+def _utf8(lines):
+    return [s.encode("utf-8") if isinstance(s, str) else bytes(s) for s in lines]
+
+
+def _labels(k, pairs):
+    arr = (LabelEntry * max(1, len(pairs)))()
+    for i, (a, b) in enumerate(pairs):
+        arr[i] = LabelEntry(k.bytes(a.encode("utf-8")), k.bytes(b.encode("utf-8")))
+    k.refs.append(arr)
+    return arr
+
+
+def _b23(name, argtypes):
+    fn = getattr(lib(), name)
+    fn.restype = ctypes.c_int32
+    fn.argtypes = argtypes
+    return fn
+
+
+def bbs2023_hmac_sha256(key, data):
+    out = ctypes.create_string_buffer(32)
+    P = ctypes.c_void_p
+    fn = _b23("cubbs_bbs2023_hmac_sha256_v2", [ctypes.c_uint32, ctypes.c_char_p, ctypes.c_size_t, ctypes.c_char_p,
+                                               ctypes.c_size_t, P])
+    rc = fn(ABI_VERSION, bytes(key), len(key), bytes(data), len(data), ctypes.cast(out, P))
+    if rc:
+        raise Bbs2023Error(rc)
+    return out.raw
+
+
+def shuffled_bnode_label_map(canonical_id_map, hmac_key):
+    """{input label: c14n label} -> {input label: "bN"} (hmac_label.rs:26-50)."""
+    k = _Keep()
+    pairs = list(canonical_id_map.items())
+    arr = _labels(k, pairs)
+    idx = (ctypes.c_uint32 * max(1, len(pairs)))()
+    P = ctypes.c_void_p
+    fn = _b23("cubbs_bbs2023_shuffled_label_map_v2", [ctypes.c_uint32, P, ctypes.c_size_t, ctypes.c_char_p,
+                                                      ctypes.c_size_t, P])
+    rc = fn(ABI_VERSION, ctypes.cast(arr, P), len(pairs), bytes(hmac_key), len(hmac_key), ctypes.cast(idx, P))
+    if rc:
+        raise Bbs2023Error(rc)
+    return {a: "b%d" % idx[i] for i, (a, _) in enumerate(pairs)}
+
+
+def canonical_label_map_from_input_map(input_to_canonical, input_to_replacement):
+    """{canonical label: replacement} for the inputs both maps hold (canonical.rs:50-62)."""
+    return {c: input_to_replacement[i] for i, c in input_to_canonical.items() if i in input_to_replacement}
+
+
+def relabel_and_sort_canonical_nquads(lines, label_map):
+    """Replaces every "_:label" through label_map and sorts the lines bytewise
+    (canonical.rs:64-92,130-150)."""
+    k = _Keep()
+    raw = _utf8(lines)
+    sl = k.slices(raw)
+    arr = _labels(k, list(label_map.items()))
+    out = (ByteSlice * max(1, len(raw)))()
+    used = ctypes.c_size_t(0)
+    P = ctypes.c_void_p
+    fn = _b23("cubbs_bbs2023_relabel_sort_v2", [ctypes.c_uint32, P, ctypes.c_size_t, P, ctypes.c_size_t, P,
+                                                ctypes.c_size_t, P, P])
+    cap = sum(len(x) for x in raw) * 2 + 64
+    while True:
+        arena = ctypes.create_string_buffer(cap)
+        rc = fn(ABI_VERSION, sl, len(raw), ctypes.cast(arr, P), len(label_map), ctypes.cast(arena, P), cap,
+                ctypes.cast(out, P), ctypes.cast(ctypes.pointer(used), P))
+        if rc == ERR_INSUFFICIENT_OUTPUT and used.value > cap:
+            cap = used.value
+            continue
+        if rc:
+            raise Bbs2023Error(rc)
+        return [ctypes.string_at(out[i].data, out[i].len).decode("utf-8", "surrogateescape") if out[i].len else ""
+                for i in range(len(raw))]
+
+
+def bbs2023_header(proof_lines, mandatory):
+    """64-byte bbs-2023 header: SHA-256 of the proof lines, then of the mandatory lines (hashing.rs:7-31)."""
+    k = _Keep()
+    pl, ml = _utf8(proof_lines), _utf8(mandatory)
+    out = ctypes.create_string_buffer(64)
+    P = ctypes.c_void_p
+    fn = _b23("cubbs_bbs2023_header_v2", [ctypes.c_uint32, P, ctypes.c_size_t, P, ctypes.c_size_t, P])
+    rc = fn(ABI_VERSION, k.slices(pl), len(pl), k.slices(ml), len(ml), ctypes.cast(out, P))
+    if rc:
+        raise Bbs2023Error(rc)
+    return out.raw
+
+
+def _key_text(form, pk):
+    P = ctypes.c_void_p
+    fn = _b23("cubbs_bbs2023_public_key_to_multibase_v2", [ctypes.c_uint32, ctypes.c_int32, ctypes.c_char_p,
+                                                           ctypes.c_size_t, P, ctypes.c_size_t, P])
+    buf = ctypes.create_string_buffer(512)
+    n = ctypes.c_size_t(0)
+    rc = fn(ABI_VERSION, form, bytes(pk), len(pk), ctypes.cast(buf, P), 512, ctypes.cast(ctypes.pointer(n), P))
+    if rc:
+        raise Bbs2023Error(rc)
+    return buf.raw[:n.value].decode("ascii")
+
+
+def _key_parse(form, text):
+    P = ctypes.c_void_p
+    fn = _b23("cubbs_bbs2023_public_key_from_multibase_v2", [ctypes.c_uint32, ctypes.c_int32, ctypes.c_char_p,
+                                                             ctypes.c_size_t, P])
+    raw = text.encode("utf-8")
+    out = ctypes.create_string_buffer(96)
+    rc = fn(ABI_VERSION, form, raw, len(raw), ctypes.cast(out, P))
+    if rc:
+        raise Bbs2023Error(rc)
+    return out.raw
+
+
+def public_key_to_multibase(pk):
+    return _key_text(0, pk)
+
+
+def did_key_from_public_key(pk):
+    return _key_text(1, pk)
+
+
+def verification_method_from_public_key(pk):
+    return _key_text(2, pk)
+
+
+def public_key_from_multibase(text):
+    return _key_parse(0, text)
+
+
+def public_key_from_did_key(text):
+    return _key_parse(1, text)
+
+
+def public_key_from_verification_method(text):
+    return _key_parse(2, text)
+
+
+def bbs2023_issue_base_proof_batch(items):
+    """items: (secret_key, public_key, proof_hash (32 B), mandatory lines, non-mandatory lines,
+    hmac_key, mandatory_pointers) -> [(code, proofValue text or None)] (prepared.rs:335-421)."""
+    k = _Keep()
+    arr = (Bbs2023IssueItem * max(1, len(items)))()
+    bufs = []
+    for i, (sk, pk, ph, mand, non, hk, ptrs) in enumerate(items):
+        m, nm = _utf8(mand), _utf8(non)
+        pp = [p.encode("utf-8") for p in ptrs]
+        cap = 4 * (80 + 64 + 96 + 32 + sum(len(p) + 9 for p in pp)) // 3 + 64
+        ob, buf = k.out(cap)
+        bufs.append(buf)
+        arr[i] = Bbs2023IssueItem(k.bytes(sk), k.bytes(pk), k.bytes(ph), k.slices(m), len(m), k.slices(nm), len(nm),
+                                  k.bytes(hk), k.slices(pp), len(pp), ob)
+    res = (Result * max(1, len(items)))()
+    P = ctypes.c_void_p
+    fn = _b23("cubbs_bbs2023_issue_base_proof_batch_v2", [ctypes.c_uint32, P, ctypes.c_size_t, P])
+    rc = fn(ABI_VERSION, ctypes.cast(arr, P), len(items), ctypes.cast(res, P))
+    if rc:
+        raise RuntimeError(f"issue_base_proof_batch returned {rc}")
+    return [(res[i].code, bufs[i].raw[:arr[i].proof_value_out.len].decode("ascii") if res[i].code == 0 else None)
+            for i in range(len(items))]
+
+
+def bbs2023_verify_base_proof_batch(items):
+    """items: (public_key, proof_hash, mandatory lines, non-mandatory lines, proofValue text)
+    -> [(code, valid)] (prepared.rs:423-513)."""
+    k = _Keep()
+    arr = (Bbs2023VerifyBaseItem * max(1, len(items)))()
+    for i, (pk, ph, mand, non, text) in enumerate(items):
+        m, nm = _utf8(mand), _utf8(non)
+        arr[i] = Bbs2023VerifyBaseItem(k.bytes(pk), k.bytes(ph), k.slices(m), len(m), k.slices(nm), len(nm),
+                                       k.bytes(text.encode("utf-8")))
+    res = (Result * max(1, len(items)))()
+    P = ctypes.c_void_p
+    fn = _b23("cubbs_bbs2023_verify_base_proof_batch_v2", [ctypes.c_uint32, P, ctypes.c_size_t, P])
+    rc = fn(ABI_VERSION, ctypes.cast(arr, P), len(items), ctypes.cast(res, P))
+    if rc:
+        raise RuntimeError(f"verify_base_proof_batch returned {rc}")
+    return [(res[i].code, bool(res[i].value)) for i in range(len(items))]

@@ -17,7 +17,7 @@ BUILD = ROOT / "_build"
 LIBDIR = ROOT / "lib"
 LIB = LIBDIR / "libcubbs_bbs_cuda.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-UNITS = ["runtime", "k_hash", "k_g1", "k_pairing", "k_bbs", "k_prims", "k_selftest", "k_noalloc", "serve", "k_msm", "proofvalue"]
+UNITS = ["runtime", "k_hash", "k_g1", "k_pairing", "k_bbs", "k_prims", "k_selftest", "k_noalloc", "serve", "k_msm", "proofvalue", "bbs2023"]
 
 
 def _nvcc() -> str:

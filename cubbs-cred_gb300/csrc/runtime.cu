@@ -106,13 +106,23 @@ template <class F> F driver_fn(const char *name) {
 // entry points looked up through the runtime).  A self-test launches a kernel
 // on each and hands an event from one to the other; if any step fails the
 // partition stays off and ProofVerify runs on the plain streams.
-// Under a profiler that injects itself (CUDA_INJECTION64_PATH set, as ncu and
-// nsys do) the partition stays off unless CUBBS_BBS_SM_PARTITION asks for it:
-// such tools may stop listing kernels at the first green-context launch.
+// Under a profiler that injects itself the partition stays off unless
+// CUBBS_BBS_SM_PARTITION asks for it: such tools may stop listing kernels at
+// the first green-context launch.  Nsight Compute marks its target process
+// with NV_NSIGHT_INJECTION_TRANSPORT_TYPE, NV_COMPUTE_PROFILER_PERFWORKS_DIR
+// and NV_TPS_LAUNCH_TOKEN; other injecting tools set CUDA_INJECTION64_PATH.
+static bool profiler_injected() {
+  for (const char *name : {"CUDA_INJECTION64_PATH", "NV_NSIGHT_INJECTION_TRANSPORT_TYPE",
+                           "NV_COMPUTE_PROFILER_PERFWORKS_DIR", "NV_TPS_LAUNCH_TOKEN"}) {
+    const char *v = std::getenv(name);
+    if (v && *v) return true;
+  }
+  return false;
+}
+
 void SharedState::init_partition() {
-  const char *inj = std::getenv("CUDA_INJECTION64_PATH");
   const char *setting = std::getenv("CUBBS_BBS_SM_PARTITION");
-  if (inj && *inj && !(setting && *setting)) {
+  if (profiler_injected() && !(setting && *setting)) {
     partition_status = 2;
     return;
   }

@@ -405,6 +405,96 @@ int32_t cubbs_bbs_proofvalue_parse_derived_v2(uint32_t abi_version, const char *
                                               size_t arena_cap, CuBbsBbsProofValueDerived *out,
                                               size_t *arena_used);
 
+/* Addition with no counterpart in the reference C ABI: the W3C bbs-2023 input
+ * producers between RDF canonicalisation and the BBS operations, host code
+ * (crates/cubbs-vc-di-bbs/src/{hashing,hmac_label,canonical,key,prepared}.rs).
+ * JSON-LD expansion and RDFC-1.0 canonicalisation come first and are the
+ * caller's.  Returns 0, CUBBS_BBS_GPU_ERR_INVALID_INPUT for malformed
+ * arguments, CUBBS_BBS_GPU_ERR_INSUFFICIENT_OUTPUT (with the size needed),
+ * or one of the codes below (the reference's error kinds). */
+#define CUBBS_BBS2023_ERR_HMAC_KEY_LENGTH 20    /* InvalidHmacKeyLength: not 32 bytes */
+#define CUBBS_BBS2023_ERR_PUBLIC_KEY_LENGTH 21  /* InvalidPublicKeyLength: not 96 bytes */
+#define CUBBS_BBS2023_ERR_MULTIBASE_PREFIX 22   /* InvalidMultibasePrefix: no leading 'z' */
+#define CUBBS_BBS2023_ERR_MULTICODEC_HEADER 23  /* InvalidMulticodecHeader: not 0xeb 0x01 */
+#define CUBBS_BBS2023_ERR_BASE58 24             /* Base58: not base58btc */
+#define CUBBS_BBS2023_ERR_VERIFICATION_METHOD 25 /* InvalidVerificationMethod: no did:key */
+
+/* A blank-node label map entry: input label -> canonical label (c14nN), both
+ * without the "_:" prefix. */
+typedef struct CuBbsBbs2023LabelEntry {
+  CuBbsBbsGpuByteSlice input;
+  CuBbsBbsGpuByteSlice canonical;
+} CuBbsBbs2023LabelEntry;
+
+/* HMAC-SHA256 (hmac_label.rs:11-16). */
+int32_t cubbs_bbs2023_hmac_sha256_v2(uint32_t abi_version, const uint8_t *key, size_t key_len,
+                                     const uint8_t *data, size_t len, uint8_t *out32);
+/* shuffled_bnode_label_map (hmac_label.rs:26-50): map[k].input gets the label
+ * "b" + b_index_out[k], the rank of 'u' || base64url(HMAC(key, canonical)). */
+int32_t cubbs_bbs2023_shuffled_label_map_v2(uint32_t abi_version, const CuBbsBbs2023LabelEntry *map,
+                                            size_t count, const uint8_t *hmac_key, size_t key_len,
+                                            uint32_t *b_index_out);
+/* relabel_and_sort_canonical_nquads (canonical.rs:64-92,130-150): each
+ * "_:label" of each line is replaced through label_map (entry input -> entry
+ * canonical; a label runs to the next Unicode whitespace; labels not in the
+ * map stay), and the lines are sorted bytewise.  The new lines are copied to
+ * arena (*arena_used bytes) and lines_out[0..line_count) points into it. */
+int32_t cubbs_bbs2023_relabel_sort_v2(uint32_t abi_version, const CuBbsBbsGpuByteSlice *lines,
+                                      size_t line_count, const CuBbsBbs2023LabelEntry *label_map,
+                                      size_t map_count, uint8_t *arena, size_t arena_cap,
+                                      CuBbsBbsGpuByteSlice *lines_out, size_t *arena_used);
+/* bbs_header (hashing.rs:7-31): SHA-256 of the canonical proof configuration
+ * lines joined without separators, then SHA-256 of the mandatory lines. */
+int32_t cubbs_bbs2023_header_v2(uint32_t abi_version, const CuBbsBbsGpuByteSlice *proof_lines,
+                                size_t proof_count, const CuBbsBbsGpuByteSlice *mandatory,
+                                size_t mandatory_count, uint8_t *header64);
+/* Multikey forms of a BLS12-381 G2 public key (key.rs:25-80): form 0 the
+ * multibase 'z' || base58btc(0xeb 0x01 || key); 1 "did:key:" + multibase;
+ * 2 the verification method "did:key:" + multibase + "#" + multibase.
+ * Parsing form 2 takes the part after the first '#' when there is one, else
+ * a did:key. */
+int32_t cubbs_bbs2023_public_key_to_multibase_v2(uint32_t abi_version, int32_t form, const uint8_t *public_key,
+                                                 size_t key_len, char *out, size_t cap, size_t *len_out);
+int32_t cubbs_bbs2023_public_key_from_multibase_v2(uint32_t abi_version, int32_t form, const char *text,
+                                                   size_t len, uint8_t *public_key96);
+
+/* A base proof to issue (IssueBaseProofRequest, prepared.rs:52-60): the BBS
+ * messages are the non-mandatory canonical N-Quads, the header is
+ * proof_hash || SHA-256(mandatory lines joined); proof_value_out receives the
+ * base proofValue text. */
+typedef struct CuBbs2023IssueItem {
+  CuBbsBbsGpuByteSlice secret_key;
+  CuBbsBbsGpuByteSlice public_key;
+  CuBbsBbsGpuByteSlice proof_hash; /* 32 bytes */
+  const CuBbsBbsGpuByteSlice *mandatory;
+  size_t mandatory_count;
+  const CuBbsBbsGpuByteSlice *non_mandatory;
+  size_t non_mandatory_count;
+  CuBbsBbsGpuByteSlice hmac_key; /* 32 bytes */
+  const CuBbsBbsGpuByteSlice *mandatory_pointers;
+  size_t mandatory_pointer_count;
+  CuBbsBbsGpuByteBuffer proof_value_out;
+} CuBbs2023IssueItem;
+/* A base proof to verify (PreparedBaseVerification, prepared.rs:83-89). */
+typedef struct CuBbs2023VerifyBaseItem {
+  CuBbsBbsGpuByteSlice public_key;
+  CuBbsBbsGpuByteSlice proof_hash; /* 32 bytes */
+  const CuBbsBbsGpuByteSlice *mandatory;
+  size_t mandatory_count;
+  const CuBbsBbsGpuByteSlice *non_mandatory;
+  size_t non_mandatory_count;
+  CuBbsBbsGpuByteSlice proof_value; /* the proofValue text */
+} CuBbs2023VerifyBaseItem;
+/* issue_base_proof_batch / verify_base_proof_batch (prepared.rs:335-513) with
+ * Sign / Verify as one device batch.  Issue: results[i] = {0, 0, text length},
+ * CUBBS_BBS2023_ERR_HMAC_KEY_LENGTH, or Sign's per-item code.  Verify:
+ * {0, 1 / 0, 0} (a proofValue whose key or header differs is value 0), or the
+ * proofValue codec's error code. */
+int32_t cubbs_bbs2023_issue_base_proof_batch_v2(uint32_t abi_version, CuBbs2023IssueItem *items,
+                                                size_t item_count, CuBbsBbsGpuResult *results);
+int32_t cubbs_bbs2023_verify_base_proof_batch_v2(uint32_t abi_version, const CuBbs2023VerifyBaseItem *items,
+                                                 size_t item_count, CuBbsBbsGpuResult *results);
+
 /* reference :268-271 */
 int32_t cubbs_bbs_gpu_g1_msm_common_points_batch_v2(uint32_t abi_version,
                                                     CuBbsBbsGpuG1MsmCommonPointsBatchItem *items,

@@ -8,7 +8,7 @@ from conftest import ROOT, load_package
 
 def declared_symbols():
     text = (ROOT / "include" / "cubbs_bbs_gpu_abi.h").read_text()
-    return sorted(set(re.findall(r"\b(cubbs_bbs_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(cubbs_bbs\w+)\s*\(", text)))
 
 
 def test_header_declares_reference_symbols():

@@ -65,7 +65,7 @@ def test_test_header_compiles_as_c_and_cpp(tmp_path):
 
 
 def _declared(path):
-    return set(re.findall(r"\b(cubbs_bbs_\w+)\s*\(", path.read_text()))
+    return set(re.findall(r"\b(cubbs_bbs\w+)\s*\(", path.read_text()))
 
 
 def test_every_export_is_declared():
