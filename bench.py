@@ -563,6 +563,8 @@ def main():
                        "batch": n, "L": L, "disclosed": R, "l2": "flushed (256 MiB write) between timed steps",
                        "fixed_base_window": table_w, "prepared_state": prepared,
                        "sm_partition": {"pairing_check": part_sms[0], "rest": part_sms[1],
+                                        "var_terms": pkg.sm_partition_var()[0],
+                                        "var_terms_status": pkg.sm_partition_var()[1],
                                         "status": part_sms[2]},
                        "parallelism": "replicas" if world > 1 else "single GPU"},
             "per_op_ops_per_s": {

@@ -546,6 +546,19 @@ def sm_partition():
     return a.value, b.value, st.value
 
 
+def sm_partition_var():
+    """(SMs, status) of the third ProofVerify partition, split off `rest`: the
+    point decode and the variable-base terms run there alone (0 SMs when off;
+    status 0 when on, else why it is off)."""
+    v, st = ctypes.c_int32(0), ctypes.c_int32(0)
+    fn = lib().cubbs_bbs_gpu_sm_partition_var_v2
+    fn.restype = ctypes.c_int32
+    fn.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    if fn(*(ctypes.cast(ctypes.pointer(x), ctypes.c_void_p) for x in (v, st))):
+        raise RuntimeError("sm_partition_var failed")
+    return v.value, st.value
+
+
 def table_window():
     """Window width of the resident fixed-base table (0 before it is built)."""
     w = ctypes.c_int32(0)

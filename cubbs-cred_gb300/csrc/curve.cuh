@@ -541,10 +541,15 @@ DEV int g1_decompress(const uint8_t in[48], g1a &out, bool check_subgroup = true
 DEVNI void glv_split(fr k, uint32_t s[4], uint32_t q[4]) {
   // schoolbook shift-subtract long division of a 256-bit k by the 128-bit lambda
   const uint64_t lam_lo = C_GLV_LAMBDA_LO, lam_hi = C_GLV_LAMBDA_HI;
-  uint64_t rem_lo = 0, rem_hi = 0;  // remainder < lambda < 2^128
+  // After the steps over bits 255..128 the remainder is k >> 128 and no step
+  // has subtracted as long as k >> 128 < lambda, which holds for every k < r
+  // (r >> 128 < lambda): start from there.  Larger k take all 256 steps.
+  uint64_t rem_lo = ((uint64_t)k.w[5] << 32) | k.w[4], rem_hi = ((uint64_t)k.w[7] << 32) | k.w[6];
+  int top = 127;
+  if (rem_hi > lam_hi || (rem_hi == lam_hi && rem_lo >= lam_lo)) { rem_lo = rem_hi = 0; top = 255; }
   uint64_t q_lo = 0, q_hi = 0;
   #pragma unroll 1
-  for (int i = 255; i >= 0; i--) {
+  for (int i = top; i >= 0; i--) {
     uint32_t bit = (k.w[i >> 5] >> (i & 31)) & 1;
     // rem = rem*2 + bit (rem < 2^128 so rem*2 < 2^129: track the carry)
     uint64_t carry = rem_hi >> 63;

@@ -180,7 +180,7 @@ __global__ void __launch_bounds__(128) k_pv_pairjobs(const PvItem *items0, uint3
 // check.  rho_i = a_i + b_i lambda with a_i in [2^31, 2^32), b_i in [0, 2^32)
 // drawn per call from OS randomness (lambda = z^2 is the eigenvalue of the GLV
 // endomorphism, so the 2^63 values are distinct below r, and
-// rho_i P = a_i P + b_i phi(P) costs 31 doublings); every pairing value lies in
+// rho_i P = a_i P + b_i phi(P) needs only 32-bit scalars); every pairing value lies in
 // the order-r subgroup of Fp12*.  A group that fails is checked item by item,
 // so every item's result equals its own check.
 struct AggSeed {
@@ -203,52 +203,118 @@ DEV void agg_rho(const AggSeed &seed, uint32_t i, uint32_t &a, uint32_t &b) {
   b = (uint32_t)h[4] << 24 | (uint32_t)h[5] << 16 | (uint32_t)h[6] << 8 | h[7];
 }
 
-// a P + b phi(P) for affine P (Shamir's trick over the 32 bits of a and b).
-// Every step adds one of {P, phi(P), P + phi(P)} or nothing and keeps the sum
-// by a select, so lanes with different scalars never diverge.
-// On a lane pair (both lanes return the result; a pair holds one point).
-DEV g1 g1_mul_rho(const LanePair &lp, const g1a &p, uint32_t a, uint32_t b) {
-  const g1 P = g1_from_aff(p);
-  const g1 E = g1_endo(P);
-  const g1 PE = g1_add_pair(lp, P, E);
-  g1 acc = (b >> 31) ? PE : P;  // bit 31 of a is set
-#pragma unroll 1
-  for (int i = 30; i >= 0; i--) {
-    acc = g1_dbl_pair(lp, acc);
-    const uint32_t sel = ((a >> i) & 1) | (((b >> i) & 1) << 1);
-    const g1 t = sel == 1 ? P : sel == 2 ? E : PE;
-    const g1 sum = g1_add_pair(lp, acc, t);
-    if (sel) acc = sum;
-  }
-  return acc;
-}
+// The sums of a group, R_s = sum_i rho_i P_{i,s} (set 0: Abar_i or A_i, set 1:
+// Bbar_i or B_i - e_i A_i), as one bucket MSM per (group, set).  With
+// rho_i P = a_i P + b_i phi(P), a group of n_g items is an MSM of 2 n_g points
+// with 32-bit scalars, cut into four 8-bit windows:
+//   k_agg_prep_*   one thread per item: rho_i, phi of its two points;
+//   k_agg_sort     per (group, set, window): counting sort of the entries by
+//                  digit (bucket), offsets in boff;
+//   k_agg_buckets  one lane pair per bucket j: the sum of its points (mixed
+//                  additions), times j; the 16 pairs of a warp add theirs;
+//   k_agg_combine  per (group, set): one warp per window adds its 16 warp sums
+//                  and doubles 8 w times (lane quad); the four windows are
+//                  added and written, affine, into the group's pairing job.
+// About a fifth of the work of one 31-step ladder per point, and the depth of
+// the chain is a few bucket additions, one 8-bit multiple and 24 doublings.
+// The order of the additions inside a bucket is not fixed (the sort places
+// entries by atomics), but the sum is a group element and its affine form is
+// unique, so the pairing input and every verdict are deterministic.
+constexpr uint32_t AGG_SLAB = 8;  // (set, window) slabs per group: 2 sets x 4 windows
 
-// One lane pair per (item, point): scaled[2i] = rho_i Abar_i, scaled[2i+1] = rho_i Bbar_i
-// for items of an aggregated group whose points decoded (infinity otherwise).
-__global__ void __launch_bounds__(32) k_agg_scale(const PvItem *items0, uint32_t n, const g1a *pts,
-                                                  const int32_t *dec, const int32_t *group_of, AggSeed seed,
-                                                  g1 *scaled) {
-  const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 1;
-  if (t >= 2 * n) return;  // both lanes of a pair leave together
-  const LanePair lp = LanePair::here();
-  const uint32_t i = t >> 1, which = t & 1;
+// pts4[4i + 2s] = P_{i,s}, pts4[4i + 2s + 1] = phi(P_{i,s}) = (beta x, -y) =
+// [lambda]P; sc[2i + s] = (a_i, b_i), or (0, 0) when the point takes no part
+// (every digit 0: bucket 0 collects it and is never summed).
+DEV void agg_put(uint32_t i, uint32_t s, bool use, const g1a &p, uint32_t a, uint32_t b, g1a *pts4, uint2 *sc) {
+  g1a e = p;
+  if (use) {
+    const fp beta = C_GLV_BETA;
+    e.x = fp_mul(p.x, beta);
+    e.y = fp_neg(p.y);
+  }
+  pts4[4 * i + 2 * s] = p;
+  pts4[4 * i + 2 * s + 1] = e;
+  sc[2 * i + s] = use ? make_uint2(a, b) : make_uint2(0u, 0u);
+}
+// ProofVerify: items of an aggregated group whose three points decoded take
+// part; an identity Abar or Bbar adds nothing (rho O = O).
+__global__ void __launch_bounds__(128) k_agg_prep_pv(const PvItem *items0, uint32_t n, const g1a *pts,
+                                                     const int32_t *dec, const int32_t *group_of, AggSeed seed,
+                                                     g1a *pts4, uint2 *sc) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || group_of[i] < 0) return;
   const PvItem it = items0[i];
-  bool use = group_of[i] >= 0 && it.status == ST_OK && it.pk_status == DEC_OK;
+  bool use = it.status == ST_OK && it.pk_status == DEC_OK;
   #pragma unroll 1
   for (int k = 0; k < 3 && use; k++) use = dec[3 * i + k] != DEC_BAD;
-  const int32_t d = dec[3 * i + which];
-  uint32_t ra, rb;
-  agg_rho(seed, i, ra, rb);
-  const g1 r = (use && d == DEC_OK) ? g1_mul_rho(lp, pts[3 * i + which], ra, rb) : g1_inf();
-  if (lp.role == 0) scaled[t] = r;
+  uint32_t a, b;
+  agg_rho(seed, i, a, b);
+  agg_put(i, 0, use && dec[3 * i] == DEC_OK, pts[3 * i], a, b, pts4, sc);
+  agg_put(i, 1, use && dec[3 * i + 1] == DEC_OK, pts[3 * i + 1], a, b, pts4, sc);
+}
+// Verify: the two points of the item's own pairing job (A and B - e A); a job
+// that is not evaluated, or a point the job skips (the identity), adds nothing.
+__global__ void __launch_bounds__(128) k_agg_prep_vf(const PairJob *pj, uint32_t n, const int32_t *group_of,
+                                                     AggSeed seed, g1a *pts4, uint2 *sc) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || group_of[i] < 0) return;
+  const PairJob j = pj[i];
+  const bool use = j.active == 1;
+  uint32_t a, b;
+  agg_rho(seed, i, a, b);
+  agg_put(i, 0, use && !(j.flags & 1u), j.pa, a, b, pts4, sc);
+  agg_put(i, 1, use && !(j.flags & 2u), j.pb, a, b, pts4, sc);
 }
 
-// Grid (groups, 2): block (g, 0) sums the scaled Abar of group g's items (in
-// perm[goff[g] .. goff[g+1])), block (g, 1) the scaled Bbar; each writes its
-// half of the group's pairing job in affine form (the job's flags start at 0).
-// 256 threads = 128 lane pairs: every pair sums a strided share of the items,
-// then the pairs' sums are added by shuffles within each warp and through
-// shared memory across the 8 warps.
+// Grid (groups, 8): block (g, 4 s + w) sorts the 2 n_g entries of set s,
+// window w of group g (entry 2m + h: item perm[goff[g] + m], h = 0 for a_i P,
+// 1 for b_i phi(P)) by their digit d = byte w of the scalar.  The indexes into
+// pts4 go to ent[(4 s + w) * 2 M + 2 goff[g] ..] bucket by bucket (M = number
+// of grouped items); bucket d spans [bo[d], bo[d + 1]) of that slab, with
+// bo = boff + (8 g + 4 s + w) * 257.
+__global__ void __launch_bounds__(256) k_agg_sort(const uint32_t *perm, const uint32_t *goff, const uint2 *sc,
+                                                  uint32_t M, uint32_t *ent, uint32_t *boff) {
+  __shared__ uint32_t cnt[256], wsum[8];
+  const uint32_t g = blockIdx.x, sw = blockIdx.y, s = sw >> 2, w = sw & 3, t = threadIdx.x;
+  const uint32_t lane = t & 31, warp = t >> 5;
+  const uint32_t g0 = goff[g], ng = goff[g + 1] - g0;
+  cnt[t] = 0;
+  __syncthreads();
+  #pragma unroll 1
+  for (uint32_t k = t; k < 2 * ng; k += 256) {
+    const uint2 v = sc[2 * perm[g0 + (k >> 1)] + s];
+    atomicAdd(&cnt[(((k & 1) ? v.y : v.x) >> (8 * w)) & 255u], 1u);
+  }
+  __syncthreads();
+  const uint32_t c = cnt[t];
+  uint32_t incl = c;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t y = __shfl_up_sync(0xffffffffu, incl, d);
+    if (lane >= (uint32_t)d) incl += y;
+  }
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  uint32_t base = 2 * g0;
+  for (uint32_t k = 0; k < warp; k++) base += wsum[k];
+  const uint32_t excl = base + incl - c;
+  uint32_t *bo = boff + (size_t)(AGG_SLAB * g + sw) * 257;
+  bo[t] = excl;
+  if (t == 255) bo[256] = excl + c;
+  __syncthreads();  // every thread has read cnt[t]
+  cnt[t] = excl;
+  __syncthreads();
+  uint32_t *e = ent + (size_t)sw * 2 * M;
+  #pragma unroll 1
+  for (uint32_t k = t; k < 2 * ng; k += 256) {
+    const uint32_t i = perm[g0 + (k >> 1)];
+    const uint2 v = sc[2 * i + s];
+    const uint32_t d = (((k & 1) ? v.y : v.x) >> (8 * w)) & 255u;
+    e[atomicAdd(&cnt[d], 1u)] = 4 * i + 2 * s + (k & 1);
+  }
+}
+
+// Sum of the 16 pairs' points of a warp (valid on lanes 0 and 1).
 DEV g1 shfl_down_g1_all(const g1 &p, int delta) {
   g1 r;
 #pragma unroll
@@ -260,7 +326,6 @@ DEV g1 shfl_down_g1_all(const g1 &p, int delta) {
   }
   return r;
 }
-// Sum of the 16 pairs' points of a warp (valid on lanes 0 and 1).
 DEV g1 warp_sum_pairs(const LanePair &lp, g1 acc) {
 #pragma unroll 1
   for (int d = 2; d < 32; d *= 2) {
@@ -271,38 +336,83 @@ DEV g1 warp_sum_pairs(const LanePair &lp, g1 acc) {
   }
   return acc;
 }
-__global__ void __launch_bounds__(256) k_agg_sum(const g1 *scaled, const uint32_t *perm, const uint32_t *goff,
-                                                 const int32_t *gslot, PairJob *gjobs) {
-  __shared__ g1 part[8];
-  const uint32_t g = blockIdx.x, which = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+
+// 64 blocks of 64 threads per group: block 8 q + c (q = 8 g + 4 s + w) gives
+// buckets 32 c .. 32 c + 31 of slab q one lane pair each.  A pair adds the
+// points of its bucket j (mixed additions) and multiplies the sum by j (from
+// its top bit down; the additions are kept by a select, and the pairs of a
+// warp share every bit but the low four, so they stay together); the 16 pairs
+// of each warp add their products, and lanes 0 and 1 write the warp's sum to
+// part[16 q + 2 c + warp].
+__global__ void __launch_bounds__(64) k_agg_buckets(const g1a *pts4, const uint32_t *ent, const uint32_t *boff,
+                                                    uint32_t M, g1 *part) {
+  const uint32_t q = blockIdx.x >> 3, c = blockIdx.x & 7, sw = q % AGG_SLAB;
   const LanePair lp = LanePair::here();
-  g1 a = g1_inf();
-  #pragma unroll 1
-  for (uint32_t k = goff[g] + (threadIdx.x >> 1); k < goff[g + 1]; k += blockDim.x >> 1)
-    a = g1_add_pair(lp, a, scaled[2 * perm[k] + which]);
-  a = warp_sum_pairs(lp, a);
-  if (lane == 0) part[warp] = a;
-  __syncthreads();
-  if (warp == 0) {
-    a = lane < 16 ? part[lane >> 1] : g1_inf();
-    a = warp_sum_pairs(lp, a);
-    if (lane == 0) {
-      g1a aff;
-      const bool finite = g1_to_aff(a, aff);
-      PairJob &j = gjobs[g];
-      if (which == 0) {
-        j.pa = aff;
-        j.slot_a = gslot[g];
-        j.slot_b = 0;
-        j.active = 1;
-      } else {
-        j.pb = aff;
-      }
-      if (!finite) atomicOr(&j.flags, which == 0 ? 1u : 2u);
-    }
+  const uint32_t j = 32 * c + (threadIdx.x >> 1);
+  const uint32_t *bo = boff + (size_t)q * 257;
+  const uint32_t *e = ent + (size_t)sw * 2 * M;
+  g1 sum = g1_inf();
+  if (j) {
+    const uint32_t k1 = bo[j + 1];
+    #pragma unroll 1
+    for (uint32_t k = bo[j]; k < k1; k++) sum = g1_add_aff_pair(lp, sum, pts4[e[k]]);
   }
+  g1 r = sum;
+  #pragma unroll 1
+  for (int bit = j ? 30 - __clz(j) : -1; bit >= 0; bit--) {
+    r = g1_dbl_pair(lp, r);
+    const g1 t = g1_add_pair(lp, r, sum);
+    if ((j >> bit) & 1) r = t;
+  }
+  r = warp_sum_pairs(lp, r);
+  if ((threadIdx.x & 31) == 0) part[(size_t)q * 16 + 2 * c + (threadIdx.x >> 5)] = r;
 }
 
+// Grid (groups, 2), 128 threads: warp w adds the 16 warp sums of window w of
+// set s (one per lane pair), then every quad of the warp doubles that sum 8 w
+// times; the four windows are added by warp 0, and lane 0 writes the affine
+// result as half of group g's pairing job (the jobs start zeroed): set 0 is
+// pa (with the key's slot), set 1 pb; an identity sum sets the job's flag.
+DEV g1 shfl_g1(const g1 &p, int src) {
+  g1 r;
+#pragma unroll
+  for (int i = 0; i < 12; i++) {
+    r.X.w[i] = __shfl_sync(0xffffffffu, p.X.w[i], src);
+    r.Y.w[i] = __shfl_sync(0xffffffffu, p.Y.w[i], src);
+    r.ZZ.w[i] = __shfl_sync(0xffffffffu, p.ZZ.w[i], src);
+    r.ZZZ.w[i] = __shfl_sync(0xffffffffu, p.ZZZ.w[i], src);
+  }
+  return r;
+}
+__global__ void __launch_bounds__(128) k_agg_combine(const g1 *part, const int32_t *gslot, PairJob *gjobs) {
+  __shared__ g1 win[4];
+  const uint32_t g = blockIdx.x, s = blockIdx.y, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const LanePair lp = LanePair::here();
+  g1 a = part[(size_t)(AGG_SLAB * g + 4 * s + w) * 16 + (lane >> 1)];
+  a = shfl_g1(warp_sum_pairs(lp, a), 0);
+  const LaneQuad lq = LaneQuad::here();
+  #pragma unroll 1
+  for (uint32_t k = 0; k < 8 * w; k++) a = g1_dbl_quad(lq, a);
+  if (lane == 0) win[w] = a;
+  __syncthreads();
+  if (w != 0) return;
+  a = warp_sum_pairs(lp, lane < 8 ? win[lane >> 1] : g1_inf());
+  if (lane == 0) {
+    g1a aff;
+    const bool finite = g1_to_aff(a, aff);
+    if (!finite) aff.x = aff.y = fp_zero();
+    PairJob &jb = gjobs[g];
+    if (s == 0) {
+      jb.pa = aff;
+      jb.slot_a = gslot[g];
+      jb.slot_b = 0;
+      jb.active = 1;
+    } else {
+      jb.pb = aff;
+    }
+    if (!finite) atomicOr(&jb.flags, s == 0 ? 1u : 2u);
+  }
+}
 // Per-item pairing jobs after the group checks: an item of a group whose check
 // passed is valid for the pairing (ok = 1, job skipped); any other item that
 // decoded gets its own check.
@@ -331,23 +441,6 @@ __global__ void __launch_bounds__(128) k_pv_pairjobs_agg(const PvItem *items0, u
   pj[i] = job;
 }
 
-// Verify: one lane pair per (item, point) of an aggregated group:
-// scaled[2i] = rho_i A_i, scaled[2i+1] = rho_i (B_i - e_i A_i), from the
-// item's own pairing job (its two G1 points); an item whose job is not
-// evaluated, or a point the job skips (the identity), contributes nothing.
-__global__ void __launch_bounds__(32) k_vf_agg_scale(const PairJob *pj, uint32_t n, const int32_t *group_of,
-                                                     AggSeed seed, g1 *scaled) {
-  const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 1;
-  if (t >= 2 * n) return;  // both lanes of a pair leave together
-  const LanePair lp = LanePair::here();
-  const uint32_t i = t >> 1, which = t & 1;
-  const PairJob j = pj[i];
-  const bool use = group_of[i] >= 0 && j.active == 1 && !(j.flags & (which ? 2u : 1u));
-  uint32_t ra, rb;
-  agg_rho(seed, i, ra, rb);
-  const g1 r = use ? g1_mul_rho(lp, which ? j.pb : j.pa, ra, rb) : g1_inf();
-  if (lp.role == 0) scaled[t] = r;
-}
 // Verify: items of groups whose check passed are settled (ok = 1, job
 // skipped); the others keep their own job.
 __global__ void __launch_bounds__(128) k_vf_pairjobs_agg(uint32_t n, const int32_t *group_of,
@@ -1029,7 +1122,11 @@ struct OpBatch {
   uint32_t *perm = nullptr, *goff = nullptr;
   PairJob *gjobs = nullptr;
   uint8_t *gok = nullptr;
-  g1 *scaled = nullptr;
+  // bucket MSM of the group sums (k_agg_*)
+  g1a *agg_pts = nullptr;
+  uint2 *agg_sc = nullptr;
+  uint32_t *agg_ent = nullptr, *agg_boff = nullptr;
+  g1 *agg_part = nullptr;
   g1 *fixed = nullptr, *v = nullptr;
   PairJob *pj = nullptr;
   uint8_t *ok = nullptr, *out = nullptr;
@@ -1097,7 +1194,12 @@ template <typename ItemT> void plan_groups_of(Runtime &rt, OpBatch &b) {
     b.gslot = upload(rt, b.h_gslot.data(), G);
     b.gjobs = rt.arena.alloc<PairJob>(G);
     b.gok = rt.arena.alloc<uint8_t>(G);
-    b.scaled = rt.arena.alloc<g1>(2 * n);
+    const size_t M = b.h_perm.size();
+    b.agg_pts = rt.arena.alloc<g1a>(4 * n);
+    b.agg_sc = rt.arena.alloc<uint2>(2 * n);
+    b.agg_ent = rt.arena.alloc<uint32_t>(2 * AGG_SLAB * M);
+    b.agg_boff = rt.arena.alloc<uint32_t>(AGG_SLAB * G * 257);
+    b.agg_part = rt.arena.alloc<g1>(AGG_SLAB * G * 16);
   }
 }
 
@@ -1111,7 +1213,8 @@ void upload(Runtime &rt, OpBatch &b) {
                 fr_rows * sizeof(fr) + 2 * n * sizeof(uint32_t) + nv * (sizeof(VarJob) + sizeof(fr) + sizeof(g1)) +
                 (b.pts48.size() / 48) * (sizeof(g1a) + 8) + 2 * n * sizeof(g1) + 2 * n * sizeof(g1a) +
                 n * b.rs_stride * sizeof(fr) + b.out_total + n * (2 * sizeof(g1) + 16 + sizeof(PairJob) + 8) +
-                64 * 256;
+                n * (4 * sizeof(g1a) + 2 * sizeof(uint2) + 4 * 2 * AGG_SLAB) +
+                (n / AGG_MIN_GROUP + 1) * AGG_SLAB * (257 * 4 + 16 * sizeof(g1)) + 64 * 256;
   rt.arena.reserve(need);
   rt.staging.reserve(65536 + 8 * nm + b.pts48.size() + n * (b.item_size + sizeof(DomainJob) + 96));
   // the blob and the message bytes are already pinned: DMA them directly
@@ -1188,6 +1291,17 @@ void span_end(cudaStream_t s, int k, const char *name) {
     span_end(stream, _k, label);          \
   } while (0)
 
+// The group sums of a batch (k_agg_prep_* has filled agg_pts / agg_sc).
+void launch_agg_buckets(cudaStream_t s, OpBatch &b, uint32_t G) {
+  const uint32_t M = (uint32_t)b.h_perm.size();
+  k_agg_sort<<<dim3(G, AGG_SLAB), 256, 0, s>>>(b.perm, b.goff, b.agg_sc, M, b.agg_ent, b.agg_boff);
+  k_agg_buckets<<<AGG_SLAB * G * 8, 64, 0, s>>>(b.agg_pts, b.agg_ent, b.agg_boff, M, b.agg_part);
+}
+void launch_agg_combine(cudaStream_t s, OpBatch &b, uint32_t G) {
+  CUBBS_CHECK(cudaMemsetAsync(b.gjobs, 0, G * sizeof(PairJob), s));
+  k_agg_combine<<<dim3(G, 2), 128, 0, s>>>(b.agg_part, b.gslot, b.gjobs);
+}
+
 // ProofVerify on four streams.  Decoding Abar, Bbar, D (stream2) is
 // independent of the message hash, the domain and the T2 fixed-base MSM
 // (stream); the variable-base terms follow the decode on stream2 and the
@@ -1197,11 +1311,12 @@ void span_end(cudaStream_t s, int k, const char *name) {
 // with a point outside G1 before any result is read.  Each of these kernels
 // fills only part of the GPU, so running them side by side shortens the step.
 // With the SM partition, the four streams are those of the larger partition
-// and the aggregated pairing chain (random-coefficient scaling, group sums,
-// one check per key group: the step's critical path, made of kernels that
-// fill only a few SMs) runs alone on the smaller one, when its groups fit
-// there two to an SM.  Sharing SMs with the MSM kernels stretched that chain
-// from about 3.5 ms to 5 ms.
+// and the aggregated pairing chain (the group sums' bucket MSM and one check
+// per key group, made of kernels that fill only a few SMs) runs alone on the
+// smaller one, when its groups fit there two to an SM.  Sharing SMs with the
+// MSM kernels stretched that chain from about 3.5 ms to 5 ms.  With the third
+// partition, stream2 (the decode and the variable-base terms) runs on it and
+// the other three streams on the SMs left.
 void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   const bool part = !b.h_gslot.empty() && rt.use_partition();
   cudaStream_t s0 = rt.stream;
@@ -1237,11 +1352,11 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
       CUBBS_CHECK(cudaEventRecord(rt.ev_gc, s3));
       CUBBS_CHECK(cudaStreamWaitEvent(sa, rt.ev_gc, 0));
     }
-    SPAN(sa, "agg_scale",
-         k_agg_scale<<<blocks_for(4 * n, 32), 32, 0, sa>>>(it0, N, b.pts, b.dec, b.group_of, seed, b.scaled));
-    SPAN(sa, "agg_sum",
-         CUBBS_CHECK(cudaMemsetAsync(b.gjobs, 0, G * sizeof(PairJob), sa));
-         k_agg_sum<<<dim3(G, 2), 256, 0, sa>>>(b.scaled, b.perm, b.goff, b.gslot, b.gjobs));
+    SPAN(sa, "agg_buckets",
+         k_agg_prep_pv<<<blocks_for(n, 128), 128, 0, sa>>>(it0, N, b.pts, b.dec, b.group_of, seed, b.agg_pts,
+                                                            b.agg_sc);
+         launch_agg_buckets(sa, b, G));
+    SPAN(sa, "agg_sum", launch_agg_combine(sa, b, G));
     SPAN(sa, "pairing_check", launch_pairing_check_split(sa, b.gjobs, G, rt.d_lines, b.gok));
     if (alone) {
       CUBBS_CHECK(cudaEventRecord(rt.ev_gc2, sa));
@@ -1278,7 +1393,7 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
     CUBBS_CHECK(cudaEventRecord(rt.ev_done, s));
     CUBBS_CHECK(cudaStreamWaitEvent(s0, rt.ev_done, 0));
   }
-  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 8 + (G ? 3 : 0);
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 8 + (G ? 5 : 0);
 }
 
 // ProofGen on three streams: the signature decode (stream3) runs beside
@@ -1367,10 +1482,10 @@ void run_verify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
       if (r <= 0) throw CudaError(cudaErrorUnknown, "getrandom");
       got += (size_t)r;
     }
-    SPAN(s, "agg_scale", k_vf_agg_scale<<<blocks_for(4 * n, 32), 32, 0, s>>>(b.pj, N, b.group_of, seed, b.scaled));
-    SPAN(s, "agg_sum",
-         CUBBS_CHECK(cudaMemsetAsync(b.gjobs, 0, G * sizeof(PairJob), s));
-         k_agg_sum<<<dim3(G, 2), 256, 0, s>>>(b.scaled, b.perm, b.goff, b.gslot, b.gjobs));
+    SPAN(s, "agg_buckets",
+         k_agg_prep_vf<<<blocks_for(n, 128), 128, 0, s>>>(b.pj, N, b.group_of, seed, b.agg_pts, b.agg_sc);
+         launch_agg_buckets(s, b, G));
+    SPAN(s, "agg_sum", launch_agg_combine(s, b, G));
     SPAN(s, "pairing_check", launch_pairing_check_split(s, b.gjobs, G, rt.d_lines, b.gok));
     SPAN(s, "pairing",
          k_vf_pairjobs_agg<<<blocks_for(n, 128), 128, 0, s>>>(N, b.group_of, b.gok, b.pj, b.ok);
@@ -1380,7 +1495,7 @@ void run_verify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   } else {
     SPAN(s, "pairing", launch_pairing_check(s, b.pj, N, rt.d_lines, b.ok));
   }
-  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 7 + (G ? 4 : 0);
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 7 + (G ? 6 : 0);
 }
 
 // The whole device pipeline of one batch (no host work, no transfers).

@@ -96,51 +96,72 @@ DEV uint32_t scalar_bits(const fr &s, int pos, int w) {
   return (uint32_t)(v & ((1u << w) - 1));
 }
 
-// One MSM row on one warp (all lanes call it): lane l takes generators
-// l, l+32, ...; per generator the scalar is recoded into signed w-bit digits
-// on the fly and each nonzero digit costs one table lookup and one mixed
-// addition; the lanes' sums are added by shuffles.
-DEV void fixed_msm_row(const FixedTable &t, const fr *scalars, uint32_t stride, const uint32_t *nterms, uint32_t row,
-                       int lane, g1 *out) {
-  uint32_t n = nterms[row];
-  g1 acc = g1_inf();
-  const uint32_t full = 1u << t.w;
+// Signed w-bit digit of window k of scalar s (digits in (-half, half], a
+// digit above half becomes d - 2^w with a carry into the next window).  The
+// carry into window k is recomputed from the windows below it, so any window
+// can be taken alone; the work is a few integer operations per window, next
+// to the mixed addition the digit costs.
+DEV uint32_t fixed_digit(const fr &s, int k, int w, uint32_t half, bool &neg) {
+  uint32_t carry = 0;
   #pragma unroll 1
-  for (uint32_t g = lane; g < n; g += 32) {
-    fr s = scalars[(size_t)row * stride + g];
-    uint32_t carry = 0;
-    const g1a *base = t.entries + (size_t)g * t.nwin * t.half;
-    #pragma unroll 1
-    for (int k = 0; k < t.nwin; k++) {
-      uint32_t d = scalar_bits(s, k * t.w, t.w) + carry;
-      bool neg = false;
-      if (d > (uint32_t)t.half) {
-        d = full - d;
-        neg = true;
-        carry = 1;
-      } else {
-        carry = 0;
-      }
-      if (d) {
-        g1a e = base[(size_t)k * t.half + d - 1];
-        if (neg) e.y = fp_neg(e.y);
-        acc = g1_add_aff(acc, e);
-      }
+  for (int i = 0; i < k; i++) carry = scalar_bits(s, i * w, w) + carry > half ? 1u : 0u;
+  uint32_t d = scalar_bits(s, k * w, w) + carry;
+  neg = d > half;
+  return neg ? (1u << w) - d : d;  // 2^w - d is 0 for d = 2^w (the carry alone)
+}
+// Sum of the points of the L-lane groups of a warp (valid on each group's first lane).
+template <int L> DEV g1 group_sum_g1(g1 acc) {
+  #pragma unroll 1
+  for (int d = L / 2; d > 0; d >>= 1) {
+    g1 o;
+#pragma unroll
+    for (int i = 0; i < 12; i++) {
+      o.X.w[i] = __shfl_down_sync(0xffffffffu, acc.X.w[i], d, L);
+      o.Y.w[i] = __shfl_down_sync(0xffffffffu, acc.Y.w[i], d, L);
+      o.ZZ.w[i] = __shfl_down_sync(0xffffffffu, acc.ZZ.w[i], d, L);
+      o.ZZZ.w[i] = __shfl_down_sync(0xffffffffu, acc.ZZZ.w[i], d, L);
     }
+    acc = g1_add(acc, o);
   }
-  acc = warp_sum_g1(acc);
-  if (lane == 0) out[row] = acc;
+  return acc;
 }
 
-// Fixed-base MSM: row r = sum_g scalars[r*stride + g] * G_g, g < nterms[r]; the
-// grid's warps take rows in a grid-stride loop.
+// Fixed-base MSM: row r = sum_g scalars[r*stride + g] * G_g, g < nterms[r].
+// A row runs on a group of L lanes (L = 4 .. 32): its (generator, window)
+// units g * nwin + k are dealt round robin to the group's lanes, so every lane
+// does the same number of mixed additions whatever the row's length (give or
+// take one); each nonzero digit costs one table lookup and one mixed addition,
+// and the lanes' sums are added by shuffles within the group.  The warps take
+// rows in a grid-stride loop, a warp 32 / L rows at a time (every lane of a
+// warp runs the same iterations, as the shuffles need).
+template <int L>
 __global__ void __launch_bounds__(128) k_fixed_msm(FixedTable t, const fr *scalars, uint32_t stride,
                                                    const uint32_t *nterms, uint32_t rows, g1 *out) {
+  constexpr uint32_t PER_WARP = 32 / L;
   const uint32_t warps = (gridDim.x * blockDim.x) >> 5;
-  const int lane = threadIdx.x & 31;
+  const uint32_t lane = threadIdx.x & 31, sub = lane % L, grp = lane / L;
+  const uint32_t half = (uint32_t)t.half, nwin = (uint32_t)t.nwin;
   #pragma unroll 1
-  for (uint32_t row = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; row < rows; row += warps)  // per warp
-    fixed_msm_row(t, scalars, stride, nterms, row, lane, out);
+  for (uint32_t base = ((blockIdx.x * blockDim.x + threadIdx.x) >> 5) * PER_WARP; base < rows;
+       base += warps * PER_WARP) {
+    const uint32_t row = base + grp;
+    const uint32_t units = row < rows ? nterms[row] * nwin : 0;
+    g1 acc = g1_inf();
+    #pragma unroll 1
+    for (uint32_t u = sub; u < units; u += L) {
+      const uint32_t g = u / nwin, k = u - g * nwin;
+      const fr sc = scalars[(size_t)row * stride + g];
+      bool neg;
+      const uint32_t d = fixed_digit(sc, (int)k, t.w, half, neg);
+      if (d) {
+        g1a e = t.entries[((size_t)g * nwin + k) * half + d - 1];
+        if (neg) e.y = fp_neg(e.y);
+        acc = g1_add_aff_inl(acc, e);  // inlined: no struct arguments through the stack
+      }
+    }
+    acc = group_sum_g1<L>(acc);
+    if (sub == 0 && row < rows) out[row] = acc;
+  }
 }
 
 // One lane pair per job (g1_mul_glv_pair): the pair splits each point
@@ -276,11 +297,34 @@ void launch_build_table(cudaStream_t s, const g1a *gens, int g0, int g1n, FixedT
   const int run = std::min(t.half, 256);
   k_table_build<<<blocks_for((size_t)nb * (t.half / run), 64), 64, 0, s>>>(bases, g0, g1n, t, run, scratch, prod);
 }
+// Lanes per row (CUBBS_BBS_FIXED_LANES forces 4, 8, 16 or 32): a launch whose
+// rows give at most two warps per SM sub-partition at 32 lanes a row is bound
+// by one row's latency, so a row gets the whole warp; a larger launch is bound
+// by issue, where the shuffle reduction (log2 L full additions on every lane)
+// outweighs a shorter chain, so short rows share a warp: 16 lanes for rows of
+// 256 units or more, else 8.
+static int fixed_lanes_for(uint32_t rows, uint32_t stride, int nwin) {
+  static const int forced = [] {
+    const char *e = std::getenv("CUBBS_BBS_FIXED_LANES");
+    const int x = e && *e ? std::atoi(e) : 0;
+    return (x == 4 || x == 8 || x == 16 || x == 32) ? x : 0;
+  }();
+  if (forced) return forced;
+  int dev = 0, sms = 152;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if ((size_t)rows <= (size_t)sms * 8) return 32;
+  return (size_t)stride * nwin >= 256 ? 16 : 8;
+}
 void launch_fixed_msm(cudaStream_t s, const FixedTable &t, const fr *scalars, uint32_t stride,
                       const uint32_t *nterms, uint32_t rows, g1 *out) {
-  // one warp per row: fewer warps with several rows each lengthen the MSM more than they
-  // relieve the kernels that share its SMs (measured in the ProofVerify step)
-  if (rows) k_fixed_msm<<<blocks_for((size_t)rows * 32, 128), 128, 0, s>>>(t, scalars, stride, nterms, rows, out);
+  if (!rows) return;
+  const int L = fixed_lanes_for(rows, stride, t.nwin);
+  const size_t threads = (size_t)(rows + 32 / L - 1) / (32 / L) * 32;
+  const unsigned blocks = blocks_for(threads, 128);
+  if (L == 32) k_fixed_msm<32><<<blocks, 128, 0, s>>>(t, scalars, stride, nterms, rows, out);
+  else if (L == 16) k_fixed_msm<16><<<blocks, 128, 0, s>>>(t, scalars, stride, nterms, rows, out);
+  else if (L == 8) k_fixed_msm<8><<<blocks, 128, 0, s>>>(t, scalars, stride, nterms, rows, out);
+  else k_fixed_msm<4><<<blocks, 128, 0, s>>>(t, scalars, stride, nterms, rows, out);
 }
 void launch_var_mul(cudaStream_t s, const g1a *points, const VarJob *jobs, const fr *scalars, uint32_t n, g1 *out,
                     int lanes) {

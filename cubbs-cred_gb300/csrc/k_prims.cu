@@ -1226,6 +1226,24 @@ extern "C" int32_t cubbs_bbs_gpu_sm_partition_v2(int32_t *small_sms, int32_t *re
   }
 }
 
+// SMs of the third ProofVerify partition (the point decode and the
+// variable-base terms), split off the rest; 0 when it is off
+// (CUBBS_BBS_VAR_SMS=0, the driver refused the split, or no partition), and
+// *status tells why (0: on; 1: not asked for; -1: no partition; else the step
+// that failed * 1000 + driver result).
+extern "C" int32_t cubbs_bbs_gpu_sm_partition_var_v2(int32_t *var_sms, int32_t *status) {
+  if (!var_sms || !status) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;
+  try {
+    CallScope scope;
+    const bool on = scope.rt.use_partition();
+    *var_sms = on ? scope.rt.sh.var_sms : 0;
+    *status = scope.rt.sh.var_status;
+    return CUBBS_BBS_GPU_SUCCESS;
+  } catch (const CudaError &) {
+    return CUBBS_BBS_GPU_ERR_INTERNAL;
+  }
+}
+
 // Window width of the resident fixed-base table (0 before the first table is built).
 extern "C" int32_t cubbs_bbs_gpu_table_window_v2(int32_t *w) {
   if (!w) return CUBBS_BBS_GPU_ERR_INVALID_INPUT;

@@ -120,6 +120,36 @@ static bool profiler_injected() {
   return false;
 }
 
+// A probe kernel on a stream of each of two green contexts, ordered by an
+// event; true when both ran.
+static bool partition_probe(CUresult (*stream_create)(CUstream *, CUgreenCtx, unsigned, int), CUgreenCtx x,
+                            CUgreenCtx y) {
+  CUstream a = nullptr, b = nullptr;
+  cudaEvent_t ev = nullptr;
+  int *flag = nullptr, got = 0;
+  bool ok = stream_create(&a, x, CU_STREAM_NON_BLOCKING, 0) == CUDA_SUCCESS &&
+            stream_create(&b, y, CU_STREAM_NON_BLOCKING, 0) == CUDA_SUCCESS &&
+            cudaEventCreateWithFlags(&ev, cudaEventDisableTiming) == cudaSuccess &&
+            cudaMalloc(&flag, sizeof(int)) == cudaSuccess && cudaMemsetAsync(flag, 0, sizeof(int), b) == cudaSuccess;
+  if (ok) {
+    k_partition_probe<<<1, 32, 0, b>>>(flag);
+    ok = cudaGetLastError() == cudaSuccess && cudaEventRecord(ev, b) == cudaSuccess &&
+         cudaStreamWaitEvent(a, ev, 0) == cudaSuccess;
+  }
+  if (ok) {
+    k_partition_probe<<<1, 32, 0, a>>>(flag);
+    ok = cudaGetLastError() == cudaSuccess &&
+         cudaMemcpyAsync(&got, flag, sizeof(int), cudaMemcpyDeviceToHost, a) == cudaSuccess &&
+         cudaStreamSynchronize(a) == cudaSuccess && got == 2;
+  }
+  (void)cudaGetLastError();
+  if (a) cudaStreamDestroy(a);
+  if (b) cudaStreamDestroy(b);
+  if (ev) cudaEventDestroy(ev);
+  if (flag) cudaFree(flag);
+  return ok;
+}
+
 void SharedState::init_partition() {
   const char *setting = std::getenv("CUBBS_BBS_SM_PARTITION");
   if (profiler_injected() && !(setting && *setting)) {
@@ -174,6 +204,64 @@ void SharedState::init_partition() {
     destroy(gs);
     return (void)fail(10, r);
   }
+  // Optionally a third partition: CUBBS_BBS_VAR_SMS SMs (default 32; 0:
+  // none) taken from the larger one for the point decode and the
+  // variable-base terms of ProofVerify, whose lane pairs then stop sharing
+  // issue slots with the fixed-base MSM and the subgroup check.  Measured on
+  // GB300 (1024 proofs, L = 100): 32 SMs 3.87 ms per step, 48 / 56 SMs 3.9 ms,
+  // 64 SMs 4.2 ms (the terms at one warp per SM sub-partition take 1.9 ms
+  // instead of 2.8, but the subgroup check on the 72 SMs left takes 3.2 ms),
+  // no third partition 4.2 ms.  The device's SMs are split into groups of 8
+  // in one call and the groups are joined into the three partitions (the
+  // chain's partition then holds the first groups, as many SMs as the two-way
+  // split gave it, and replaces that split's own small partition so that the
+  // three come from one split and do not overlap).  var_status records why it
+  // is off; any failure here leaves the two-way split as it is.
+  CUgreenCtx gv = nullptr, gr2 = nullptr, gs3 = nullptr;
+  int var_count = 0, small3 = 0;
+  const int var_want = env_int("CUBBS_BBS_VAR_SMS", 32);
+  var_status = 1;
+  if (var_want > 0 && var_want + 16 <= (int)rest.sm.smCount) {
+    constexpr unsigned GMAX = 64;
+    CUdevResource grp[GMAX], left{};
+    unsigned ng = GMAX;
+    var_status = 2;
+    r = split(grp, &ng, &all, &left, 0, 8u);
+    if (r != CUDA_SUCCESS) var_status = 3000 + (int)r;
+    if (r == CUDA_SUCCESS) {
+      // groups [0, k0): the chain's SMs; [k0, k1): the variable-base terms; the rest
+      unsigned k0 = 0, k1 = 0;
+      while (k0 < ng && small3 < (int)small.sm.smCount) small3 += (int)grp[k0++].sm.smCount;
+      k1 = k0;
+      while (k1 < ng && var_count < var_want) var_count += (int)grp[k1++].sm.smCount;
+      CUdevResource rest_parts[GMAX + 1];
+      unsigned nr = 0;
+      for (unsigned k = k1; k < ng; k++) rest_parts[nr++] = grp[k];
+      if (left.sm.smCount) rest_parts[nr++] = left;
+      CUdevResourceDesc dvar, drest2, dsmall3;
+      if (k0 == 0 || k1 == k0 || nr == 0) {
+        var_status = 4;
+      } else if ((r = gen_desc(&dsmall3, grp, k0)) != CUDA_SUCCESS) {
+        var_status = 4000 + (int)r;
+      } else if ((r = gen_desc(&dvar, grp + k0, k1 - k0)) != CUDA_SUCCESS) {
+        var_status = 5000 + (int)r;
+      } else if ((r = gen_desc(&drest2, rest_parts, nr)) != CUDA_SUCCESS) {
+        var_status = 6000 + (int)r;
+      } else if ((r = create(&gv, dvar, dev, CU_GREEN_CTX_DEFAULT_STREAM)) != CUDA_SUCCESS) {
+        var_status = 7000 + (int)r;
+        gv = nullptr;
+      } else if ((r = create(&gr2, drest2, dev, CU_GREEN_CTX_DEFAULT_STREAM)) != CUDA_SUCCESS) {
+        var_status = 8000 + (int)r;
+        destroy(gv);
+        gv = gr2 = nullptr;
+      } else if ((r = create(&gs3, dsmall3, dev, CU_GREEN_CTX_DEFAULT_STREAM)) != CUDA_SUCCESS) {
+        var_status = 10000 + (int)r;
+        destroy(gv);
+        destroy(gr2);
+        gv = gr2 = gs3 = nullptr;
+      }
+    }
+  }
   // self-test: a kernel on each partition, ordered by an event
   CUstream a = nullptr, b = nullptr;
   cudaEvent_t ev = nullptr;
@@ -208,6 +296,9 @@ void SharedState::init_partition() {
   if (!ok) {
     destroy(gs);
     destroy(gr);
+    if (gv) destroy(gv);
+    if (gr2) destroy(gr2);
+    if (gs3) destroy(gs3);
     partition_status = 1000 * step + (int)last;
     return;
   }
@@ -215,6 +306,20 @@ void SharedState::init_partition() {
   green_rest = gr;
   small_sms = (int)small.sm.smCount;
   rest_sms = (int)rest.sm.smCount;
+  if (gv && partition_probe(stream_create, gv, gr2) && partition_probe(stream_create, gs3, gv)) {
+    destroy(gs);
+    green_small = gs3;
+    small_sms = small3;
+    green_var = gv;
+    green_rest2 = gr2;
+    var_sms = var_count;
+    var_status = 0;
+  } else if (gv) {
+    var_status = 9;
+    destroy(gv);
+    destroy(gr2);
+    destroy(gs3);
+  }
   green_stream_create = stream_create;
   partition_status = 0;
 }
@@ -426,8 +531,12 @@ bool Runtime::use_partition() {
   CUBBS_CHECK(cudaDeviceGetStreamPriorityRange(&lo, &hi));
   cudaStream_t p[4] = {nullptr, nullptr, nullptr, nullptr}, pc = nullptr;
   bool ok = true;
-  for (int k = 0; k < 4 && ok; k++)
-    ok = sh.green_stream_create(&p[k], sh.green_rest, CU_STREAM_NON_BLOCKING, k == 2 ? hi : 0) == CUDA_SUCCESS;
+  // with the third partition, part[1] (decode, variable-base terms) runs on it
+  // and the other three on the remaining SMs
+  for (int k = 0; k < 4 && ok; k++) {
+    CUgreenCtx where = sh.green_var ? (k == 1 ? sh.green_var : sh.green_rest2) : sh.green_rest;
+    ok = sh.green_stream_create(&p[k], where, CU_STREAM_NON_BLOCKING, k == 2 ? hi : 0) == CUDA_SUCCESS;
+  }
   ok = ok && sh.green_stream_create(&pc, sh.green_small, CU_STREAM_NON_BLOCKING, hi) == CUDA_SUCCESS;
   if (!ok) {
     for (auto q : p)

@@ -172,6 +172,12 @@ struct SharedState {
   // partition or CUBBS_BBS_SM_PARTITION is 0.
   CUgreenCtx green_small = nullptr, green_rest = nullptr;
   int small_sms = 0, rest_sms = 0;
+  // green_rest split once more (CUBBS_BBS_VAR_SMS): green_var for the decode
+  // and the variable-base terms, green_rest2 for the other kernels (null when
+  // the split is off or failed; green_rest is then used whole)
+  CUgreenCtx green_var = nullptr, green_rest2 = nullptr;
+  int var_sms = 0;
+  int var_status = -1;  // 0: on; 1: not asked for; else the step that failed (* 1000 + driver result)
   int partition_status = -1;  // 0: on; -1: not tried yet; else why it is off (step * 1000 + driver result)
   bool partition_tried = false;
   CUresult (*green_stream_create)(CUstream *, CUgreenCtx, unsigned, int) = nullptr;

@@ -28,6 +28,12 @@ int32_t cubbs_bbs_gpu_table_window_v2(int32_t *w);
  * partition on first use. */
 int32_t cubbs_bbs_gpu_sm_partition_v2(int32_t *small_sms, int32_t *rest_sms, int32_t *status);
 
+/* SMs of the third ProofVerify partition (point decode and variable-base
+ * terms), split off rest_sms; 0 when off (CUBBS_BBS_VAR_SMS=0 or refused),
+ * with the reason in *status (0: on; 1: not asked for; -1: no partition;
+ * else failed step * 1000 + driver result). */
+int32_t cubbs_bbs_gpu_sm_partition_var_v2(int32_t *var_sms, int32_t *status);
+
 /* Fixed-base table width sweep w_lo..w_hi (4..20) over rows x terms scalars
  * against the first `terms` generators [P1, Q1, H1, ...]: each width's first
  * 64 rows are compared with a table-free recomputation (ms_per_w = -1 and
