@@ -56,49 +56,67 @@ DEV fp fp_mul_cios_inl(const fp &a, const fp &b) {
 }
 
 // The Montgomery product a b / 2^384 mod p (fully reduced) used everywhere:
-// carry-save accumulation instead of carry chains.  T_j are 64-bit partial
-// sums of limb position j; each row adds a_j b_i to every T_j (one
-// mad.wide.u32 each), splits every sum into its low word and the high word of
-// its right neighbour (N_j = lo(T_j) + hi(T_{j-1}) <= 2^33 - 2, so the next
-// 32 x 32-bit product cannot overflow 64 bits), adds m p_j, and splits again
-// while shifting one limb down.  No step depends on a carry from another
-// limb, so the twelve products of a row issue back to back and a lone warp
-// is bound by issue rate rather than by one ~640-step dependent carry chain.
-// One carry pass at the end and one conditional subtraction of p finish it.
+// carry-save accumulation instead of carry chains.  T_j = (hi_j : lo_j) are
+// 64-bit partial sums of limb position j; each row adds a_j b_i to every T_j
+// (a mad.lo.cc / madc.hi pair), splits every sum into its low word and the
+// high word of its right neighbour (N_j = lo(T_j) + hi(T_{j-1}) <= 2^33 - 2,
+// an add.cc / addc pair, so the next 32 x 32-bit product cannot overflow 64
+// bits), adds m p_j, and splits again while shifting one limb down.  No step
+// depends on a carry from another limb, so the twelve products of a row
+// issue back to back.  One carry pass at the end and one conditional
+// subtraction of p finish it.
 // Bounds: a, b < p; every partial sum stays below 2^64 (the worst case is
 // (2^33 - 2) + (2^32 - 1)^2 = 2^64 - 1) and the final value is below 2p.
-// Measured on GB300 against the CIOS form: 9 % more products per second at
-// full occupancy, 25 % more with one warp per SM sub-partition.
+// Written in PTX: from the same arithmetic in C++ 64-bit integers the
+// compiler put many of the splits' carry additions on the FMA pipe, beside
+// the multiplies (522 FMA-pipe and 511 ALU instructions a product); here 324
+// and 587.  Measured on GB300, one warp, chains of dependent products: 1965
+// cycles a product against 2316 for the C++ form (and 2802 for CIOS); about
+// the same with two warps per SM sub-partition (1830 vs 1860 cycles of the
+// sub-partition a product) and 3 % slower with four (1813 vs 1753).  Every
+// carry flag lives inside one asm statement.
 DEV fp fp_mul_inl(const fp &a, const fp &b) {
   const fp pm = FP_MOD_INIT;
-  uint64_t T[12];
+  uint32_t lo[12], hi[12];  // T_j = hi_j : lo_j
 #pragma unroll
-  for (int j = 0; j < 12; j++) T[j] = 0;
+  for (int j = 0; j < 12; j++) lo[j] = hi[j] = 0;
 #pragma unroll
   for (int i = 0; i < 12; i++) {
     const uint32_t bi = b.w[i];
 #pragma unroll
-    for (int j = 0; j < 12; j++) T[j] += (uint64_t)a.w[j] * bi;
-    uint64_t N[12];
-    N[0] = (uint32_t)T[0];
+    for (int j = 0; j < 12; j++)
+      asm("mad.lo.cc.u32 %0, %2, %3, %0;\n\tmadc.hi.u32 %1, %2, %3, %1;"
+          : "+r"(lo[j]), "+r"(hi[j])
+          : "r"(a.w[j]), "r"(bi));
+    uint32_t nl[12], nh[12];  // N_j = nh_j : nl_j
+    nl[0] = lo[0];
+    nh[0] = 0;
 #pragma unroll
-    for (int j = 1; j < 12; j++) N[j] = (uint64_t)(uint32_t)T[j] + (T[j - 1] >> 32);
-    const uint64_t N12 = T[11] >> 32;
-    const uint32_t m = (uint32_t)N[0] * FP_PINV;
+    for (int j = 1; j < 12; j++)
+      asm("add.cc.u32 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=r"(nl[j]), "=r"(nh[j]) : "r"(lo[j]), "r"(hi[j - 1]));
+    const uint32_t n12 = hi[11];
+    const uint32_t m = nl[0] * FP_PINV;
 #pragma unroll
-    for (int j = 0; j < 12; j++) N[j] += (uint64_t)m * pm.w[j];
+    for (int j = 0; j < 12; j++)
+      asm("mad.lo.cc.u32 %0, %2, %3, %0;\n\tmadc.hi.u32 %1, %2, %3, %1;"
+          : "+r"(nl[j]), "+r"(nh[j])
+          : "r"(m), "r"(pm.w[j]));
 #pragma unroll
-    for (int j = 0; j < 11; j++) T[j] = (uint64_t)(uint32_t)N[j + 1] + (N[j] >> 32);
-    T[11] = N12 + (N[11] >> 32);
+    for (int j = 0; j < 11; j++)
+      asm("add.cc.u32 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=r"(lo[j]), "=r"(hi[j]) : "r"(nl[j + 1]), "r"(nh[j]));
+    asm("add.cc.u32 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=r"(lo[11]), "=r"(hi[11]) : "r"(n12), "r"(nh[11]));
   }
+  // t = sum_j T_j 2^(32 j): t_j = lo_j + hi_(j-1) + carry (the value is below 2p < 2^384)
   uint32_t t[12];
-  uint64_t acc = 0;
-#pragma unroll
-  for (int j = 0; j < 12; j++) {
-    acc += T[j];
-    t[j] = (uint32_t)acc;
-    acc >>= 32;
-  }
+  asm("add.cc.u32 %0, %12, 0;\n\taddc.cc.u32 %1, %13, %24;\n\taddc.cc.u32 %2, %14, %25;\n\t"
+      "addc.cc.u32 %3, %15, %26;\n\taddc.cc.u32 %4, %16, %27;\n\taddc.cc.u32 %5, %17, %28;\n\t"
+      "addc.cc.u32 %6, %18, %29;\n\taddc.cc.u32 %7, %19, %30;\n\taddc.cc.u32 %8, %20, %31;\n\t"
+      "addc.cc.u32 %9, %21, %32;\n\taddc.cc.u32 %10, %22, %33;\n\taddc.u32 %11, %23, %34;"
+      : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7]), "=r"(t[8]),
+        "=r"(t[9]), "=r"(t[10]), "=r"(t[11])
+      : "r"(lo[0]), "r"(lo[1]), "r"(lo[2]), "r"(lo[3]), "r"(lo[4]), "r"(lo[5]), "r"(lo[6]), "r"(lo[7]), "r"(lo[8]),
+        "r"(lo[9]), "r"(lo[10]), "r"(lo[11]), "r"(hi[0]), "r"(hi[1]), "r"(hi[2]), "r"(hi[3]), "r"(hi[4]), "r"(hi[5]),
+        "r"(hi[6]), "r"(hi[7]), "r"(hi[8]), "r"(hi[9]), "r"(hi[10]));
   fp r;
   fp_reduce_once(r.w, t);
   return r;
