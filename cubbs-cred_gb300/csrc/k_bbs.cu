@@ -384,6 +384,23 @@ DEV g1 shfl_g1(const g1 &p, int src) {
   }
   return r;
 }
+// Set s's half of group g's pairing job, affine: set 0 is pa (with the key's
+// slot), set 1 pb; an identity sum sets the job's flag.
+DEV void agg_write_job(const g1 &a, uint32_t g, uint32_t s, const int32_t *gslot, PairJob *gjobs) {
+  g1a aff;
+  const bool finite = g1_to_aff(a, aff);
+  if (!finite) aff.x = aff.y = fp_zero();
+  PairJob &jb = gjobs[g];
+  if (s == 0) {
+    jb.pa = aff;
+    jb.slot_a = gslot[g];
+    jb.slot_b = 0;
+    jb.active = 1;
+  } else {
+    jb.pb = aff;
+  }
+  if (!finite) atomicOr(&jb.flags, s == 0 ? 1u : 2u);
+}
 __global__ void __launch_bounds__(128) k_agg_combine(const g1 *part, const int32_t *gslot, PairJob *gjobs) {
   __shared__ g1 win[4];
   const uint32_t g = blockIdx.x, s = blockIdx.y, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -397,22 +414,63 @@ __global__ void __launch_bounds__(128) k_agg_combine(const g1 *part, const int32
   __syncthreads();
   if (w != 0) return;
   a = warp_sum_pairs(lp, lane < 8 ? win[lane >> 1] : g1_inf());
-  if (lane == 0) {
-    g1a aff;
-    const bool finite = g1_to_aff(a, aff);
-    if (!finite) aff.x = aff.y = fp_zero();
-    PairJob &jb = gjobs[g];
-    if (s == 0) {
-      jb.pa = aff;
-      jb.slot_a = gslot[g];
-      jb.slot_b = 0;
-      jb.active = 1;
-    } else {
-      jb.pb = aff;
+  if (lane == 0) agg_write_job(a, g, s, gslot, gjobs);
+}
+// Small groups: one ladder per point instead of the bucket MSM, whose
+// 255 bucket weights per (set, window) cost the same whatever the group size
+// (per group about 16 n mixed additions plus 8 x 255 x 15 point operations,
+// against 2 n x 62 for the ladders: the buckets win from about 280 items).
+// k_agg_ladder: one lane pair per (item, set) of a grouped item,
+// scaled[2i + s] = a P + b phi(P) from the prepared pts4 / sc (Shamir's trick
+// over the 32 bits of a and b; every step adds one of {P, phi(P), P + phi(P)}
+// or nothing and keeps the sum by a select, so pairs never diverge).
+__global__ void __launch_bounds__(32) k_agg_ladder(const g1a *pts4, const uint2 *sc, const int32_t *group_of,
+                                                   uint32_t n, g1 *scaled) {
+  const uint32_t t = (blockIdx.x * blockDim.x + threadIdx.x) >> 1;
+  if (t >= 2 * n) return;  // both lanes of a pair leave together
+  const LanePair lp = LanePair::here();
+  const uint32_t i = t >> 1, s = t & 1;
+  g1 acc = g1_inf();
+  const uint2 v = group_of[i] >= 0 ? sc[2 * i + s] : make_uint2(0u, 0u);
+  if (v.x) {  // a_i has its top bit set when the point takes part
+    const uint32_t a = v.x, b = v.y;
+    const g1 P = g1_from_aff(pts4[4 * i + 2 * s]), E = g1_from_aff(pts4[4 * i + 2 * s + 1]);
+    const g1 PE = g1_add_pair(lp, P, E);
+    acc = (b >> 31) ? PE : P;
+    #pragma unroll 1
+    for (int k = 30; k >= 0; k--) {
+      acc = g1_dbl_pair(lp, acc);
+      const uint32_t sel = ((a >> k) & 1) | (((b >> k) & 1) << 1);
+      const g1 q = sel == 1 ? P : sel == 2 ? E : PE;
+      const g1 sum = g1_add_pair(lp, acc, q);
+      if (sel) acc = sum;
     }
-    if (!finite) atomicOr(&jb.flags, s == 0 ? 1u : 2u);
+  }
+  if (lp.role == 0) scaled[t] = acc;
+}
+// Grid (groups, 2): block (g, s) sums scaled[2 i + s] over group g's items
+// (perm[goff[g] .. goff[g+1])) and writes its half of the group's pairing job
+// in affine form (the jobs start zeroed).  256 threads = 128 lane pairs: every
+// pair sums a strided share of the items, then the pairs' sums are added by
+// shuffles within each warp and through shared memory across the 8 warps.
+__global__ void __launch_bounds__(256) k_agg_sum(const g1 *scaled, const uint32_t *perm, const uint32_t *goff,
+                                                 const int32_t *gslot, PairJob *gjobs) {
+  __shared__ g1 part[8];
+  const uint32_t g = blockIdx.x, s = blockIdx.y, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const LanePair lp = LanePair::here();
+  g1 a = g1_inf();
+  #pragma unroll 1
+  for (uint32_t k = goff[g] + (threadIdx.x >> 1); k < goff[g + 1]; k += blockDim.x >> 1)
+    a = g1_add_pair(lp, a, scaled[2 * perm[k] + s]);
+  a = warp_sum_pairs(lp, a);
+  if (lane == 0) part[warp] = a;
+  __syncthreads();
+  if (warp == 0) {
+    a = warp_sum_pairs(lp, lane < 16 ? part[lane >> 1] : g1_inf());
+    if (lane == 0) agg_write_job(a, g, s, gslot, gjobs);
   }
 }
+
 // Per-item pairing jobs after the group checks: an item of a group whose check
 // passed is valid for the pairing (ok = 1, job skipped); any other item that
 // decoded gets its own check.
@@ -1127,6 +1185,7 @@ struct OpBatch {
   uint2 *agg_sc = nullptr;
   uint32_t *agg_ent = nullptr, *agg_boff = nullptr;
   g1 *agg_part = nullptr;
+  g1 *scaled = nullptr;  // per-point ladders of small groups
   g1 *fixed = nullptr, *v = nullptr;
   PairJob *pj = nullptr;
   uint8_t *ok = nullptr, *out = nullptr;
@@ -1200,6 +1259,7 @@ template <typename ItemT> void plan_groups_of(Runtime &rt, OpBatch &b) {
     b.agg_ent = rt.arena.alloc<uint32_t>(2 * AGG_SLAB * M);
     b.agg_boff = rt.arena.alloc<uint32_t>(AGG_SLAB * G * 257);
     b.agg_part = rt.arena.alloc<g1>(AGG_SLAB * G * 16);
+    b.scaled = rt.arena.alloc<g1>(2 * n);
   }
 }
 
@@ -1291,15 +1351,29 @@ void span_end(cudaStream_t s, int k, const char *name) {
     span_end(stream, _k, label);          \
   } while (0)
 
-// The group sums of a batch (k_agg_prep_* has filled agg_pts / agg_sc).
+// The group sums of a batch (k_agg_prep_* has filled agg_pts / agg_sc): the
+// bucket MSM when a group has AGG_BUCKET_MIN items or more, else the ladders.
+const size_t AGG_BUCKET_MIN = 256;
+bool agg_by_buckets(const OpBatch &b) {
+  for (size_t g = 0; g + 1 < b.h_goff.size(); g++)
+    if (b.h_goff[g + 1] - b.h_goff[g] >= AGG_BUCKET_MIN) return true;
+  return false;
+}
 void launch_agg_buckets(cudaStream_t s, OpBatch &b, uint32_t G) {
   const uint32_t M = (uint32_t)b.h_perm.size();
-  k_agg_sort<<<dim3(G, AGG_SLAB), 256, 0, s>>>(b.perm, b.goff, b.agg_sc, M, b.agg_ent, b.agg_boff);
-  k_agg_buckets<<<AGG_SLAB * G * 8, 64, 0, s>>>(b.agg_pts, b.agg_ent, b.agg_boff, M, b.agg_part);
+  if (agg_by_buckets(b)) {
+    k_agg_sort<<<dim3(G, AGG_SLAB), 256, 0, s>>>(b.perm, b.goff, b.agg_sc, M, b.agg_ent, b.agg_boff);
+    k_agg_buckets<<<AGG_SLAB * G * 8, 64, 0, s>>>(b.agg_pts, b.agg_ent, b.agg_boff, M, b.agg_part);
+  } else {
+    k_agg_ladder<<<blocks_for(4 * b.n, 32), 32, 0, s>>>(b.agg_pts, b.agg_sc, b.group_of, (uint32_t)b.n, b.scaled);
+  }
 }
 void launch_agg_combine(cudaStream_t s, OpBatch &b, uint32_t G) {
   CUBBS_CHECK(cudaMemsetAsync(b.gjobs, 0, G * sizeof(PairJob), s));
-  k_agg_combine<<<dim3(G, 2), 128, 0, s>>>(b.agg_part, b.gslot, b.gjobs);
+  if (agg_by_buckets(b))
+    k_agg_combine<<<dim3(G, 2), 128, 0, s>>>(b.agg_part, b.gslot, b.gjobs);
+  else
+    k_agg_sum<<<dim3(G, 2), 256, 0, s>>>(b.scaled, b.perm, b.goff, b.gslot, b.gjobs);
 }
 
 // ProofVerify on four streams.  Decoding Abar, Bbar, D (stream2) is
@@ -1310,15 +1384,17 @@ void launch_agg_combine(cudaStream_t s, OpBatch &b, uint32_t G) {
 // need only the affine points, and the challenge kernel rejects every proof
 // with a point outside G1 before any result is read.  Each of these kernels
 // fills only part of the GPU, so running them side by side shortens the step.
-// With the SM partition, the four streams are those of the larger partition
-// and the aggregated pairing chain (the group sums' bucket MSM and one check
-// per key group, made of kernels that fill only a few SMs) runs alone on the
-// smaller one, when its groups fit there two to an SM.  Sharing SMs with the
-// MSM kernels stretched that chain from about 3.5 ms to 5 ms.  With the third
-// partition, stream2 (the decode and the variable-base terms) runs on it and
-// the other three streams on the SMs left.
+// The SM partition is used when the batch's key groups fit its small part
+// two to an SM: the four streams are then those of the larger partition and
+// the aggregated pairing chain (the group sums and one check per key group,
+// made of kernels that fill only a few SMs) runs alone on the smaller one;
+// sharing SMs with the MSM kernels stretched that chain from about 3.5 ms to
+// 5 ms.  With the third partition, stream2 (the decode and the variable-base
+// terms) runs on it and the other three streams on the SMs left.  A batch with
+// more groups runs on the plain streams (64 keys of 16 proofs: 1.5 % faster on
+// the whole GPU than with the chain beside the MSM kernels on the larger part).
 void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
-  const bool part = !b.h_gslot.empty() && rt.use_partition();
+  const bool part = !b.h_gslot.empty() && rt.use_partition() && b.h_gslot.size() <= 2 * (size_t)rt.sh.small_sms;
   cudaStream_t s0 = rt.stream;
   cudaStream_t s = part ? rt.part[0] : rt.stream, s2 = part ? rt.part[1] : rt.stream2;
   cudaStream_t s3 = part ? rt.part[2] : rt.stream3, s4 = part ? rt.part[3] : rt.stream4;
@@ -1344,11 +1420,9 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
       if (r <= 0) throw CudaError(cudaErrorUnknown, "getrandom");
       got += (size_t)r;
     }
-    // the random-coefficient scaling, the group sums and the group checks
-    // run on the small partition when the groups fit there two to an SM
-    const bool alone = part && G <= 2 * (uint32_t)rt.sh.small_sms;
-    cudaStream_t sa = alone ? rt.part_check : s3;
-    if (alone) {
+    // the group sums and the group checks run on the small partition
+    cudaStream_t sa = part ? rt.part_check : s3;
+    if (part) {
       CUBBS_CHECK(cudaEventRecord(rt.ev_gc, s3));
       CUBBS_CHECK(cudaStreamWaitEvent(sa, rt.ev_gc, 0));
     }
@@ -1358,7 +1432,7 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
          launch_agg_buckets(sa, b, G));
     SPAN(sa, "agg_sum", launch_agg_combine(sa, b, G));
     SPAN(sa, "pairing_check", launch_pairing_check_split(sa, b.gjobs, G, rt.d_lines, b.gok));
-    if (alone) {
+    if (part) {
       CUBBS_CHECK(cudaEventRecord(rt.ev_gc2, sa));
       CUBBS_CHECK(cudaStreamWaitEvent(s3, rt.ev_gc2, 0));
     }
@@ -1393,7 +1467,7 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
     CUBBS_CHECK(cudaEventRecord(rt.ev_done, s));
     CUBBS_CHECK(cudaStreamWaitEvent(s0, rt.ev_done, 0));
   }
-  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 8 + (G ? 5 : 0);
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 8 + (G ? (agg_by_buckets(b) ? 5 : 4) : 0);
 }
 
 // ProofGen on three streams: the signature decode (stream3) runs beside
@@ -1495,7 +1569,7 @@ void run_verify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   } else {
     SPAN(s, "pairing", launch_pairing_check(s, b.pj, N, rt.d_lines, b.ok));
   }
-  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 7 + (G ? 6 : 0);
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 7 + (G ? (agg_by_buckets(b) ? 6 : 5) : 0);
 }
 
 // The whole device pipeline of one batch (no host work, no transfers).
