@@ -52,12 +52,12 @@ MODEL_M = {
 
 
 # DRAM bytes per launch of a stage's kernel at this workload, from one ncu capture
-# (dram__bytes_read.sum + dram__bytes_write.sum): k_fixed_msm read 12.77 MB for
-# 512 rows x 12 terms x 16 windows at L = 10; table reads scale with rows x terms,
-# so a 1024 x 102-term launch moves 12.82 MB x (1024 x 102) / (512 x 12) = 218 MB.
-# k_var_mul_pair read 0.25 MB for 1024 terms (points, scalars, jobs); the bench's
-# launch has 4 terms per proof, 4096 terms: 0.25 MB x 4096 / 1024 = 1.0 MB.
-TRAFFIC_BYTES = {"fixed_msm": 12.82e6 * (1024 * 102) / (512 * 12), "var_mul": 0.25e6 * 4096 / 1024}
+# of the 1024-proof, L = 100 step (dram__bytes_read.sum + dram__bytes_write.sum):
+# k_var_mul_pair moved 0.638 + 0.004 MB for its 4096 terms (points, scalars, jobs);
+# k_fixed_msm<32> moved 170.4 + 3.5 MB with the table narrowed to window 14 (19
+# windows per term, so that the capture fits); table reads scale with the windows,
+# so the window-20 launch (13 windows) moves about 173.9 MB x 13 / 19 = 119 MB.
+TRAFFIC_BYTES = {"fixed_msm": 173.9e6 * 13 / 19, "var_mul": 0.6415e6}
 
 
 def drbg(seed: bytes, label: bytes, i: int, n: int) -> bytes:
@@ -461,6 +461,7 @@ def main():
                 "first_call": "Sign of the 1024-item batch on a fresh process: generators by hash_to_curve, "
                               "the fixed-base table, the key's Miller lines, then the batch"}
     part_sms = pkg.sm_partition()
+    var_sms = pkg.sm_partition_var()[0]
 
     # ---------------- timed: device-resident ProofVerify (headline) + ProofGen
     def barrier():
@@ -537,8 +538,12 @@ def main():
         roof = {"bound": "imad", "kernel": stage[0], "achieved": round(achieved, 3), "peak": round(tera_imad, 3),
                 "unit": "T IMAD/s (32-bit integer multiply-add)", "frac": round(achieved / tera_imad, 4),
                 "traffic": round(traffic) if traffic else None,
-                "traffic_unit": "bytes per launch (ncu capture of a smaller case, scaled to this launch)",
+                "traffic_unit": "bytes per launch (ncu capture of this step; the fixed-base MSM's with the table at "
+                                "window 14, scaled to window 20)",
                 "peak_source": "measured in this run (k_imad_peak, 16 independent mad.lo chains)",
+                "partition_sms": var_sms if stage[0] == "var_mul" and var_sms else None,
+                "frac_of_partition": round(achieved / tera_imad * (part_sms[0] + part_sms[1]) / var_sms, 4)
+                if stage[0] == "var_mul" and var_sms else None,
                 "model_m_per_op": model, "stage_ms": round(stage[1], 3)}
     whole = n * MODEL_M["proof_verify"]["total"] * IMAD_PER_M / (pv_step / 1e3) / 1e12
 

@@ -1548,7 +1548,7 @@ void run_verify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   const uint32_t G = (uint32_t)b.h_gslot.size();
   if (G) {
     // random-coefficient group checks per key, then the per-item checks of the
-    // items outside passing groups (as ProofVerify does; see k_agg_scale)
+    // items outside passing groups (as ProofVerify does; see k_agg_prep_pv)
     AggSeed seed;
     size_t got = 0;
     while (got < sizeof(seed)) {
