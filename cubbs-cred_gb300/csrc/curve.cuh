@@ -611,35 +611,74 @@ DEV g1 g1_mul_glv(g1a p, fr k) {
   return acc;
 }
 
-// g1_mul_glv on a lane pair (both lanes return k * P).
+// g1_mul_glv on a lane pair (both lanes return k * P).  The multiples
+// 1P..8P are brought to one common denominator, Z_c^2 = prod ZZ_j and
+// Z_c^3 = prod ZZZ_j, by suffix and prefix products (no inversion): entry k
+// becomes (X_k', Y_k') = (X_k prod_{j != k} ZZ_j, Y_k prod_{j != k} ZZZ_j), the
+// affine point (x Z_c^2, y Z_c^3) of the isomorphic curve y^2 = x^3 + 4 Z_c^6.
+// The doubling and mixed-addition formulas do not involve the curve's b, so
+// the ladder runs on that curve with mixed additions (5 product rounds on a
+// pair instead of 7 for an XYZZ addition) and precomputed phi-images
+// (beta X_k', -Y_k'); the sum comes back with ZZ *= Z_c^2, ZZZ *= Z_c^3.  A
+// point of small order (not in G1: rejected by the subgroup check) can make
+// a multiple the identity, Z_c = 0 and the result meaningless, never a fault.
 DEV g1 g1_mul_glv_pair(const LanePair &lp, g1a p, fr k) {
   uint32_t s[4], q[4];
   glv_split(k, s, q);
   int8_t ds[33], dq[33];
   recode_w4(s, ds);
   recode_w4(q, dq);
-  g1 tab[8];
-  tab[0] = g1_from_aff(p);
-  tab[1] = g1_dbl_pair(lp, g1_from_aff(p));
+  g1 t[8];
+  t[0] = g1_from_aff(p);
+  t[1] = g1_dbl_pair(lp, t[0]);
   #pragma unroll 1
-  for (int i = 2; i < 8; i++) tab[i] = g1_add_aff_pair(lp, tab[i - 1], p);
+  for (int i = 2; i < 8; i++) t[i] = g1_add_aff_pair(lp, t[i - 1], p);
+  // suffix products sz[k] = prod_{j > k} ZZ_j, szz[k] = prod_{j > k} ZZZ_j
+  fp sz[8], szz[8];
+  sz[7] = szz[7] = fp_one();
+  sz[6] = t[7].ZZ;
+  szz[6] = t[7].ZZZ;
+  #pragma unroll 1
+  for (int i = 5; i >= 0; i--) pair_mul(lp, sz[i + 1], t[i + 1].ZZ, szz[i + 1], t[i + 1].ZZZ, sz[i], szz[i]);
+  const fp zc2 = sz[0], zc3 = szz[0];  // ZZ_0 = ZZZ_0 = 1
+  // forward: pz = prod_{j < k} ZZ_j; X_k' = X_k pz sz[k], Y_k' = Y_k pzz szz[k] (in place)
+  fp pz = fp_one(), pzz = fp_one();
+  #pragma unroll 1
+  for (int i = 0; i < 8; i++) {
+    fp f = sz[i], g = szz[i];
+    if (i > 0) pair_mul(lp, pz, sz[i], pzz, szz[i], f, g);
+    if (i > 0 && i < 7) pair_mul(lp, pz, t[i].ZZ, pzz, t[i].ZZZ, pz, pzz);
+    else if (i == 0) { pz = t[0].ZZ; pzz = t[0].ZZZ; }
+    pair_mul(lp, t[i].X, f, t[i].Y, g, t[i].X, t[i].Y);
+  }
+  // phi-images: X of phi(entry k) in t[k].ZZ
+  const fp beta = C_GLV_BETA;
+  #pragma unroll 1
+  for (int i = 0; i < 8; i += 2) pair_mul(lp, t[i].X, beta, t[i + 1].X, beta, t[i].ZZ, t[i + 1].ZZ);
   g1 acc = g1_inf();
   #pragma unroll 1
   for (int i = 32; i >= 0; i--) {
     if (i != 32) {
       acc = g1_dbl_pair(lp, acc); acc = g1_dbl_pair(lp, acc); acc = g1_dbl_pair(lp, acc); acc = g1_dbl_pair(lp, acc);
     }
-    int a = ds[i];
+    const int a = ds[i];
     if (a) {
-      g1 t = tab[(a > 0 ? a : -a) - 1];
-      acc = g1_add_pair(lp, acc, a > 0 ? t : g1_neg(t));
+      const g1 &e = t[(a > 0 ? a : -a) - 1];
+      g1a pt;
+      pt.x = e.X;
+      pt.y = a > 0 ? e.Y : fp_neg(e.Y);
+      acc = g1_add_aff_pair(lp, acc, pt);
     }
-    int b = dq[i];
+    const int b = dq[i];
     if (b) {
-      g1 t = g1_endo(tab[(b > 0 ? b : -b) - 1]);
-      acc = g1_add_pair(lp, acc, b > 0 ? t : g1_neg(t));
+      const g1 &e = t[(b > 0 ? b : -b) - 1];
+      g1a pt;
+      pt.x = e.ZZ;  // beta X'
+      pt.y = b > 0 ? fp_neg(e.Y) : e.Y;
+      acc = g1_add_aff_pair(lp, acc, pt);
     }
   }
+  pair_mul(lp, acc.ZZ, zc2, acc.ZZZ, zc3, acc.ZZ, acc.ZZZ);  // back to y^2 = x^3 + 4 (identity stays ZZ = 0)
   return acc;
 }
 
