@@ -511,11 +511,39 @@ __global__ void __launch_bounds__(128) k_vf_pairjobs_agg(uint32_t n, const int32
   }
 }
 
-// T1, T2 -> compressed; recompute the challenge (a mismatch marks the item invalid).
+// The part of the challenge hash that comes before T1 and T2 (R, the disclosed
+// indexes and message scalars, Abar || Bbar || D: about 34 SHA-256 blocks at
+// 50 disclosed messages) needs no point arithmetic, so it is absorbed early,
+// beside the MSMs, and the expander's state is kept per item for k_pv_finish.
+// It reads the input items as packed (items0): an item the host rejected is
+// skipped, and k_pv_finish skips it as well (a status never returns to ST_OK).
+template <int S>
+__global__ void __launch_bounds__(64) k_pv_chal_prefix(const PvItem *items0, uint32_t n, const uint8_t *blob,
+                                                       const fr *msc, hash_ctx<S> *chal) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PvItem it = items0[i];
+  if (it.status != ST_OK) return;
+  const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
+  hash_ctx<S> c;
+  msg_begin(c);
+  msg_u64be(c, it.R, 8);
+  #pragma unroll 1
+  for (uint32_t k = 0; k < it.R; k++) {
+    msg_u64be(c, idx[k], 8);
+    msg_fr_be(c, msc[it.msg_base + k]);
+  }
+  msg_bytes(c, blob + it.proof_off, 144);
+  chal[i] = c;
+}
+
+// T1, T2 -> compressed; finish the challenge from the state k_pv_chal_prefix
+// kept (a mismatch marks the item invalid).
 template <int S>
 __global__ void __launch_bounds__(64) k_pv_finish(PvItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
                                                   const fr *domain, const int32_t *dec_status,
-                                                  const int32_t *outside_g1, const g1 *t2fix, const g1 *v) {
+                                                  const int32_t *outside_g1, const g1 *t2fix, const g1 *v,
+                                                  const hash_ctx<S> *chal) {
   // every lane of the warp reaches the shared affine conversion below
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   bool act = i < n;
@@ -545,15 +573,7 @@ __global__ void __launch_bounds__(64) k_pv_finish(PvItem *items, uint32_t n, con
   g1_compress_aff_or_inf(aff[1], fin[1], t2c);
   const uint8_t *pr = blob + it.proof_off;
   const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
-  hash_ctx<S> c;
-  msg_begin(c);
-  msg_u64be(c, it.R, 8);
-  #pragma unroll 1
-  for (uint32_t k = 0; k < it.R; k++) {
-    msg_u64be(c, idx[k], 8);
-    msg_fr_be(c, msc[it.msg_base + k]);
-  }
-  msg_bytes(c, pr, 144);
+  hash_ctx<S> c = chal[i];
   msg_bytes(c, t1c, 48);
   msg_bytes(c, t2c, 48);
   msg_fr_be(c, domain[i]);
@@ -1186,6 +1206,7 @@ struct OpBatch {
   uint32_t *agg_ent = nullptr, *agg_boff = nullptr;
   g1 *agg_part = nullptr;
   g1 *scaled = nullptr;  // per-point ladders of small groups
+  uint8_t *chal = nullptr;  // ProofVerify: challenge-hash state per item (hash_ctx of the suite)
   g1 *fixed = nullptr, *v = nullptr;
   PairJob *pj = nullptr;
   uint8_t *ok = nullptr, *out = nullptr;
@@ -1274,7 +1295,8 @@ void upload(Runtime &rt, OpBatch &b) {
                 (b.pts48.size() / 48) * (sizeof(g1a) + 8) + 2 * n * sizeof(g1) + 2 * n * sizeof(g1a) +
                 n * b.rs_stride * sizeof(fr) + b.out_total + n * (2 * sizeof(g1) + 16 + sizeof(PairJob) + 8) +
                 n * (4 * sizeof(g1a) + 2 * sizeof(uint2) + 4 * 2 * AGG_SLAB) +
-                (n / AGG_MIN_GROUP + 1) * AGG_SLAB * (257 * 4 + 16 * sizeof(g1)) + 64 * 256;
+                (n / AGG_MIN_GROUP + 1) * AGG_SLAB * (257 * 4 + 16 * sizeof(g1)) +
+                n * std::max(sizeof(sha_ctx), sizeof(shake_ctx)) + 64 * 256;
   rt.arena.reserve(need);
   rt.staging.reserve(65536 + 8 * nm + b.pts48.size() + n * (b.item_size + sizeof(DomainJob) + 96));
   // the blob and the message bytes are already pinned: DMA them directly
@@ -1314,7 +1336,10 @@ void upload(Runtime &rt, OpBatch &b) {
   b.e = rt.arena.alloc<fr>(n);
   b.vpts = rt.arena.alloc<g1a>(2 * n);
   if (b.op == OP_PGEN) b.rs = rt.arena.alloc<fr>(n * b.rs_stride);
-  if (b.op == OP_PVERIFY) plan_groups_of<PvItem>(rt, b);
+  if (b.op == OP_PVERIFY) {
+    plan_groups_of<PvItem>(rt, b);
+    b.chal = rt.arena.alloc<uint8_t>(n * std::max(sizeof(sha_ctx), sizeof(shake_ctx)));
+  }
   if (b.op == OP_VERIFY) plan_groups_of<VerifyItem>(rt, b);
   b.out = rt.arena.alloc<uint8_t>(b.out_total + 1);
 }
@@ -1405,8 +1430,19 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   CUBBS_CHECK(cudaEventRecord(rt.ev_fork, s0));
   if (part) CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_fork, 0));
   CUBBS_CHECK(cudaStreamWaitEvent(s2, rt.ev_fork, 0));
+  if (nm)
+    SPAN(s, "hash_messages",
+         launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
+                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, map_dst_len(rt), b.msc, rt.suite));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_hash, s));
   SPAN(s2, "g1_decode", launch_g1_decode(s2, b.dpts48, 48, (uint32_t)npts, b.pts, b.dec, false));
   CUBBS_CHECK(cudaEventRecord(rt.ev_mid, s2));
+  // stream4: the challenge-hash prefix (needs the message scalars), then the
+  // subgroup check (needs the decoded points)
+  CUBBS_CHECK(cudaStreamWaitEvent(s4, rt.ev_hash, 0));
+  SPAN(s4, "challenge_prefix",
+       CUBBS_SUITE_DISPATCH(rt.suite, k_pv_chal_prefix<S><<<blocks_for(n, 64), 64, 0, s4>>>(
+                                          it0, N, b.dblob, b.msc, reinterpret_cast<hash_ctx<S> *>(b.chal))));
   CUBBS_CHECK(cudaStreamWaitEvent(s4, rt.ev_mid, 0));
   SPAN(s4, "g1_subgroup", launch_g1_subgroup(s4, b.pts, b.dec, (uint32_t)npts, b.sub));
   CUBBS_CHECK(cudaEventRecord(rt.ev_sub, s4));
@@ -1450,10 +1486,6 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
        k_pv_jobs<<<blocks_for(n, 128), 128, 0, s2>>>(it0, N, b.dblob, b.dec, b.jobs, b.jscal);
        launch_var_mul(s2, b.pts, b.jobs, b.jscal, 4 * N, b.v));
   CUBBS_CHECK(cudaEventRecord(rt.ev_side, s2));
-  if (nm)
-    SPAN(s, "hash_messages",
-         launch_h2s_flat(s, b.dmsg + 8 * nm, reinterpret_cast<uint32_t *>(b.dmsg),
-                         reinterpret_cast<uint32_t *>(b.dmsg) + nm, (uint32_t)nm, dmapdst, map_dst_len(rt), b.msc, rt.suite));
   SPAN(s, "domain", launch_domain(s, b.ddj, N, b.dblob, rt.d_gens_c(), rt.ss().d_dom_prefix, b.domain, rt.suite));
   SPAN(s, "scalar_prep",
        k_pv_rows<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms));
@@ -1461,13 +1493,14 @@ void run_pverify(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_side, 0));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_sub, 0));
   SPAN(s, "challenge",
-       CUBBS_SUITE_DISPATCH(rt.suite, k_pv_finish<S><<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.sub, b.fixed, b.v)));
+       CUBBS_SUITE_DISPATCH(rt.suite, k_pv_finish<S><<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.dec, b.sub, b.fixed, b.v,
+                                                                                      reinterpret_cast<const hash_ctx<S> *>(b.chal))));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_join, 0));
   if (part) {
     CUBBS_CHECK(cudaEventRecord(rt.ev_done, s));
     CUBBS_CHECK(cudaStreamWaitEvent(s0, rt.ev_done, 0));
   }
-  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 8 + (G ? (agg_by_buckets(b) ? 5 : 4) : 0);
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 9 + (G ? (agg_by_buckets(b) ? 5 : 4) : 0);
 }
 
 // ProofGen on three streams: the signature decode (stream3) runs beside

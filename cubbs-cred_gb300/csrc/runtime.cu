@@ -514,6 +514,7 @@ Runtime::Runtime(SharedState &s)
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_side, cudaEventDisableTiming));
   CUBBS_CHECK(cudaStreamCreateWithFlags(&stream4, cudaStreamNonBlocking));
   CUBBS_CHECK(cudaEventCreateWithFlags(&ev_sub, cudaEventDisableTiming));
+  CUBBS_CHECK(cudaEventCreateWithFlags(&ev_hash, cudaEventDisableTiming));
   arena.reserve((size_t)256 << 20);
   staging.reserve((size_t)64 << 20);
   pack.reserve((size_t)64 << 20);

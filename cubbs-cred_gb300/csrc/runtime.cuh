@@ -218,6 +218,7 @@ struct Runtime {
   // stream -> stream2 (ev_fork), stream2 -> stream3, stream4 (ev_mid), back to stream
   // (ev_side, ev_join, ev_sub)
   cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_mid = nullptr, ev_side = nullptr, ev_sub = nullptr;
+  cudaEvent_t ev_hash = nullptr;  // ProofVerify: message scalars ready (stream -> stream4)
   // ProofVerify on the SM partition: part[0..3] play stream..stream4 on the
   // larger partition, part_check runs the aggregated pairing chain on the
   // smaller one (all null without a partition)
