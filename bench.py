@@ -293,7 +293,7 @@ def serving_pv_section(pkg, rank, pv_reqs):
     res, _, _ = pkg.serve_replay(pool, [(i, 0) for i in range(len(pool))], mode=pkg.SERVE_QUEUE)  # warm
     assert all(c == 0 and v == 1 for c, v, _ in res)
     rows, best = [], {"served": None, "plain": None}
-    for rate in (25000, 50000, 100000, 150000, 175000, 200000, 225000, 250000, 275000, 300000):
+    for rate in (25000, 50000, 100000, 150000, 175000, 200000, 225000, 250000, 275000, 300000, 350000, 400000):
         count = max(4096, min(60000, int(rate * 0.2)))
         row = {"rate_req_s": rate, "requests": count, "repeats": REPEATS}
         runs = {"served": [], "plain": []}
