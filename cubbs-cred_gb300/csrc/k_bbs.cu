@@ -938,7 +938,8 @@ __global__ void __launch_bounds__(64) k_pg_vars(PgItem *items, uint32_t n, const
 template <int S>
 __global__ void __launch_bounds__(64) k_pg_finish(PgItem *items, uint32_t n, const uint8_t *blob, const fr *msc,
                                                   const fr *domain, const fr *rs, uint32_t rs_stride,
-                                                  const g1 *t2fix, const g1 *v, uint8_t *out) {
+                                                  const g1 *t2fix, const g1 *v, uint8_t *out, const hash_ctx<S> *chal,
+                                                  const fr *r3inv) {
   // every lane of the warp reaches the shared affine conversion below
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool act = i < n && items[i].status == ST_OK;
@@ -964,14 +965,7 @@ __global__ void __launch_bounds__(64) k_pg_finish(PgItem *items, uint32_t n, con
   g1_compress_aff_or_inf(aff[3], fin[3], t1c);
   g1_compress_aff_or_inf(aff[4], fin[4], t2c);
   const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
-  hash_ctx<S> c;
-  msg_begin(c);
-  msg_u64be(c, it.R, 8);
-  #pragma unroll 1
-  for (uint32_t k = 0; k < it.R; k++) {
-    msg_u64be(c, idx[k], 8);
-    msg_fr_be(c, msc[it.msg_base + idx[k]]);
-  }
+  hash_ctx<S> c = chal[i];  // R and the disclosed messages, absorbed by k_pg_early
   msg_bytes(c, o, 144);
   msg_bytes(c, t1c, 48);
   msg_bytes(c, t2c, 48);
@@ -988,7 +982,7 @@ __global__ void __launch_bounds__(64) k_pg_finish(PgItem *items, uint32_t n, con
   }
   fr e;
   fr_raw_from_be32(blob + it.sig_off + 48, e);
-  fr r3 = frr_inv(r2);
+  const fr r3 = r3inv[i];
   fr_raw_to_be32(fr_add(et, frr_mul(e, ch)), o + 144);
   fr_raw_to_be32(fr_sub(r1t, frr_mul(r1, ch)), o + 176);
   fr_raw_to_be32(fr_sub(r3t, frr_mul(r3, ch)), o + 208);
@@ -1003,6 +997,33 @@ __global__ void __launch_bounds__(64) k_pg_finish(PgItem *items, uint32_t n, con
     u++;
   }
   fr_raw_to_be32(ch, o + 240 + 32 * it.U);
+}
+
+// Work of k_pg_finish that needs neither the MSMs nor the proof's points, done
+// beside them: the challenge hash's leading part (R, the disclosed indexes and
+// message scalars: about 31 SHA-256 blocks at 50 disclosed messages), kept as
+// the expander's state per item, and r3 = r2^-1 (a Fermat inversion in Fr).
+// It reads the input items as packed; an item the host rejected is skipped
+// (k_pg_finish skips it as well).
+template <int S>
+__global__ void __launch_bounds__(64) k_pg_early(const PgItem *items0, uint32_t n, const uint8_t *blob,
+                                                 const fr *msc, const fr *rs, uint32_t rs_stride, hash_ctx<S> *chal,
+                                                 fr *r3inv) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const PgItem it = items0[i];
+  if (it.status != ST_OK) return;
+  const uint32_t *idx = reinterpret_cast<const uint32_t *>(blob + it.idx_off);
+  hash_ctx<S> c;
+  msg_begin(c);
+  msg_u64be(c, it.R, 8);
+  #pragma unroll 1
+  for (uint32_t k = 0; k < it.R; k++) {
+    msg_u64be(c, idx[k], 8);
+    msg_fr_be(c, msc[it.msg_base + idx[k]]);
+  }
+  chal[i] = c;
+  r3inv[i] = frr_inv(rs[(size_t)i * rs_stride + 1]);  // r2 == 0 gives 0; k_pg_finish reports it
 }
 
 // ============================================================================ host side
@@ -1206,7 +1227,8 @@ struct OpBatch {
   uint32_t *agg_ent = nullptr, *agg_boff = nullptr;
   g1 *agg_part = nullptr;
   g1 *scaled = nullptr;  // per-point ladders of small groups
-  uint8_t *chal = nullptr;  // ProofVerify: challenge-hash state per item (hash_ctx of the suite)
+  uint8_t *chal = nullptr;  // ProofVerify, ProofGen: challenge-hash state per item (hash_ctx of the suite)
+  fr *r3inv = nullptr;      // ProofGen: r2^-1 per item
   g1 *fixed = nullptr, *v = nullptr;
   PairJob *pj = nullptr;
   uint8_t *ok = nullptr, *out = nullptr;
@@ -1335,7 +1357,11 @@ void upload(Runtime &rt, OpBatch &b) {
   b.ok = rt.arena.alloc<uint8_t>(n);
   b.e = rt.arena.alloc<fr>(n);
   b.vpts = rt.arena.alloc<g1a>(2 * n);
-  if (b.op == OP_PGEN) b.rs = rt.arena.alloc<fr>(n * b.rs_stride);
+  if (b.op == OP_PGEN) {
+    b.rs = rt.arena.alloc<fr>(n * b.rs_stride);
+    b.chal = rt.arena.alloc<uint8_t>(n * std::max(sizeof(sha_ctx), sizeof(shake_ctx)));
+    b.r3inv = rt.arena.alloc<fr>(n);
+  }
   if (b.op == OP_PVERIFY) {
     plan_groups_of<PvItem>(rt, b);
     b.chal = rt.arena.alloc<uint8_t>(n * std::max(sizeof(sha_ctx), sizeof(shake_ctx)));
@@ -1520,6 +1546,7 @@ void run_pgen(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   SPAN(s3, "g1_subgroup", launch_g1_subgroup(s3, b.pts, b.dec, (uint32_t)npts, b.sub));
   CUBBS_CHECK(cudaEventRecord(rt.ev_join, s3));
   SPAN(s2, "random_scalars", CUBBS_SUITE_DISPATCH(rt.suite, k_pg_random<S><<<blocks_for(n, 64), 64, 0, s2>>>(it0, N, b.dblob, b.rs, rss)));
+  CUBBS_CHECK(cudaEventRecord(rt.ev_mid, s2));
   SPAN(s2, "fixed_msm_t2",
        k_pg_rows_t2<<<blocks_for(n, 128), 128, 0, s2>>>(it0, N, b.dblob, b.rs, rss, b.rows, stride, b.nterms);
        launch_fixed_msm(s2, rt.table(), b.rows + (size_t)n * stride, stride, b.nterms + n, N, b.fixed + n));
@@ -1532,6 +1559,11 @@ void run_pgen(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   SPAN(s, "fixed_msm",
        k_pg_rows_b<<<blocks_for(n, 128), 128, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rows, stride, b.nterms);
        launch_fixed_msm(s, rt.table(), b.rows, stride, b.nterms, N, b.fixed));
+  CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_mid, 0));  // the blinding scalars
+  SPAN(s, "finish_early",
+       CUBBS_SUITE_DISPATCH(rt.suite, k_pg_early<S><<<blocks_for(n, 64), 64, 0, s>>>(
+                                          it0, N, b.dblob, b.msc, b.rs, rss, reinterpret_cast<hash_ctx<S> *>(b.chal),
+                                          b.r3inv)));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_side, 0));
   CUBBS_CHECK(cudaStreamWaitEvent(s, rt.ev_join, 0));
   SPAN(s, "var_prep",
@@ -1540,8 +1572,8 @@ void run_pgen(Runtime &rt, OpBatch &b, uint8_t *dmapdst) {
   SPAN(s, "var_mul", launch_var_mul(s, b.vpts, b.jobs, b.jscal, 7 * N, b.v));
   SPAN(s, "finish",
        CUBBS_SUITE_DISPATCH(rt.suite, k_pg_finish<S><<<blocks_for(n, 64), 64, 0, s>>>(it, N, b.dblob, b.msc, b.domain, b.rs, rss, b.fixed + n, b.v,
-                                                    b.out)));
-  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 9;
+                                                    b.out, reinterpret_cast<const hash_ctx<S> *>(b.chal), b.r3inv)));
+  b.launches_per_run = (nm ? 1 : 0) + (npts ? 2 : 0) + 10;
 }
 
 // Verify on three streams, as ProofVerify: the signature decode (stream2, no
