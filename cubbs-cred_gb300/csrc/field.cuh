@@ -423,7 +423,52 @@ DEV bool fr_eq(const fr &a, const fr &b) {
 }
 DEV fr fr_add(const fr &a, const fr &b) { fr r; fr_add_raw(r.w, a.w, b.w); return r; }
 DEV fr fr_sub(const fr &a, const fr &b) { fr r; fr_sub_raw(r.w, a.w, b.w); return r; }
+// Montgomery product mod r (R = 2^256, fully reduced): the carry-save rows of
+// fp_mul_inl over 8 limbs, in PTX for the same reason (the carry additions stay
+// on the ALU pipe).  Bounds: a, b < r; partial sums below 2^64; result below 2r.
 DEV fr fr_mul_inl(const fr &a, const fr &b) {
+  const fr rm = FR_MOD_INIT;
+  uint32_t lo[8], hi[8];
+#pragma unroll
+  for (int j = 0; j < 8; j++) lo[j] = hi[j] = 0;
+#pragma unroll
+  for (int i = 0; i < 8; i++) {
+    const uint32_t bi = b.w[i];
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      asm("mad.lo.cc.u32 %0, %2, %3, %0;\n\tmadc.hi.u32 %1, %2, %3, %1;"
+          : "+r"(lo[j]), "+r"(hi[j])
+          : "r"(a.w[j]), "r"(bi));
+    uint32_t nl[8], nh[8];
+    nl[0] = lo[0];
+    nh[0] = 0;
+#pragma unroll
+    for (int j = 1; j < 8; j++)
+      asm("add.cc.u32 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=r"(nl[j]), "=r"(nh[j]) : "r"(lo[j]), "r"(hi[j - 1]));
+    const uint32_t n8 = hi[7];
+    const uint32_t m = nl[0] * FR_PINV;
+#pragma unroll
+    for (int j = 0; j < 8; j++)
+      asm("mad.lo.cc.u32 %0, %2, %3, %0;\n\tmadc.hi.u32 %1, %2, %3, %1;"
+          : "+r"(nl[j]), "+r"(nh[j])
+          : "r"(m), "r"(rm.w[j]));
+#pragma unroll
+    for (int j = 0; j < 7; j++)
+      asm("add.cc.u32 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=r"(lo[j]), "=r"(hi[j]) : "r"(nl[j + 1]), "r"(nh[j]));
+    asm("add.cc.u32 %0, %2, %3;\n\taddc.u32 %1, 0, 0;" : "=r"(lo[7]), "=r"(hi[7]) : "r"(n8), "r"(nh[7]));
+  }
+  uint32_t t[8];
+  asm("add.cc.u32 %0, %8, 0;\n\taddc.cc.u32 %1, %9, %16;\n\taddc.cc.u32 %2, %10, %17;\n\taddc.cc.u32 %3, %11, %18;\n\t"
+      "addc.cc.u32 %4, %12, %19;\n\taddc.cc.u32 %5, %13, %20;\n\taddc.cc.u32 %6, %14, %21;\n\taddc.u32 %7, %15, %22;"
+      : "=r"(t[0]), "=r"(t[1]), "=r"(t[2]), "=r"(t[3]), "=r"(t[4]), "=r"(t[5]), "=r"(t[6]), "=r"(t[7])
+      : "r"(lo[0]), "r"(lo[1]), "r"(lo[2]), "r"(lo[3]), "r"(lo[4]), "r"(lo[5]), "r"(lo[6]), "r"(lo[7]),
+        "r"(hi[0]), "r"(hi[1]), "r"(hi[2]), "r"(hi[3]), "r"(hi[4]), "r"(hi[5]), "r"(hi[6]));
+  fr r;
+  fr_reduce_once(r.w, t);
+  return r;
+}
+// The CIOS form it replaced (carry chains of field_ptx.cuh), kept for the tests.
+DEV fr fr_mul_cios_inl(const fr &a, const fr &b) {
   uint32_t t[17];
   _Pragma("unroll") for (int i = 0; i < 9; i++) t[i] = 0;
   _Pragma("unroll") for (int i = 0; i < 8; i++) {
