@@ -299,6 +299,42 @@ def test_proof_verify_aggregated_groups(gpu, oracle):
     assert all(v for _, v in gpu.proof_verify_batch(ok_items))
 
 
+def test_proof_verify_bucket_groups(gpu, oracle):
+    """A key group of 256 items or more takes the bucket MSM for its group sums
+    (smaller groups one ladder per point): with pairing-only failures and a
+    challenge mismatch inside the 300-item group every verdict equals the
+    oracle's, and the group of the valid items passes its check."""
+    items = _pv_items(oracle, b"bucket-a", 300, 6, fake={11, 150, 299}) + \
+        _pv_items(oracle, b"bucket-b", 20, 6, fake={4})
+    items[60] = items[60][:3] + (b"p!",) + items[60][4:]   # challenge mismatch
+    want = [oracle.proof_verify(pk, pr, hd, ph, dm, di) == 0 for pk, pr, hd, ph, dm, di, _ in items]
+    assert want.count(False) == 5
+    got = [v for _, v in gpu.proof_verify_batch(items)]
+    assert got == want
+    ok_items = [it for it, w in zip(items, want) if w]
+    assert all(v for _, v in gpu.proof_verify_batch(ok_items))
+
+
+def test_verify_bucket_groups(gpu, oracle):
+    """Verify with a 280-item key group (bucket MSM for the group sums): a
+    signature over other messages and one with a changed e inside the group;
+    every verdict equals the oracle's."""
+    seed = b"verify-bucket"
+    sk, pk = keypair(oracle, seed, 0)
+    items = []
+    for i in range(280):
+        msgs = messages(seed, i, 4, 32)
+        items.append((pk, oracle.sign(sk, pk, b"hdr", msgs)[0], b"hdr", msgs))
+    items[9] = (pk, items[9][1], b"hdr", messages(seed + b"-o", 9, 4, 32))
+    e = (int.from_bytes(items[200][1][48:], "big") + 1).to_bytes(32, "big")
+    items[200] = (pk, items[200][1][:48] + e, b"hdr", items[200][3])
+    want = [oracle.verify(*it) == 0 for it in items]
+    assert want.count(False) == 2
+    assert [v for _, v in gpu.verify_batch(items)] == want
+    ok_items = [it for it, w in zip(items, want) if w]
+    assert all(v for _, v in gpu.verify_batch(ok_items))
+
+
 def test_sign_e_resident(gpu, oracle):
     import ctypes
     seed = b"sign-e"
